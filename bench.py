@@ -1,0 +1,296 @@
+#!/usr/bin/env python3
+"""Benchmark: PISO time steps of the 128^3 channel on one GB300.
+
+Metric (the benchmark spec): PISO steps/s and the p'-solve time to a 1e-6
+relative residual.  A "step" is one PISO time step of main.f90:134-207:
+time-level shift, CourantNo.h, ghost-cell update, calcuvw (gradients,
+fluxuvw x3, wall terms, three sipsol solves), PISO_multiple_correction
+(2 correctors, PCG-SIP p solves to sor(ip)=0.1 then 1e-6).
+
+  value        steps/s with every field resident in HBM (device-timed with
+               CUDA events on the library's stream)
+  e2e          the same steps through the C ABI with host buffers: each
+               step copies u,v,w,p,f1,f2,f3 from pinned host memory, runs
+               cappgpu_piso_steps(1), and copies them back
+  roofline     the SIP forward substitution (the hottest unit of the p
+               solve) against the measured HBM copy bandwidth
+  cpu_baseline the C oracle (the reference's algorithm restated,
+               single-threaded as the reference's recurrences are) on one
+               step of the same case on this machine's host
+
+--impl reference times the oracle (the reference's CPU algorithm) on the
+same config; the reference itself is Fortran and no Fortran compiler exists
+in the build image.
+
+Multi-GPU: the step has no data-parallel split (the SIP recurrences are
+global), so N GPUs run N independent replicas (weak scaling), launched
+with torch.distributed.run; the barrier/max use a gloo group.
+"""
+import argparse
+import json
+import os
+import pathlib
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_DEFAULT = 128
+METRIC = "PISO steps/s & p'-solve ms to 1e-6 res: FP64 plain vs FP32+learned, 1 GB300"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Group:
+    """Barrier and max-reduce across replica ranks (gloo); no-ops at N=1."""
+
+    def __init__(self, ws):
+        self.ws = ws
+        self.dist = None
+        if ws > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(n)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def make_case(n):
+    import cappgpu
+    return cappgpu.cases.channel(N=(n, n, n))
+
+
+def cpu_case_state(case):
+    """Oracle state of the case (geometry by the oracle itself)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    import cappgpu
+    oracle.build()
+    st = oracle.State.from_case(case)
+    for n in ("ar1x", "ar1y", "ar1z", "ar2x", "ar2y", "ar2z", "ar3x", "ar3y", "ar3z", "fx", "fy", "fz"):
+        case.fields[n] = st.field(n).copy()
+    for n, a in cappgpu.cases.initial_face_fluxes(case).items():
+        st.set_field(n, a)
+    return st
+
+
+def time_oracle_steps(n, steps, warmup):
+    case = make_case(n)
+    st = cpu_case_state(case)
+    for _ in range(warmup):
+        st.piso_steps(1)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st.piso_steps(1)
+    return time.perf_counter() - t0
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    steps = max(1, args.steps)
+    warm = max(0, args.warmup)
+    # each timed step is one PISO step of the same 128^3 case; warm-up steps
+    # are capped at 1 to keep the arm within a few minutes
+    warm = min(warm, 1)
+    steps = min(steps, 3)
+    t = time_oracle_steps(args.n, steps, warm)
+    v = steps / t
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": ws,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * t / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"channel {args.n}^3 PISO (2 correctors, PCG-SIP p to 1e-6)",
+                   "cells": args.n ** 3},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                         "sample": f"{steps} PISO step(s) of the {args.n}^3 channel after {warm} warm-up"},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is Fortran (no compiler in the image); its algorithm restated in C "
+                "(oracle/) and run single-threaded, as its sequential SIP recurrences run",
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_gpu(args, ws, rank, local):
+    import cappgpu
+    group = Group(ws)
+    lib = cappgpu.Library()
+    case = make_case(args.n)
+    lib.load_case(case)
+    cells = args.n ** 3
+    for _ in range(args.warmup):
+        lib.piso_steps(1)
+    clocks = ClockSampler(local)
+    launches0 = lib.stats().launches
+    group.barrier()
+    clocks.start()
+    lib.timer_start()
+    lib.piso_steps(args.steps)
+    ms = lib.timer_stop()
+    clk = clocks.stop()
+    group.barrier()
+    launches = lib.stats().launches - launches0
+    st = lib.stats()
+    ms = group.max(ms)
+    value = ws * args.steps / (ms / 1e3)
+
+    # end to end through the C ABI with host buffers
+    names = ["u", "v", "w", "p", "f1", "f2", "f3"]
+    host = {n: lib.pinned(lib.nijk) for n in names}
+    for n in names:
+        host[n][:] = lib.get_field(n)
+    e2e_steps = max(1, min(args.steps, 3))
+    group.barrier()
+    lib.timer_start()
+    for _ in range(e2e_steps):
+        for n in names:
+            lib.set_field(n, host[n])
+        lib.piso_steps(1)
+        for n in names:
+            host[n][:] = lib.get_field(n)
+    e2e_ms = group.max(lib.timer_stop())
+    lib.free_pinned()
+    nbytes = len(names) * lib.nijk * 8
+
+    # roofline of the SIP forward substitution on the current state
+    peak, peak_kind = measured_peaks()
+    ms_fwd, bytes_fwd = lib.profile_kernel(0, reps=3)
+    achieved = bytes_fwd / (ms_fwd / 1e3) / 1e9
+    units = {}
+    for w, name in ((1, "sip_backward"), (2, "spmv_dot"), (6, "sip_factor"), (3, "grad_gauss")):
+        m, b = lib.profile_kernel(w, reps=3)
+        units[name] = {"ms": m, "GBps": b / (m / 1e3) / 1e9}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"channel {args.n}^3 PISO (2 correctors, PCG-SIP p to 1e-6, FP64 plain)",
+                   "cells": cells, "parallelism": f"replicas{ws}",
+                   "l2": "working set (~80 fields x 19 MB) far larger than the 129 MB L2"},
+        "cell_updates_per_s": value * cells,
+        "p_solve_ms": st.p_solve_ms, "p_iters": st.p_report.iters,
+        "p_rel_residual": st.p_report.resl / st.p_report.res0 if st.p_report.res0 else None,
+        "e2e": {"value": ws * e2e_steps / (e2e_ms / 1e3), "unit": "steps/s",
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "roofline": {"bound": "hbm", "kernel": "SIP forward substitution (pcg-sip.f90:204-212)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes": bytes_fwd, "ms_per_launch": ms_fwd},
+        "units": units,
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        t = time_oracle_steps(args.n, 1, 0)
+        out["cpu_baseline"] = {"value": 1.0 / t, "unit": "steps/s", "cores": 1, "kind": "port",
+                               "sample": f"1 PISO step of the {args.n}^3 channel (C oracle, 1 thread)"}
+    group.close()
+    lib.finalize()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT, help="interior cells per axis")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,36 @@
+// kernels.cuh -- internal (stream-ordered, non-synchronising) entry points
+// shared between the library's translation units.
+#pragma once
+#include "common.cuh"
+
+namespace cap {
+
+int ghost_update();
+int grad_gauss(int uf, int dxf, int dyf, int dzf);
+int bpres(int pf);
+int correct_bc();
+
+// linear solvers on field fi with parameter slot ifi (1-based)
+int solve(int solver, int fi, int ifi, cappgpu_solve_report* rep);
+int sipsol(int fi, int ifi, cappgpu_solve_report* rep);
+int pcgsip(int fi, int ifi, cappgpu_solve_report* rep);
+int iccg(int fi, int ifi, cappgpu_solve_report* rep);
+int bicgstab(int fi, int ifi, bool sip, cappgpu_solve_report* rep);
+int dpcg(int fi, int ifi, cappgpu_solve_report* rep);
+
+// assembly
+int fluxuvw(int idew, int idns, int idtb, int arvx, int arvy, int arvz, int fif, int acfe, int acfw, int fcf);
+int calcuvw(cappgpu_solve_report* rep3);
+int piso_assemble(int idew, int idns, int idtb, int arvx, int arvy, int arvz, int fif, int acfe, int acfw,
+                  int fcf, int ipc, int bp);
+int assemble_pressure_eq(int idew, int idns, int idtb, int arvx, int arvy, int arvz, int fif, int acfe,
+                         int acfw, int fcf);
+int piso_gethbya();
+int piso_multiple_correction(cappgpu_solve_report* reps);
+int fluxmass(int idew, int idns, int idtb, int arvx, int arvy, int arvz, int fif, int acfe, int acfw, int fcf);
+int calcp(cappgpu_solve_report* reps);
+int outbc();
+int courant();
+int continuity_errors();
+
+}  // namespace cap

@@ -1,0 +1,310 @@
+/*
+ * cappgpu.h -- C ABI of the GB300 (sm_103a) implementation of Cappuccino's
+ * SIMPLE/PISO step on a structured single-block ghost-cell grid.
+ *
+ * Reference: kiranhegde/cappuccino-ghostcells-mpi (Fortran 90).  The
+ * reference routines communicate through Fortran module globals
+ * (modules_allocatable.f90:111-398) rather than arguments.  This ABI keeps
+ * that model: one process owns one grid on one GPU ("the context"), module
+ * arrays live on the device as named fields, and every routine of the hot
+ * path is an entry point with the reference's name and argument meaning.
+ *
+ * Conventions (identical to the reference):
+ *  - a field is a double array of length nijk = ni*nj*nk; element
+ *    ijk-1 (0-based) holds the reference's element ijk (1-based), with
+ *    ijk = lk(k)+li(i)+j, li(i)=(i-1)*nj, lk(k)=(k-1)*ni*nj (setind.f90:34-40);
+ *  - interior cells are i=3..ni-2, j=3..nj-2, k=3..nk-2; layers 2 and n-1
+ *    are ghost cells, layers 1 and n are storage padding;
+ *  - integer indices are 1-based i,j,k exactly as in the reference loops.
+ *
+ * Return codes: 0 = OK, >0 = informational (linear solver hit nsw without
+ * reaching sor, as the reference does silently), <0 = error (see
+ * CAPPGPU_E_*).  cappgpu_last_error() gives a one-line message.
+ *
+ * Threading: the library is single-threaded, not re-entrant, and uses one
+ * CUDA stream.  Every entry point is synchronous at return.
+ */
+#ifndef CAPPGPU_H
+#define CAPPGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- errors */
+#define CAPPGPU_OK               0
+#define CAPPGPU_NOT_CONVERGED    1   /* solver used nsw(ifi) sweeps          */
+#define CAPPGPU_E_NOINIT        -1   /* cappgpu_init not called              */
+#define CAPPGPU_E_ARG           -2   /* bad argument (field id, size, dims)  */
+#define CAPPGPU_E_CUDA          -3   /* CUDA runtime error                   */
+#define CAPPGPU_E_NONFINITE     -4   /* NaN/Inf in a solver residual         */
+#define CAPPGPU_E_SPIN          -5   /* wavefront spin limit exceeded        */
+#define CAPPGPU_E_DIVERGED      -6   /* main.f90:227 divergence guard        */
+#define CAPPGPU_E_NOMEM         -7   /* device allocation failed             */
+
+/* ------------------------------------------------- variable identifiers  */
+/* modules_allocatable.f90:37 (iu=1 .. icon=10); 1-based like the reference */
+#define CAP_IU   1
+#define CAP_IV   2
+#define CAP_IW   3
+#define CAP_IP   4
+#define CAP_ITE  5
+#define CAP_IED  6
+#define CAP_IEN  7
+#define CAP_IVIS 8
+#define CAP_IVART 9
+#define CAP_ICON 10
+#define CAP_NPHI 10
+
+/* ------------------------------------------------------------ field ids  */
+/* One id per reference module array that the hot path reads or writes.   */
+enum cappgpu_field {
+  /* module geometry (modules_allocatable.f90:147-159) */
+  CAP_X = 0, CAP_Y, CAP_Z, CAP_XC, CAP_YC, CAP_ZC, CAP_VOL,
+  CAP_FX, CAP_FY, CAP_FZ,
+  CAP_AR1X, CAP_AR1Y, CAP_AR1Z, CAP_AR2X, CAP_AR2Y, CAP_AR2Z,
+  CAP_AR3X, CAP_AR3Y, CAP_AR3Z, CAP_WALLDIST,
+  /* module variables (:274-296) */
+  CAP_U, CAP_V, CAP_W, CAP_P, CAP_PP, CAP_F1, CAP_F2, CAP_F3,
+  CAP_VIS, CAP_DEN, CAP_TE, CAP_ED, CAP_T, CAP_STRAIN,
+  /* module time_mod (:337-343) */
+  CAP_UO, CAP_VO, CAP_WO, CAP_UOO, CAP_VOO, CAP_WOO,
+  /* module coef (:161-170) */
+  CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP,
+  CAP_SP, CAP_SPV, CAP_SU, CAP_SV, CAP_SW, CAP_RES,
+  CAP_APU, CAP_APV, CAP_APW,
+  /* module coefb (:172-180) -- SIP factors, full extent (ghost layers are
+     read by the factorisation, sipsol.f90:34-46) */
+  CAP_BB, CAP_BS, CAP_BW, CAP_BP, CAP_BN, CAP_BE, CAP_BT,
+  /* module hcoef (:182-190) */
+  CAP_HE, CAP_HW, CAP_HN, CAP_HS, CAP_HT, CAP_HB,
+  /* module gradients (:389-398), stored as three component arrays each
+     (the reference stores (3,nxyza); component c of cell ijk is
+     gradX(c,ijk)) */
+  CAP_GRADU_X, CAP_GRADU_Y, CAP_GRADU_Z,
+  CAP_GRADV_X, CAP_GRADV_Y, CAP_GRADV_Z,
+  CAP_GRADW_X, CAP_GRADW_Y, CAP_GRADW_Z,
+  CAP_GRADP_X, CAP_GRADP_Y, CAP_GRADP_Z,
+  CAP_NFIELDS
+};
+
+/* BC code arrays (module bc, modules_allocatable.f90:215-219):
+   lbw/lbe indexed (j-1)*nk+k (length nj*nk), lbs/lbn (i-1)*nk+k (ni*nk),
+   lbb/lbt (i-1)*nj+j (ni*nj).  Codes: 1 inlet, 2 outlet, 3 symmetry,
+   4 wall (update_values_at_ghostcells_nonperiodic.f90:73,88,103,119). */
+enum cappgpu_bcface { CAP_LBW = 0, CAP_LBE, CAP_LBS, CAP_LBN, CAP_LBB, CAP_LBT, CAP_NBC };
+
+/* ------------------------------------------------------------ parameters */
+/* Scalars of modules parameters/time_mod/inlet/boundc that the hot path
+   reads or writes (modules_allocatable.f90:15-109, 324-344, 380-387).
+   Arrays indexed [ifi-1].  Logical flags are 0/1 ints. */
+typedef struct cappgpu_params {
+  double alfa;          /* SIP factor, init.f90:164 (0.92)                 */
+  double densit, viscos;
+  double timestep, btime, time;
+  double uin, vin, win, tein, edin, tin;
+  double flowin, zero;  /* zero == 0.0d0, init.f90:342                   */
+  double cappa, elog;   /* init.f90:167-168                                */
+  double gradpcmf;
+  double gravx, gravy, gravz, beta, tref;
+  double conumfixvalue, conum, meanconum;
+  double localconterr, sumlocalconterr, globalconterr, cumulativeconterr;
+  double sor[CAP_NPHI], resor[CAP_NPHI], snorin[CAP_NPHI];
+  double urf[CAP_NPHI], gds[CAP_NPHI];
+  int    nsw[CAP_NPHI];
+  int    lcal[CAP_NPHI];
+  int    ipr, jpr, kpr;             /* pressure reference cell             */
+  int    ncorr, npcor, icorr, ipcorr;
+  int    bdf, cn;
+  int    lcds, lluds, lquds, lsmart, lavl, lmuscl, lumist, lgamma, lcds4;
+  int    flux_limiter;
+  int    const_mflux, lbuoy, boussinesq, lout, ltransient, lles;
+  int    periodic;                  /* 1: update_values_at_ghostcells.f90,
+                                       0: ..._nonperiodic.f90              */
+  int    conumfix;
+  int    isol_p;                    /* calcp p' solver, calcp...f90:22 (5)  */
+  int    piso_solver;               /* PISO p solver, PISO_multiple_correction.f90:138-142 (4 = pcgsip) */
+  int    pad_;
+} cappgpu_params;
+
+/* Report of one linear solve (the reference writes these three numbers to
+   unit 66, e.g. pcg-sip.f90:301-303). */
+typedef struct cappgpu_solve_report {
+  double res0;      /* initial L1 residual                                 */
+  double resl;      /* final L1 residual                                   */
+  int    iters;     /* sweeps / iterations done (the reference's l or n)   */
+  int    status;    /* CAPPGPU_OK / CAPPGPU_NOT_CONVERGED / <0             */
+} cappgpu_solve_report;
+
+/* Solver selector values (match the reference's isol switches,
+   calcp-multiple_correction_SIMPLE.f90:98-102). */
+#define CAPPGPU_SOLVER_SIPSOL     1
+#define CAPPGPU_SOLVER_CGSTAB     2
+#define CAPPGPU_SOLVER_ICCG       3
+#define CAPPGPU_SOLVER_PCGSIP     4
+#define CAPPGPU_SOLVER_CGSTAB_SIP 5
+#define CAPPGPU_SOLVER_DPCG       6
+
+/* ======================================================= lifecycle / data */
+
+/* Create the context for an ni x nj x nk grid (storage extents, i.e.
+   interior cells + 4 per axis).  Replaces set_parameters (set_parameters.f90:22-41,
+   with nxyza := nxyz) + allocate_arrays + setind (setind.f90:21-58).
+   Every field is zero-initialised on the device. */
+int cappgpu_init(int ni, int nj, int nk);
+int cappgpu_finalize(void);
+const char* cappgpu_last_error(void);
+const char* cappgpu_field_name(int field);
+int cappgpu_field_id(const char* name);     /* -1 if unknown */
+
+/* Copy a whole field host->device / device->host (n must equal nijk). */
+int cappgpu_set_field(int field, const double* host, int64_t n);
+int cappgpu_get_field(int field, double* host, int64_t n);
+/* BC codes (read_grid.f90:136-140). */
+int cappgpu_set_bc(int face, const int* codes, int64_t n);
+/* Module scalars (read_input.f90:28-59 / init.f90:164-344). */
+int cappgpu_set_params(const cappgpu_params* p);
+int cappgpu_get_params(cappgpu_params* p);
+
+/* Address registry for the drop-in (host-pointer) entry points: associates
+   a host module array (e.g. the Fortran shim's c_loc(u)) with a field.
+   Entry points ending in _h accept host pointers; a registered pointer is
+   copied to its field before the call and back after it. */
+int cappgpu_register(int field, double* host);
+int cappgpu_unregister_all(void);
+
+/* ============================================================== geometry */
+/* Face area vectors ar1*,ar2*,ar3* and interpolation factors fx,fy,fz from
+   the nodes x,y,z and cell centres xc,yc,zc already set in the context:
+   init.f90:54-136 (face areas) and init.f90:142-144 -> intfac.f90:25-48.
+   orient = 0 keeps init.f90's cross products verbatim (on a right-handed
+   grid they point east faces to +i but north/top faces to -j/-k);
+   orient = 1 negates ar2*,ar3* so that all three point to increasing index,
+   the orientation GRAD_GAUSS.f90:57-81 and the flux routines assume. */
+int cappgpu_build_geometry(int orient);
+/* find_intersection_point.f90:1-76 evaluated on the device; p holds
+   x1,y1,z1,...,x5,y5,z5 (15 doubles), out receives xj,yj,zj. */
+int cappgpu_find_intersection_point(const double* p, double* out);
+
+/* ======================================================= index maps (a1) */
+/* setind.f90:34-40: li(i)=(i-1)*nj for i=1..ni, lk(k)=(k-1)*nij.  Writes
+   the device copies back (tests compare them element-wise). */
+int cappgpu_get_index_maps(int* li, int* lk);
+/* ijk of the pressure reference cell, setind.f90:56 */
+int cappgpu_ijkpr(void);
+
+/* ====================================================== ghost cells (a2) */
+/* update_values_at_ghostcells: nonperiodic variant
+   (update_values_at_ghostcells_nonperiodic.f90:47-640) when
+   params.periodic == 0, periodic variant (update_values_at_ghostcells.f90:40-145)
+   otherwise.  Writes ghost values of u,v,w,te,ed,t,vis. */
+int cappgpu_update_values_at_ghostcells(void);
+/* exchange(phi), exchange_mpi.f90:4-89: on one GPU there is no neighbour
+   rank, so the halo exchange is the identity on phi (the reference's
+   single-rank self-SENDRECV_REPLACE). Kept for drop-in completeness. */
+int cappgpu_exchange(int field);
+/* global_sum / global_max (global_sum_mpi.f90:4-36, global_max_mpi.f90:4-35):
+   identity on one rank; the device reductions inside the kernels replace
+   the MPI_ALLREDUCE. */
+int cappgpu_global_sum(double* phi);
+int cappgpu_global_max(double* phi);
+
+/* ========================================================= gradient (a3) */
+/* grad_gauss(u,dudx,dudy,dudz), GRAD_GAUSS.f90:1-105. */
+int cappgpu_grad_gauss(int u, int dudx, int dudy, int dudz);
+int cappgpu_grad_gauss_h(const double* u, double* dudx, double* dudy, double* dudz);
+
+/* ======================================================= linear solvers  */
+/* Each solves the 7-diagonal system ae..ab,ap,su of module coef for field
+   fi with parameters sor(ifi), nsw(ifi); writes resor(ifi), res and (SIP
+   based) the factors bb..bt, exactly as the reference routine.
+   sipsol.f90:3-106, pcg-sip.f90:3-200, iccg.f90:3-197, cgstab.f90:3-283,
+   cgstab_sip.f90:3-279, pcg-jacobi.f90:3-155. */
+int cappgpu_sipsol(int fi, int ifi, cappgpu_solve_report* rep);
+int cappgpu_pcgsip(int fi, int ifi, cappgpu_solve_report* rep);
+int cappgpu_iccg(int fi, int ifi, cappgpu_solve_report* rep);
+int cappgpu_cgstab(int fi, int ifi, cappgpu_solve_report* rep);
+int cappgpu_cgstab_sip(int fi, int ifi, cappgpu_solve_report* rep);
+int cappgpu_dpcg(int fi, int ifi, cappgpu_solve_report* rep);
+/* Host-pointer drop-ins: fi is a registered host module array. */
+int cappgpu_sipsol_h(double* fi, int ifi);
+int cappgpu_pcgsip_h(double* fi, int ifi);
+int cappgpu_iccg_h(double* fi, int ifi);
+int cappgpu_cgstab_h(double* fi, int ifi);
+int cappgpu_cgstab_sip_h(double* fi, int ifi);
+
+/* 7-point product z = A p (the pcgsip SpMV pass, pcg-sip.f90:143-155) with
+   the fused dot pk.z over the interior; exposed for tests and benches. */
+int cappgpu_spmv(int pk, int zk, double* dot);
+
+/* ================================================ assembly / PISO / SIMPLE */
+/* fluxuvw(idew,idns,idtb, arvx,arvy,arvz, fif,acfe,acfw,fcf),
+   fluxuvw-overrelaxed-correction.f90:3-659.  Field ids for the arrays. */
+int cappgpu_fluxuvw(int idew, int idns, int idtb, int arvx, int arvy, int arvz,
+                    int fif, int acfe, int acfw, int fcf);
+/* calcuvw (calcuvw.f90:3-464): gradients, sources, face fluxes, wall terms,
+   assembly and three sipsol solves.  rep may be NULL or point to 3 reports. */
+int cappgpu_calcuvw(cappgpu_solve_report* rep);
+/* piso_assemble_pressure_eq(..., ipc, bp), PISO_assemble_pressure_eq.f90:3-257 */
+int cappgpu_piso_assemble_pressure_eq(int idew, int idns, int idtb, int arvx, int arvy,
+                                      int arvz, int fif, int acfe, int acfw, int fcf,
+                                      int ipc, int bp);
+/* assemble_pressure_eq(...), assemble_pressure_eq.f90:3-124 (not in the
+   reference build; drop-in interface only). */
+int cappgpu_assemble_pressure_eq(int idew, int idns, int idtb, int arvx, int arvy,
+                                 int arvz, int fif, int acfe, int acfw, int fcf);
+/* PISO_getHbyA, PISO_getHbyA.f90:3-233 */
+int cappgpu_piso_gethbya(void);
+/* bpres(p), bpres.f90:3-81 */
+int cappgpu_bpres(int p);
+/* PISO_multiple_correction, PISO_multiple_correction.f90:3-296.  rep may be
+   NULL or point to ncorr*npcor reports (one per pressure solve). */
+int cappgpu_piso_multiple_correction(cappgpu_solve_report* rep);
+/* fluxmass(...), fluxmass2.f90:3-195 (Rhie-Chow face flux) */
+int cappgpu_fluxmass(int idew, int idns, int idtb, int arvx, int arvy, int arvz,
+                     int fif, int acfe, int acfw, int fcf);
+/* calcp (SIMPLE), calcp-multiple_correction_SIMPLE.f90:3-238 */
+int cappgpu_calcp(cappgpu_solve_report* rep);
+/* outbc, outbc.f90:3-318 */
+int cappgpu_outbc(void);
+/* correctBoundaryConditions, correctBoundaryConditions.f90:1-86 */
+int cappgpu_correct_boundary_conditions(void);
+/* CourantNo.h:10-66 (timestep may change when conumfix) */
+int cappgpu_courant(void);
+/* continuityErrors.h:55-83 */
+int cappgpu_continuity_errors(void);
+
+/* ============================================================ step drivers */
+/* One iteration of main.f90:178-207 for PISO (ghost update, calcuvw, outbc,
+   PISO_multiple_correction) preceded, when transient, by the time-level
+   shift of main.f90:140-157 and CourantNo.h.  nsteps time steps. */
+int cappgpu_piso_steps(int nsteps, cappgpu_solve_report* last_p_report);
+/* nsteps SIMPLE outer iterations (ghost update, calcuvw, calcp). */
+int cappgpu_simple_iters(int niters, cappgpu_solve_report* last_p_report);
+
+/* ======================================================= instrumentation */
+typedef struct cappgpu_stats {
+  long long launches;               /* kernels launched since cappgpu_init  */
+  double    p_solve_ms;             /* device time of the last pressure solve */
+  cappgpu_solve_report p_report;    /* its report                           */
+} cappgpu_stats;
+
+/* CUDA events on the library's stream around a region of calls. */
+int cappgpu_timer_start(void);
+int cappgpu_timer_stop(double* ms);
+int cappgpu_get_stats(cappgpu_stats* s);
+/* Page-locked host buffers (for host<->device copies at full speed). */
+int cappgpu_host_alloc(void** p, int64_t bytes);
+int cappgpu_host_free(void* p);
+/* Time reps runs of one hot-path unit (0 SIP forward sweep, 1 SIP backward
+   sweep, 2 7-point product + dot, 3 grad_gauss, 4 fluxuvw east, 5 PISO
+   pressure assembly east, 6 SIP factorisation) on the current state;
+   returns device ms per unit and its algorithmic bytes. */
+int cappgpu_profile_kernel(int which, int reps, double* ms_per_unit, double* algo_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CAPPGPU_H */

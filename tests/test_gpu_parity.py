@@ -1,0 +1,366 @@
+"""GPU-vs-oracle parity of every hot-path routine, through the C ABI.
+
+Each test fills a full state (ghost and padding cells included, so the
+reference's reads of stale ghost values are exercised), copies it to the
+GPU context, runs the routine on both sides and compares every module
+array.  Routines without reductions must agree bit for bit; where a
+deterministic device reduction replaces the reference's serial sum (solver
+norms and dot products) fields agree to 1e-10 relative L2, the plain-form
+tolerance, and iteration counts must be equal."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cappgpu
+from cappgpu import FIELD_NAMES
+from helpers import compare, diag_dominant_matrix, push, randomize, with_fluxes
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10   # plain FP64 form vs the FP64 oracle, relative L2
+IU, IV, IW, IP = 1, 2, 3, 4
+
+
+def cases_small():
+    return {
+        "cavity": lambda: cappgpu.cases.cavity(N=(8, 7, 9)),
+        "skewed": lambda: cappgpu.cases.poisson(N=(10, 9, 8)),
+        "channel": lambda: cappgpu.cases.channel(N=(8, 6, 8)),
+    }
+
+
+def state(oracle_mod, kind, orient=1):
+    case = cases_small()[kind]()
+    st = oracle_mod.State.from_case(case, geometry_orient=orient)
+    with_fluxes(case, st)
+    return case, st
+
+
+def run_both(gpu_lib, st, fn):
+    push(gpu_lib, st)
+    r_gpu = fn(gpu_lib)
+    r_ora = fn(st)
+    return r_gpu, r_ora
+
+
+# ------------------------------------------------------------------ geometry
+
+@pytest.mark.parametrize("kind", ["cavity", "skewed", "channel"])
+@pytest.mark.parametrize("orient", [0, 1])
+def test_geometry_bit_exact(gpu_lib, oracle_mod, kind, orient):
+    case = cases_small()[kind]()
+    st = oracle_mod.State.from_case(case, geometry_orient=orient)
+    gpu_lib.load_case(case, geometry_orient=orient)
+    compare(gpu_lib, st, exact=["ar1x", "ar1y", "ar1z", "ar2x", "ar2y", "ar2z", "ar3x", "ar3y", "ar3z",
+                                "fx", "fy", "fz"],
+            names=["ar1x", "ar1y", "ar1z", "ar2x", "ar2y", "ar2z", "ar3x", "ar3y", "ar3z", "fx", "fy", "fz"])
+
+
+def test_intersection_kat_on_gpu(gpu_lib):
+    from test_oracle_kat import KAT
+    gpu_lib.init(8, 8, 8)
+    for pts, expected in KAT:
+        np.testing.assert_array_equal(gpu_lib.find_intersection_point(pts), expected)
+
+
+def test_index_maps(gpu_lib):
+    ni, nj, nk = 13, 9, 7
+    gpu_lib.init(ni, nj, nk)
+    li, lk = gpu_lib.index_maps()
+    np.testing.assert_array_equal(li, (np.arange(1, ni + 1) - 1) * nj)
+    np.testing.assert_array_equal(lk, (np.arange(1, nk + 1) - 1) * ni * nj)
+    p = gpu_lib.get_params()
+    p.ipr, p.jpr, p.kpr = 4, 5, 3
+    gpu_lib.set_params(p)
+    assert gpu_lib.lib.cappgpu_ijkpr() == (3 - 1) * ni * nj + (4 - 1) * nj + 5   # setind.f90:56
+
+
+# --------------------------------------------------------------- ghost cells
+
+@pytest.mark.parametrize("periodic", [0, 1])
+def test_ghost_update_bit_exact(gpu_lib, oracle_mod, periodic):
+    case, st = state(oracle_mod, "skewed")
+    rng = np.random.default_rng(10 + periodic)
+    randomize(st, rng, ["u", "v", "w", "te", "ed", "t", "vis"], 0.1, 1.0)
+    for face in cappgpu.params.BC_NAMES:
+        st.bc(face)[:] = rng.integers(1, 5, st.bc(face).size)   # inlet/outlet/symmetry/wall mixed
+    st.params.periodic = periodic
+    st.params.update(dict(uin=0.3, vin=-0.2, win=0.1, tein=0.05, edin=0.7, tin=1.5))
+    run_both(gpu_lib, st, lambda s: s.update_values_at_ghostcells())
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+def test_exchange_and_global_reductions_are_identity(gpu_lib, oracle_mod):
+    case, st = state(oracle_mod, "cavity")
+    push(gpu_lib, st)
+    before = gpu_lib.get_field("p")
+    assert gpu_lib.lib.cappgpu_exchange(cappgpu.FIELD["p"]) == 0
+    np.testing.assert_array_equal(gpu_lib.get_field("p"), before)
+    x = ctypes.c_double(3.25)
+    assert gpu_lib.lib.cappgpu_global_sum(ctypes.byref(x)) == 0 and x.value == 3.25
+    assert gpu_lib.lib.cappgpu_global_max(ctypes.byref(x)) == 0 and x.value == 3.25
+
+
+# ------------------------------------------------------------------ gradient
+
+@pytest.mark.parametrize("kind", ["cavity", "skewed", "channel"])
+def test_grad_gauss_bit_exact(gpu_lib, oracle_mod, kind):
+    case, st = state(oracle_mod, kind)
+    randomize(st, np.random.default_rng(2), ["u", "gradu_x", "gradu_y", "gradu_z"])
+    run_both(gpu_lib, st, lambda s: s.grad_gauss("u", "gradu_x", "gradu_y", "gradu_z"))
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+def test_grad_gauss_host_pointer(gpu_lib, oracle_mod):
+    case, st = state(oracle_mod, "skewed")
+    rng = np.random.default_rng(4)
+    u = rng.uniform(-1, 1, st.nijk)
+    st.set_field("u", u)
+    push(gpu_lib, st)
+    st.grad_gauss("u", "gradu_x", "gradu_y", "gradu_z")
+    out = [np.empty(st.nijk) for _ in range(3)]
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert gpu_lib.lib.cappgpu_grad_gauss_h(dp(u), *map(dp, out)) == 0
+    for a, n in zip(out, ("gradu_x", "gradu_y", "gradu_z")):
+        np.testing.assert_array_equal(a, st.field(n))
+
+
+def test_bpres_bit_exact(gpu_lib, oracle_mod):
+    case, st = state(oracle_mod, "skewed")
+    randomize(st, np.random.default_rng(6), ["p"])
+    run_both(gpu_lib, st, lambda s: s.bpres("p"))
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+def test_correct_boundary_conditions_bit_exact(gpu_lib, oracle_mod):
+    case, st = state(oracle_mod, "cavity")
+    randomize(st, np.random.default_rng(8), ["u", "v", "w", "f1", "f2"])
+    run_both(gpu_lib, st, lambda s: s.correct_boundary_conditions())
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+# -------------------------------------------------------------------- solvers
+
+def solver_state(oracle_mod, seed, symmetric):
+    st = oracle_mod.State(14, 13, 12)
+    rng = np.random.default_rng(seed)
+    diag_dominant_matrix(st, rng, symmetric=symmetric)
+    # stale SIP factors in every cell: the factorisation reads ghost-layer
+    # values of bn, be, bt (sipsol.f90:34-46)
+    randomize(st, rng, ["bb", "bs", "bw", "bp", "bn", "be", "bt"], -0.3, 0.3)
+    randomize(st, rng, ["p", "res", "u"])
+    st.params.update(dict(alfa=0.92, sor=[1e-8] * 10, nsw=[300] * 10))
+    return st
+
+
+def test_spmv_bit_exact(gpu_lib, oracle_mod):
+    st = solver_state(oracle_mod, 1, False)
+    push(gpu_lib, st)
+    dg = gpu_lib.spmv("u", "pp")
+    do = st.spmv("u", "pp")
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+    assert abs(dg - do) <= 1e-13 * abs(do)
+
+
+@pytest.mark.parametrize("solver,symmetric", [("sipsol", False), ("pcgsip", True), ("iccg", True),
+                                              ("cgstab", False), ("cgstab_sip", False), ("dpcg", True)])
+def test_solver_parity(gpu_lib, oracle_mod, solver, symmetric):
+    st = solver_state(oracle_mod, 20, symmetric)
+    push(gpu_lib, st)
+    rg = gpu_lib.solve(solver, "p", IP)
+    ro = st.solve(solver, "p", IP)
+    assert rg.iters == ro.iters, (rg, ro)
+    assert rg.status == ro.status
+    assert abs(rg.res0 - ro.res0) <= 1e-12 * ro.res0
+    assert abs(rg.resl - ro.resl) <= 1e-6 * ro.resl + 1e-300
+    params = gpu_lib.get_params()
+    assert abs(params.resor[IP - 1] - st.params.resor[IP - 1]) <= 1e-12 * abs(st.params.resor[IP - 1])
+    sip = ["bb", "bs", "bw", "bp", "bn", "be", "bt"]
+    exact = sip if solver in ("sipsol", "pcgsip", "cgstab_sip") else []
+    if solver == "sipsol":
+        exact = exact + ["p"]   # no reduction reaches fi: bit-exact at equal sweep count
+    compare(gpu_lib, st, exact=exact, rtol=RTOL, names=["p"] + sip)
+    r = compare(gpu_lib, st, names=["res"])
+    assert r["res"][0] <= 1e-8 * np.abs(st.field("res")).max() + 1e-12
+
+
+def test_solver_nonfinite_is_reported(gpu_lib, oracle_mod):
+    st = solver_state(oracle_mod, 3, True)
+    su = st.field("su")
+    su[st.nijk // 2] = np.nan
+    push(gpu_lib, st)
+    with pytest.raises(cappgpu.CappError, match="-4"):
+        gpu_lib.solve("pcgsip", "p", IP)
+
+
+def test_solver_host_pointer_dropin(gpu_lib, oracle_mod):
+    st = solver_state(oracle_mod, 5, True)
+    push(gpu_lib, st)
+    host = {n: st.field(n).copy() for n in FIELD_NAMES}
+    for n in ("ae", "aw", "an", "as", "at", "ab", "ap", "su", "p", "res",
+              "bb", "bs", "bw", "bp", "bn", "be", "bt"):
+        assert gpu_lib.lib.cappgpu_register(cappgpu.FIELD[n], host[n].ctypes.data_as(
+            ctypes.POINTER(ctypes.c_double))) == 0
+    rc = gpu_lib.lib.cappgpu_pcgsip_h(host["p"].ctypes.data_as(ctypes.POINTER(ctypes.c_double)), IP)
+    assert rc >= 0
+    st.solve("pcgsip", "p", IP)
+    np.testing.assert_allclose(host["p"], st.field("p"), rtol=0, atol=1e-10 * np.abs(st.field("p")).max())
+    np.testing.assert_array_equal(host["bp"], st.field("bp"))
+    gpu_lib.lib.cappgpu_unregister_all()
+    with pytest.raises(AssertionError):
+        assert gpu_lib.lib.cappgpu_pcgsip_h(host["p"].ctypes.data_as(ctypes.POINTER(ctypes.c_double)), IP) == 0
+
+
+# ------------------------------------------------------------------- assembly
+
+def assembly_state(oracle_mod, kind, seed):
+    case, st = state(oracle_mod, kind)
+    rng = np.random.default_rng(seed)
+    randomize(st, rng, ["u", "v", "w", "p", "pp"])
+    randomize(st, rng, ["gradu_x", "gradu_y", "gradu_z", "gradv_x", "gradv_y", "gradv_z",
+                        "gradw_x", "gradw_y", "gradw_z", "gradp_x", "gradp_y", "gradp_z"])
+    randomize(st, rng, ["f1", "f2", "f3"], -0.5, 0.5)
+    randomize(st, rng, ["vis", "den", "apu", "apv", "apw"], 0.5, 1.5)
+    randomize(st, rng, ["su", "sv", "sw", "ae", "aw", "an", "as", "at", "ab", "ap", "sp", "spv"])
+    randomize(st, rng, ["bb", "bs", "bw", "bp", "bn", "be", "bt", "he", "hw", "hn", "hs", "ht", "hb"])
+    randomize(st, rng, ["uo", "vo", "wo", "uoo", "voo", "woo", "t"])
+    return case, st
+
+
+SCHEMES = {
+    "uds": {}, "cds": {"lcds": 1}, "cds4": {"lcds4": 1}, "luds": {"lluds": 1}, "quick": {"lquds": 1},
+    "smart": {"flux_limiter": 1, "lsmart": 1}, "avl": {"flux_limiter": 1, "lavl": 1},
+    "muscl": {"flux_limiter": 1, "lmuscl": 1}, "umist": {"flux_limiter": 1, "lumist": 1},
+    "gamma": {"flux_limiter": 1, "lgamma": 1},
+}
+
+
+def dir_args(case, d):
+    nj, nij = case.nj, case.ni * case.nj
+    return [(nj, 1, nij, "ar1x", "ar1y", "ar1z", "fx", "ae", "aw", "f1"),
+            (1, nij, nj, "ar2x", "ar2y", "ar2z", "fy", "an", "as", "f2"),
+            (nij, nj, 1, "ar3x", "ar3y", "ar3z", "fz", "at", "ab", "f3")][d]
+
+
+@pytest.mark.parametrize("scheme", list(SCHEMES))
+@pytest.mark.parametrize("d", [0, 1, 2])
+def test_fluxuvw_bit_exact(gpu_lib, oracle_mod, scheme, d):
+    case, st = assembly_state(oracle_mod, "skewed", 30 + d)
+    flags = dict(lcds=0, lcds4=0, lluds=0, lquds=0, flux_limiter=0, lsmart=0, lavl=0, lmuscl=0, lumist=0, lgamma=0)
+    flags.update(SCHEMES[scheme])
+    st.params.update(flags)
+    st.params.gds[0] = 0.9
+    a = dir_args(case, d)
+    run_both(gpu_lib, st, lambda s: s.fluxuvw(*a))
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+@pytest.mark.parametrize("ipc", [0, 1])
+@pytest.mark.parametrize("d", [0, 1, 2])
+def test_piso_assemble_bit_exact(gpu_lib, oracle_mod, ipc, d):
+    case, st = assembly_state(oracle_mod, "skewed", 40 + d)
+    a = dir_args(case, d)
+    bp = ["be", "bn", "bt"][d]
+    run_both(gpu_lib, st, lambda s: s.piso_assemble_pressure_eq(*a, ipc, bp))
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+@pytest.mark.parametrize("d", [0, 1, 2])
+def test_assemble_pressure_eq_bit_exact(gpu_lib, oracle_mod, d):
+    case, st = assembly_state(oracle_mod, "skewed", 50 + d)
+    a = dir_args(case, d)
+    run_both(gpu_lib, st, lambda s: s.assemble_pressure_eq(*a))
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+@pytest.mark.parametrize("d", [0, 1, 2])
+def test_fluxmass_bit_exact(gpu_lib, oracle_mod, d):
+    case, st = assembly_state(oracle_mod, "skewed", 60 + d)
+    a = dir_args(case, d)
+    run_both(gpu_lib, st, lambda s: s.fluxmass(*a))
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+@pytest.mark.parametrize("cn", [0, 1])
+def test_gethbya_bit_exact(gpu_lib, oracle_mod, cn):
+    case, st = assembly_state(oracle_mod, "skewed", 70)
+    st.params.update(dict(bdf=1, btime=1.0, cn=cn, timestep=0.01))
+    run_both(gpu_lib, st, lambda s: s.piso_gethbya())
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+# ---------------------------------------------------------- composite routines
+
+@pytest.mark.parametrize("kind", ["cavity", "channel"])
+def test_calcuvw_parity(gpu_lib, oracle_mod, kind):
+    case, st = state(oracle_mod, kind)
+    st.update_values_at_ghostcells()
+    if kind == "channel":
+        st.params.update(dict(timestep=0.05))
+    rg, ro = run_both(gpu_lib, st, lambda s: s.calcuvw())
+    for a, b in zip(rg, ro):
+        assert a.iters == b.iters, (rg, ro)
+    compare(gpu_lib, st, rtol=RTOL)
+
+
+def test_piso_multiple_correction_parity(gpu_lib, oracle_mod):
+    case, st = state(oracle_mod, "channel")
+    st.params.update(dict(timestep=0.05))
+    st.update_values_at_ghostcells()
+    st.calcuvw()
+    rg, ro = run_both(gpu_lib, st, lambda s: s.piso_multiple_correction())
+    for a, b in zip(rg[:2], ro[:2]):
+        assert a.iters == b.iters, (a, b)
+    compare(gpu_lib, st, rtol=RTOL, names=["u", "v", "w", "p", "pp", "f1", "f2", "f3", "su", "ap",
+                                           "gradp_x", "gradp_y", "gradp_z", "be", "bn", "bt"])
+    P = gpu_lib.get_params()
+    assert abs(P.sumlocalconterr - st.params.sumlocalconterr) <= 1e-9 * abs(st.params.sumlocalconterr)
+
+
+@pytest.mark.parametrize("npcor", [1, 2])
+def test_calcp_parity(gpu_lib, oracle_mod, npcor):
+    case, st = state(oracle_mod, "cavity")
+    st.params.update(dict(npcor=npcor))
+    st.update_values_at_ghostcells()
+    st.calcuvw()
+    run_both(gpu_lib, st, lambda s: s.calcp())
+    compare(gpu_lib, st, rtol=RTOL, names=["u", "v", "w", "p", "pp", "f1", "f2", "f3", "gradp_x",
+                                           "gradp_y", "gradp_z"])
+
+
+def test_courant_and_continuity(gpu_lib, oracle_mod):
+    case, st = assembly_state(oracle_mod, "channel", 80)
+    st.params.update(dict(ltransient=1, conumfix=1, conumfixvalue=0.5, timestep=0.01))
+    run_both(gpu_lib, st, lambda s: (s.courant(), s.continuity_errors()))
+    P = gpu_lib.get_params()
+    for n in ("timestep", "conum", "meanconum", "time", "globalconterr", "sumlocalconterr"):
+        a, b = getattr(P, n), getattr(st.params, n)
+        assert abs(a - b) <= 1e-12 * max(abs(b), 1e-300), (n, a, b)
+    assert P.localconterr == st.params.localconterr
+    compare(gpu_lib, st, exact=["su"], names=["su"])
+
+
+# -------------------------------------------------------------- step drivers
+
+def test_piso_steps_parity(gpu_lib, oracle_mod):
+    case, st = state(oracle_mod, "channel")
+    rg, ro = run_both(gpu_lib, st, lambda s: s.piso_steps(3))
+    assert rg.iters == ro.iters
+    compare(gpu_lib, st, rtol=RTOL, names=["u", "v", "w", "p", "f1", "f2", "f3", "uo", "vo", "wo"])
+    P = gpu_lib.get_params()
+    assert abs(P.timestep - st.params.timestep) <= 1e-12 * st.params.timestep
+
+
+def test_simple_iters_parity(gpu_lib, oracle_mod):
+    case, st = state(oracle_mod, "cavity")
+    rg, ro = run_both(gpu_lib, st, lambda s: s.simple_iters(3))
+    compare(gpu_lib, st, rtol=RTOL, names=["u", "v", "w", "p", "f1", "f2", "f3"])
+
+
+def test_top_wall_index_guard(gpu_lib, oracle_mod):
+    """calcuvw.f90:254 addresses the top wall with lk(nimm); a grid with
+    ni > nk would put it outside the array: refused, not run."""
+    gpu_lib.init(14, 8, 8)
+    with pytest.raises(cappgpu.CappError):
+        gpu_lib.piso_steps(1)
