@@ -75,6 +75,7 @@ struct Ctx {
   double p_solve_ms = 0.0;             // last PISO/SIMPLE pressure solve
   cappgpu_solve_report p_rep{};        // its report
   cudaEvent_t ev[4] = {};
+  int wave_impl = 1;                   // 1 persistent wavefront, 0 one launch per hyperplane
 };
 
 Ctx& ctx();

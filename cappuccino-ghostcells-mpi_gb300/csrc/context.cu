@@ -8,6 +8,7 @@
 #include <string>
 
 #include "common.cuh"
+#include "kernels.cuh"
 
 namespace cap {
 
@@ -72,6 +73,7 @@ static const char* kFieldNames[CAP_NFIELDS] = {
     "gradw_x", "gradw_y", "gradw_z", "gradp_x", "gradp_y", "gradp_z"};
 
 static void free_all() {
+  fast_free();
   Ctx& c = ctx();
   for (auto& p : c.f) { if (p) cudaFree(p); p = nullptr; }
   for (auto& p : c.bc) { if (p) cudaFree(p); p = nullptr; }
@@ -253,6 +255,16 @@ int cappgpu_get_index_maps(int* li, int* lk) {
   CAP_CUDA(cudaMemcpy(li, c.li + 1, sizeof(int) * c.d.ni, cudaMemcpyDeviceToHost));
   CAP_CUDA(cudaMemcpy(lk, c.lk + 1, sizeof(int) * c.d.nk, cudaMemcpyDeviceToHost));
   return CAPPGPU_OK;
+}
+
+// Run-time options: "wave" = 1 (persistent hyperplane wavefront, default)
+// or 0 (one kernel launch per hyperplane, the simple form kept for checks).
+int cappgpu_set_option(const char* key, int value) {
+  CAP_REQUIRE_INIT();
+  if (!key) return CAPPGPU_E_ARG;
+  if (strcmp(key, "wave") == 0 && (value == 0 || value == 1)) { ctx().wave_impl = value; return CAPPGPU_OK; }
+  set_error("unknown option %s=%d", key, value);
+  return CAPPGPU_E_ARG;
 }
 
 int cappgpu_ijkpr(void) {

@@ -17,6 +17,9 @@ int pcgsip(int fi, int ifi, cappgpu_solve_report* rep);
 int iccg(int fi, int ifi, cappgpu_solve_report* rep);
 int bicgstab(int fi, int ifi, bool sip, cappgpu_solve_report* rep);
 int dpcg(int fi, int ifi, cappgpu_solve_report* rep);
+int pcgsip_fast(int fi, int ifi, cappgpu_solve_report* rep);
+int fast_profile_unit(int which, double* bytes);
+void fast_free();
 
 // assembly
 int fluxuvw(int idew, int idns, int idtb, int arvx, int arvy, int arvz, int fif, int acfe, int acfw, int fcf);

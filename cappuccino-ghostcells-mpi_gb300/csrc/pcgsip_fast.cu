@@ -1,0 +1,356 @@
+// pcgsip_fast.cu -- pcgsip (pcg-sip.f90:3-200) with the SIP factorisation
+// and both substitutions as persistent wavefronts (wave.cuh) and every
+// per-iteration vector in the hyperplane layout (dlayout.cuh).
+//
+// Arithmetic per cell is the reference's; the scalars alpha, beta and the
+// norms come from deterministic device reductions and stay on the device
+// (the host reads one residual norm per iteration for the convergence
+// test, as the reference evaluates rsm < resmax).
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "dlayout.cuh"
+#include "kernels.cuh"
+#include "wave.cuh"
+
+namespace cap {
+
+namespace {
+
+constexpr int BA = 16, BC = 8;   // lines per wavefront block (a x c)
+
+enum DBuf { D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_RES, D_FI, D_Z, D_ZZ, D_PK0, D_PK1, D_NBUF };
+
+struct Fast {
+  Dims dims{};
+  bool ready = false;
+  DG g{};
+  double* d[D_NBUF] = {};
+  F4* f4 = nullptr;
+  B4* b4 = nullptr;
+  int nBA = 0, nBC = 0, nblk = 0;
+  int2* order = nullptr;
+  unsigned long long* prog = nullptr;
+  unsigned* ticket = nullptr;
+  unsigned ticket_base = 0;
+  unsigned epoch = 0;
+  int* flags = nullptr;       // [0] abort, [1] err
+  double* wpart = nullptr;    // per-block partials of the wavefront
+  double* hres = nullptr;     // pinned host copy of the residual norm
+};
+
+Fast F;
+
+void fast_release() {
+  for (auto& p : F.d) { if (p) cudaFree(p); p = nullptr; }
+  if (F.f4) cudaFree(F.f4);
+  if (F.b4) cudaFree(F.b4);
+  if (F.order) cudaFree(F.order);
+  if (F.prog) cudaFree(F.prog);
+  if (F.ticket) cudaFree(F.ticket);
+  if (F.flags) cudaFree(F.flags);
+  if (F.wpart) cudaFree(F.wpart);
+  if (F.hres) cudaFreeHost(F.hres);
+  F = Fast();
+}
+
+int fast_setup() {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  if (F.ready && memcmp(&F.dims, &d, sizeof(Dims)) == 0) return CAPPGPU_OK;
+  fast_release();
+  F.dims = d;
+  F.g = make_dg(d);
+  size_t n = (size_t)F.g.size();
+  for (int q = 0; q < D_NBUF; ++q) {
+    if (cudaMalloc(&F.d[q], n * sizeof(double)) != cudaSuccess) { fast_release(); set_error("out of device memory"); return CAPPGPU_E_NOMEM; }
+    CAP_CUDA(cudaMemsetAsync(F.d[q], 0, n * sizeof(double), c.st));
+  }
+  CAP_CUDA(cudaMalloc(&F.f4, n * sizeof(F4)));
+  CAP_CUDA(cudaMalloc(&F.b4, n * sizeof(B4)));
+  CAP_CUDA(cudaMemsetAsync(F.f4, 0, n * sizeof(F4), c.st));
+  CAP_CUDA(cudaMemsetAsync(F.b4, 0, n * sizeof(B4), c.st));
+  F.nBA = (F.g.Ni + BA - 1) / BA;
+  F.nBC = (F.g.Nk + BC - 1) / BC;
+  F.nblk = F.nBA * F.nBC;
+  // topological order: by diagonal ba+bc
+  std::vector<int2> ord;
+  ord.reserve(F.nblk);
+  for (int dsum = 0; dsum <= F.nBA + F.nBC - 2; ++dsum)
+    for (int bc = 0; bc < F.nBC; ++bc) {
+      int ba = dsum - bc;
+      if (ba >= 0 && ba < F.nBA) ord.push_back(make_int2(ba, bc));
+    }
+  CAP_CUDA(cudaMalloc(&F.order, sizeof(int2) * F.nblk));
+  CAP_CUDA(cudaMemcpy(F.order, ord.data(), sizeof(int2) * F.nblk, cudaMemcpyHostToDevice));
+  CAP_CUDA(cudaMalloc(&F.prog, sizeof(unsigned long long) * F.nblk));
+  CAP_CUDA(cudaMemset(F.prog, 0, sizeof(unsigned long long) * F.nblk));
+  CAP_CUDA(cudaMalloc(&F.ticket, sizeof(unsigned)));
+  CAP_CUDA(cudaMemset(F.ticket, 0, sizeof(unsigned)));
+  CAP_CUDA(cudaMalloc(&F.flags, sizeof(int) * 2));
+  CAP_CUDA(cudaMemset(F.flags, 0, sizeof(int) * 2));
+  CAP_CUDA(cudaMalloc(&F.wpart, sizeof(double) * F.nblk));
+  CAP_CUDA(cudaMallocHost(&F.hres, sizeof(double) * 4));
+  F.ticket_base = 0;
+  F.epoch = 0;
+  CAP_CUDA(cudaStreamSynchronize(c.st));
+  F.ready = true;
+  return CAPPGPU_OK;
+}
+
+WaveCtl next_ctl() {
+  WaveCtl w;
+  w.ticket = F.ticket;
+  w.ticket_base = F.ticket_base;
+  w.order = F.order;
+  w.prog = F.prog;
+  ++F.epoch;
+  w.tag = (unsigned long long)F.epoch << 32;
+  w.nBA = F.nBA;
+  w.nBC = F.nBC;
+  w.nblk = F.nblk;
+  w.abort = F.flags;
+  w.err = F.flags + 1;
+  w.partials = F.wpart;
+  w.spin_limit = 1LL << 22;
+  w.publish_every = 2;
+  F.ticket_base += (unsigned)F.nblk;
+  return w;
+}
+
+template <class Op, bool BWD>
+int run_wave(const Op& op) {
+  Ctx& c = ctx();
+  WaveCtl w = next_ctl();
+  launch(k_wave<Op, BA, BC, BWD>, F.nblk, BA * BC, c.st, op, F.g, w);
+  CAP_CHECK_LAUNCH();
+  return CAPPGPU_OK;
+}
+
+// ------------------------------------------------------ vector kernels (D)
+#define D_LOOP(g)                                                                                  \
+  for (long long t_ = blockIdx.x * (long long)blockDim.x + threadIdx.x, n_ = (g).size(); t_ < n_;   \
+       t_ += (long long)gridDim.x * blockDim.x)
+
+__device__ inline bool d_cell(const DG& g, long long t, int& a, int& b, int& c) {
+  long long row = t / g.Ni;
+  a = (int)(t - row * g.Ni);
+  int s = (int)(row / g.Nk);
+  c = (int)(row - (long long)s * g.Nk);
+  b = s - a - c;
+  return b >= 0 && b < g.Nj;
+}
+
+// pk_new = zk + bet pk_old (pcg-sip.f90:241) at the cell and its six
+// neighbours (pk is zero outside the interior); zz = A pk_new
+// (pcg-sip.f90:253-255); partial sum pk_new . zz.
+__global__ void k_pk_spmv_d(DG g, const double* __restrict__ ae, const double* __restrict__ aw,
+                            const double* __restrict__ an, const double* __restrict__ as,
+                            const double* __restrict__ at, const double* __restrict__ ab,
+                            const double* __restrict__ ap, const double* __restrict__ zk,
+                            const double* __restrict__ pko, double* __restrict__ pkn, double* __restrict__ zz,
+                            const double* __restrict__ scal, double* part) {
+  const double bet = scal[4];
+  double v[1] = {0.0};
+  D_LOOP(g) {
+    int a, b, c;
+    if (!d_cell(g, t_, a, b, c)) continue;
+    const long long P = t_;
+    auto pnew = [&](long long q) { return zk[q] + bet * pko[q]; };
+    const double pP = pnew(P);
+    const double pE = a + 1 < g.Ni ? pnew(P + g.plane + 1) : 0.0;
+    const double pW = a > 0 ? pnew(P - g.plane - 1) : 0.0;
+    const double pN = b + 1 < g.Nj ? pnew(P + g.plane) : 0.0;
+    const double pS = b > 0 ? pnew(P - g.plane) : 0.0;
+    const double pT = c + 1 < g.Nk ? pnew(P + g.plane + g.Ni) : 0.0;
+    const double pB = c > 0 ? pnew(P - g.plane - g.Ni) : 0.0;
+    const double r = ap[P] * pP - ae[P] * pE - aw[P] * pW - an[P] * pN - as[P] * pS - at[P] * pT - ab[P] * pB;
+    pkn[P] = pP;
+    zz[P] = r;
+    v[0] += pP * r;
+  }
+  block_reduce_store<1>(v, part);
+}
+
+// fi += alf pk; res -= alf zz; partial sum |res| (pcg-sip.f90:268-281)
+__global__ void k_update_d(DG g, double* __restrict__ fi, double* __restrict__ res, const double* __restrict__ pk,
+                           const double* __restrict__ zz, const double* __restrict__ scal, double* part) {
+  const double alf = scal[3];
+  double v[1] = {0.0};
+  D_LOOP(g) {
+    int a, b, c;
+    if (!d_cell(g, t_, a, b, c)) continue;
+    fi[t_] = fi[t_] + alf * pk[t_];
+    const double r = res[t_] - alf * zz[t_];
+    res[t_] = r;
+    v[0] += fabs(r);
+  }
+  block_reduce_store<1>(v, part);
+}
+
+// scalar steps of the CG iteration; one warp, fixed summation order
+// mode 0: sk = sum(wave partials); bet = sk/s0      (pcg-sip.f90:229-233)
+// mode 1: pkapk = sum(partials); alf = sk/pkapk       (pcg-sip.f90:261-263)
+// mode 2: resl = sum(partials); s0 = sk               (pcg-sip.f90:283-287)
+__global__ void k_cg_scalars(int mode, const double* part, int n, double* scal) {
+  const int lane = threadIdx.x;
+  double s = 0.0;
+  for (int b = lane; b < n; b += 32) s += part[b];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    if (mode == 0) { scal[1] = s; scal[4] = s / scal[0]; }
+    else if (mode == 1) { scal[2] = s; scal[3] = scal[1] / s; }
+    else { scal[5] = s; scal[0] = scal[1]; }
+  }
+}
+
+__global__ void k_set_scal(double* scal, double v0) { scal[0] = v0; }
+
+}  // namespace
+
+void fast_free() { fast_release(); }
+
+static int check_wave_error() {
+  int h[2];
+  CAP_CUDA(cudaMemcpy(h, F.flags, sizeof(h), cudaMemcpyDeviceToHost));
+  if (h[1] != 0) {
+    cudaMemset(F.flags, 0, sizeof(int) * 2);
+    cudaMemset(F.ticket, 0, sizeof(unsigned));
+    cudaMemset(F.prog, 0, sizeof(unsigned long long) * F.nblk);
+    F.ticket_base = 0;
+    F.epoch = 0;
+    set_error(h[1] == 1 ? "wavefront: a block waited beyond the spin limit for its predecessor"
+                        : "wavefront: block ticket out of range");
+    return CAPPGPU_E_SPIN;
+  }
+  return CAPPGPU_OK;
+}
+
+// SIP factorisation as a persistent wavefront (coefficients already in the
+// hyperplane layout); writes coefb in the natural layout and the packed
+// factors in the hyperplane layout.
+static int factor_wave() {
+  Ctx& c = ctx();
+  double** Fd = c.f;
+  SipFactorD op{F.d[D_AE], F.d[D_AW], F.d[D_AN], F.d[D_AS], F.d[D_AT], F.d[D_AB], F.d[D_AP],
+                Fd[CAP_BB], Fd[CAP_BW], Fd[CAP_BS], Fd[CAP_BP], Fd[CAP_BN], Fd[CAP_BE], Fd[CAP_BT],
+                F.f4, F.b4, c.prm.alfa};
+  return run_wave<SipFactorD, false>(op);
+}
+
+static int to_d(int field, int dbuf) {
+  Ctx& c = ctx();
+  launch(k_nat_to_d<double>, grid_for((long long)F.g.Ni * F.g.Nj * F.g.Nk), kThreads, c.st, F.g,
+         (const double*)c.f[field], F.d[dbuf]);
+  CAP_CHECK_LAUNCH();
+  return CAPPGPU_OK;
+}
+
+static int from_d(int dbuf, int field) {
+  Ctx& c = ctx();
+  launch(k_d_to_nat<double>, grid_for((long long)F.g.Ni * F.g.Nj * F.g.Nk), kThreads, c.st, F.g,
+         (const double*)F.d[dbuf], c.f[field]);
+  CAP_CHECK_LAUNCH();
+  return CAPPGPU_OK;
+}
+
+// resid kernel of solvers.cu (natural layout, interior box)
+int resid_natural(int fif, double* res0);
+
+int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  cappgpu_params& P = c.prm;
+  int rc = fast_setup();
+  if (rc) return rc;
+  CAP_CUDA(cudaMemsetAsync(F.flags, 0, sizeof(int) * 2, c.st));
+  const double resmax = P.sor[ifi - 1];
+  // res = 0 (pcg-sip.f90:150), then the initial residual and its L1 norm
+  CAP_CUDA(cudaMemsetAsync(c.f[CAP_RES], 0, sizeof(double) * d.nijk, c.st));
+  double res0 = 0.0;
+  if ((rc = resid_natural(fif, &res0))) return rc;
+  // hyperplane copies of the matrix, residual and solution
+  const int cf[7] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP};
+  for (int q = 0; q < 7; ++q)
+    if ((rc = to_d(cf[q], D_AE + q))) return rc;
+  if ((rc = to_d(CAP_RES, D_RES))) return rc;
+  if ((rc = to_d(fif, D_FI))) return rc;
+  const size_t nb = sizeof(double) * (size_t)F.g.size();
+  CAP_CUDA(cudaMemsetAsync(F.d[D_PK0], 0, nb, c.st));   // pk = 0 (pcg-sip.f90:148)
+  CAP_CUDA(cudaMemsetAsync(F.d[D_Z], 0, nb, c.st));     // zk = 0 (pcg-sip.f90:149)
+  if ((rc = factor_wave())) return rc;
+  launch(k_set_scal, 1, 1, c.st, c.dscal, (double)1.e20f);   // s0 = 1.e20 (default real)
+  SipFwdD fwd{F.d[D_RES], F.f4, F.d[D_Z], nullptr};
+  SipBwdD bwd{F.b4, F.d[D_Z], F.d[D_RES], nullptr};
+  int ns = P.nsw[ifi - 1], l;
+  double resl = 0.0, rsm;
+  bool done = false;
+  int cur = 0;
+  for (l = 1; l <= ns; ++l) {
+    if ((rc = run_wave<SipFwdD, false>(fwd))) return rc;
+    if ((rc = run_wave<SipBwdD, true>(bwd))) return rc;
+    launch(k_cg_scalars, 1, 32, c.st, 0, (const double*)F.wpart, F.nblk, c.dscal);
+    double* pko = F.d[cur ? D_PK1 : D_PK0];
+    double* pkn = F.d[cur ? D_PK0 : D_PK1];
+    launch(k_pk_spmv_d, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
+           (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
+           (const double*)F.d[D_AP], (const double*)F.d[D_Z], (const double*)pko, pkn, F.d[D_ZZ],
+           (const double*)c.dscal, c.partials);
+    launch(k_cg_scalars, 1, 32, c.st, 1, (const double*)c.partials, kRedBlocks, c.dscal);
+    launch(k_update_d, kRedBlocks, kThreads, c.st, F.g, F.d[D_FI], F.d[D_RES], (const double*)pkn,
+           (const double*)F.d[D_ZZ], (const double*)c.dscal, c.partials);
+    launch(k_cg_scalars, 1, 32, c.st, 2, (const double*)c.partials, kRedBlocks, c.dscal);
+    CAP_CHECK_LAUNCH();
+    cur ^= 1;
+    CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 5, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    CAP_CUDA(cudaStreamSynchronize(c.st));
+    if ((rc = check_wave_error())) return rc;
+    resl = F.hres[0];
+    if (l == 1) P.resor[ifi - 1] = res0;
+    rsm = resl / (P.resor[ifi - 1] + CAP_SMALL);
+    if (!isfinite(resl)) break;
+    if (rsm < resmax) { done = true; break; }
+  }
+  if ((rc = from_d(D_FI, fif))) return rc;
+  if ((rc = from_d(D_RES, CAP_RES))) return rc;
+  if (rep) {
+    rep->res0 = res0;
+    rep->resl = resl;
+    rep->iters = done ? l : ns;
+    rep->status = done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+  }
+  if (!isfinite(resl)) {
+    set_error("linear solver residual is not finite");
+    if (rep) rep->status = CAPPGPU_E_NONFINITE;
+    return CAPPGPU_E_NONFINITE;
+  }
+  return done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+}
+
+// Unit timing for the persistent sweeps (cappgpu_profile_kernel): state
+// must have been set up by a previous fast solve.
+int fast_profile_unit(int which, double* bytes) {
+  if (!F.ready) {
+    int rc = fast_setup();
+    if (rc) return rc;
+  }
+  double cells = (double)F.g.Ni * F.g.Nj * F.g.Nk;
+  if (which == 0) {
+    SipFwdD fwd{F.d[D_RES], F.f4, F.d[D_Z], nullptr};
+    *bytes = 6.0 * 8.0 * cells;   // r + 4 factors read, z written
+    return run_wave<SipFwdD, false>(fwd);
+  }
+  if (which == 1) {
+    SipBwdD bwd{F.b4, F.d[D_Z], F.d[D_RES], nullptr};
+    *bytes = 6.0 * 8.0 * cells;   // z + 3 factors + res read, z written
+    return run_wave<SipBwdD, true>(bwd);
+  }
+  *bytes = 21.0 * 8.0 * cells;    // 7 coefficients read, 7 factors natural + 7 hyperplane written
+  return factor_wave();
+}
+
+}  // namespace cap

@@ -211,8 +211,18 @@ int sipsol(int fif, int ifi, cappgpu_solve_report* rep) {
 
 // ------------------------------------------------------------------ PCGSIP
 // pcg-sip.f90:3-200
+int resid_natural(int fif, double* res0) {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  Box b{3, d.nimm, 3, d.njmm, 3, d.nkmm};
+  launch(k_resid, kRedBlocks, kThreads, c.st, d, b, coef(), (const double*)c.f[fif], c.f[CAP_RES], c.partials);
+  CAP_CHECK_LAUNCH();
+  return reduce_fetch(1, res0);
+}
+
 int pcgsip(int fif, int ifi, cappgpu_solve_report* rep) {
   Ctx& c = ctx();
+  if (c.wave_impl == 1 && c.d.nimm >= 4 && c.d.njmm >= 4 && c.d.nkmm >= 4) return pcgsip_fast(fif, ifi, rep);
   const Dims& d = c.d;
   double** F = c.f;
   cappgpu_params& P = c.prm;
@@ -557,6 +567,7 @@ int profile_unit(int which, double* bytes) {
   double cells = (double)b.count();
   double* zk = c.work[1];
   double* pk = c.work[0];
+  if (c.wave_impl == 1 && (which == 0 || which == 1 || which == 6)) return fast_profile_unit(which, bytes);
   switch (which) {
     case 0: {
       SipFwdOp fwd{F[CAP_RES], F[CAP_BB], F[CAP_BW], F[CAP_BS], F[CAP_BP], zk, d.nj, d.nij};

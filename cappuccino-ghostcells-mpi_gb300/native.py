@@ -78,6 +78,7 @@ SIGNATURES = {
     "cappgpu_host_alloc": [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int64],
     "cappgpu_host_free": [ctypes.c_void_p],
     "cappgpu_profile_kernel": [_INT, _INT, _DP, _DP],
+    "cappgpu_set_option": [ctypes.c_char_p, _INT],
 }
 RESTYPES = {"cappgpu_last_error": ctypes.c_char_p, "cappgpu_field_name": ctypes.c_char_p}
 
@@ -194,6 +195,9 @@ class Library:
                 if name in ("f1", "f2", "f3") or name not in before:
                     self.set_field(name, case.fields[name])
         return self
+
+    def set_option(self, key, value):
+        self._check(self.lib.cappgpu_set_option(key.encode(), int(value)), f"set_option({key})")
 
     def index_maps(self):
         ni, nj, nk = self.dims

@@ -188,6 +188,11 @@ int cappgpu_build_geometry(int orient);
    x1,y1,z1,...,x5,y5,z5 (15 doubles), out receives xj,yj,zj. */
 int cappgpu_find_intersection_point(const double* p, double* out);
 
+/* Run-time options.  "wave": 1 = SIP factorisation/substitutions of pcgsip
+   as persistent hyperplane wavefronts (default), 0 = one kernel launch per
+   hyperplane (the simple form, kept for cross-checks). */
+int cappgpu_set_option(const char* key, int value);
+
 /* ======================================================= index maps (a1) */
 /* setind.f90:34-40: li(i)=(i-1)*nj for i=1..ni, lk(k)=(k-1)*nij.  Writes
    the device copies back (tests compare them element-wise). */

@@ -46,6 +46,7 @@ cap_state* cap_new(int ni, int nj, int nk) {
   s->prm.densit = 1.0;
   s->prm.isol_p = CAPPGPU_SOLVER_CGSTAB_SIP;
   s->prm.piso_solver = CAPPGPU_SOLVER_PCGSIP;
+  s->prm.ipr = s->prm.jpr = s->prm.kpr = 3;
   return s;
 }
 

@@ -150,7 +150,7 @@ def solver_state(oracle_mod, seed, symmetric):
     # values of bn, be, bt (sipsol.f90:34-46)
     randomize(st, rng, ["bb", "bs", "bw", "bp", "bn", "be", "bt"], -0.3, 0.3)
     randomize(st, rng, ["p", "res", "u"])
-    st.params.update(dict(alfa=0.92, sor=[1e-8] * 10, nsw=[300] * 10))
+    st.params.update(dict(alfa=0.92, sor=[1e-8] * 10, nsw=[300] * 10, ipr=3, jpr=3, kpr=3))
     return st
 
 
@@ -188,7 +188,8 @@ def test_solver_parity(gpu_lib, oracle_mod, solver, symmetric):
 def test_solver_nonfinite_is_reported(gpu_lib, oracle_mod):
     st = solver_state(oracle_mod, 3, True)
     su = st.field("su")
-    su[st.nijk // 2] = np.nan
+    ni, nj, nk = st.dims
+    su[(nk // 2 - 1) * ni * nj + (ni // 2 - 1) * nj + nj // 2 - 1] = np.nan   # an interior cell
     push(gpu_lib, st)
     with pytest.raises(cappgpu.CappError, match="-4"):
         gpu_lib.solve("pcgsip", "p", IP)
@@ -364,3 +365,46 @@ def test_top_wall_index_guard(gpu_lib, oracle_mod):
     gpu_lib.init(14, 8, 8)
     with pytest.raises(cappgpu.CappError):
         gpu_lib.piso_steps(1)
+
+
+# ------------------------------------------------ persistent wavefront path
+
+@pytest.mark.parametrize("shape", [(40, 12, 30), (37, 21, 19), (5, 3, 70)])
+@pytest.mark.parametrize("wave", [1, 0])
+def test_pcgsip_wavefront_multiblock(gpu_lib, oracle_mod, shape, wave):
+    """pcgsip with the persistent wavefront over many line blocks (and with
+    one launch per hyperplane) against the oracle: SIP factors bit-exact,
+    solution within the plain-form tolerance, same iteration count."""
+    st = oracle_mod.State(*[n + 4 for n in shape])
+    rng = np.random.default_rng(sum(shape))
+    diag_dominant_matrix(st, rng, symmetric=True)
+    randomize(st, rng, ["bb", "bs", "bw", "bp", "bn", "be", "bt"], -0.3, 0.3)
+    randomize(st, rng, ["p", "res"])
+    st.params.update(dict(alfa=0.92, sor=[1e-9] * 10, nsw=[400] * 10, ipr=3, jpr=3, kpr=3))
+    push(gpu_lib, st)
+    gpu_lib.set_option("wave", wave)
+    try:
+        rg = gpu_lib.solve("pcgsip", "p", IP)
+    finally:
+        gpu_lib.set_option("wave", 1)
+    ro = st.solve("pcgsip", "p", IP)
+    assert rg.iters == ro.iters, (rg, ro)
+    compare(gpu_lib, st, exact=["bb", "bs", "bw", "bp", "bn", "be", "bt"], rtol=RTOL,
+            names=["p", "bb", "bs", "bw", "bp", "bn", "be", "bt"])
+    r = compare(gpu_lib, st, names=["res"])
+    assert r["res"][0] <= 1e-8 * np.abs(st.field("res")).max() + 1e-12
+
+
+def test_pcgsip_wavefront_repeated_calls_are_deterministic(gpu_lib, oracle_mod):
+    st = oracle_mod.State(44, 16, 36)
+    rng = np.random.default_rng(9)
+    diag_dominant_matrix(st, rng, symmetric=True)
+    st.params.update(dict(alfa=0.92, sor=[1e-9] * 10, nsw=[400] * 10, ipr=3, jpr=3, kpr=3))
+    push(gpu_lib, st)
+    outs = []
+    for _ in range(3):
+        gpu_lib.set_field("p", st.field("p"))
+        gpu_lib.solve("pcgsip", "p", IP)
+        outs.append(gpu_lib.get_field("p"))
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
