@@ -1,6 +1,7 @@
-// pcgsip_fast.cu -- pcgsip (pcg-sip.f90:3-200) with the SIP factorisation
-// and both substitutions as persistent wavefronts (wave.cuh) and every
-// per-iteration vector in the hyperplane layout (dlayout.cuh).
+// sip_fast.cu -- pcgsip (pcg-sip.f90:3-200) and sipsol (sipsol.f90:3-106)
+// with the SIP factorisation and both substitutions as persistent
+// wavefronts (wave.cuh) and every per-iteration vector in the hyperplane
+// layout (dlayout.cuh).
 //
 // Arithmetic per cell is the reference's; the scalars alpha, beta and the
 // norms come from deterministic device reductions and stay on the device
@@ -22,7 +23,7 @@ namespace {
 
 constexpr int BA = 16, BC = 8;   // lines per wavefront block (a x c)
 
-enum DBuf { D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_RES, D_FI, D_Z, D_ZZ, D_PK0, D_PK1, D_NBUF };
+enum DBuf { D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_SU, D_RES, D_FI, D_Z, D_ZZ, D_PK0, D_PK1, D_NBUF };
 
 struct Fast {
   Dims dims{};
@@ -125,7 +126,7 @@ template <class Op, bool BWD>
 int run_wave(const Op& op) {
   Ctx& c = ctx();
   WaveCtl w = next_ctl();
-  launch(k_wave<Op, BA, BC, BWD>, F.nblk, BA * BC, c.st, op, F.g, w);
+  launch(k_wave<Op, BA, BC, BWD>, F.nblk, BA * BC + 32, c.st, op, F.g, w);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
 }
@@ -195,6 +196,7 @@ __global__ void k_update_d(DG g, double* __restrict__ fi, double* __restrict__ r
 // mode 0: sk = sum(wave partials); bet = sk/s0      (pcg-sip.f90:229-233)
 // mode 1: pkapk = sum(partials); alf = sk/pkapk       (pcg-sip.f90:261-263)
 // mode 2: resl = sum(partials); s0 = sk               (pcg-sip.f90:283-287)
+// mode 3: res1 = sum(partials)                       (sipsol.f90:69)
 __global__ void k_cg_scalars(int mode, const double* part, int n, double* scal) {
   const int lane = threadIdx.x;
   double s = 0.0;
@@ -204,11 +206,60 @@ __global__ void k_cg_scalars(int mode, const double* part, int n, double* scal) 
   if (lane == 0) {
     if (mode == 0) { scal[1] = s; scal[4] = s / scal[0]; }
     else if (mode == 1) { scal[2] = s; scal[3] = scal[1] / s; }
-    else { scal[5] = s; scal[0] = scal[1]; }
+    else if (mode == 2) { scal[5] = s; scal[0] = scal[1]; }
+    else scal[6] = s;   // mode 3: sipsol RES1 (sipsol.f90:69)
   }
 }
 
 __global__ void k_set_scal(double* scal, double v0) { scal[0] = v0; }
+
+// sipsol residual (sipsol.f90:66-69) in the hyperplane layout: fi of
+// interior neighbours from the hyperplane copy, of ghost neighbours from the
+// module array; partial sum |res|.
+__global__ void k_resid_d(DG g, const double* __restrict__ ae, const double* __restrict__ aw,
+                          const double* __restrict__ an, const double* __restrict__ as,
+                          const double* __restrict__ at, const double* __restrict__ ab,
+                          const double* __restrict__ ap, const double* __restrict__ su,
+                          const double* __restrict__ fid, const double* __restrict__ fin,
+                          double* __restrict__ res, double* part) {
+  double v[1] = {0.0};
+  D_LOOP(g) {
+    int a, b, c;
+    if (!d_cell(g, t_, a, b, c)) continue;
+    const long long P = t_;
+    const int n = g.nat(a, b, c);
+    const double fE = a + 1 < g.Ni ? fid[P + g.plane + 1] : fin[n + g.nj];
+    const double fW = a > 0 ? fid[P - g.plane - 1] : fin[n - g.nj];
+    const double fN = b + 1 < g.Nj ? fid[P + g.plane] : fin[n + 1];
+    const double fS = b > 0 ? fid[P - g.plane] : fin[n - 1];
+    const double fT = c + 1 < g.Nk ? fid[P + g.plane + g.Ni] : fin[n + g.nij];
+    const double fB = c > 0 ? fid[P - g.plane - g.Ni] : fin[n - g.nij];
+    const double r = ae[P] * fE + aw[P] * fW + an[P] * fN + as[P] * fS + at[P] * fT + ab[P] * fB + su[P] -
+                     ap[P] * fid[P];
+    res[P] = r;
+    v[0] += fabs(r);
+  }
+  block_reduce_store<1>(v, part);
+}
+
+// SIP backward substitution with fi += z (sipsol.f90:86-88)
+struct SipBwdFiD {
+  using St = double;
+  static constexpr bool kReduce = false;
+  const B4* f;
+  double* z;
+  double* fi;                 // hyperplane layout
+  const double* ghost_src;    // module res (stale ghost values, as the reference reads them)
+  __device__ St ghost(int nat) const { return ghost_src[nat]; }
+  __device__ St load(long long di) const { return __ldcg(z + di); }
+  __device__ St compute(long long di, int, St W, St S, St B, double&) const {
+    const B4 q = f[di];
+    const double v = z[di] - q.bn * S - q.be * W - q.bt * B;
+    z[di] = v;
+    fi[di] = fi[di] + v;
+    return v;
+  }
+};
 
 }  // namespace
 
@@ -324,6 +375,59 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
     rep->status = done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
   }
   if (!isfinite(resl)) {
+    set_error("linear solver residual is not finite");
+    if (rep) rep->status = CAPPGPU_E_NONFINITE;
+    return CAPPGPU_E_NONFINITE;
+  }
+  return done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+}
+
+int sipsol_fast(int fif, int ifi, cappgpu_solve_report* rep) {
+  Ctx& c = ctx();
+  cappgpu_params& P = c.prm;
+  int rc = fast_setup();
+  if (rc) return rc;
+  CAP_CUDA(cudaMemsetAsync(F.flags, 0, sizeof(int) * 2, c.st));
+  const int cf[8] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_SU};
+  for (int q = 0; q < 8; ++q)
+    if ((rc = to_d(cf[q], D_AE + q))) return rc;
+  if ((rc = to_d(fif, D_FI))) return rc;
+  // RES is not cleared by sipsol: its interior is rewritten each sweep, its
+  // ghost layers keep whatever earlier routines left there
+  if ((rc = factor_wave())) return rc;
+  SipFwdD fwd{F.d[D_RES], F.f4, F.d[D_RES], c.f[CAP_RES]};
+  SipBwdFiD bwd{F.b4, F.d[D_RES], F.d[D_FI], c.f[CAP_RES]};
+  const int ns = P.nsw[ifi - 1];
+  double res1 = 0.0, rsm = 0.0;
+  int n;
+  bool done = false;
+  for (n = 1; n <= ns; ++n) {
+    launch(k_resid_d, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
+           (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
+           (const double*)F.d[D_AP], (const double*)F.d[D_SU], (const double*)F.d[D_FI], (const double*)c.f[fif],
+           F.d[D_RES], c.partials);
+    launch(k_cg_scalars, 1, 32, c.st, 3, (const double*)c.partials, kRedBlocks, c.dscal);
+    CAP_CHECK_LAUNCH();
+    if ((rc = run_wave<SipFwdD, false>(fwd))) return rc;
+    if ((rc = run_wave<SipBwdFiD, true>(bwd))) return rc;
+    CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 6, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    CAP_CUDA(cudaStreamSynchronize(c.st));
+    if ((rc = check_wave_error())) return rc;
+    res1 = F.hres[0];
+    if (n == 1) P.resor[ifi - 1] = res1;
+    rsm = res1 / (P.resor[ifi - 1] + CAP_SMALL);
+    if (!isfinite(res1)) break;
+    if (rsm < P.sor[ifi - 1]) { done = true; break; }
+  }
+  if ((rc = from_d(D_FI, fif))) return rc;
+  if ((rc = from_d(D_RES, CAP_RES))) return rc;
+  if (rep) {
+    rep->res0 = P.resor[ifi - 1];
+    rep->resl = res1;
+    rep->iters = done ? n : ns;
+    rep->status = done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+  }
+  if (!isfinite(res1)) {
     set_error("linear solver residual is not finite");
     if (rep) rep->status = CAPPGPU_E_NONFINITE;
     return CAPPGPU_E_NONFINITE;

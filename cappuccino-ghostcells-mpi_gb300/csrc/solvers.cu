@@ -180,6 +180,7 @@ static int finish_status(double resl, bool done, cappgpu_solve_report* rep) {
 // sipsol.f90:3-106
 int sipsol(int fif, int ifi, cappgpu_solve_report* rep) {
   Ctx& c = ctx();
+  if (c.wave_impl == 1 && c.d.nimm >= 4 && c.d.njmm >= 4 && c.d.nkmm >= 4) return sipsol_fast(fif, ifi, rep);
   const Dims& d = c.d;
   double** F = c.f;
   cappgpu_params& P = c.prm;

@@ -11,8 +11,8 @@
 // Predecessor states: along j from the thread's own previous step; across
 // the CTA's lines through shared memory; across CTA blocks from the
 // neighbour block's published output in global memory.  Each block
-// publishes "planes < s done" with st.release.gpu after a CTA barrier and
-// waits for its two predecessor blocks with ld.acquire.gpu.  Blocks are
+// publishes "planes < s done" with st.release.gpu and its successors wait
+// for it through their communication warp (see k_wave).  Blocks are
 // taken by ticket in topological (diagonal) order, so a block only ever
 // waits on blocks that were started before it: no deadlock whatever the
 // residency.  Every wait is bounded: on timeout the kernel raises a
@@ -41,27 +41,27 @@ struct WaveCtl {
   int publish_every;
 };
 
-__device__ inline bool wave_wait(const unsigned long long* p, unsigned long long need, unsigned long long& seen,
-                                 const WaveCtl& w) {
-  for (long long it = 0; it < w.spin_limit; ++it) {
-    unsigned long long v = ld_acquire_u64(p);
-    if (v >= need) { seen = v; return true; }
-    if ((it & 31) == 31 && ld_relaxed_i32(w.abort)) return false;
-    __nanosleep(32);
-  }
-  atomicExch(w.abort, 1);
-  atomicCAS(w.err, 0, 1);
-  return false;
-}
-
+// Block structure: BA*BC compute threads (one per line) plus one
+// communication warp.  Compute warps synchronise per hyperplane with named
+// barrier 1 and never touch global synchronisation variables; lane 0 of the
+// communication warp polls the two predecessor blocks' progress (relaxed
+// loads + acquire fence) and mirrors it into shared memory, and publishes
+// this block's progress (release store) whenever the compute warps finish
+// planes.  Shared-memory handoffs use cta-scope release/acquire, so a compute
+// thread that has seen the mirrored progress also sees the producer's data.
 template <class Op, int BA, int BC, bool BWD>
-__global__ void __launch_bounds__(BA * BC) k_wave(Op op, DG g, WaveCtl w) {
+__global__ void __launch_bounds__(BA * BC + 32) k_wave(Op op, DG g, WaveCtl w) {
   using St = typename Op::St;
+  constexpr int NC = BA * BC;
   __shared__ St sbuf[2][BC][BA];
   __shared__ int s_blk[2];
-  __shared__ int s_bail;
-  const int tid = threadIdx.x, al = tid % BA, cl = tid / BA;
+  __shared__ volatile int s_bail;
+  __shared__ unsigned long long s_seenW, s_seenB, s_done;
+  const int tid = threadIdx.x;
   if (tid == 0) {
+    s_seenW = 0;
+    s_seenB = 0;
+    s_done = 0;
     unsigned t = atomicAdd(w.ticket, 1u) - w.ticket_base;
     if (t < (unsigned)w.nblk) {
       int2 blk = w.order[t];
@@ -78,38 +78,87 @@ __global__ void __launch_bounds__(BA * BC) k_wave(Op op, DG g, WaveCtl w) {
   __syncthreads();
   if (s_bail) return;
   const int ba = s_blk[0], bc = s_blk[1];
+  const int s0 = ba * BA + bc * BC;
+  const int s1 = min(g.S - 1, s0 + (BA - 1) + (BC - 1) + (g.Nj - 1));
+  // a predecessor block publishes planes up to its own last plane only; its
+  // lines have no cells beyond it, so waits are capped there
+  const int s1W = min(g.S - 1, s0 - BA + (BA - 1) + (BC - 1) + (g.Nj - 1));
+  const int s1B = min(g.S - 1, s0 - BC + (BA - 1) + (BC - 1) + (g.Nj - 1));
+  const int blk_id = bc * w.nBA + ba;
+  const bool hasW = ba > 0, hasB = bc > 0;
+
+  if (tid >= NC) {
+    // ------------------------------------------------ communication warp
+    if (tid != NC) return;
+    unsigned long long* myprog = w.prog + blk_id;
+    const unsigned long long* pW = hasW ? w.prog + (blk_id - 1) : nullptr;
+    const unsigned long long* pB = hasB ? w.prog + (blk_id - w.nBA) : nullptr;
+    const unsigned long long lastW = w.tag | (unsigned long long)(unsigned)(s1W + 1);
+    const unsigned long long lastB = w.tag | (unsigned long long)(unsigned)(s1B + 1);
+    const unsigned long long fin = (unsigned long long)(unsigned)(s1 + 1);
+    unsigned long long seenW = 0, seenB = 0, pub = 0;
+    long long idle = 0;
+    for (;;) {
+      bool act = false;
+      unsigned long long vW = (pW && seenW < lastW) ? ld_relaxed_u64(pW) : 0;
+      unsigned long long vB = (pB && seenB < lastB) ? ld_relaxed_u64(pB) : 0;
+      if (vW > seenW || vB > seenB) {
+        fence_acq_rel_gpu();   // acquire: the producers' data is visible from here on
+        if (vW > seenW) { seenW = vW; st_release_cta_shared(&s_seenW, vW); }
+        if (vB > seenB) { seenB = vB; st_release_cta_shared(&s_seenB, vB); }
+        act = true;
+      }
+      const unsigned long long dn = ld_acquire_cta_shared(&s_done);
+      if (dn > pub) {
+        st_release_u64(myprog, w.tag | dn);
+        pub = dn;
+        act = true;
+        if (dn == fin) break;
+      }
+      if (s_bail) break;
+      if (act) {
+        idle = 0;
+      } else {
+        if (++idle > w.spin_limit) {
+          atomicExch(w.abort, 1);
+          atomicCAS(w.err, 0, 1);
+          s_bail = 1;
+          break;
+        }
+        if ((idle & 31) == 31 && ld_relaxed_i32(w.abort)) { s_bail = 1; break; }
+        __nanosleep(20);
+      }
+    }
+    return;
+  }
+
+  // ------------------------------------------------------ compute warps
+  const int al = tid % BA, cl = tid / BA;
   const int av = ba * BA + al, cv = bc * BC + cl;     // virtual (mirrored when BWD) line
   const bool line_ok = av < g.Ni && cv < g.Nk;
   const int a = BWD ? g.Ni - 1 - av : av;
   const int c = BWD ? g.Nk - 1 - cv : cv;
   const int da = BWD ? 1 : -1;                         // real offset of a predecessor
-  const int s0 = ba * BA + bc * BC;
-  const int s1 = min(g.S - 1, s0 + (BA - 1) + (BC - 1) + (g.Nj - 1));
-  const int blk_id = bc * w.nBA + ba;
-  unsigned long long* myprog = w.prog + blk_id;
-  const unsigned long long* pW = ba > 0 ? w.prog + (blk_id - 1) : nullptr;
-  const unsigned long long* pB = bc > 0 ? w.prog + (blk_id - w.nBA) : nullptr;
-  // a predecessor block publishes planes up to its own last plane only; its
-  // lines have no cells beyond it, so the wait is capped there
-  const int s1W = min(g.S - 1, s0 - BA + (BA - 1) + (BC - 1) + (g.Nj - 1));
-  const int s1B = min(g.S - 1, s0 - BC + (BA - 1) + (BC - 1) + (g.Nj - 1));
-  unsigned long long seenW = 0, seenB = 0;
   St prevS{};
   double part = 0.0;
   for (int s = s0; s <= s1; ++s) {
     if (tid == 0) {
-      // need: predecessor planes <= s-1 done (capped at its last plane)
       const unsigned long long needW = w.tag | (unsigned long long)(unsigned)min(s, s1W + 1);
       const unsigned long long needB = w.tag | (unsigned long long)(unsigned)min(s, s1B + 1);
-      bool ok = true;
-      if (pW && seenW < needW) ok = wave_wait(pW, needW, seenW, w);
-      if (ok && pB && seenB < needB) ok = wave_wait(pB, needB, seenB, w);
-      if (!ok) s_bail = 1;
+      long long it = 0;
+      while ((hasW && ld_acquire_cta_shared(&s_seenW) < needW) || (hasB && ld_acquire_cta_shared(&s_seenB) < needB)) {
+        if (s_bail) break;
+        if (++it > 64LL * w.spin_limit) {
+          atomicExch(w.abort, 1);
+          atomicCAS(w.err, 0, 1);
+          s_bail = 1;
+          break;
+        }
+      }
     }
-    __syncthreads();   // plane s-1 of this block complete; neighbours' planes <= s-1 visible
+    named_bar_sync(1, NC);   // plane s-1 done in this block; predecessors' planes <= s-1 visible
     if (s_bail) break;
-    if (tid == 0 && s > s0 && ((s - s0) % w.publish_every) == 0)
-      st_release_u64(myprog, w.tag | (unsigned long long)(unsigned)s);
+    if (tid == 0 && s > s0) st_release_cta_shared(&s_done, (unsigned long long)(unsigned)s);
     const int bv = s - av - cv;
     if (line_ok && bv >= 0 && bv < g.Nj) {
       const int b = BWD ? g.Nj - 1 - bv : bv;
@@ -127,20 +176,19 @@ __global__ void __launch_bounds__(BA * BC) k_wave(Op op, DG g, WaveCtl w) {
       prevS = out;
     }
   }
-  __syncthreads();
-  if (tid == 0 && !s_bail) st_release_u64(myprog, w.tag | (unsigned long long)(unsigned)(s1 + 1));
+  named_bar_sync(1, NC);
+  if (tid == 0 && !s_bail) st_release_cta_shared(&s_done, (unsigned long long)(unsigned)(s1 + 1));
   if (Op::kReduce) {
-    double v[1] = {part};
-    __shared__ double sh[BA * BC / 32];
+    __shared__ double sh[NC / 32];
     const int lane = tid & 31, wid = tid >> 5;
-    double x = v[0];
+    double x = part;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (lane == 0) sh[wid] = x;
-    __syncthreads();
+    named_bar_sync(1, NC);
     if (tid == 0) {
       double sum = 0.0;
-      for (int q = 0; q < BA * BC / 32; ++q) sum += sh[q];
+      for (int q = 0; q < NC / 32; ++q) sum += sh[q];
       w.partials[blk_id] = sum;
     }
   }

@@ -371,26 +371,27 @@ def test_top_wall_index_guard(gpu_lib, oracle_mod):
 
 @pytest.mark.parametrize("shape", [(40, 12, 30), (37, 21, 19), (5, 3, 70)])
 @pytest.mark.parametrize("wave", [1, 0])
-def test_pcgsip_wavefront_multiblock(gpu_lib, oracle_mod, shape, wave):
-    """pcgsip with the persistent wavefront over many line blocks (and with
-    one launch per hyperplane) against the oracle: SIP factors bit-exact,
-    solution within the plain-form tolerance, same iteration count."""
+@pytest.mark.parametrize("solver", ["pcgsip", "sipsol"])
+def test_sip_wavefront_multiblock(gpu_lib, oracle_mod, shape, wave, solver):
+    """pcgsip and sipsol with the persistent wavefront over many line blocks
+    (and with one launch per hyperplane) against the oracle: SIP factors
+    bit-exact (sipsol: the solution too), same iteration count."""
     st = oracle_mod.State(*[n + 4 for n in shape])
     rng = np.random.default_rng(sum(shape))
-    diag_dominant_matrix(st, rng, symmetric=True)
+    diag_dominant_matrix(st, rng, symmetric=solver == "pcgsip")
     randomize(st, rng, ["bb", "bs", "bw", "bp", "bn", "be", "bt"], -0.3, 0.3)
     randomize(st, rng, ["p", "res"])
     st.params.update(dict(alfa=0.92, sor=[1e-9] * 10, nsw=[400] * 10, ipr=3, jpr=3, kpr=3))
     push(gpu_lib, st)
     gpu_lib.set_option("wave", wave)
     try:
-        rg = gpu_lib.solve("pcgsip", "p", IP)
+        rg = gpu_lib.solve(solver, "p", IP)
     finally:
         gpu_lib.set_option("wave", 1)
-    ro = st.solve("pcgsip", "p", IP)
+    ro = st.solve(solver, "p", IP)
     assert rg.iters == ro.iters, (rg, ro)
-    compare(gpu_lib, st, exact=["bb", "bs", "bw", "bp", "bn", "be", "bt"], rtol=RTOL,
-            names=["p", "bb", "bs", "bw", "bp", "bn", "be", "bt"])
+    exact = ["bb", "bs", "bw", "bp", "bn", "be", "bt"] + (["p"] if solver == "sipsol" else [])
+    compare(gpu_lib, st, exact=exact, rtol=RTOL, names=["p", "bb", "bs", "bw", "bp", "bn", "be", "bt"])
     r = compare(gpu_lib, st, names=["res"])
     assert r["res"][0] <= 1e-8 * np.abs(st.field("res")).max() + 1e-12
 
