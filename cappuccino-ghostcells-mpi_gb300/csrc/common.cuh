@@ -107,6 +107,13 @@ inline void launch(void (*k)(KArgs...), int grid, int block, cudaStream_t s, Arg
   k<<<grid, block, 0, s>>>(args...);
 }
 
+// launch() with dynamic shared memory
+template <typename... KArgs, typename... Args>
+inline void launch_smem(void (*k)(KArgs...), int grid, int block, size_t smem, cudaStream_t s, Args... args) {
+  ++ctx().launches;
+  k<<<grid, block, smem, s>>>(args...);
+}
+
 inline int grid_for(long long n, int threads = kThreads) {
   long long b = (n + threads - 1) / threads;
   if (b < 1) b = 1;

@@ -1,16 +1,22 @@
 // dlayout.cuh -- the hyperplane-major ("diagonal") layout used inside the
-// fast SIP-based solvers, plus the memory-ordering helpers of the
-// persistent wavefront.
+// fast SIP-based solvers, plus the memory-ordering, mbarrier and TMA helpers
+// of the persistent wavefront.
 //
 // Interior cell (i,j,k), i=3..nimm etc., has local coordinates a=i-3,
 // b=j-3, c=k-3 and hyperplane s=a+b+c.  Its diagonal-layout index is
-//     D(a,b,c) = (s*Nk + c)*Ni + a
-// so that all cells of one hyperplane are contiguous, ordered by (c, a).
+//     D(a,b,c) = (s*Nk + c)*P + a          (P = pitch >= Ni, even)
+// so that all cells of one hyperplane are contiguous rows ordered by c.
 // A thread that owns the line (a,c) and walks j meets hyperplane s at
 // step s: the threads of a warp (consecutive a) then touch consecutive
 // addresses, which the natural j-fastest layout cannot give along a
-// diagonal.  The layout holds S*Nk*Ni slots (S = Ni+Nj+Nk-2); only the
-// Ni*Nj*Nk slots with 0 <= b < Nj are used.
+// diagonal.  The layout holds S*Nk*P slots (S = Ni+Nj+Nk-2); only the
+// Ni*Nj*Nk slots with a < Ni and 0 <= b < Nj are used.  The even pitch makes
+// every row start on a 16-byte boundary, which the tensor-memory-access
+// (TMA) copies of the wavefront require.
+//
+// Factors with several components per cell use the component-major variant
+//     Dc(a,b,c,q) = ((s*Nk + c)*NQ + q)*P + a
+// so that one component of a row of cells is contiguous.
 #pragma once
 #include "common.cuh"
 
@@ -18,10 +24,15 @@ namespace cap {
 
 struct DG {
   int Ni, Nj, Nk, S;   // interior extents and hyperplane count
+  int P;               // row pitch (Ni rounded up to even)
   int nj, nij;         // natural strides
-  long long plane;     // Nk*Ni
+  long long plane;     // Nk*P
   __host__ __device__ long long d(int a, int b, int c) const {
-    return (long long)(a + b + c) * plane + (long long)c * Ni + a;
+    return (long long)(a + b + c) * plane + (long long)c * P + a;
+  }
+  // component q of NQ at (a,b,c)
+  __host__ __device__ long long dq(int a, int b, int c, int q, int NQ) const {
+    return ((long long)(a + b + c) * Nk * NQ + (long long)c * NQ + q) * P + a;
   }
   // 0-based natural index of interior-local (a,b,c); valid for a,b,c >= -1
   __host__ __device__ int nat(int a, int b, int c) const { return (c + 2) * nij + (a + 2) * nj + (b + 2); }
@@ -34,9 +45,10 @@ inline DG make_dg(const Dims& d) {
   g.Nj = d.njmm - 2;
   g.Nk = d.nkmm - 2;
   g.S = g.Ni + g.Nj + g.Nk - 2;
+  g.P = (g.Ni + 1) & ~1;
   g.nj = d.nj;
   g.nij = d.nij;
-  g.plane = (long long)g.Nk * g.Ni;
+  g.plane = (long long)g.Nk * g.P;
   return g;
 }
 
@@ -68,10 +80,56 @@ __device__ __forceinline__ unsigned long long ld_acquire_cta_shared(const unsign
 __device__ __forceinline__ void named_bar_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
+__device__ __forceinline__ unsigned long long ld_relaxed_b64(const void* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_b64(void* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 __device__ __forceinline__ int ld_relaxed_i32(const int* p) {
   int v;
   asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
+}
+
+// ------------------------------------------------------- mbarrier / TMA
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// 3-D / 4-D tiled tensor loads into shared memory, completion on an mbarrier
+__device__ __forceinline__ void tma_load3(void* dst, const void* map, int x, int y, int z, unsigned long long* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(b))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load4(void* dst, const void* map, int x, int q, int y, int z, unsigned long long* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(q), "r"(y), "r"(z), "r"(smem_u32(b))
+      : "memory");
 }
 
 // ---------------------------------------------------- layout conversion

@@ -1,12 +1,14 @@
 // sip_fast.cu -- pcgsip (pcg-sip.f90:3-200) and sipsol (sipsol.f90:3-106)
 // with the SIP factorisation and both substitutions as persistent
 // wavefronts (wave.cuh) and every per-iteration vector in the hyperplane
-// layout (dlayout.cuh).
+// layout (dlayout.cuh).  The wavefront reads its inputs through TMA tensor
+// maps built here once per grid.
 //
 // Arithmetic per cell is the reference's; the scalars alpha, beta and the
 // norms come from deterministic device reductions and stay on the device
 // (the host reads one residual norm per iteration for the convergence
 // test, as the reference evaluates rsm < resmax).
+#include <cuda.h>
 #include <math.h>
 #include <string.h>
 
@@ -30,16 +32,18 @@ struct Fast {
   bool ready = false;
   DG g{};
   double* d[D_NBUF] = {};
-  F4* f4 = nullptr;
-  B4* b4 = nullptr;
+  double* fq = nullptr;       // forward factors bb, bw, bs, bp (component-major)
+  double* bq = nullptr;       // backward factors bn, be, bt (component-major)
+  CUtensorMap map[D_NBUF];    // scalar tensor maps of d[]
+  CUtensorMap map_fq, map_bq;
   int nBA = 0, nBC = 0, nblk = 0;
   int2* order = nullptr;
-  unsigned long long* prog = nullptr;
   unsigned* ticket = nullptr;
   unsigned ticket_base = 0;
-  unsigned epoch = 0;
   int* flags = nullptr;       // [0] abort, [1] err
   double* wpart = nullptr;    // per-block partials of the wavefront
+  double* mail = nullptr;     // edge mailboxes (sentinel when empty)
+  size_t mail_n = 0;
   double* hres = nullptr;     // pinned host copy of the residual norm
 };
 
@@ -47,15 +51,65 @@ Fast F;
 
 void fast_release() {
   for (auto& p : F.d) { if (p) cudaFree(p); p = nullptr; }
-  if (F.f4) cudaFree(F.f4);
-  if (F.b4) cudaFree(F.b4);
+  if (F.fq) cudaFree(F.fq);
+  if (F.bq) cudaFree(F.bq);
   if (F.order) cudaFree(F.order);
-  if (F.prog) cudaFree(F.prog);
+  if (F.mail) cudaFree(F.mail);
   if (F.ticket) cudaFree(F.ticket);
   if (F.flags) cudaFree(F.flags);
   if (F.wpart) cudaFree(F.wpart);
   if (F.hres) cudaFreeHost(F.hres);
   F = Fast();
+}
+
+__global__ void k_fill_u64(unsigned long long* p, size_t n, unsigned long long v) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) p[t] = v;
+}
+
+void fill_mail(cudaStream_t st) {
+  launch(k_fill_u64, grid_for((long long)F.mail_n), kThreads, st, (unsigned long long*)F.mail, F.mail_n, kSentinel);
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+// Tensor map of a hyperplane-layout array with NQ components per cell: dims
+// (P, [NQ,] Nk, S), box (BA+2, [NQ,] BC, kG) doubles, zero fill outside.
+int make_map(CUtensorMap* m, double* ptr, int nq) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) { set_error("cuTensorMapEncodeTiled is not available"); return CAPPGPU_E_CUDA; }
+  const DG& g = F.g;
+  cuuint64_t dims[4], strides[3];
+  cuuint32_t box[4], es[4] = {1, 1, 1, 1};
+  cuuint32_t rank;
+  if (nq == 1) {
+    rank = 3;
+    dims[0] = (cuuint64_t)g.P; dims[1] = (cuuint64_t)g.Nk; dims[2] = (cuuint64_t)g.S;
+    strides[0] = (cuuint64_t)g.P * 8; strides[1] = (cuuint64_t)g.P * g.Nk * 8;
+    box[0] = BA + 2; box[1] = BC; box[2] = kG;
+  } else {
+    rank = 4;
+    dims[0] = (cuuint64_t)g.P; dims[1] = (cuuint64_t)nq; dims[2] = (cuuint64_t)g.Nk; dims[3] = (cuuint64_t)g.S;
+    strides[0] = (cuuint64_t)g.P * 8; strides[1] = (cuuint64_t)g.P * nq * 8; strides[2] = (cuuint64_t)g.P * nq * g.Nk * 8;
+    box[0] = BA + 2; box[1] = (cuuint32_t)nq; box[2] = BC; box[3] = kG;
+  }
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, rank, ptr, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed"); return CAPPGPU_E_CUDA; }
+  return CAPPGPU_OK;
 }
 
 int fast_setup() {
@@ -70,10 +124,19 @@ int fast_setup() {
     if (cudaMalloc(&F.d[q], n * sizeof(double)) != cudaSuccess) { fast_release(); set_error("out of device memory"); return CAPPGPU_E_NOMEM; }
     CAP_CUDA(cudaMemsetAsync(F.d[q], 0, n * sizeof(double), c.st));
   }
-  CAP_CUDA(cudaMalloc(&F.f4, n * sizeof(F4)));
-  CAP_CUDA(cudaMalloc(&F.b4, n * sizeof(B4)));
-  CAP_CUDA(cudaMemsetAsync(F.f4, 0, n * sizeof(F4), c.st));
-  CAP_CUDA(cudaMemsetAsync(F.b4, 0, n * sizeof(B4), c.st));
+  CAP_CUDA(cudaMalloc(&F.fq, 4 * n * sizeof(double)));
+  CAP_CUDA(cudaMalloc(&F.bq, 3 * n * sizeof(double)));
+  CAP_CUDA(cudaMemsetAsync(F.fq, 0, 4 * n * sizeof(double), c.st));
+  CAP_CUDA(cudaMemsetAsync(F.bq, 0, 3 * n * sizeof(double), c.st));
+  for (int q = 0; q < D_NBUF; ++q) {
+    int rc = make_map(&F.map[q], F.d[q], 1);
+    if (rc) { fast_release(); return rc; }
+  }
+  {
+    int rc = make_map(&F.map_fq, F.fq, 4);
+    if (!rc) rc = make_map(&F.map_bq, F.bq, 3);
+    if (rc) { fast_release(); return rc; }
+  }
   F.nBA = (F.g.Ni + BA - 1) / BA;
   F.nBC = (F.g.Nk + BC - 1) / BC;
   F.nblk = F.nBA * F.nBC;
@@ -87,8 +150,9 @@ int fast_setup() {
     }
   CAP_CUDA(cudaMalloc(&F.order, sizeof(int2) * F.nblk));
   CAP_CUDA(cudaMemcpy(F.order, ord.data(), sizeof(int2) * F.nblk, cudaMemcpyHostToDevice));
-  CAP_CUDA(cudaMalloc(&F.prog, sizeof(unsigned long long) * F.nblk));
-  CAP_CUDA(cudaMemset(F.prog, 0, sizeof(unsigned long long) * F.nblk));
+  F.mail_n = (size_t)F.nblk * (BA + BC) * F.g.Nj * 3;   // up to 3 doubles per state
+  CAP_CUDA(cudaMalloc(&F.mail, F.mail_n * sizeof(double)));
+  fill_mail(c.st);
   CAP_CUDA(cudaMalloc(&F.ticket, sizeof(unsigned)));
   CAP_CUDA(cudaMemset(F.ticket, 0, sizeof(unsigned)));
   CAP_CUDA(cudaMalloc(&F.flags, sizeof(int) * 2));
@@ -96,7 +160,6 @@ int fast_setup() {
   CAP_CUDA(cudaMalloc(&F.wpart, sizeof(double) * F.nblk));
   CAP_CUDA(cudaMallocHost(&F.hres, sizeof(double) * 4));
   F.ticket_base = 0;
-  F.epoch = 0;
   CAP_CUDA(cudaStreamSynchronize(c.st));
   F.ready = true;
   return CAPPGPU_OK;
@@ -107,17 +170,15 @@ WaveCtl next_ctl() {
   w.ticket = F.ticket;
   w.ticket_base = F.ticket_base;
   w.order = F.order;
-  w.prog = F.prog;
-  ++F.epoch;
-  w.tag = (unsigned long long)F.epoch << 32;
   w.nBA = F.nBA;
   w.nBC = F.nBC;
   w.nblk = F.nblk;
   w.abort = F.flags;
   w.err = F.flags + 1;
   w.partials = F.wpart;
-  w.spin_limit = 1LL << 22;
-  w.publish_every = 2;
+  w.mailW = F.mail;
+  w.mailB = F.mail + (size_t)F.nblk * BC * F.g.Nj * 3;
+  w.spin_limit = 1LL << 21;
   F.ticket_base += (unsigned)F.nblk;
   return w;
 }
@@ -125,8 +186,14 @@ WaveCtl next_ctl() {
 template <class Op, bool BWD>
 int run_wave(const Op& op) {
   Ctx& c = ctx();
+  constexpr size_t smem = wave_smem_bytes<Op, BA, BC>();
+  static bool attr_set = false;   // once per process (one device per context)
+  if (!attr_set) {
+    CAP_CUDA(cudaFuncSetAttribute(k_wave<Op, BA, BC, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
   WaveCtl w = next_ctl();
-  launch(k_wave<Op, BA, BC, BWD>, F.nblk, BA * BC + 32, c.st, op, F.g, w);
+  launch_smem(k_wave<Op, BA, BC, BWD>, F.nblk, wave_threads<BA, BC>(), smem, c.st, op, F.g, w);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
 }
@@ -137,12 +204,12 @@ int run_wave(const Op& op) {
        t_ += (long long)gridDim.x * blockDim.x)
 
 __device__ inline bool d_cell(const DG& g, long long t, int& a, int& b, int& c) {
-  long long row = t / g.Ni;
-  a = (int)(t - row * g.Ni);
+  long long row = t / g.P;
+  a = (int)(t - row * g.P);
   int s = (int)(row / g.Nk);
   c = (int)(row - (long long)s * g.Nk);
   b = s - a - c;
-  return b >= 0 && b < g.Nj;
+  return a < g.Ni && b >= 0 && b < g.Nj;
 }
 
 // pk_new = zk + bet pk_old (pcg-sip.f90:241) at the cell and its six
@@ -166,8 +233,8 @@ __global__ void k_pk_spmv_d(DG g, const double* __restrict__ ae, const double* _
     const double pW = a > 0 ? pnew(P - g.plane - 1) : 0.0;
     const double pN = b + 1 < g.Nj ? pnew(P + g.plane) : 0.0;
     const double pS = b > 0 ? pnew(P - g.plane) : 0.0;
-    const double pT = c + 1 < g.Nk ? pnew(P + g.plane + g.Ni) : 0.0;
-    const double pB = c > 0 ? pnew(P - g.plane - g.Ni) : 0.0;
+    const double pT = c + 1 < g.Nk ? pnew(P + g.plane + g.P) : 0.0;
+    const double pB = c > 0 ? pnew(P - g.plane - g.P) : 0.0;
     const double r = ap[P] * pP - ae[P] * pE - aw[P] * pW - an[P] * pN - as[P] * pS - at[P] * pT - ab[P] * pB;
     pkn[P] = pP;
     zz[P] = r;
@@ -232,8 +299,8 @@ __global__ void k_resid_d(DG g, const double* __restrict__ ae, const double* __r
     const double fW = a > 0 ? fid[P - g.plane - 1] : fin[n - g.nj];
     const double fN = b + 1 < g.Nj ? fid[P + g.plane] : fin[n + 1];
     const double fS = b > 0 ? fid[P - g.plane] : fin[n - 1];
-    const double fT = c + 1 < g.Nk ? fid[P + g.plane + g.Ni] : fin[n + g.nij];
-    const double fB = c > 0 ? fid[P - g.plane - g.Ni] : fin[n - g.nij];
+    const double fT = c + 1 < g.Nk ? fid[P + g.plane + g.P] : fin[n + g.nij];
+    const double fB = c > 0 ? fid[P - g.plane - g.P] : fin[n - g.nij];
     const double r = ae[P] * fE + aw[P] * fW + an[P] * fN + as[P] * fS + at[P] * fT + ab[P] * fB + su[P] -
                      ap[P] * fid[P];
     res[P] = r;
@@ -242,24 +309,6 @@ __global__ void k_resid_d(DG g, const double* __restrict__ ae, const double* __r
   block_reduce_store<1>(v, part);
 }
 
-// SIP backward substitution with fi += z (sipsol.f90:86-88)
-struct SipBwdFiD {
-  using St = double;
-  static constexpr bool kReduce = false;
-  const B4* f;
-  double* z;
-  double* fi;                 // hyperplane layout
-  const double* ghost_src;    // module res (stale ghost values, as the reference reads them)
-  __device__ St ghost(int nat) const { return ghost_src[nat]; }
-  __device__ St load(long long di) const { return __ldcg(z + di); }
-  __device__ St compute(long long di, int, St W, St S, St B, double&) const {
-    const B4 q = f[di];
-    const double v = z[di] - q.bn * S - q.be * W - q.bt * B;
-    z[di] = v;
-    fi[di] = fi[di] + v;
-    return v;
-  }
-};
 
 }  // namespace
 
@@ -271,9 +320,9 @@ static int check_wave_error() {
   if (h[1] != 0) {
     cudaMemset(F.flags, 0, sizeof(int) * 2);
     cudaMemset(F.ticket, 0, sizeof(unsigned));
-    cudaMemset(F.prog, 0, sizeof(unsigned long long) * F.nblk);
+    fill_mail(ctx().st);
+    cudaStreamSynchronize(ctx().st);
     F.ticket_base = 0;
-    F.epoch = 0;
     set_error(h[1] == 1 ? "wavefront: a block waited beyond the spin limit for its predecessor"
                         : "wavefront: block ticket out of range");
     return CAPPGPU_E_SPIN;
@@ -287,9 +336,13 @@ static int check_wave_error() {
 static int factor_wave() {
   Ctx& c = ctx();
   double** Fd = c.f;
-  SipFactorD op{F.d[D_AE], F.d[D_AW], F.d[D_AN], F.d[D_AS], F.d[D_AT], F.d[D_AB], F.d[D_AP],
-                Fd[CAP_BB], Fd[CAP_BW], Fd[CAP_BS], Fd[CAP_BP], Fd[CAP_BN], Fd[CAP_BE], Fd[CAP_BT],
-                F.f4, F.b4, c.prm.alfa};
+  SipFactorD op;
+  for (int q = 0; q < 7; ++q) op.map[q] = F.map[D_AE + q];
+  op.bbn = Fd[CAP_BB]; op.bwn = Fd[CAP_BW]; op.bsn = Fd[CAP_BS]; op.bpn = Fd[CAP_BP];
+  op.bnn = Fd[CAP_BN]; op.ben = Fd[CAP_BE]; op.btn = Fd[CAP_BT];
+  op.fq = F.fq;
+  op.bq = F.bq;
+  op.alfa = c.prm.alfa;
   return run_wave<SipFactorD, false>(op);
 }
 
@@ -311,6 +364,34 @@ static int from_d(int dbuf, int field) {
 
 // resid kernel of solvers.cu (natural layout, interior box)
 int resid_natural(int fif, double* res0);
+
+static SipFwdD make_fwd(int rbuf, int zbuf, const double* ghost) {
+  SipFwdD op;
+  op.map[0] = F.map[rbuf];
+  op.map[1] = F.map_fq;
+  op.z = F.d[zbuf];
+  op.ghost_src = ghost;
+  return op;
+}
+static SipBwdD make_bwd(int zbuf, int resbuf) {
+  SipBwdD op;
+  op.map[0] = F.map[zbuf];
+  op.map[1] = F.map_bq;
+  op.map[2] = F.map[resbuf];
+  op.z = F.d[zbuf];
+  op.ghost_src = nullptr;
+  return op;
+}
+static SipBwdFiD make_bwd_fi(int zbuf, int fibuf, const double* ghost) {
+  SipBwdFiD op;
+  op.map[0] = F.map[zbuf];
+  op.map[1] = F.map_bq;
+  op.map[2] = F.map[fibuf];
+  op.z = F.d[zbuf];
+  op.fi = F.d[fibuf];
+  op.ghost_src = ghost;
+  return op;
+}
 
 int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   Ctx& c = ctx();
@@ -335,8 +416,8 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   CAP_CUDA(cudaMemsetAsync(F.d[D_Z], 0, nb, c.st));     // zk = 0 (pcg-sip.f90:149)
   if ((rc = factor_wave())) return rc;
   launch(k_set_scal, 1, 1, c.st, c.dscal, (double)1.e20f);   // s0 = 1.e20 (default real)
-  SipFwdD fwd{F.d[D_RES], F.f4, F.d[D_Z], nullptr};
-  SipBwdD bwd{F.b4, F.d[D_Z], F.d[D_RES], nullptr};
+  const SipFwdD fwd = make_fwd(D_RES, D_Z, nullptr);
+  const SipBwdD bwd = make_bwd(D_Z, D_RES);
   int ns = P.nsw[ifi - 1], l;
   double resl = 0.0, rsm;
   bool done = false;
@@ -395,8 +476,8 @@ int sipsol_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   // RES is not cleared by sipsol: its interior is rewritten each sweep, its
   // ghost layers keep whatever earlier routines left there
   if ((rc = factor_wave())) return rc;
-  SipFwdD fwd{F.d[D_RES], F.f4, F.d[D_RES], c.f[CAP_RES]};
-  SipBwdFiD bwd{F.b4, F.d[D_RES], F.d[D_FI], c.f[CAP_RES]};
+  const SipFwdD fwd = make_fwd(D_RES, D_RES, c.f[CAP_RES]);
+  const SipBwdFiD bwd = make_bwd_fi(D_RES, D_FI, c.f[CAP_RES]);
   const int ns = P.nsw[ifi - 1];
   double res1 = 0.0, rsm = 0.0;
   int n;
@@ -444,12 +525,12 @@ int fast_profile_unit(int which, double* bytes) {
   }
   double cells = (double)F.g.Ni * F.g.Nj * F.g.Nk;
   if (which == 0) {
-    SipFwdD fwd{F.d[D_RES], F.f4, F.d[D_Z], nullptr};
+    const SipFwdD fwd = make_fwd(D_RES, D_Z, nullptr);
     *bytes = 6.0 * 8.0 * cells;   // r + 4 factors read, z written
     return run_wave<SipFwdD, false>(fwd);
   }
   if (which == 1) {
-    SipBwdD bwd{F.b4, F.d[D_Z], F.d[D_RES], nullptr};
+    const SipBwdD bwd = make_bwd(D_Z, D_RES);
     *bytes = 6.0 * 8.0 * cells;   // z + 3 factors + res read, z written
     return run_wave<SipBwdD, true>(bwd);
   }

@@ -1,27 +1,41 @@
 // wave.cuh -- persistent hyperplane wavefront for the SIP recurrences.
 //
 // The interior (Ni x Nj x Nk cells) is cut into lines along j; a CTA owns
-// a BA x BC block of lines (a = i-3, c = k-3) with one thread per line.
-// Thread (a,c) computes cell (a, b, c) at hyperplane step s = a+b+c, so a
-// whole CTA works on one hyperplane per step and every cell is computed
+// a BA x BC block of lines (a = i-3, c = k-3) with one compute thread per
+// line.  Thread (a,c) computes cell (a, b, c) at hyperplane step s = a+b+c,
+// so a whole CTA works on one hyperplane per step and every cell is computed
 // after its three predecessors (a-1), (b-1), (c-1) -- the same per-cell
-// arithmetic on the same final inputs as the reference's sequential
-// k,i,j loop, hence bit-identical results.
+// arithmetic on the same final inputs as the reference's sequential k,i,j
+// loop, hence bit-identical results.
 //
-// Predecessor states: along j from the thread's own previous step; across
-// the CTA's lines through shared memory; across CTA blocks from the
-// neighbour block's published output in global memory.  Each block
-// publishes "planes < s done" with st.release.gpu and its successors wait
-// for it through their communication warp (see k_wave).  Blocks are
-// taken by ticket in topological (diagonal) order, so a block only ever
-// waits on blocks that were started before it: no deadlock whatever the
-// residency.  Every wait is bounded: on timeout the kernel raises a
-// device-wide abort flag and an error code, all blocks leave their loops,
-// and the host reports CAPPGPU_E_SPIN.
+// On GB300 a double-precision instruction occupies its SM sub-partition
+// for 64 cycles whatever the number of active lanes, so a step costs at
+// least the op's FP64 instruction count x 64 cycles.  Everything else is
+// kept off the step:
+//  * a producer thread streams the block's inputs with tensor-memory-access
+//    (TMA) copies, kG hyperplanes per copy, into kSlots shared-memory slots
+//    (mbarrier full/empty handoff);
+//  * edge states cross blocks through global mailboxes in which the data is
+//    its own flag: every entry holds a signalling-NaN sentinel that no
+//    arithmetic result can equal, the producing block stores the value, the
+//    successor's communication warp polls it, stages it into a shared-memory
+//    ring indexed by plane and puts the sentinel back for the next launch.
+//    No progress counters, no GPU-scope fences;
+//  * compute warps synchronise once per hyperplane with named barrier 1;
+//    thread 0 re-reads the staging counters only when its cached value falls
+//    short.
+//
+// Blocks are taken by ticket in topological (diagonal) order, so a block only
+// waits on blocks started before it: no deadlock whatever the residency.
+// Every wait is bounded: on timeout the kernel raises a device-wide abort flag
+// and an error code, all warps leave their loops (the producer after its
+// copies in flight have landed), and the host reports CAPPGPU_E_SPIN.
 //
 // Backward recurrences (successors i+1, j+1, k+1) run the same engine in
 // mirrored coordinates.
 #pragma once
+#include <cuda.h>
+
 #include "common.cuh"
 #include "dlayout.cuh"
 
@@ -31,102 +45,289 @@ struct WaveCtl {
   unsigned* ticket;               // monotonically increasing ticket counter
   unsigned ticket_base;           // its value when this launch started
   const int2* order;              // blocks in topological order
-  unsigned long long* prog;       // per-block progress: tag | planes done
-  unsigned long long tag;         // launch epoch << 32
   int nBA, nBC, nblk;
   int* abort;                     // device-wide abort flag
-  int* err;                       // first error (1 = spin limit)
+  int* err;                       // first error (1 = spin limit, 2 = ticket)
   double* partials;               // per-block partial sums (reducing ops)
+  double* mailW;                  // per block: BC x Nj states of its last a-line
+  double* mailB;                  // per block: BA x Nj states of its last c-row
   long long spin_limit;
-  int publish_every;
 };
 
-// Block structure: BA*BC compute threads (one per line) plus one
-// communication warp.  Compute warps synchronise per hyperplane with named
-// barrier 1 and never touch global synchronisation variables; lane 0 of the
-// communication warp polls the two predecessor blocks' progress (relaxed
-// loads + acquire fence) and mirrors it into shared memory, and publishes
-// this block's progress (release store) whenever the compute warps finish
-// planes.  Shared-memory handoffs use cta-scope release/acquire, so a compute
-// thread that has seen the mirrored progress also sees the producer's data.
-template <class Op, int BA, int BC, bool BWD>
-__global__ void __launch_bounds__(BA * BC + 32) k_wave(Op op, DG g, WaveCtl w) {
+constexpr int kG = 4;        // hyperplanes per TMA copy
+constexpr int kSlots = 3;    // copies in flight
+constexpr int kRing = 32;    // planes of staged edge states
+constexpr int kPW = 8;       // edge planes examined per communication pass
+constexpr unsigned long long kSentinel = 0x7FF0DEAD5EA1F00DULL;   // signalling NaN
+// a slot is released at the start of the next group, so two slots at least;
+// the ring holds the planes between two updates of the consumed-plane count
+static_assert(kSlots >= 2, "TMA slots");
+static_assert(kRing >= kG + 3, "edge ring capacity");
+
+__host__ __device__ constexpr int ring_slot(int q) { return (q + kRing) % kRing; }   // valid for q >= -kRing
+
+// Shared-memory input slots: per map a box of (BA+2) x NQ x BC x kG doubles
+// (the two extra columns let a mirrored block start on an even, 16-byte
+// aligned column).
+template <class Op, int BA, int BC>
+struct WaveLayout {
+  static constexpr int kBW = BA + 2;
+  __host__ __device__ static constexpr size_t map_bytes(int m) { return (size_t)kBW * BC * kG * Op::nq(m) * 8; }
+  __host__ __device__ static constexpr size_t map_off(int m) {
+    size_t o = 0;
+    for (int q = 0; q < m; ++q) o += map_bytes(q);
+    return o;
+  }
+  static constexpr size_t tx_bytes = map_off(Op::kMaps);
+  static constexpr size_t slot_bytes = (tx_bytes + 127) / 128 * 128;
+  static constexpr size_t in_bytes = kSlots * slot_bytes;
+};
+
+template <class St, int BA, int BC>
+struct WaveSmem {
+  St sbuf[2][BC][BA];                      // states of the two latest planes
+  St ringW[kRing][BC];                     // W edge states by plane
+  St ringB[kRing][BA];                     // B edge states by plane
+  St sghost[BA * BC];                      // j-predecessor (ghost) state of each line's first cell
+  unsigned long long full[kSlots], empty[kSlots];
+  unsigned long long stagedW, stagedB;     // edge planes <= value-2 are staged
+  double red[BA * BC / 32];
+  int done;                                // compute steps < done finished (updated per copy group)
+  int blk[2];
+  int start_ok;
+  int stop[2];                             // per-step parity flags, written by compute thread 0
+  int bail;                                // any warp gave up
+};
+
+// compute warps (one thread per line) + communication warp + producer warp
+template <int BA, int BC>
+constexpr int wave_threads() { return BA * BC + 64; }
+
+template <class Op, int BA, int BC>
+constexpr size_t wave_smem_bytes() {
+  return 128 + WaveLayout<Op, BA, BC>::in_bytes + sizeof(WaveSmem<typename Op::St, BA, BC>);
+}
+
+__device__ __forceinline__ void wave_fail(const WaveCtl& w, volatile int* bail, int code) {
+  atomicExch(w.abort, 1);
+  atomicCAS(w.err, 0, code);
+  *bail = 1;
+}
+
+// Stage up to kPW planes of one edge (E entries per plane) into a ring.
+// Entry e of plane q belongs to consumer line (av, cv) = line(e) whose
+// predecessor (pa, pc) is read either from the producer block's mailbox (mail[e][bv])
+// or, on the domain boundary, from the ghost layer.  Returns the number of
+// leading planes that were complete (warp-uniform).
+template <class Op, int E, bool BWD, class LineFn>
+__device__ __forceinline__ int stage_edge(const Op& op, const DG& g, int lane, int loaded, int hi,
+                                          double* mail, typename Op::St (*ring)[E], LineFn line) {
   using St = typename Op::St;
+  constexpr int NS = sizeof(St) / 8;
+  constexpr int R = kPW * E / 32;   // entries per lane
+  St val[R];
+  bool need[R];
+  unsigned bal[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int x = lane + 32 * r, j = x / E, e = x % E, q = loaded + 1 + j;
+    int av, cv, pa, pc;   // consumer line and its predecessor line (virtual)
+    line(e, av, cv, pa, pc);
+    const int bv = q - pa - pc;   // the predecessor cell lies on plane q; the consumer has the same b
+    const bool in_dom = av < g.Ni && cv < g.Nk;
+    need[r] = q <= hi && in_dom && bv >= 0 && bv < g.Nj;
+    bool ok = q <= hi;
+    if (need[r]) {
+      if (mail) {
+        const double* m = mail + ((size_t)e * g.Nj + bv) * NS;
+        unsigned long long u[NS];
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+          u[k] = ld_relaxed_b64(m + k);
+          ok = ok && u[k] != kSentinel;
+        }
+        memcpy(&val[r], u, sizeof(St));
+      } else {
+        const int a = BWD ? g.Ni - 1 - pa : pa;
+        const int b = BWD ? g.Nj - 1 - bv : bv;
+        const int c = BWD ? g.Nk - 1 - pc : pc;
+        val[r] = op.ghost(g.nat(a, b, c));
+      }
+    }
+    bal[r] = __ballot_sync(0xffffffffu, ok);
+  }
+  int n = 0;
+#pragma unroll
+  for (int j = 0; j < kPW; ++j) {
+    const unsigned m = E >= 32 ? 0xffffffffu : ((1u << E) - 1u);
+    if (((bal[(j * E) / 32] >> ((j * E) % 32)) & m) != m) break;
+    ++n;
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int x = lane + 32 * r, j = x / E, e = x % E, q = loaded + 1 + j;
+    if (j < n && need[r]) {
+      ring[ring_slot(q)][e] = val[r];
+      if (mail) {
+        int av, cv, pa, pc;
+        line(e, av, cv, pa, pc);
+        double* m = mail + ((size_t)e * g.Nj + (q - pa - pc)) * NS;
+#pragma unroll
+        for (int k = 0; k < NS; ++k) st_relaxed_b64(m + k, kSentinel);
+      }
+    }
+  }
+  return n;
+}
+
+template <class Op, int BA, int BC, bool BWD>
+__global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid_constant__ Op op, const DG g, const WaveCtl w) {
+  using St = typename Op::St;
+  using L = WaveLayout<Op, BA, BC>;
   constexpr int NC = BA * BC;
-  __shared__ St sbuf[2][BC][BA];
-  __shared__ int s_blk[2];
-  __shared__ volatile int s_bail;
-  __shared__ unsigned long long s_seenW, s_seenB, s_done;
+  constexpr int NS = sizeof(St) / 8;
+  static_assert(NC % 32 == 0, "block shape");
+  static_assert(32 % BC == 0 && (kPW * BC) % 32 == 0 && (kPW * BA) % 32 == 0, "edge staging shape");
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = (unsigned char*)(((size_t)smem_raw + 127) & ~(size_t)127);
+  unsigned char* inbuf = base;
+  WaveSmem<St, BA, BC>& sm = *reinterpret_cast<WaveSmem<St, BA, BC>*>(base + L::in_bytes);
+  volatile int* bail = &sm.bail;
   const int tid = threadIdx.x;
   if (tid == 0) {
-    s_seenW = 0;
-    s_seenB = 0;
-    s_done = 0;
+    sm.stagedW = 0;
+    sm.stagedB = 0;
+    sm.done = 0;
+    sm.stop[0] = sm.stop[1] = 0;
+    sm.bail = 0;
+    for (int k = 0; k < kSlots; ++k) {
+      mbar_init(&sm.full[k], 1);
+      mbar_init(&sm.empty[k], 1);
+    }
+    mbar_fence_init();
     unsigned t = atomicAdd(w.ticket, 1u) - w.ticket_base;
     if (t < (unsigned)w.nblk) {
       int2 blk = w.order[t];
-      s_blk[0] = blk.x;
-      s_blk[1] = blk.y;
-      s_bail = 0;
+      sm.blk[0] = blk.x;
+      sm.blk[1] = blk.y;
+      sm.start_ok = 1;
     } else {   // ticket counter out of step with the host: refuse to run
-      s_blk[0] = s_blk[1] = 0;
-      s_bail = 1;
+      sm.blk[0] = sm.blk[1] = 0;
+      sm.start_ok = 0;
       atomicExch(w.abort, 1);
       atomicCAS(w.err, 0, 2);
     }
   }
   __syncthreads();
-  if (s_bail) return;
-  const int ba = s_blk[0], bc = s_blk[1];
+  if (!sm.start_ok) return;
+  const int ba = sm.blk[0], bc = sm.blk[1];
   const int s0 = ba * BA + bc * BC;
   const int s1 = min(g.S - 1, s0 + (BA - 1) + (BC - 1) + (g.Nj - 1));
-  // a predecessor block publishes planes up to its own last plane only; its
-  // lines have no cells beyond it, so waits are capped there
-  const int s1W = min(g.S - 1, s0 - BA + (BA - 1) + (BC - 1) + (g.Nj - 1));
-  const int s1B = min(g.S - 1, s0 - BC + (BA - 1) + (BC - 1) + (g.Nj - 1));
+  // last plane of the W / B predecessor lines
+  const int s1W = min(g.S - 1, s0 - 1 + (BC - 1) + (g.Nj - 1));
+  const int s1B = min(g.S - 1, s0 - 1 + (BA - 1) + (g.Nj - 1));
   const int blk_id = bc * w.nBA + ba;
-  const bool hasW = ba > 0, hasB = bc > 0;
+  const int ngroups = (s1 - s0 + kG) / kG;
+
+  if (tid >= NC + 32) {
+    // ---------------------------------------------------- TMA producer
+    if (tid != NC + 32) return;
+    int issued = 0;
+    for (int gi = 0; gi < ngroups; ++gi) {
+      const int slot = gi % kSlots;
+      if (gi >= kSlots) {
+        const unsigned par = (unsigned)((gi / kSlots - 1) & 1);
+        long long it = 0;
+        bool ok = true;
+        while (!mbar_test(&sm.empty[slot], par)) {
+          if (*bail) { ok = false; break; }
+          if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); ok = false; break; }
+        }
+        if (!ok) break;
+      }
+      const int sg = s0 + gi * kG;
+      int x0, y0, z0;
+      if (!BWD) {
+        x0 = ba * BA;
+        y0 = bc * BC;
+        z0 = sg;
+      } else {
+        x0 = (g.Ni - (ba + 1) * BA) & ~1;   // even: 16-byte aligned start
+        y0 = g.Nk - (bc + 1) * BC;
+        z0 = g.S - sg - kG;
+      }
+      unsigned char* dst = inbuf + slot * L::slot_bytes;
+      mbar_arrive_tx(&sm.full[slot], (unsigned)L::tx_bytes);
+#pragma unroll
+      for (int m = 0; m < Op::kMaps; ++m) {
+        if (Op::nq(m) == 1) tma_load3(dst + L::map_off(m), &op.map[m], x0, y0, z0, &sm.full[slot]);
+        else tma_load4(dst + L::map_off(m), &op.map[m], x0, 0, y0, z0, &sm.full[slot]);
+      }
+      ++issued;
+    }
+    // the copies in flight land before the block exits
+    for (int gi = max(0, issued - kSlots); gi < issued; ++gi) {
+      long long it = 0;
+      while (!mbar_test(&sm.full[gi % kSlots], (unsigned)((gi / kSlots) & 1))) {
+        if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); break; }
+      }
+    }
+    return;
+  }
 
   if (tid >= NC) {
-    // ------------------------------------------------ communication warp
-    if (tid != NC) return;
-    unsigned long long* myprog = w.prog + blk_id;
-    const unsigned long long* pW = hasW ? w.prog + (blk_id - 1) : nullptr;
-    const unsigned long long* pB = hasB ? w.prog + (blk_id - w.nBA) : nullptr;
-    const unsigned long long lastW = w.tag | (unsigned long long)(unsigned)(s1W + 1);
-    const unsigned long long lastB = w.tag | (unsigned long long)(unsigned)(s1B + 1);
-    const unsigned long long fin = (unsigned long long)(unsigned)(s1 + 1);
-    unsigned long long seenW = 0, seenB = 0, pub = 0;
+    // --------------------------------------------- communication warp
+    const int lane = tid - NC;
+    double* srcW = ba > 0 ? w.mailW + (size_t)(blk_id - 1) * BC * g.Nj * NS : nullptr;
+    double* srcB = bc > 0 ? w.mailB + (size_t)(blk_id - w.nBA) * BA * g.Nj * NS : nullptr;
+    auto lineW = [&](int e, int& av, int& cv, int& pa, int& pc) {
+      av = ba * BA; cv = bc * BC + e; pa = av - 1; pc = cv;
+    };
+    auto lineB = [&](int e, int& av, int& cv, int& pa, int& pc) {
+      av = ba * BA + e; cv = bc * BC; pa = av; pc = cv - 1;
+    };
+    int loadedW = s0 - 2, loadedB = s0 - 2;   // last staged plane
     long long idle = 0;
-    for (;;) {
-      bool act = false;
-      unsigned long long vW = (pW && seenW < lastW) ? ld_relaxed_u64(pW) : 0;
-      unsigned long long vB = (pB && seenB < lastB) ? ld_relaxed_u64(pB) : 0;
-      if (vW > seenW || vB > seenB) {
-        fence_acq_rel_gpu();   // acquire: the producers' data is visible from here on
-        if (vW > seenW) { seenW = vW; st_release_cta_shared(&s_seenW, vW); }
-        if (vB > seenB) { seenB = vB; st_release_cta_shared(&s_seenB, vB); }
-        act = true;
+    while (loadedW < s1W || loadedB < s1B) {
+      // warp-uniform decisions: the staging below uses warp-wide ballots
+      if (__any_sync(0xffffffffu, *bail)) break;
+      const int cur = __shfl_sync(0xffffffffu, *(volatile int*)&sm.done, 0);
+      const int limit = max(cur, s0) + kRing - 2;   // ring capacity
+      bool prog = false;
+      if (loadedW < s1W) {
+        const int hi = min(s1W, limit);
+        if (hi > loadedW) {
+          const int n = stage_edge<Op, BC, BWD>(op, g, lane, loadedW, hi, srcW, sm.ringW, lineW);
+          if (n > 0) {
+            loadedW += n;
+            __syncwarp();
+            if (lane == 0) st_release_cta_shared(&sm.stagedW, (unsigned long long)(unsigned)(loadedW + 2));
+            prog = true;
+          }
+        }
       }
-      const unsigned long long dn = ld_acquire_cta_shared(&s_done);
-      if (dn > pub) {
-        st_release_u64(myprog, w.tag | dn);
-        pub = dn;
-        act = true;
-        if (dn == fin) break;
+      if (loadedB < s1B) {
+        const int hi = min(s1B, limit);
+        if (hi > loadedB) {
+          const int n = stage_edge<Op, BA, BWD>(op, g, lane, loadedB, hi, srcB, sm.ringB, lineB);
+          if (n > 0) {
+            loadedB += n;
+            __syncwarp();
+            if (lane == 0) st_release_cta_shared(&sm.stagedB, (unsigned long long)(unsigned)(loadedB + 2));
+            prog = true;
+          }
+        }
       }
-      if (s_bail) break;
-      if (act) {
+      if (prog) {
         idle = 0;
       } else {
-        if (++idle > w.spin_limit) {
-          atomicExch(w.abort, 1);
-          atomicCAS(w.err, 0, 1);
-          s_bail = 1;
-          break;
+        int stop = 0;
+        if (lane == 0) {
+          if (++idle > w.spin_limit) { wave_fail(w, bail, 1); stop = 1; }
+          else if ((idle & 31) == 31 && ld_relaxed_i32(w.abort)) { *bail = 1; stop = 1; }
         }
-        if ((idle & 31) == 31 && ld_relaxed_i32(w.abort)) { s_bail = 1; break; }
-        __nanosleep(20);
+        if (__shfl_sync(0xffffffffu, stop, 0)) break;
+        __nanosleep(32);
       }
     }
     return;
@@ -138,82 +339,120 @@ __global__ void __launch_bounds__(BA * BC + 32) k_wave(Op op, DG g, WaveCtl w) {
   const bool line_ok = av < g.Ni && cv < g.Nk;
   const int a = BWD ? g.Ni - 1 - av : av;
   const int c = BWD ? g.Nk - 1 - cv : cv;
-  const int da = BWD ? 1 : -1;                         // real offset of a predecessor
+  const int sfirst = av + cv;                         // step of this line's first cell
+  int xb, yb;                                         // this line's column and row in an input box
+  if (!BWD) {
+    xb = al;
+    yb = cl;
+  } else {
+    const int alo = g.Ni - (ba + 1) * BA;
+    xb = (alo - (alo & ~1)) + BA - 1 - al;
+    yb = BC - 1 - cl;
+  }
+  const bool edgeE = al == BA - 1 && ba + 1 < w.nBA;   // feeds the next block along a
+  const bool edgeT = cl == BC - 1 && bc + 1 < w.nBC;   // feeds the next block along c
+  double* mW = w.mailW + ((size_t)blk_id * BC + cl) * g.Nj * NS;
+  double* mB = w.mailB + ((size_t)blk_id * BA + al) * g.Nj * NS;
+  if (line_ok) sm.sghost[tid] = op.ghost(g.nat(a, BWD ? g.Nj : -1, c));
   St prevS{};
   double part = 0.0;
+  unsigned long long knownW = 0, knownB = 0;
+  int gi = 0, ds = 0;
   for (int s = s0; s <= s1; ++s) {
     if (tid == 0) {
-      const unsigned long long needW = w.tag | (unsigned long long)(unsigned)min(s, s1W + 1);
-      const unsigned long long needB = w.tag | (unsigned long long)(unsigned)min(s, s1B + 1);
-      long long it = 0;
-      while ((hasW && ld_acquire_cta_shared(&s_seenW) < needW) || (hasB && ld_acquire_cta_shared(&s_seenB) < needB)) {
-        if (s_bail) break;
-        if (++it > 64LL * w.spin_limit) {
-          atomicExch(w.abort, 1);
-          atomicCAS(w.err, 0, 1);
-          s_bail = 1;
-          break;
+      int st = 0;
+      if (ds == 0) {   // the copy of this group of planes has landed
+        long long it = 0;
+        while (!mbar_test(&sm.full[gi % kSlots], (unsigned)((gi / kSlots) & 1))) {
+          if (*bail) { st = 1; break; }
+          if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); st = 1; break; }
+        }
+      }
+      const unsigned long long needW = (unsigned long long)(unsigned)(min(s, s1W + 1) + 1);
+      const unsigned long long needB = (unsigned long long)(unsigned)(min(s, s1B + 1) + 1);
+      if (!st && (knownW < needW || knownB < needB)) {
+        long long it = 0;
+        for (;;) {
+          knownW = ld_acquire_cta_shared(&sm.stagedW);
+          knownB = ld_acquire_cta_shared(&sm.stagedB);
+          if (knownW >= needW && knownB >= needB) break;
+          if (*bail) { st = 1; break; }
+          if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); st = 1; break; }
+        }
+      }
+      sm.stop[s & 1] = st;
+    }
+    named_bar_sync(1, NC);   // plane s-1 computed here; inputs and edge states of plane s ready
+    if (sm.stop[s & 1]) break;
+    if (tid == 0 && ds == 0 && gi > 0) {   // the previous group's slot is free again
+      mbar_arrive(&sm.empty[(gi - 1) % kSlots]);
+      *(volatile int*)&sm.done = s;
+    }
+    const int bv = s - sfirst;
+    if (line_ok && bv >= 0 && bv < g.Nj) {
+      const int b = BWD ? g.Nj - 1 - bv : bv;
+      const St W = al > 0 ? sm.sbuf[(s - 1) & 1][cl][al - 1] : sm.ringW[ring_slot(s - 1)][cl];
+      const St B = cl > 0 ? sm.sbuf[(s - 1) & 1][cl - 1][al] : sm.ringB[ring_slot(s - 1)][al];
+      const St S = bv > 0 ? prevS : sm.sghost[tid];
+      const double* slotp = reinterpret_cast<const double*>(inbuf + (gi % kSlots) * L::slot_bytes);
+      const int zb = BWD ? kG - 1 - ds : ds;
+      auto in = [&](int m, int q) -> double {
+        return slotp[L::map_off(m) / 8 + ((zb * BC + yb) * Op::nq(m) + q) * L::kBW + xb];
+      };
+      const St out = op.compute(in, g, a, b, c, W, S, B, part);
+      sm.sbuf[s & 1][cl][al] = out;
+      prevS = out;
+      if (edgeE || edgeT) {
+        unsigned long long u[NS];
+        memcpy(u, &out, sizeof(St));
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+          if (edgeE) st_relaxed_b64(mW + (size_t)bv * NS + k, u[k]);
+          if (edgeT) st_relaxed_b64(mB + (size_t)bv * NS + k, u[k]);
         }
       }
     }
-    named_bar_sync(1, NC);   // plane s-1 done in this block; predecessors' planes <= s-1 visible
-    if (s_bail) break;
-    if (tid == 0 && s > s0) st_release_cta_shared(&s_done, (unsigned long long)(unsigned)s);
-    const int bv = s - av - cv;
-    if (line_ok && bv >= 0 && bv < g.Nj) {
-      const int b = BWD ? g.Nj - 1 - bv : bv;
-      St W, B, S;
-      if (al > 0) W = sbuf[(s - 1) & 1][cl][al - 1];
-      else if (av > 0) W = op.load(g.d(a + da, b, c));
-      else W = op.ghost(g.nat(a + da, b, c));
-      if (cl > 0) B = sbuf[(s - 1) & 1][cl - 1][al];
-      else if (cv > 0) B = op.load(g.d(a, b, c + da));
-      else B = op.ghost(g.nat(a, b, c + da));
-      if (bv > 0) S = prevS;
-      else S = op.ghost(g.nat(a, b + da, c));
-      St out = op.compute(g.d(a, b, c), g.nat(a, b, c), W, S, B, part);
-      sbuf[s & 1][cl][al] = out;
-      prevS = out;
-    }
+    if (++ds == kG) { ds = 0; ++gi; }
   }
   named_bar_sync(1, NC);
-  if (tid == 0 && !s_bail) st_release_cta_shared(&s_done, (unsigned long long)(unsigned)(s1 + 1));
   if (Op::kReduce) {
-    __shared__ double sh[NC / 32];
     const int lane = tid & 31, wid = tid >> 5;
     double x = part;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[wid] = x;
+    if (lane == 0) sm.red[wid] = x;
     named_bar_sync(1, NC);
     if (tid == 0) {
       double sum = 0.0;
-      for (int q = 0; q < NC / 32; ++q) sum += sh[q];
+      for (int q = 0; q < NC / 32; ++q) sum += sm.red[q];
       w.partials[blk_id] = sum;
     }
   }
 }
 
 // ------------------------------------------------------------------ ops
+// An op defines St (the state passed to successors), kMaps tensor maps of
+// inputs with nq(m) components each (1 = scalar hyperplane layout, >1 =
+// component-major layout), ghost (the state of a ghost cell, read from the
+// module arrays) and compute (one cell: reads its inputs through in(m,q),
+// writes its outputs, returns its state).
 
-struct __align__(32) F4 { double bb, bw, bs, bp; };
-struct __align__(32) B4 { double bn, be, bt, pad; };
 struct St3 { double bn, be, bt; };
 
 // SIP forward substitution z = (r - bb zB - bw zW - bs zS) bp (pcg-sip.f90:208-209)
 struct SipFwdD {
   using St = double;
+  static constexpr int kMaps = 2;   // r, forward factors (bb, bw, bs, bp)
   static constexpr bool kReduce = false;
-  const double* r;            // diagonal layout
-  const F4* f;                // diagonal layout
-  double* z;                  // diagonal layout (output)
+  __host__ __device__ static constexpr int nq(int m) { return m == 0 ? 1 : 4; }
+  CUtensorMap map[kMaps];
+  double* z;                  // hyperplane layout (output; may alias r)
   const double* ghost_src;    // natural array of ghost values, or null (zero)
   __device__ St ghost(int nat) const { return ghost_src ? ghost_src[nat] : 0.0; }
-  __device__ St load(long long di) const { return __ldcg(z + di); }
-  __device__ St compute(long long di, int, St W, St S, St B, double&) const {
-    const F4 q = f[di];
-    const double v = (r[di] - q.bb * B - q.bw * W - q.bs * S) * q.bp;
-    z[di] = v;
+  template <class In>
+  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+    const double v = (in(0, 0) - in(1, 0) * B - in(1, 1) * W - in(1, 2) * S) * in(1, 3);
+    z[g.d(a, b, c)] = v;
     return v;
   }
 };
@@ -223,18 +462,39 @@ struct SipFwdD {
 // neighbours are the j+1, i+1, k+1 cells here.
 struct SipBwdD {
   using St = double;
+  static constexpr int kMaps = 3;   // z, backward factors (bn, be, bt), res
   static constexpr bool kReduce = true;
-  const B4* f;
+  __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
+  CUtensorMap map[kMaps];
   double* z;
-  const double* res;          // diagonal layout (dot), may be null
   const double* ghost_src;
   __device__ St ghost(int nat) const { return ghost_src ? ghost_src[nat] : 0.0; }
-  __device__ St load(long long di) const { return __ldcg(z + di); }
-  __device__ St compute(long long di, int, St W, St S, St B, double& part) const {
-    const B4 q = f[di];
-    const double v = z[di] - q.bn * S - q.be * W - q.bt * B;
+  template <class In>
+  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double& part) const {
+    const double v = in(0, 0) - in(1, 0) * S - in(1, 1) * W - in(1, 2) * B;
+    z[g.d(a, b, c)] = v;
+    part += in(2, 0) * v;
+    return v;
+  }
+};
+
+// SIP backward substitution with fi += z (sipsol.f90:86-88)
+struct SipBwdFiD {
+  using St = double;
+  static constexpr int kMaps = 3;   // z, backward factors, fi
+  static constexpr bool kReduce = false;
+  __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
+  CUtensorMap map[kMaps];
+  double* z;
+  double* fi;                 // hyperplane layout
+  const double* ghost_src;    // module res (stale ghost values, as the reference reads them)
+  __device__ St ghost(int nat) const { return ghost_src[nat]; }
+  template <class In>
+  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+    const double v = in(0, 0) - in(1, 0) * S - in(1, 1) * W - in(1, 2) * B;
+    const long long di = g.d(a, b, c);
     z[di] = v;
-    if (res) part += res[di] * v;
+    fi[di] = in(2, 0) + v;
     return v;
   }
 };
@@ -242,32 +502,37 @@ struct SipBwdD {
 // SIP factorisation (pcg-sip.f90:178-190); state passed on = (bn, be, bt)
 struct SipFactorD {
   using St = St3;
+  static constexpr int kMaps = 7;   // ae, aw, an, as, at, ab, ap
   static constexpr bool kReduce = false;
-  const double *ae, *aw, *an, *as, *at, *ab, *ap;   // diagonal layout
+  __host__ __device__ static constexpr int nq(int) { return 1; }
+  CUtensorMap map[kMaps];
   double *bbn, *bwn, *bsn, *bpn, *bnn, *ben, *btn;  // natural layout outputs (module coefb)
-  F4* f;                                            // diagonal layout outputs
-  B4* g4;
+  double* fq;                                       // forward factors, 4 components
+  double* bq;                                       // backward factors, 3 components
   double alfa;
   __device__ St ghost(int nat) const { return St3{bnn[nat], ben[nat], btn[nat]}; }
-  __device__ St load(long long di) const {
-    const double* p = reinterpret_cast<const double*>(g4 + di);
-    return St3{__ldcg(p), __ldcg(p + 1), __ldcg(p + 2)};
-  }
-  __device__ St compute(long long di, int nat, St W, St S, St B, double&) const {
-    const double bbv = -ab[di] / (1.0 + alfa * (B.bn + B.be));
-    const double bwv = -aw[di] / (1.0 + alfa * (W.bn + W.bt));
-    const double bsv = -as[di] / (1.0 + alfa * (S.be + S.bt));
+  template <class In>
+  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+    const double bbv = -in(5, 0) / (1.0 + alfa * (B.bn + B.be));
+    const double bwv = -in(1, 0) / (1.0 + alfa * (W.bn + W.bt));
+    const double bsv = -in(3, 0) / (1.0 + alfa * (S.be + S.bt));
     const double p1 = alfa * (bbv * B.bn + bwv * W.bn);
     const double p2 = alfa * (bbv * B.be + bsv * S.be);
     const double p3 = alfa * (bwv * W.bt + bsv * S.bt);
-    const double bpv = 1.0 / (ap[di] + p1 + p2 + p3 - bbv * B.bt - bwv * W.be - bsv * S.bn + CAP_SMALL);
-    const double bnv = (-an[di] - p1) * bpv;
-    const double bev = (-ae[di] - p2) * bpv;
-    const double btv = (-at[di] - p3) * bpv;
+    const double bpv = 1.0 / (in(6, 0) + p1 + p2 + p3 - bbv * B.bt - bwv * W.be - bsv * S.bn + CAP_SMALL);
+    const double bnv = (-in(2, 0) - p1) * bpv;
+    const double bev = (-in(0, 0) - p2) * bpv;
+    const double btv = (-in(4, 0) - p3) * bpv;
+    const int nat = g.nat(a, b, c);
     bbn[nat] = bbv; bwn[nat] = bwv; bsn[nat] = bsv; bpn[nat] = bpv;
     bnn[nat] = bnv; ben[nat] = bev; btn[nat] = btv;
-    f[di] = F4{bbv, bwv, bsv, bpv};
-    g4[di] = B4{bnv, bev, btv, 0.0};
+    fq[g.dq(a, b, c, 0, 4)] = bbv;
+    fq[g.dq(a, b, c, 1, 4)] = bwv;
+    fq[g.dq(a, b, c, 2, 4)] = bsv;
+    fq[g.dq(a, b, c, 3, 4)] = bpv;
+    bq[g.dq(a, b, c, 0, 3)] = bnv;
+    bq[g.dq(a, b, c, 1, 3)] = bev;
+    bq[g.dq(a, b, c, 2, 3)] = btv;
     return St3{bnv, bev, btv};
   }
 };
