@@ -10,25 +10,26 @@
 //
 // On GB300 a double-precision instruction occupies its SM sub-partition
 // for 64 cycles whatever the number of active lanes, so a step costs at
-// least the op's FP64 instruction count x 64 cycles.  Everything else is
-// kept off the step:
-//  * a producer thread streams the block's inputs with tensor-memory-access
-//    (TMA) copies, kG hyperplanes per copy, into kSlots shared-memory slots
-//    (mbarrier full/empty handoff);
-//  * edge states cross blocks through global mailboxes in which the data is
-//    its own flag: every entry holds a signalling-NaN sentinel that no
-//    arithmetic result can equal, the producing block stores the value, the
-//    successor's communication warp polls it, stages it into a shared-memory
-//    ring indexed by plane and puts the sentinel back for the next launch.
-//    No progress counters, no GPU-scope fences;
-//  * compute warps synchronise once per hyperplane with named barrier 1;
-//    thread 0 re-reads the staging counters only when its cached value falls
-//    short.
+// least the op's FP64 instruction count x 64 cycles.  The compute warps do
+// nothing but that arithmetic and one barrier per hyperplane; three other
+// roles run beside them:
+//  * the pacing warp streams the block's inputs with tensor-memory-access
+//    (TMA) copies, kG hyperplanes per copy, into kSlots shared-memory slots,
+//    checks ahead of each step that the copy has landed (mbarrier) and that
+//    the edge states are staged, and releases the step through named
+//    barrier 1 (bar.red.or, which also carries the stop flag);
+//  * the communication warp moves edge states across blocks through global
+//    mailboxes in which the data is its own flag: every entry holds a
+//    signalling-NaN sentinel that no arithmetic result can equal, the
+//    producing block stores the value, the successor's communication warp
+//    polls it, stages it into a shared-memory ring indexed by plane and puts
+//    the sentinel back for the next launch.  No progress counters, no
+//    GPU-scope fences.
 //
 // Blocks are taken by ticket in topological (diagonal) order, so a block only
 // waits on blocks started before it: no deadlock whatever the residency.
 // Every wait is bounded: on timeout the kernel raises a device-wide abort flag
-// and an error code, all warps leave their loops (the producer after its
+// and an error code, all warps leave their loops (the pacing warp after its
 // copies in flight have landed), and the host reports CAPPGPU_E_SPIN.
 //
 // Backward recurrences (successors i+1, j+1, k+1) run the same engine in
@@ -59,7 +60,7 @@ constexpr int kSlots = 3;    // copies in flight
 constexpr int kRing = 32;    // planes of staged edge states
 constexpr int kPW = 8;       // edge planes examined per communication pass
 constexpr unsigned long long kSentinel = 0x7FF0DEAD5EA1F00DULL;   // signalling NaN
-// a slot is released at the start of the next group, so two slots at least;
+// a slot is refilled at the start of the next group, so two slots at least;
 // the ring holds the planes between two updates of the consumed-plane count
 static_assert(kSlots >= 2, "TMA slots");
 static_assert(kRing >= kG + 3, "edge ring capacity");
@@ -88,18 +89,16 @@ struct WaveSmem {
   St sbuf[2][BC][BA];                      // states of the two latest planes
   St ringW[kRing][BC];                     // W edge states by plane
   St ringB[kRing][BA];                     // B edge states by plane
-  St sghost[BA * BC];                      // j-predecessor (ghost) state of each line's first cell
-  unsigned long long full[kSlots], empty[kSlots];
+  unsigned long long full[kSlots];
   unsigned long long stagedW, stagedB;     // edge planes <= value-2 are staged
   double red[BA * BC / 32];
   int done;                                // compute steps < done finished (updated per copy group)
   int blk[2];
   int start_ok;
-  int stop[2];                             // per-step parity flags, written by compute thread 0
   int bail;                                // any warp gave up
 };
 
-// compute warps (one thread per line) + communication warp + producer warp
+// compute warps (one thread per line) + communication warp + pacing warp
 template <int BA, int BC>
 constexpr int wave_threads() { return BA * BC + 64; }
 
@@ -114,45 +113,60 @@ __device__ __forceinline__ void wave_fail(const WaveCtl& w, volatile int* bail, 
   *bail = 1;
 }
 
-// Stage up to kPW planes of one edge (E entries per plane) into a ring.
-// Entry e of plane q belongs to consumer line (av, cv) = line(e) whose
-// predecessor (pa, pc) is read either from the producer block's mailbox (mail[e][bv])
-// or, on the domain boundary, from the ghost layer.  Returns the number of
-// leading planes that were complete (warp-uniform).
+// Edge staging, split in two phases so that the loads of both edges are in
+// flight together: probe_edge reads up to kPW planes of one edge (E entries
+// per plane), commit_edge keeps the leading complete planes.  Entry e of
+// plane q belongs to consumer line (av, cv) = line(e) whose predecessor line
+// (pa, pc) is read either from the producer block's mailbox (mail[e][bv]) or,
+// on the domain boundary, from the ghost layer.
+template <class St, int R>
+struct EdgeProbe {
+  unsigned long long u[R][sizeof(St) / 8];
+  bool need[R];   // the consumer cell exists
+  bool inwin[R];  // plane within the window this pass may stage
+};
+
 template <class Op, int E, bool BWD, class LineFn>
-__device__ __forceinline__ int stage_edge(const Op& op, const DG& g, int lane, int loaded, int hi,
-                                          double* mail, typename Op::St (*ring)[E], LineFn line) {
+__device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, kPW * E / 32>& P, const Op& op, const DG& g,
+                                           int lane, int loaded, int hi, const double* mail, LineFn line) {
   using St = typename Op::St;
   constexpr int NS = sizeof(St) / 8;
-  constexpr int R = kPW * E / 32;   // entries per lane
-  St val[R];
-  bool need[R];
-  unsigned bal[R];
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
+  for (int r = 0; r < kPW * E / 32; ++r) {
     const int x = lane + 32 * r, j = x / E, e = x % E, q = loaded + 1 + j;
-    int av, cv, pa, pc;   // consumer line and its predecessor line (virtual)
+    int av, cv, pa, pc;
     line(e, av, cv, pa, pc);
     const int bv = q - pa - pc;   // the predecessor cell lies on plane q; the consumer has the same b
-    const bool in_dom = av < g.Ni && cv < g.Nk;
-    need[r] = q <= hi && in_dom && bv >= 0 && bv < g.Nj;
-    bool ok = q <= hi;
-    if (need[r]) {
+    P.inwin[r] = q <= hi;
+    P.need[r] = q <= hi && av < g.Ni && cv < g.Nk && bv >= 0 && bv < g.Nj;
+    if (P.need[r]) {
       if (mail) {
         const double* m = mail + ((size_t)e * g.Nj + bv) * NS;
-        unsigned long long u[NS];
 #pragma unroll
-        for (int k = 0; k < NS; ++k) {
-          u[k] = ld_relaxed_b64(m + k);
-          ok = ok && u[k] != kSentinel;
-        }
-        memcpy(&val[r], u, sizeof(St));
+        for (int k = 0; k < NS; ++k) P.u[r][k] = ld_relaxed_b64(m + k);
       } else {
         const int a = BWD ? g.Ni - 1 - pa : pa;
         const int b = BWD ? g.Nj - 1 - bv : bv;
         const int c = BWD ? g.Nk - 1 - pc : pc;
-        val[r] = op.ghost(g.nat(a, b, c));
+        const St v = op.ghost(g.nat(a, b, c));
+        memcpy(P.u[r], &v, sizeof(St));
       }
+    }
+  }
+}
+
+template <class St, int E, class LineFn>
+__device__ __forceinline__ int commit_edge(EdgeProbe<St, kPW * E / 32>& P, const DG& g, int lane, int loaded,
+                                           double* mail, St (*ring)[E], LineFn line) {
+  constexpr int NS = sizeof(St) / 8;
+  constexpr int R = kPW * E / 32;
+  unsigned bal[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    bool ok = P.inwin[r];
+    if (P.need[r] && mail) {
+#pragma unroll
+      for (int k = 0; k < NS; ++k) ok = ok && P.u[r][k] != kSentinel;
     }
     bal[r] = __ballot_sync(0xffffffffu, ok);
   }
@@ -166,8 +180,8 @@ __device__ __forceinline__ int stage_edge(const Op& op, const DG& g, int lane, i
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int x = lane + 32 * r, j = x / E, e = x % E, q = loaded + 1 + j;
-    if (j < n && need[r]) {
-      ring[ring_slot(q)][e] = val[r];
+    if (j < n && P.need[r]) {
+      memcpy(&ring[ring_slot(q)][e], P.u[r], sizeof(St));
       if (mail) {
         int av, cv, pa, pc;
         line(e, av, cv, pa, pc);
@@ -198,12 +212,8 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
     sm.stagedW = 0;
     sm.stagedB = 0;
     sm.done = 0;
-    sm.stop[0] = sm.stop[1] = 0;
     sm.bail = 0;
-    for (int k = 0; k < kSlots; ++k) {
-      mbar_init(&sm.full[k], 1);
-      mbar_init(&sm.empty[k], 1);
-    }
+    for (int k = 0; k < kSlots; ++k) mbar_init(&sm.full[k], 1);
     mbar_fence_init();
     unsigned t = atomicAdd(w.ticket, 1u) - w.ticket_base;
     if (t < (unsigned)w.nblk) {
@@ -230,22 +240,10 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
   const int ngroups = (s1 - s0 + kG) / kG;
 
   if (tid >= NC + 32) {
-    // ---------------------------------------------------- TMA producer
-    if (tid != NC + 32) return;
-    int issued = 0;
-    for (int gi = 0; gi < ngroups; ++gi) {
-      const int slot = gi % kSlots;
-      if (gi >= kSlots) {
-        const unsigned par = (unsigned)((gi / kSlots - 1) & 1);
-        long long it = 0;
-        bool ok = true;
-        while (!mbar_test(&sm.empty[slot], par)) {
-          if (*bail) { ok = false; break; }
-          if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); ok = false; break; }
-        }
-        if (!ok) break;
-      }
-      const int sg = s0 + gi * kG;
+    // ------------------------------------------------------- pacing warp
+    const int lane = tid - (NC + 32);
+    auto issue = [&](int gq) {   // TMA copy of group gq (planes s0 + gq*kG ...) into its slot
+      const int slot = gq % kSlots, sg = s0 + gq * kG;
       int x0, y0, z0;
       if (!BWD) {
         x0 = ba * BA;
@@ -263,13 +261,57 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
         if (Op::nq(m) == 1) tma_load3(dst + L::map_off(m), &op.map[m], x0, y0, z0, &sm.full[slot]);
         else tma_load4(dst + L::map_off(m), &op.map[m], x0, 0, y0, z0, &sm.full[slot]);
       }
-      ++issued;
+    };
+    int issued = min(kSlots, ngroups);
+    if (lane == 0)
+      for (int gq = 0; gq < issued; ++gq) issue(gq);
+    unsigned long long knownW = 0, knownB = 0;
+    int gi = 0, ds = 0;
+    for (int s = s0; s <= s1; ++s) {
+      int st = 0;
+      if (lane == 0) {
+        if (ds == 0) {   // the copy of this group of planes has landed
+          long long it = 0;
+          while (!mbar_test(&sm.full[gi % kSlots], (unsigned)((gi / kSlots) & 1))) {
+            if (*bail) { st = 1; break; }
+            if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); st = 1; break; }
+          }
+        }
+        const unsigned long long needW = (unsigned long long)(unsigned)(min(s, s1W + 1) + 1);
+        const unsigned long long needB = (unsigned long long)(unsigned)(min(s, s1B + 1) + 1);
+        if (!st && (knownW < needW || knownB < needB)) {   // the edge states of plane s-1 are staged
+          long long it = 0;
+          for (;;) {
+            knownW = ld_acquire_cta_shared(&sm.stagedW);
+            knownB = ld_acquire_cta_shared(&sm.stagedB);
+            if (knownW >= needW && knownB >= needB) break;
+            if (*bail) { st = 1; break; }
+            if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); st = 1; break; }
+          }
+        }
+      }
+      st = __shfl_sync(0xffffffffu, st, 0);
+      if (named_bar_red_or(1, NC + 32, st != 0)) break;   // the compute warps start step s
+      if (lane == 0 && ds == 0 && gi > 0) {
+        // step s-1 is complete: the edge rings up to plane s-2 and the slot
+        // of the previous group are free
+        *(volatile int*)&sm.done = s;
+        const int gq = gi - 1 + kSlots;
+        if (gq < ngroups) {
+          fence_proxy_async_smem();
+          issue(gq);
+          issued = gq + 1;
+        }
+      }
+      if (++ds == kG) { ds = 0; ++gi; }
     }
     // the copies in flight land before the block exits
-    for (int gi = max(0, issued - kSlots); gi < issued; ++gi) {
-      long long it = 0;
-      while (!mbar_test(&sm.full[gi % kSlots], (unsigned)((gi / kSlots) & 1))) {
-        if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); break; }
+    if (lane == 0) {
+      for (int gq = max(0, issued - kSlots); gq < issued; ++gq) {
+        long long it = 0;
+        while (!mbar_test(&sm.full[gq % kSlots], (unsigned)((gq / kSlots) & 1))) {
+          if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); break; }
+        }
       }
     }
     return;
@@ -286,39 +328,28 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
     auto lineB = [&](int e, int& av, int& cv, int& pa, int& pc) {
       av = ba * BA + e; cv = bc * BC; pa = av; pc = cv - 1;
     };
+    EdgeProbe<St, kPW * BC / 32> PW;
+    EdgeProbe<St, kPW * BA / 32> PB;
     int loadedW = s0 - 2, loadedB = s0 - 2;   // last staged plane
     long long idle = 0;
     while (loadedW < s1W || loadedB < s1B) {
-      // warp-uniform decisions: the staging below uses warp-wide ballots
+      // warp-uniform decisions: the staging uses warp-wide ballots
       if (__any_sync(0xffffffffu, *bail)) break;
       const int cur = __shfl_sync(0xffffffffu, *(volatile int*)&sm.done, 0);
       const int limit = max(cur, s0) + kRing - 2;   // ring capacity
-      bool prog = false;
-      if (loadedW < s1W) {
-        const int hi = min(s1W, limit);
-        if (hi > loadedW) {
-          const int n = stage_edge<Op, BC, BWD>(op, g, lane, loadedW, hi, srcW, sm.ringW, lineW);
-          if (n > 0) {
-            loadedW += n;
-            __syncwarp();
-            if (lane == 0) st_release_cta_shared(&sm.stagedW, (unsigned long long)(unsigned)(loadedW + 2));
-            prog = true;
-          }
+      const int hiW = min(s1W, limit), hiB = min(s1B, limit);
+      probe_edge<Op, BC, BWD>(PW, op, g, lane, loadedW, hiW, srcW, lineW);
+      probe_edge<Op, BA, BWD>(PB, op, g, lane, loadedB, hiB, srcB, lineB);
+      const int nW = commit_edge<St, BC>(PW, g, lane, loadedW, srcW, sm.ringW, lineW);
+      const int nB = commit_edge<St, BA>(PB, g, lane, loadedB, srcB, sm.ringB, lineB);
+      if (nW + nB > 0) {
+        loadedW += nW;
+        loadedB += nB;
+        __syncwarp();
+        if (lane == 0) {
+          if (nW) st_release_cta_shared(&sm.stagedW, (unsigned long long)(unsigned)(loadedW + 2));
+          if (nB) st_release_cta_shared(&sm.stagedB, (unsigned long long)(unsigned)(loadedB + 2));
         }
-      }
-      if (loadedB < s1B) {
-        const int hi = min(s1B, limit);
-        if (hi > loadedB) {
-          const int n = stage_edge<Op, BA, BWD>(op, g, lane, loadedB, hi, srcB, sm.ringB, lineB);
-          if (n > 0) {
-            loadedB += n;
-            __syncwarp();
-            if (lane == 0) st_release_cta_shared(&sm.stagedB, (unsigned long long)(unsigned)(loadedB + 2));
-            prog = true;
-          }
-        }
-      }
-      if (prog) {
         idle = 0;
       } else {
         int stop = 0;
@@ -327,7 +358,6 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
           else if ((idle & 31) == 31 && ld_relaxed_i32(w.abort)) { *bail = 1; stop = 1; }
         }
         if (__shfl_sync(0xffffffffu, stop, 0)) break;
-        __nanosleep(32);
       }
     }
     return;
@@ -353,47 +383,18 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
   const bool edgeT = cl == BC - 1 && bc + 1 < w.nBC;   // feeds the next block along c
   double* mW = w.mailW + ((size_t)blk_id * BC + cl) * g.Nj * NS;
   double* mB = w.mailB + ((size_t)blk_id * BA + al) * g.Nj * NS;
-  if (line_ok) sm.sghost[tid] = op.ghost(g.nat(a, BWD ? g.Nj : -1, c));
+  const St sg = line_ok ? op.ghost(g.nat(a, BWD ? g.Nj : -1, c)) : St{};   // j-predecessor of the first cell
   St prevS{};
   double part = 0.0;
-  unsigned long long knownW = 0, knownB = 0;
   int gi = 0, ds = 0;
   for (int s = s0; s <= s1; ++s) {
-    if (tid == 0) {
-      int st = 0;
-      if (ds == 0) {   // the copy of this group of planes has landed
-        long long it = 0;
-        while (!mbar_test(&sm.full[gi % kSlots], (unsigned)((gi / kSlots) & 1))) {
-          if (*bail) { st = 1; break; }
-          if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); st = 1; break; }
-        }
-      }
-      const unsigned long long needW = (unsigned long long)(unsigned)(min(s, s1W + 1) + 1);
-      const unsigned long long needB = (unsigned long long)(unsigned)(min(s, s1B + 1) + 1);
-      if (!st && (knownW < needW || knownB < needB)) {
-        long long it = 0;
-        for (;;) {
-          knownW = ld_acquire_cta_shared(&sm.stagedW);
-          knownB = ld_acquire_cta_shared(&sm.stagedB);
-          if (knownW >= needW && knownB >= needB) break;
-          if (*bail) { st = 1; break; }
-          if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); st = 1; break; }
-        }
-      }
-      sm.stop[s & 1] = st;
-    }
-    named_bar_sync(1, NC);   // plane s-1 computed here; inputs and edge states of plane s ready
-    if (sm.stop[s & 1]) break;
-    if (tid == 0 && ds == 0 && gi > 0) {   // the previous group's slot is free again
-      mbar_arrive(&sm.empty[(gi - 1) % kSlots]);
-      *(volatile int*)&sm.done = s;
-    }
+    if (named_bar_red_or(1, NC + 32, false)) break;   // plane s-1 computed; inputs of plane s ready
     const int bv = s - sfirst;
     if (line_ok && bv >= 0 && bv < g.Nj) {
       const int b = BWD ? g.Nj - 1 - bv : bv;
       const St W = al > 0 ? sm.sbuf[(s - 1) & 1][cl][al - 1] : sm.ringW[ring_slot(s - 1)][cl];
       const St B = cl > 0 ? sm.sbuf[(s - 1) & 1][cl - 1][al] : sm.ringB[ring_slot(s - 1)][al];
-      const St S = bv > 0 ? prevS : sm.sghost[tid];
+      const St S = bv > 0 ? prevS : sg;
       const double* slotp = reinterpret_cast<const double*>(inbuf + (gi % kSlots) * L::slot_bytes);
       const int zb = BWD ? kG - 1 - ds : ds;
       auto in = [&](int m, int q) -> double {
@@ -414,14 +415,13 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
     }
     if (++ds == kG) { ds = 0; ++gi; }
   }
-  named_bar_sync(1, NC);
   if (Op::kReduce) {
     const int lane = tid & 31, wid = tid >> 5;
     double x = part;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (lane == 0) sm.red[wid] = x;
-    named_bar_sync(1, NC);
+    named_bar_sync(2, NC);
     if (tid == 0) {
       double sum = 0.0;
       for (int q = 0; q < NC / 32; ++q) sum += sm.red[q];
