@@ -57,6 +57,7 @@ SIGNATURES = {
     "cappgpu_cgstab_h": [_DP, _INT],
     "cappgpu_cgstab_sip_h": [_DP, _INT],
     "cappgpu_spmv": [_INT, _INT, _DP],
+    "cappgpu_spmv_noalloc": [_INT, _INT, _DP],
     "cappgpu_fluxuvw": [_INT] * 10,
     "cappgpu_calcuvw": [_REP],
     "cappgpu_piso_assemble_pressure_eq": [_INT] * 12,

@@ -244,6 +244,18 @@ int cappgpu_cgstab_sip_h(double* fi, int ifi);
    the fused dot pk.z over the interior; exposed for tests and benches. */
 int cappgpu_spmv(int pk, int zk, double* dot);
 
+/* cappgpu_spmv without any device allocation; no counterpart in the
+   reference.  For callers that cannot allocate device memory where they need
+   the product (the device pool is held by another allocator, or cudaMalloc's
+   implicit synchronisation is not acceptable inside the step loop).  zk is
+   the same as cappgpu_spmv's; the dot is summed in a different fixed order.
+   The reduction scratch is a fixed 32 KB device array: grids with more than
+   8,388,608 interior cells are rejected with CAPPGPU_E_ARG.  The first call
+   on a device performs a one-time set-up (it looks up the array's device
+   address) and should come before any stream capture.  Calls that overlap
+   share the scratch and race. */
+int cappgpu_spmv_noalloc(int pk, int zk, double* dot);
+
 /* ================================================ assembly / PISO / SIMPLE */
 /* fluxuvw(idew,idns,idtb, arvx,arvy,arvz, fif,acfe,acfw,fcf),
    fluxuvw-overrelaxed-correction.f90:3-659.  Field ids for the arrays. */
