@@ -138,6 +138,31 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def snapshot(lib):
+    """Every field and the parameters (outside any timed region)."""
+    import cappgpu
+    return {n: lib.get_field(n) for n in cappgpu.FIELD_NAMES}, lib.get_params()
+
+
+def restore(lib, snap):
+    fields, params = snap
+    for n, a in fields.items():
+        lib.set_field(n, a)
+    lib.set_params(params)
+
+
+def profiled_traffic(n):
+    """DRAM bytes per launch of the forward sweep from the committed ncu
+    capture of the same workload (profiles/), or None."""
+    f = ROOT / "profiles" / "k_wave_sip_sweeps_channel128.md"
+    if n != 128 or not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch_fwd"):
+            return float(line.split("=")[1])
+    return None
+
+
 def make_case(n):
     import cappgpu
     return cappgpu.cases.channel(N=(n, n, n))
@@ -203,6 +228,7 @@ def run_gpu(args, ws, rank, local):
     cells = args.n ** 3
     for _ in range(args.warmup):
         lib.piso_steps(1)
+    snap = snapshot(lib)
     clocks = ClockSampler(local)
     launches0 = lib.stats().launches
     group.barrier()
@@ -217,12 +243,14 @@ def run_gpu(args, ws, rank, local):
     ms = group.max(ms)
     value = ws * args.steps / (ms / 1e3)
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers, from the same state
+    # as the device-timed steps
+    restore(lib, snap)
     names = ["u", "v", "w", "p", "f1", "f2", "f3"]
     host = {n: lib.pinned(lib.nijk) for n in names}
     for n in names:
         host[n][:] = lib.get_field(n)
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = args.steps
     group.barrier()
     lib.timer_start()
     for _ in range(e2e_steps):
@@ -258,7 +286,7 @@ def run_gpu(args, ws, rank, local):
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "roofline": {"bound": "hbm", "kernel": "SIP forward substitution (pcg-sip.f90:204-212)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": None,
+                     "peak_source": peak_kind, "traffic": profiled_traffic(args.n),
                      "algorithmic_bytes": bytes_fwd, "ms_per_launch": ms_fwd},
         "units": units,
         "gpu_launches": launches,

@@ -212,31 +212,39 @@ __device__ inline bool d_cell(const DG& g, long long t, int& a, int& b, int& c) 
   return a < g.Ni && b >= 0 && b < g.Nj;
 }
 
-// pk_new = zk + bet pk_old (pcg-sip.f90:241) at the cell and its six
-// neighbours (pk is zero outside the interior); zz = A pk_new
-// (pcg-sip.f90:253-255); partial sum pk_new . zz.
-__global__ void k_pk_spmv_d(DG g, const double* __restrict__ ae, const double* __restrict__ aw,
-                            const double* __restrict__ an, const double* __restrict__ as,
-                            const double* __restrict__ at, const double* __restrict__ ab,
-                            const double* __restrict__ ap, const double* __restrict__ zk,
-                            const double* __restrict__ pko, double* __restrict__ pkn, double* __restrict__ zz,
-                            const double* __restrict__ scal, double* part) {
+// pk = zk + bet pk (pcg-sip.f90:241).  A pass of its own: fusing it into
+// the product would recompute pk at all seven stencil points, and on GB300
+// the FP64 issue rate, not HBM, bounds these passes.
+__global__ void k_pk_d(DG g, const double* __restrict__ zk, const double* __restrict__ pko, double* __restrict__ pkn,
+                       const double* __restrict__ scal) {
   const double bet = scal[4];
+  D_LOOP(g) {
+    int a, b, c;
+    if (!d_cell(g, t_, a, b, c)) continue;
+    pkn[t_] = zk[t_] + bet * pko[t_];
+  }
+}
+
+// zz = A pk (pcg-sip.f90:253-255; pk is zero outside the interior) and the
+// partial sums of pk.zz (pcg-sip.f90:258-261)
+__global__ void k_spmv_d(DG g, const double* __restrict__ ae, const double* __restrict__ aw,
+                         const double* __restrict__ an, const double* __restrict__ as,
+                         const double* __restrict__ at, const double* __restrict__ ab,
+                         const double* __restrict__ ap, const double* __restrict__ pk, double* __restrict__ zz,
+                         double* part) {
   double v[1] = {0.0};
   D_LOOP(g) {
     int a, b, c;
     if (!d_cell(g, t_, a, b, c)) continue;
     const long long P = t_;
-    auto pnew = [&](long long q) { return zk[q] + bet * pko[q]; };
-    const double pP = pnew(P);
-    const double pE = a + 1 < g.Ni ? pnew(P + g.plane + 1) : 0.0;
-    const double pW = a > 0 ? pnew(P - g.plane - 1) : 0.0;
-    const double pN = b + 1 < g.Nj ? pnew(P + g.plane) : 0.0;
-    const double pS = b > 0 ? pnew(P - g.plane) : 0.0;
-    const double pT = c + 1 < g.Nk ? pnew(P + g.plane + g.P) : 0.0;
-    const double pB = c > 0 ? pnew(P - g.plane - g.P) : 0.0;
+    const double pP = pk[P];
+    const double pE = a + 1 < g.Ni ? pk[P + g.plane + 1] : 0.0;
+    const double pW = a > 0 ? pk[P - g.plane - 1] : 0.0;
+    const double pN = b + 1 < g.Nj ? pk[P + g.plane] : 0.0;
+    const double pS = b > 0 ? pk[P - g.plane] : 0.0;
+    const double pT = c + 1 < g.Nk ? pk[P + g.plane + g.P] : 0.0;
+    const double pB = c > 0 ? pk[P - g.plane - g.P] : 0.0;
     const double r = ap[P] * pP - ae[P] * pE - aw[P] * pW - an[P] * pN - as[P] * pS - at[P] * pT - ab[P] * pB;
-    pkn[P] = pP;
     zz[P] = r;
     v[0] += pP * r;
   }
@@ -428,10 +436,11 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
     launch(k_cg_scalars, 1, 32, c.st, 0, (const double*)F.wpart, F.nblk, c.dscal);
     double* pko = F.d[cur ? D_PK1 : D_PK0];
     double* pkn = F.d[cur ? D_PK0 : D_PK1];
-    launch(k_pk_spmv_d, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
+    launch(k_pk_d, grid_for(F.g.size()), kThreads, c.st, F.g, (const double*)F.d[D_Z], (const double*)pko, pkn,
+           (const double*)c.dscal);
+    launch(k_spmv_d, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
            (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
-           (const double*)F.d[D_AP], (const double*)F.d[D_Z], (const double*)pko, pkn, F.d[D_ZZ],
-           (const double*)c.dscal, c.partials);
+           (const double*)F.d[D_AP], (const double*)pkn, F.d[D_ZZ], c.partials);
     launch(k_cg_scalars, 1, 32, c.st, 1, (const double*)c.partials, kRedBlocks, c.dscal);
     launch(k_update_d, kRedBlocks, kThreads, c.st, F.g, F.d[D_FI], F.d[D_RES], (const double*)pkn,
            (const double*)F.d[D_ZZ], (const double*)c.dscal, c.partials);
