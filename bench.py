@@ -263,6 +263,23 @@ def run_gpu(args, ws, rank, local):
     lib.free_pinned()
     nbytes = len(names) * lib.nijk * 8
 
+    # the FP32 + FP64-refinement form of the pressure solve (precision mode
+    # 1), same steps from the same state
+    restore(lib, snap)
+    lib.precision(1)
+    lib.piso_steps(1)   # warm-up of the FP32 buffers and kernels
+    restore(lib, snap)
+    group.barrier()
+    lib.timer_start()
+    lib.piso_steps(args.steps)
+    ms32 = group.max(lib.timer_stop())
+    st32 = lib.stats()
+    lib.precision(0)
+    fp32 = {"value": ws * args.steps / (ms32 / 1e3), "unit": "steps/s", "ms_per_step": ms32 / args.steps,
+            "p_solve_ms": st32.p_solve_ms, "p_iters": st32.p_report.iters,
+            "p_rel_residual": st32.p_report.resl / st32.p_report.res0 if st32.p_report.res0 else None,
+            "form": "FP32 SIP-preconditioned CG inside FP64 iterative refinement (exit test on the FP64 residual)"}
+
     # roofline of the SIP forward substitution on the current state
     peak, peak_kind = measured_peaks()
     ms_fwd, bytes_fwd = lib.profile_kernel(0, reps=3)
@@ -289,6 +306,7 @@ def run_gpu(args, ws, rank, local):
                      "peak_source": peak_kind, "traffic": profiled_traffic(args.n),
                      "algorithmic_bytes": bytes_fwd, "ms_per_launch": ms_fwd},
         "units": units,
+        "fp32_refined": fp32,
         "gpu_launches": launches,
         "clocks": clk,
     }

@@ -267,6 +267,19 @@ int cappgpu_set_option(const char* key, int value) {
   return CAPPGPU_E_ARG;
 }
 
+// Precision of the pressure solve (pcgsip): 0 = FP64 plain, the reference's
+// arithmetic (default); 1 = FP32 SIP-preconditioned CG inside FP64
+// iterative refinement.
+int cappgpu_precision(int mode) {
+  CAP_REQUIRE_INIT();
+  if (mode != 0 && mode != 1) {
+    set_error("precision mode %d: 0 (FP64 plain) or 1 (FP32 + FP64 refinement)", mode);
+    return CAPPGPU_E_ARG;
+  }
+  ctx().precision = mode;
+  return CAPPGPU_OK;
+}
+
 int cappgpu_ijkpr(void) {
   if (!ctx().init) return CAPPGPU_E_NOINIT;
   const cappgpu_params& p = ctx().prm;

@@ -4,15 +4,15 @@
 //
 // Interior cell (i,j,k), i=3..nimm etc., has local coordinates a=i-3,
 // b=j-3, c=k-3 and hyperplane s=a+b+c.  Its diagonal-layout index is
-//     D(a,b,c) = (s*Nk + c)*P + a          (P = pitch >= Ni, even)
+//     D(a,b,c) = (s*Nk + c)*P + a          (P = pitch >= Ni, multiple of 4)
 // so that all cells of one hyperplane are contiguous rows ordered by c.
 // A thread that owns the line (a,c) and walks j meets hyperplane s at
 // step s: the threads of a warp (consecutive a) then touch consecutive
 // addresses, which the natural j-fastest layout cannot give along a
 // diagonal.  The layout holds S*Nk*P slots (S = Ni+Nj+Nk-2); only the
-// Ni*Nj*Nk slots with a < Ni and 0 <= b < Nj are used.  The even pitch makes
-// every row start on a 16-byte boundary, which the tensor-memory-access
-// (TMA) copies of the wavefront require.
+// Ni*Nj*Nk slots with a < Ni and 0 <= b < Nj are used.  The pitch makes every
+// row of doubles or floats start on a 16-byte boundary, which the
+// tensor-memory-access (TMA) copies of the wavefront require.
 //
 // Factors with several components per cell use the component-major variant
 //     Dc(a,b,c,q) = ((s*Nk + c)*NQ + q)*P + a
@@ -24,7 +24,7 @@ namespace cap {
 
 struct DG {
   int Ni, Nj, Nk, S;   // interior extents and hyperplane count
-  int P;               // row pitch (Ni rounded up to even)
+  int P;               // row pitch (Ni rounded up to a multiple of 4)
   int nj, nij;         // natural strides
   long long plane;     // Nk*P
   __host__ __device__ long long d(int a, int b, int c) const {
@@ -45,7 +45,7 @@ inline DG make_dg(const Dims& d) {
   g.Nj = d.njmm - 2;
   g.Nk = d.nkmm - 2;
   g.S = g.Ni + g.Nj + g.Nk - 2;
-  g.P = (g.Ni + 1) & ~1;
+  g.P = (g.Ni + 3) & ~3;
   g.nj = d.nj;
   g.nij = d.nij;
   g.plane = (long long)g.Nk * g.P;

@@ -18,6 +18,7 @@ int iccg(int fi, int ifi, cappgpu_solve_report* rep);
 int bicgstab(int fi, int ifi, bool sip, cappgpu_solve_report* rep);
 int dpcg(int fi, int ifi, cappgpu_solve_report* rep);
 int pcgsip_fast(int fi, int ifi, cappgpu_solve_report* rep);
+int pcgsip_mixed(int fi, int ifi, cappgpu_solve_report* rep);
 int sipsol_fast(int fi, int ifi, cappgpu_solve_report* rep);
 int fast_profile_unit(int which, double* bytes);
 void fast_free();

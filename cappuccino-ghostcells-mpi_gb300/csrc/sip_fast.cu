@@ -49,7 +49,29 @@ struct Fast {
 
 Fast F;
 
+// FP32 copies for the FP32 + FP64-refinement form of pcgsip
+enum EBuf { E_AE, E_AW, E_AN, E_AS, E_AT, E_AB, E_AP, E_R, E_Z, E_P0, E_P1, E_ZZ, E_X, E_NBUF };
+
+struct Fast32 {
+  bool ready = false;
+  float* e[E_NBUF] = {};
+  float* fq = nullptr;   // forward factors, 4 components
+  float* bq = nullptr;   // backward factors, 3 components
+  CUtensorMap map[E_NBUF];
+  CUtensorMap map_fq, map_bq;
+};
+
+Fast32 G;
+
+void fast32_release() {
+  for (auto& p : G.e) { if (p) cudaFree(p); p = nullptr; }
+  if (G.fq) cudaFree(G.fq);
+  if (G.bq) cudaFree(G.bq);
+  G = Fast32();
+}
+
 void fast_release() {
+  fast32_release();
   for (auto& p : F.d) { if (p) cudaFree(p); p = nullptr; }
   if (F.fq) cudaFree(F.fq);
   if (F.bq) cudaFree(F.bq);
@@ -86,28 +108,32 @@ EncodeTiledFn encode_tiled() {
   return fn;
 }
 
-// Tensor map of a hyperplane-layout array with NQ components per cell: dims
-// (P, [NQ,] Nk, S), box (BA+2, [NQ,] BC, kG) doubles, zero fill outside.
-int make_map(CUtensorMap* m, double* ptr, int nq) {
+// Tensor map of a hyperplane-layout array of esize-byte elements with NQ
+// components per cell: dims (P, [NQ,] Nk, S), box (BA + 16/esize, [NQ,] BC, kG),
+// zero fill outside.
+int make_map(CUtensorMap* m, void* ptr, int nq, int esize) {
   EncodeTiledFn enc = encode_tiled();
   if (!enc) { set_error("cuTensorMapEncodeTiled is not available"); return CAPPGPU_E_CUDA; }
   const DG& g = F.g;
+  const cuuint64_t es = (cuuint64_t)esize;
   cuuint64_t dims[4], strides[3];
-  cuuint32_t box[4], es[4] = {1, 1, 1, 1};
+  cuuint32_t box[4], estr[4] = {1, 1, 1, 1};
   cuuint32_t rank;
+  const cuuint32_t bw = (cuuint32_t)(BA + 16 / esize);
   if (nq == 1) {
     rank = 3;
     dims[0] = (cuuint64_t)g.P; dims[1] = (cuuint64_t)g.Nk; dims[2] = (cuuint64_t)g.S;
-    strides[0] = (cuuint64_t)g.P * 8; strides[1] = (cuuint64_t)g.P * g.Nk * 8;
-    box[0] = BA + 2; box[1] = BC; box[2] = kG;
+    strides[0] = (cuuint64_t)g.P * es; strides[1] = (cuuint64_t)g.P * g.Nk * es;
+    box[0] = bw; box[1] = BC; box[2] = kG;
   } else {
     rank = 4;
     dims[0] = (cuuint64_t)g.P; dims[1] = (cuuint64_t)nq; dims[2] = (cuuint64_t)g.Nk; dims[3] = (cuuint64_t)g.S;
-    strides[0] = (cuuint64_t)g.P * 8; strides[1] = (cuuint64_t)g.P * nq * 8; strides[2] = (cuuint64_t)g.P * nq * g.Nk * 8;
-    box[0] = BA + 2; box[1] = (cuuint32_t)nq; box[2] = BC; box[3] = kG;
+    strides[0] = (cuuint64_t)g.P * es; strides[1] = (cuuint64_t)g.P * nq * es; strides[2] = (cuuint64_t)g.P * nq * g.Nk * es;
+    box[0] = bw; box[1] = (cuuint32_t)nq; box[2] = BC; box[3] = kG;
   }
-  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, rank, ptr, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r = enc(m, esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, ptr, dims,
+                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed"); return CAPPGPU_E_CUDA; }
   return CAPPGPU_OK;
 }
@@ -129,12 +155,12 @@ int fast_setup() {
   CAP_CUDA(cudaMemsetAsync(F.fq, 0, 4 * n * sizeof(double), c.st));
   CAP_CUDA(cudaMemsetAsync(F.bq, 0, 3 * n * sizeof(double), c.st));
   for (int q = 0; q < D_NBUF; ++q) {
-    int rc = make_map(&F.map[q], F.d[q], 1);
+    int rc = make_map(&F.map[q], F.d[q], 1, 8);
     if (rc) { fast_release(); return rc; }
   }
   {
-    int rc = make_map(&F.map_fq, F.fq, 4);
-    if (!rc) rc = make_map(&F.map_bq, F.bq, 3);
+    int rc = make_map(&F.map_fq, F.fq, 4, 8);
+    if (!rc) rc = make_map(&F.map_bq, F.bq, 3, 8);
     if (rc) { fast_release(); return rc; }
   }
   F.nBA = (F.g.Ni + BA - 1) / BA;
@@ -162,6 +188,30 @@ int fast_setup() {
   F.ticket_base = 0;
   CAP_CUDA(cudaStreamSynchronize(c.st));
   F.ready = true;
+  return CAPPGPU_OK;
+}
+
+int fast32_setup() {
+  if (G.ready) return CAPPGPU_OK;
+  Ctx& c = ctx();
+  const size_t n = (size_t)F.g.size();
+  for (int q = 0; q < E_NBUF; ++q) {
+    if (cudaMalloc(&G.e[q], n * sizeof(float)) != cudaSuccess) { fast32_release(); set_error("out of device memory"); return CAPPGPU_E_NOMEM; }
+    CAP_CUDA(cudaMemsetAsync(G.e[q], 0, n * sizeof(float), c.st));
+  }
+  if (cudaMalloc(&G.fq, 4 * n * sizeof(float)) != cudaSuccess || cudaMalloc(&G.bq, 3 * n * sizeof(float)) != cudaSuccess) {
+    fast32_release();
+    set_error("out of device memory");
+    return CAPPGPU_E_NOMEM;
+  }
+  CAP_CUDA(cudaMemsetAsync(G.fq, 0, 4 * n * sizeof(float), c.st));
+  CAP_CUDA(cudaMemsetAsync(G.bq, 0, 3 * n * sizeof(float), c.st));
+  int rc = CAPPGPU_OK;
+  for (int q = 0; q < E_NBUF && !rc; ++q) rc = make_map(&G.map[q], G.e[q], 1, 4);
+  if (!rc) rc = make_map(&G.map_fq, G.fq, 4, 4);
+  if (!rc) rc = make_map(&G.map_bq, G.bq, 3, 4);
+  if (rc) { fast32_release(); return rc; }
+  G.ready = true;
   return CAPPGPU_OK;
 }
 
@@ -317,6 +367,86 @@ __global__ void k_resid_d(DG g, const double* __restrict__ ae, const double* __r
   block_reduce_store<1>(v, part);
 }
 
+
+// ---------------------------------------- FP32 + FP64-refinement kernels
+// D-layout FP64 -> FP32 copy of the cells
+__global__ void k_d_to_f(DG g, const double* __restrict__ src, float* __restrict__ dst) {
+  D_LOOP(g) {
+    int a, b, c;
+    if (!d_cell(g, t_, a, b, c)) continue;
+    dst[t_] = (float)src[t_];
+  }
+}
+
+// x += dx (the refinement step)
+__global__ void k_add_f(DG g, double* __restrict__ x, const float* __restrict__ dx) {
+  D_LOOP(g) {
+    int a, b, c;
+    if (!d_cell(g, t_, a, b, c)) continue;
+    x[t_] = x[t_] + (double)dx[t_];
+  }
+}
+
+// partial sums of a.b (FP32 products and per-thread sums, FP64 across threads)
+__global__ void k_dot_f(DG g, const float* __restrict__ x, const float* __restrict__ y, double* part) {
+  float acc = 0.0f;
+  D_LOOP(g) {
+    int a, b, c;
+    if (!d_cell(g, t_, a, b, c)) continue;
+    acc += x[t_] * y[t_];
+  }
+  double v[1] = {(double)acc};
+  block_reduce_store<1>(v, part);
+}
+
+// pk_new = z + bet pk_old at the cell and its neighbours (FP32 arithmetic is
+// cheap on GB300, so the neighbours' values are recomputed rather than
+// stored), zz = A pk_new, partial sums of pk_new.zz
+__global__ void k_pk_spmv_f(DG g, const float* __restrict__ ae, const float* __restrict__ aw,
+                            const float* __restrict__ an, const float* __restrict__ as,
+                            const float* __restrict__ at, const float* __restrict__ ab,
+                            const float* __restrict__ ap, const float* __restrict__ zk,
+                            const float* __restrict__ pko, float* __restrict__ pkn, float* __restrict__ zz,
+                            const double* __restrict__ scal, double* part) {
+  const float bet = (float)scal[4];
+  float acc = 0.0f;
+  D_LOOP(g) {
+    int a, b, c;
+    if (!d_cell(g, t_, a, b, c)) continue;
+    const long long P = t_;
+    auto pnew = [&](long long q) { return zk[q] + bet * pko[q]; };
+    const float pP = pnew(P);
+    const float pE = a + 1 < g.Ni ? pnew(P + g.plane + 1) : 0.0f;
+    const float pW = a > 0 ? pnew(P - g.plane - 1) : 0.0f;
+    const float pN = b + 1 < g.Nj ? pnew(P + g.plane) : 0.0f;
+    const float pS = b > 0 ? pnew(P - g.plane) : 0.0f;
+    const float pT = c + 1 < g.Nk ? pnew(P + g.plane + g.P) : 0.0f;
+    const float pB = c > 0 ? pnew(P - g.plane - g.P) : 0.0f;
+    const float r = ap[P] * pP - ae[P] * pE - aw[P] * pW - an[P] * pN - as[P] * pS - at[P] * pT - ab[P] * pB;
+    pkn[P] = pP;
+    zz[P] = r;
+    acc += pP * r;
+  }
+  double v[1] = {(double)acc};
+  block_reduce_store<1>(v, part);
+}
+
+// x += alf pk; r -= alf zz; partial sums |r|
+__global__ void k_update_f(DG g, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ pk,
+                           const float* __restrict__ zz, const double* __restrict__ scal, double* part) {
+  const float alf = (float)scal[3];
+  float acc = 0.0f;
+  D_LOOP(g) {
+    int a, b, c;
+    if (!d_cell(g, t_, a, b, c)) continue;
+    x[t_] = x[t_] + alf * pk[t_];
+    const float rr = r[t_] - alf * zz[t_];
+    r[t_] = rr;
+    acc += fabsf(rr);
+  }
+  double v[1] = {(double)acc};
+  block_reduce_store<1>(v, part);
+}
 
 }  // namespace
 
@@ -518,6 +648,125 @@ int sipsol_fast(int fif, int ifi, cappgpu_solve_report* rep) {
     rep->status = done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
   }
   if (!isfinite(res1)) {
+    set_error("linear solver residual is not finite");
+    if (rep) rep->status = CAPPGPU_E_NONFINITE;
+    return CAPPGPU_E_NONFINITE;
+  }
+  return done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+}
+
+// pcgsip in the FP32 + FP64-refinement form (cappgpu_precision(1)).
+// Outer loop in FP64: r = su - A fi over the interior with the reference's
+// residual (pcg-sip.f90:150-165) and its exit test resl/res0 < sor(ifi)
+// (pcg-sip.f90:283-289).  Inner loop: conjugate gradients on A d = r in
+// FP32 with the FP32 SIP preconditioner (factorisation and substitutions as
+// wavefronts), stopped once the FP32 residual has dropped far enough for the
+// FP64 test or by the FP32 floor; then fi += d.  iters counts inner
+// iterations; nsw(ifi) bounds them.
+int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  cappgpu_params& P = c.prm;
+  int rc = fast_setup();
+  if (rc) return rc;
+  if ((rc = fast32_setup())) return rc;
+  CAP_CUDA(cudaMemsetAsync(F.flags, 0, sizeof(int) * 2, c.st));
+  const double resmax = P.sor[ifi - 1];
+  const int ns = P.nsw[ifi - 1];
+  CAP_CUDA(cudaMemsetAsync(c.f[CAP_RES], 0, sizeof(double) * d.nijk, c.st));
+  double res0 = 0.0;
+  if ((rc = resid_natural(fif, &res0))) return rc;
+  P.resor[ifi - 1] = res0;
+  const int cf[8] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_SU};
+  for (int q = 0; q < 8; ++q)
+    if ((rc = to_d(cf[q], D_AE + q))) return rc;
+  if ((rc = to_d(fif, D_FI))) return rc;
+  const DG& g = F.g;
+  for (int q = 0; q < 7; ++q)
+    launch(k_d_to_f, grid_for(g.size()), kThreads, c.st, g, (const double*)F.d[D_AE + q], G.e[E_AE + q]);
+  CAP_CHECK_LAUNCH();
+  {   // FP32 SIP factorisation
+    SipFactorF op;
+    for (int q = 0; q < 7; ++q) op.map[q] = G.map[E_AE + q];
+    op.bnn = c.f[CAP_BN];
+    op.ben = c.f[CAP_BE];
+    op.btn = c.f[CAP_BT];
+    op.fq = G.fq;
+    op.bq = G.bq;
+    op.alfa = (float)P.alfa;
+    if ((rc = run_wave<SipFactorF, false>(op))) return rc;
+  }
+  SipFwdF fwd;
+  fwd.map[0] = G.map[E_R];
+  fwd.map[1] = G.map_fq;
+  fwd.z = G.e[E_Z];
+  SipBwdF bwd;
+  bwd.map[0] = G.map[E_Z];
+  bwd.map[1] = G.map_bq;
+  bwd.z = G.e[E_Z];
+  const size_t nf = sizeof(float) * (size_t)g.size();
+  int total = 0;
+  double resl = res0;
+  bool done = false, bad = false;
+  for (int outer = 0; outer < 64; ++outer) {
+    // FP64 residual of the current iterate and its L1 norm
+    launch(k_resid_d, kRedBlocks, kThreads, c.st, g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
+           (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
+           (const double*)F.d[D_AP], (const double*)F.d[D_SU], (const double*)F.d[D_FI], (const double*)c.f[fif],
+           F.d[D_RES], c.partials);
+    launch(k_cg_scalars, 1, 32, c.st, 3, (const double*)c.partials, kRedBlocks, c.dscal);
+    CAP_CHECK_LAUNCH();
+    CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 6, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    CAP_CUDA(cudaStreamSynchronize(c.st));
+    resl = F.hres[0];
+    if (!isfinite(resl)) { bad = true; break; }
+    if (resl / (res0 + CAP_SMALL) < resmax) { done = true; break; }
+    if (total >= ns) break;
+    // inner FP32 conjugate gradients on A d = r, d = 0
+    launch(k_d_to_f, grid_for(g.size()), kThreads, c.st, g, (const double*)F.d[D_RES], G.e[E_R]);
+    CAP_CHECK_LAUNCH();
+    CAP_CUDA(cudaMemsetAsync(G.e[E_X], 0, nf, c.st));
+    CAP_CUDA(cudaMemsetAsync(G.e[E_P0], 0, nf, c.st));
+    launch(k_set_scal, 1, 1, c.st, c.dscal, (double)1.e20f);
+    // reduce the residual far enough for the FP64 test, not below what FP32 holds
+    const double target = fmax(0.5 * resmax * res0, 2e-5 * resl);
+    int cur = 0;
+    for (;;) {
+      if ((rc = run_wave<SipFwdF, false>(fwd))) return rc;
+      if ((rc = run_wave<SipBwdF, true>(bwd))) return rc;
+      launch(k_dot_f, kRedBlocks, kThreads, c.st, g, (const float*)G.e[E_R], (const float*)G.e[E_Z], c.partials);
+      launch(k_cg_scalars, 1, 32, c.st, 0, (const double*)c.partials, kRedBlocks, c.dscal);
+      float* pko = G.e[cur ? E_P1 : E_P0];
+      float* pkn = G.e[cur ? E_P0 : E_P1];
+      launch(k_pk_spmv_f, kRedBlocks, kThreads, c.st, g, (const float*)G.e[E_AE], (const float*)G.e[E_AW],
+             (const float*)G.e[E_AN], (const float*)G.e[E_AS], (const float*)G.e[E_AT], (const float*)G.e[E_AB],
+             (const float*)G.e[E_AP], (const float*)G.e[E_Z], (const float*)pko, pkn, G.e[E_ZZ],
+             (const double*)c.dscal, c.partials);
+      launch(k_cg_scalars, 1, 32, c.st, 1, (const double*)c.partials, kRedBlocks, c.dscal);
+      launch(k_update_f, kRedBlocks, kThreads, c.st, g, G.e[E_X], G.e[E_R], (const float*)pkn,
+             (const float*)G.e[E_ZZ], (const double*)c.dscal, c.partials);
+      launch(k_cg_scalars, 1, 32, c.st, 2, (const double*)c.partials, kRedBlocks, c.dscal);
+      CAP_CHECK_LAUNCH();
+      cur ^= 1;
+      ++total;
+      CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 5, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+      CAP_CUDA(cudaStreamSynchronize(c.st));
+      if ((rc = check_wave_error())) return rc;
+      const double rin = F.hres[0];
+      if (!isfinite(rin) || rin <= target || total >= ns) break;
+    }
+    launch(k_add_f, grid_for(g.size()), kThreads, c.st, g, F.d[D_FI], (const float*)G.e[E_X]);
+    CAP_CHECK_LAUNCH();
+  }
+  if ((rc = from_d(D_FI, fif))) return rc;
+  if ((rc = from_d(D_RES, CAP_RES))) return rc;
+  if (rep) {
+    rep->res0 = res0;
+    rep->resl = resl;
+    rep->iters = total;
+    rep->status = done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+  }
+  if (bad) {
     set_error("linear solver residual is not finite");
     if (rep) rep->status = CAPPGPU_E_NONFINITE;
     return CAPPGPU_E_NONFINITE;

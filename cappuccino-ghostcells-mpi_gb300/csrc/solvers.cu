@@ -223,7 +223,8 @@ int resid_natural(int fif, double* res0) {
 
 int pcgsip(int fif, int ifi, cappgpu_solve_report* rep) {
   Ctx& c = ctx();
-  if (c.wave_impl == 1 && c.d.nimm >= 4 && c.d.njmm >= 4 && c.d.nkmm >= 4) return pcgsip_fast(fif, ifi, rep);
+  if (c.wave_impl == 1 && c.d.nimm >= 4 && c.d.njmm >= 4 && c.d.nkmm >= 4)
+    return c.precision == 1 ? pcgsip_mixed(fif, ifi, rep) : pcgsip_fast(fif, ifi, rep);
   const Dims& d = c.d;
   double** F = c.f;
   cappgpu_params& P = c.prm;

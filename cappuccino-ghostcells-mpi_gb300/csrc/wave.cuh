@@ -56,24 +56,26 @@ struct WaveCtl {
 };
 
 constexpr int kG = 4;        // hyperplanes per TMA copy
-constexpr int kSlots = 3;    // copies in flight
+constexpr int kMaxSlots = 8; // copies in flight (per op: Op::kSlots)
 constexpr int kRing = 32;    // planes of staged edge states
 constexpr int kPW = 8;       // edge planes examined per communication pass
 constexpr unsigned long long kSentinel = 0x7FF0DEAD5EA1F00DULL;   // signalling NaN
 // a slot is refilled at the start of the next group, so two slots at least;
 // the ring holds the planes between two updates of the consumed-plane count
-static_assert(kSlots >= 2, "TMA slots");
 static_assert(kRing >= kG + 3, "edge ring capacity");
 
 __host__ __device__ constexpr int ring_slot(int q) { return (q + kRing) % kRing; }   // valid for q >= -kRing
 
-// Shared-memory input slots: per map a box of (BA+2) x NQ x BC x kG doubles
-// (the two extra columns let a mirrored block start on an even, 16-byte
-// aligned column).
+// Shared-memory input slots: per map a box of (BA + 16/esize) x NQ x BC x kG
+// elements (the extra columns let a mirrored block start its copy on a
+// 16-byte aligned column).
 template <class Op, int BA, int BC>
 struct WaveLayout {
-  static constexpr int kBW = BA + 2;
-  __host__ __device__ static constexpr size_t map_bytes(int m) { return (size_t)kBW * BC * kG * Op::nq(m) * 8; }
+  __host__ __device__ static constexpr int align(int m) { return 16 / Op::esize(m); }   // elements per 16 bytes
+  __host__ __device__ static constexpr int bw(int m) { return BA + align(m); }
+  __host__ __device__ static constexpr size_t map_bytes(int m) {
+    return (size_t)bw(m) * BC * kG * Op::nq(m) * Op::esize(m);
+  }
   __host__ __device__ static constexpr size_t map_off(int m) {
     size_t o = 0;
     for (int q = 0; q < m; ++q) o += map_bytes(q);
@@ -81,7 +83,26 @@ struct WaveLayout {
   }
   static constexpr size_t tx_bytes = map_off(Op::kMaps);
   static constexpr size_t slot_bytes = (tx_bytes + 127) / 128 * 128;
-  static constexpr size_t in_bytes = kSlots * slot_bytes;
+  static constexpr size_t in_bytes = Op::kSlots * slot_bytes;
+  static_assert(Op::kSlots >= 2 && Op::kSlots <= kMaxSlots, "TMA slots");
+};
+
+// The compute thread's view of its inputs in one slot: element q of map m
+// at the current plane and line.
+template <class Op, int BA, int BC>
+struct InView {
+  using L = WaveLayout<Op, BA, BC>;
+  const unsigned char* slot;
+  int zb, yb, xb8, xb4;   // plane and row in the box; column for 8- and 4-byte maps
+  __device__ __forceinline__ int at(int m, int q) const {
+    return ((zb * BC + yb) * Op::nq(m) + q) * L::bw(m) + (Op::esize(m) == 8 ? xb8 : xb4);
+  }
+  __device__ __forceinline__ double d(int m, int q) const {
+    return reinterpret_cast<const double*>(slot + L::map_off(m))[at(m, q)];
+  }
+  __device__ __forceinline__ float f(int m, int q) const {
+    return reinterpret_cast<const float*>(slot + L::map_off(m))[at(m, q)];
+  }
 };
 
 template <class St, int BA, int BC>
@@ -89,7 +110,7 @@ struct WaveSmem {
   St sbuf[2][BC][BA];                      // states of the two latest planes
   St ringW[kRing][BC];                     // W edge states by plane
   St ringB[kRing][BA];                     // B edge states by plane
-  unsigned long long full[kSlots];
+  unsigned long long full[kMaxSlots];
   unsigned long long stagedW, stagedB;     // edge planes <= value-2 are staged
   double red[BA * BC / 32];
   int done;                                // compute steps < done finished (updated per copy group)
@@ -119,9 +140,12 @@ __device__ __forceinline__ void wave_fail(const WaveCtl& w, volatile int* bail, 
 // plane q belongs to consumer line (av, cv) = line(e) whose predecessor line
 // (pa, pc) is read either from the producer block's mailbox (mail[e][bv]) or,
 // on the domain boundary, from the ghost layer.
+template <class St>
+__host__ __device__ constexpr int state_words() { return (int)((sizeof(St) + 7) / 8); }   // 8-byte mailbox words per state
+
 template <class St, int R>
 struct EdgeProbe {
-  unsigned long long u[R][sizeof(St) / 8];
+  unsigned long long u[R][state_words<St>()];
   bool need[R];   // the consumer cell exists
   bool inwin[R];  // plane within the window this pass may stage
 };
@@ -130,7 +154,7 @@ template <class Op, int E, bool BWD, class LineFn>
 __device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, kPW * E / 32>& P, const Op& op, const DG& g,
                                            int lane, int loaded, int hi, const double* mail, LineFn line) {
   using St = typename Op::St;
-  constexpr int NS = sizeof(St) / 8;
+  constexpr int NS = state_words<St>();
 #pragma unroll
   for (int r = 0; r < kPW * E / 32; ++r) {
     const int x = lane + 32 * r, j = x / E, e = x % E, q = loaded + 1 + j;
@@ -149,6 +173,8 @@ __device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, kPW * E / 
         const int b = BWD ? g.Nj - 1 - bv : bv;
         const int c = BWD ? g.Nk - 1 - pc : pc;
         const St v = op.ghost(g.nat(a, b, c));
+#pragma unroll
+        for (int k = 0; k < NS; ++k) P.u[r][k] = 0;
         memcpy(P.u[r], &v, sizeof(St));
       }
     }
@@ -158,7 +184,7 @@ __device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, kPW * E / 
 template <class St, int E, class LineFn>
 __device__ __forceinline__ int commit_edge(EdgeProbe<St, kPW * E / 32>& P, const DG& g, int lane, int loaded,
                                            double* mail, St (*ring)[E], LineFn line) {
-  constexpr int NS = sizeof(St) / 8;
+  constexpr int NS = state_words<St>();
   constexpr int R = kPW * E / 32;
   unsigned bal[R];
 #pragma unroll
@@ -199,7 +225,8 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
   using St = typename Op::St;
   using L = WaveLayout<Op, BA, BC>;
   constexpr int NC = BA * BC;
-  constexpr int NS = sizeof(St) / 8;
+  constexpr int NS = state_words<St>();
+  constexpr int NSLOT = Op::kSlots;
   static_assert(NC % 32 == 0, "block shape");
   static_assert(32 % BC == 0 && (kPW * BC) % 32 == 0 && (kPW * BA) % 32 == 0, "edge staging shape");
   extern __shared__ unsigned char smem_raw[];
@@ -213,7 +240,7 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
     sm.stagedB = 0;
     sm.done = 0;
     sm.bail = 0;
-    for (int k = 0; k < kSlots; ++k) mbar_init(&sm.full[k], 1);
+    for (int k = 0; k < NSLOT; ++k) mbar_init(&sm.full[k], 1);
     mbar_fence_init();
     unsigned t = atomicAdd(w.ticket, 1u) - w.ticket_base;
     if (t < (unsigned)w.nblk) {
@@ -243,26 +270,20 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
     // ------------------------------------------------------- pacing warp
     const int lane = tid - (NC + 32);
     auto issue = [&](int gq) {   // TMA copy of group gq (planes s0 + gq*kG ...) into its slot
-      const int slot = gq % kSlots, sg = s0 + gq * kG;
-      int x0, y0, z0;
-      if (!BWD) {
-        x0 = ba * BA;
-        y0 = bc * BC;
-        z0 = sg;
-      } else {
-        x0 = (g.Ni - (ba + 1) * BA) & ~1;   // even: 16-byte aligned start
-        y0 = g.Nk - (bc + 1) * BC;
-        z0 = g.S - sg - kG;
-      }
+      const int slot = gq % NSLOT, sg = s0 + gq * kG;
+      const int alo = BWD ? g.Ni - (ba + 1) * BA : ba * BA;   // first column of the block's lines
+      const int y0 = BWD ? g.Nk - (bc + 1) * BC : bc * BC;
+      const int z0 = BWD ? g.S - sg - kG : sg;
       unsigned char* dst = inbuf + slot * L::slot_bytes;
       mbar_arrive_tx(&sm.full[slot], (unsigned)L::tx_bytes);
 #pragma unroll
       for (int m = 0; m < Op::kMaps; ++m) {
+        const int x0 = alo & ~(L::align(m) - 1);   // 16-byte aligned start
         if (Op::nq(m) == 1) tma_load3(dst + L::map_off(m), &op.map[m], x0, y0, z0, &sm.full[slot]);
         else tma_load4(dst + L::map_off(m), &op.map[m], x0, 0, y0, z0, &sm.full[slot]);
       }
     };
-    int issued = min(kSlots, ngroups);
+    int issued = min(NSLOT, ngroups);
     if (lane == 0)
       for (int gq = 0; gq < issued; ++gq) issue(gq);
     unsigned long long knownW = 0, knownB = 0;
@@ -272,7 +293,7 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
       if (lane == 0) {
         if (ds == 0) {   // the copy of this group of planes has landed
           long long it = 0;
-          while (!mbar_test(&sm.full[gi % kSlots], (unsigned)((gi / kSlots) & 1))) {
+          while (!mbar_test(&sm.full[gi % NSLOT], (unsigned)((gi / NSLOT) & 1))) {
             if (*bail) { st = 1; break; }
             if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); st = 1; break; }
           }
@@ -290,13 +311,12 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
           }
         }
       }
-      st = __shfl_sync(0xffffffffu, st, 0);
-      if (named_bar_red_or(1, NC + 32, st != 0)) break;   // the compute warps start step s
+      if (named_bar_red_or(1, NC + 32, st != 0)) break;   // (only lane 0's flag can be set) the compute warps start step s
       if (lane == 0 && ds == 0 && gi > 0) {
         // step s-1 is complete: the edge rings up to plane s-2 and the slot
         // of the previous group are free
         *(volatile int*)&sm.done = s;
-        const int gq = gi - 1 + kSlots;
+        const int gq = gi - 1 + NSLOT;
         if (gq < ngroups) {
           fence_proxy_async_smem();
           issue(gq);
@@ -307,9 +327,9 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
     }
     // the copies in flight land before the block exits
     if (lane == 0) {
-      for (int gq = max(0, issued - kSlots); gq < issued; ++gq) {
+      for (int gq = max(0, issued - NSLOT); gq < issued; ++gq) {
         long long it = 0;
-        while (!mbar_test(&sm.full[gq % kSlots], (unsigned)((gq / kSlots) & 1))) {
+        while (!mbar_test(&sm.full[gq % NSLOT], (unsigned)((gq / NSLOT) & 1))) {
           if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); break; }
         }
       }
@@ -370,14 +390,16 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
   const int a = BWD ? g.Ni - 1 - av : av;
   const int c = BWD ? g.Nk - 1 - cv : cv;
   const int sfirst = av + cv;                         // step of this line's first cell
-  int xb, yb;                                         // this line's column and row in an input box
+  InView<Op, BA, BC> in;                              // this line's column and row in an input box
   if (!BWD) {
-    xb = al;
-    yb = cl;
+    in.xb8 = al;
+    in.xb4 = al;
+    in.yb = cl;
   } else {
     const int alo = g.Ni - (ba + 1) * BA;
-    xb = (alo - (alo & ~1)) + BA - 1 - al;
-    yb = BC - 1 - cl;
+    in.xb8 = (alo - (alo & ~1)) + BA - 1 - al;
+    in.xb4 = (alo - (alo & ~3)) + BA - 1 - al;
+    in.yb = BC - 1 - cl;
   }
   const bool edgeE = al == BA - 1 && ba + 1 < w.nBA;   // feeds the next block along a
   const bool edgeT = cl == BC - 1 && bc + 1 < w.nBC;   // feeds the next block along c
@@ -395,16 +417,15 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
       const St W = al > 0 ? sm.sbuf[(s - 1) & 1][cl][al - 1] : sm.ringW[ring_slot(s - 1)][cl];
       const St B = cl > 0 ? sm.sbuf[(s - 1) & 1][cl - 1][al] : sm.ringB[ring_slot(s - 1)][al];
       const St S = bv > 0 ? prevS : sg;
-      const double* slotp = reinterpret_cast<const double*>(inbuf + (gi % kSlots) * L::slot_bytes);
-      const int zb = BWD ? kG - 1 - ds : ds;
-      auto in = [&](int m, int q) -> double {
-        return slotp[L::map_off(m) / 8 + ((zb * BC + yb) * Op::nq(m) + q) * L::kBW + xb];
-      };
+      in.slot = inbuf + (gi % NSLOT) * L::slot_bytes;
+      in.zb = BWD ? kG - 1 - ds : ds;
       const St out = op.compute(in, g, a, b, c, W, S, B, part);
       sm.sbuf[s & 1][cl][al] = out;
       prevS = out;
       if (edgeE || edgeT) {
         unsigned long long u[NS];
+#pragma unroll
+        for (int k = 0; k < NS; ++k) u[k] = 0;
         memcpy(u, &out, sizeof(St));
 #pragma unroll
         for (int k = 0; k < NS; ++k) {
@@ -444,14 +465,16 @@ struct SipFwdD {
   using St = double;
   static constexpr int kMaps = 2;   // r, forward factors (bb, bw, bs, bp)
   static constexpr bool kReduce = false;
+  static constexpr int kSlots = 3;
   __host__ __device__ static constexpr int nq(int m) { return m == 0 ? 1 : 4; }
+  __host__ __device__ static constexpr int esize(int) { return 8; }
   CUtensorMap map[kMaps];
   double* z;                  // hyperplane layout (output; may alias r)
   const double* ghost_src;    // natural array of ghost values, or null (zero)
   __device__ St ghost(int nat) const { return ghost_src ? ghost_src[nat] : 0.0; }
   template <class In>
   __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
-    const double v = (in(0, 0) - in(1, 0) * B - in(1, 1) * W - in(1, 2) * S) * in(1, 3);
+    const double v = (in.d(0, 0) - in.d(1, 0) * B - in.d(1, 1) * W - in.d(1, 2) * S) * in.d(1, 3);
     z[g.d(a, b, c)] = v;
     return v;
   }
@@ -464,16 +487,18 @@ struct SipBwdD {
   using St = double;
   static constexpr int kMaps = 3;   // z, backward factors (bn, be, bt), res
   static constexpr bool kReduce = true;
+  static constexpr int kSlots = 3;
   __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
+  __host__ __device__ static constexpr int esize(int) { return 8; }
   CUtensorMap map[kMaps];
   double* z;
   const double* ghost_src;
   __device__ St ghost(int nat) const { return ghost_src ? ghost_src[nat] : 0.0; }
   template <class In>
   __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double& part) const {
-    const double v = in(0, 0) - in(1, 0) * S - in(1, 1) * W - in(1, 2) * B;
+    const double v = in.d(0, 0) - in.d(1, 0) * S - in.d(1, 1) * W - in.d(1, 2) * B;
     z[g.d(a, b, c)] = v;
-    part += in(2, 0) * v;
+    part += in.d(2, 0) * v;
     return v;
   }
 };
@@ -483,7 +508,9 @@ struct SipBwdFiD {
   using St = double;
   static constexpr int kMaps = 3;   // z, backward factors, fi
   static constexpr bool kReduce = false;
+  static constexpr int kSlots = 3;
   __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
+  __host__ __device__ static constexpr int esize(int) { return 8; }
   CUtensorMap map[kMaps];
   double* z;
   double* fi;                 // hyperplane layout
@@ -491,10 +518,10 @@ struct SipBwdFiD {
   __device__ St ghost(int nat) const { return ghost_src[nat]; }
   template <class In>
   __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
-    const double v = in(0, 0) - in(1, 0) * S - in(1, 1) * W - in(1, 2) * B;
+    const double v = in.d(0, 0) - in.d(1, 0) * S - in.d(1, 1) * W - in.d(1, 2) * B;
     const long long di = g.d(a, b, c);
     z[di] = v;
-    fi[di] = in(2, 0) + v;
+    fi[di] = in.d(2, 0) + v;
     return v;
   }
 };
@@ -504,7 +531,9 @@ struct SipFactorD {
   using St = St3;
   static constexpr int kMaps = 7;   // ae, aw, an, as, at, ab, ap
   static constexpr bool kReduce = false;
+  static constexpr int kSlots = 3;
   __host__ __device__ static constexpr int nq(int) { return 1; }
+  __host__ __device__ static constexpr int esize(int) { return 8; }
   CUtensorMap map[kMaps];
   double *bbn, *bwn, *bsn, *bpn, *bnn, *ben, *btn;  // natural layout outputs (module coefb)
   double* fq;                                       // forward factors, 4 components
@@ -513,16 +542,16 @@ struct SipFactorD {
   __device__ St ghost(int nat) const { return St3{bnn[nat], ben[nat], btn[nat]}; }
   template <class In>
   __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
-    const double bbv = -in(5, 0) / (1.0 + alfa * (B.bn + B.be));
-    const double bwv = -in(1, 0) / (1.0 + alfa * (W.bn + W.bt));
-    const double bsv = -in(3, 0) / (1.0 + alfa * (S.be + S.bt));
+    const double bbv = -in.d(5, 0) / (1.0 + alfa * (B.bn + B.be));
+    const double bwv = -in.d(1, 0) / (1.0 + alfa * (W.bn + W.bt));
+    const double bsv = -in.d(3, 0) / (1.0 + alfa * (S.be + S.bt));
     const double p1 = alfa * (bbv * B.bn + bwv * W.bn);
     const double p2 = alfa * (bbv * B.be + bsv * S.be);
     const double p3 = alfa * (bwv * W.bt + bsv * S.bt);
-    const double bpv = 1.0 / (in(6, 0) + p1 + p2 + p3 - bbv * B.bt - bwv * W.be - bsv * S.bn + CAP_SMALL);
-    const double bnv = (-in(2, 0) - p1) * bpv;
-    const double bev = (-in(0, 0) - p2) * bpv;
-    const double btv = (-in(4, 0) - p3) * bpv;
+    const double bpv = 1.0 / (in.d(6, 0) + p1 + p2 + p3 - bbv * B.bt - bwv * W.be - bsv * S.bn + CAP_SMALL);
+    const double bnv = (-in.d(2, 0) - p1) * bpv;
+    const double bev = (-in.d(0, 0) - p2) * bpv;
+    const double btv = (-in.d(4, 0) - p3) * bpv;
     const int nat = g.nat(a, b, c);
     bbn[nat] = bbv; bwn[nat] = bwv; bsn[nat] = bsv; bpn[nat] = bpv;
     bnn[nat] = bnv; ben[nat] = bev; btn[nat] = btv;
@@ -534,6 +563,87 @@ struct SipFactorD {
     bq[g.dq(a, b, c, 1, 3)] = bev;
     bq[g.dq(a, b, c, 2, 3)] = btv;
     return St3{bnv, bev, btv};
+  }
+};
+
+// ------------------------------------------------- single-precision ops
+// The preconditioner of the FP32 + FP64-refinement form of the pressure
+// solve: the same SIP recurrences (pcg-sip.f90:178-223) on FP32 copies of
+// the matrix, FP32 arithmetic, zero ghost states for the substitutions.
+// These do not reproduce the reference's FP64 results bit for bit and are
+// not meant to; the refinement loop around them restores the FP64 residual.
+
+struct St3f { float bn, be, bt; };
+
+struct SipFwdF {
+  using St = float;
+  static constexpr int kMaps = 2;   // r, forward factors (bb, bw, bs, bp)
+  static constexpr bool kReduce = false;
+  static constexpr int kSlots = 6;
+  __host__ __device__ static constexpr int nq(int m) { return m == 0 ? 1 : 4; }
+  __host__ __device__ static constexpr int esize(int) { return 4; }
+  CUtensorMap map[kMaps];
+  float* z;
+  __device__ St ghost(int) const { return 0.0f; }
+  template <class In>
+  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+    const float v = (in.f(0, 0) - in.f(1, 0) * B - in.f(1, 1) * W - in.f(1, 2) * S) * in.f(1, 3);
+    z[g.d(a, b, c)] = v;
+    return v;
+  }
+};
+
+struct SipBwdF {
+  using St = float;
+  static constexpr int kMaps = 2;   // z, backward factors (bn, be, bt)
+  static constexpr bool kReduce = false;
+  static constexpr int kSlots = 6;
+  __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
+  __host__ __device__ static constexpr int esize(int) { return 4; }
+  CUtensorMap map[kMaps];
+  float* z;
+  __device__ St ghost(int) const { return 0.0f; }
+  template <class In>
+  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+    const float v = in.f(0, 0) - in.f(1, 0) * S - in.f(1, 1) * W - in.f(1, 2) * B;
+    z[g.d(a, b, c)] = v;
+    return v;
+  }
+};
+
+struct SipFactorF {
+  using St = St3f;
+  static constexpr int kMaps = 7;   // ae, aw, an, as, at, ab, ap (FP32 copies)
+  static constexpr bool kReduce = false;
+  static constexpr int kSlots = 4;
+  __host__ __device__ static constexpr int nq(int) { return 1; }
+  __host__ __device__ static constexpr int esize(int) { return 4; }
+  CUtensorMap map[kMaps];
+  const double *bnn, *ben, *btn;   // module factors: the ghost-layer states the factorisation reads
+  float* fq;                       // forward factors, 4 components
+  float* bq;                       // backward factors, 3 components
+  float alfa;
+  __device__ St ghost(int nat) const { return St3f{(float)bnn[nat], (float)ben[nat], (float)btn[nat]}; }
+  template <class In>
+  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+    const float bbv = -in.f(5, 0) / (1.0f + alfa * (B.bn + B.be));
+    const float bwv = -in.f(1, 0) / (1.0f + alfa * (W.bn + W.bt));
+    const float bsv = -in.f(3, 0) / (1.0f + alfa * (S.be + S.bt));
+    const float p1 = alfa * (bbv * B.bn + bwv * W.bn);
+    const float p2 = alfa * (bbv * B.be + bsv * S.be);
+    const float p3 = alfa * (bwv * W.bt + bsv * S.bt);
+    const float bpv = 1.0f / (in.f(6, 0) + p1 + p2 + p3 - bbv * B.bt - bwv * W.be - bsv * S.bn + 1e-30f);
+    const float bnv = (-in.f(2, 0) - p1) * bpv;
+    const float bev = (-in.f(0, 0) - p2) * bpv;
+    const float btv = (-in.f(4, 0) - p3) * bpv;
+    fq[g.dq(a, b, c, 0, 4)] = bbv;
+    fq[g.dq(a, b, c, 1, 4)] = bwv;
+    fq[g.dq(a, b, c, 2, 4)] = bsv;
+    fq[g.dq(a, b, c, 3, 4)] = bpv;
+    bq[g.dq(a, b, c, 0, 3)] = bnv;
+    bq[g.dq(a, b, c, 1, 3)] = bev;
+    bq[g.dq(a, b, c, 2, 3)] = btv;
+    return St3f{bnv, bev, btv};
   }
 };
 

@@ -58,6 +58,7 @@ SIGNATURES = {
     "cappgpu_cgstab_sip_h": [_DP, _INT],
     "cappgpu_spmv": [_INT, _INT, _DP],
     "cappgpu_spmv_noalloc": [_INT, _INT, _DP],
+    "cappgpu_precision": [_INT],
     "cappgpu_fluxuvw": [_INT] * 10,
     "cappgpu_calcuvw": [_REP],
     "cappgpu_piso_assemble_pressure_eq": [_INT] * 12,
@@ -241,6 +242,10 @@ class Library:
 
     def dpcg(self, fi, ifi):
         return self.solve("dpcg", fi, ifi)
+
+    def precision(self, mode):
+        """0 = FP64 plain (reference arithmetic), 1 = FP32 preconditioned CG in FP64 refinement."""
+        self._check(self.lib.cappgpu_precision(int(mode)), "precision")
 
     def spmv(self, pk, zk):
         dot = ctypes.c_double()

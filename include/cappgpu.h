@@ -193,6 +193,16 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    hyperplane (the simple form, kept for cross-checks). */
 int cappgpu_set_option(const char* key, int value);
 
+/* Precision of the pressure solve (cappgpu_pcgsip and the PISO correctors
+   that call it).  0 = FP64 plain, the reference's arithmetic (default).
+   1 = the SIP factors and both substitutions in FP32 inside conjugate
+   gradients in FP32, wrapped in FP64 iterative refinement: the exit test is
+   the reference's (L1 norm of the FP64 residual su - A fi over res0 below
+   sor(ifi)), the iterates are not the reference's.  Replaces the
+   reference's fixed FP64 arithmetic (pcg-sip.f90:3-200); returns
+   CAPPGPU_E_ARG for other modes. */
+int cappgpu_precision(int mode);
+
 /* ======================================================= index maps (a1) */
 /* setind.f90:34-40: li(i)=(i-1)*nj for i=1..ni, lk(k)=(k-1)*nij.  Writes
    the device copies back (tests compare them element-wise). */

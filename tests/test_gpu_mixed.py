@@ -1,0 +1,66 @@
+"""The FP32 + FP64-refinement form of the pressure solve (cappgpu_precision(1)).
+
+Not bit-compatible with the reference by design: the checks are the
+reference's own exit test on the FP64 residual and closeness to the FP64
+plain solution."""
+import numpy as np
+import pytest
+
+import cappgpu
+from helpers import diag_dominant_matrix, push, randomize
+
+pytestmark = pytest.mark.gpu
+IP = 4
+
+
+def _state(oracle_mod, dims, seed, sor):
+    st = oracle_mod.State(*dims)
+    rng = np.random.default_rng(seed)
+    diag_dominant_matrix(st, rng, symmetric=True)
+    randomize(st, rng, ["bb", "bs", "bw", "bp", "bn", "be", "bt"], -0.3, 0.3)
+    randomize(st, rng, ["p", "res"])
+    st.params.update(dict(alfa=0.92, sor=[sor] * 10, nsw=[2000] * 10, ipr=3, jpr=3, kpr=3))
+    return st
+
+
+@pytest.mark.parametrize("dims,sor", [((14, 13, 12), 1e-8), ((40, 37, 35), 1e-6), ((21, 36, 19), 1e-10)])
+def test_mixed_pcgsip_meets_fp64_exit_test(gpu_lib, oracle_mod, dims, sor):
+    st = _state(oracle_mod, dims, 3, sor)
+    push(gpu_lib, st)
+    gpu_lib.precision(0)
+    r64 = gpu_lib.pcgsip("p", IP)
+    p64 = gpu_lib.get_field("p")
+    push(gpu_lib, st)
+    gpu_lib.precision(1)
+    try:
+        r32 = gpu_lib.pcgsip("p", IP)
+    finally:
+        gpu_lib.precision(0)
+    p32 = gpu_lib.get_field("p")
+    assert r32.status == 0 and r64.status == 0
+    assert r32.res0 == pytest.approx(r64.res0, rel=1e-12)
+    assert r32.resl / r32.res0 < sor                  # FP64 residual, the reference's test
+    # the module residual array holds the true FP64 residual of the result
+    ni, nj, nk = dims
+    res = gpu_lib.get_field("res").reshape(nk, ni, nj)[2:-2, 2:-2, 2:-2]
+    assert abs(np.abs(res).sum() - r32.resl) <= 1e-9 * r32.res0
+    # both solves stop within the tolerance of the exact solution
+    assert np.linalg.norm(p32 - p64) <= 1e3 * sor * np.linalg.norm(p64)
+
+
+def test_mixed_piso_step_channel(gpu_lib):
+    case = cappgpu.cases.channel(N=(10, 8, 12))
+    gpu_lib.load_case(case)
+    gpu_lib.precision(1)
+    try:
+        rep = gpu_lib.piso_steps(2)
+    finally:
+        gpu_lib.precision(0)
+    assert rep.status == 0
+    assert rep.resl / rep.res0 < case.params["sor"][IP - 1]
+
+
+def test_precision_rejects_unknown_mode(gpu_lib):
+    gpu_lib.init(8, 8, 8)
+    with pytest.raises(cappgpu.CappError):
+        gpu_lib.precision(2)
