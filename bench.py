@@ -285,7 +285,8 @@ def run_gpu(args, ws, rank, local):
     ms_fwd, bytes_fwd = lib.profile_kernel(0, reps=3)
     achieved = bytes_fwd / (ms_fwd / 1e3) / 1e9
     units = {}
-    for w, name in ((1, "sip_backward"), (2, "spmv_dot"), (6, "sip_factor"), (3, "grad_gauss")):
+    for w, name in ((1, "sip_backward"), (2, "spmv_dot"), (6, "sip_factor"), (3, "grad_gauss"),
+                    (7, "sip_forward_fp32"), (8, "sip_backward_fp32")):
         m, b = lib.profile_kernel(w, reps=3)
         units[name] = {"ms": m, "GBps": b / (m / 1e3) / 1e9}
 

@@ -32,7 +32,11 @@ struct DG {
   }
   // component q of NQ at (a,b,c)
   __host__ __device__ long long dq(int a, int b, int c, int q, int NQ) const {
-    return ((long long)(a + b + c) * Nk * NQ + (long long)c * NQ + q) * P + a;
+    return dqs(a + b + c, c, a, q, NQ);
+  }
+  // the same from the cell's hyperplane s = a+b+c
+  __host__ __device__ long long dqs(int s, int c, int a, int q, int NQ) const {
+    return ((long long)s * Nk * NQ + (long long)c * NQ + q) * P + a;
   }
   // 0-based natural index of interior-local (a,b,c); valid for a,b,c >= -1
   __host__ __device__ int nat(int a, int b, int c) const { return (c + 2) * nij + (a + 2) * nj + (b + 2); }

@@ -61,11 +61,12 @@ int cappgpu_host_free(void* p) {
 //         4: fluxuvw, east faces (fluxuvw-overrelaxed-correction.f90)
 //         5: piso_assemble_pressure_eq, east faces, ipc=1
 //         6: SIP factorisation (pcg-sip.f90:174-193)
-// Units 0,1,2,6 work on solver scratch vectors; 3-5 overwrite the module
+//         7, 8: FP32 forward / backward substitution of the precision-1 form
+// Units 0,1,2,6,7,8 work on solver scratch vectors; 3-5 overwrite the module
 // arrays they write (gradu, su.., ae/aw, f1, be), as the routines do.
 int cappgpu_profile_kernel(int which, int reps, double* ms_per_unit, double* algo_bytes) {
   CAP_REQUIRE_INIT();
-  if (reps < 1 || which < 0 || which > 6) { set_error("profile_kernel: bad arguments"); return CAPPGPU_E_ARG; }
+  if (reps < 1 || which < 0 || which > 8) { set_error("profile_kernel: bad arguments"); return CAPPGPU_E_ARG; }
   Ctx& c = ctx();
   double bytes = 0.0;
   int rc = profile_unit(which, &bytes);   // warm-up

@@ -24,6 +24,7 @@ namespace cap {
 namespace {
 
 constexpr int BA = 16, BC = 8;   // lines per wavefront block (a x c)
+constexpr int kBatch = 4;        // CG iterations launched between two host reads of the exit test
 
 enum DBuf { D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_SU, D_RES, D_FI, D_Z, D_ZZ, D_PK0, D_PK1, D_NBUF };
 
@@ -39,8 +40,8 @@ struct Fast {
   int nBA = 0, nBC = 0, nblk = 0;
   int2* order = nullptr;
   unsigned* ticket = nullptr;
-  unsigned ticket_base = 0;
   int* flags = nullptr;       // [0] abort, [1] err
+  int* ctl = nullptr;         // iteration control: [0] stop at iteration, [1] iterations, [2] non-finite, [3] converged
   double* wpart = nullptr;    // per-block partials of the wavefront
   double* mail = nullptr;     // edge mailboxes (sentinel when empty)
   size_t mail_n = 0;
@@ -78,6 +79,7 @@ void fast_release() {
   if (F.order) cudaFree(F.order);
   if (F.mail) cudaFree(F.mail);
   if (F.ticket) cudaFree(F.ticket);
+  if (F.ctl) cudaFree(F.ctl);
   if (F.flags) cudaFree(F.flags);
   if (F.wpart) cudaFree(F.wpart);
   if (F.hres) cudaFreeHost(F.hres);
@@ -185,7 +187,8 @@ int fast_setup() {
   CAP_CUDA(cudaMemset(F.flags, 0, sizeof(int) * 2));
   CAP_CUDA(cudaMalloc(&F.wpart, sizeof(double) * F.nblk));
   CAP_CUDA(cudaMallocHost(&F.hres, sizeof(double) * 4));
-  F.ticket_base = 0;
+  CAP_CUDA(cudaMalloc(&F.ctl, sizeof(int) * 4));
+  CAP_CUDA(cudaMemset(F.ctl, 0, sizeof(int) * 4));
   CAP_CUDA(cudaStreamSynchronize(c.st));
   F.ready = true;
   return CAPPGPU_OK;
@@ -218,7 +221,6 @@ int fast32_setup() {
 WaveCtl next_ctl() {
   WaveCtl w;
   w.ticket = F.ticket;
-  w.ticket_base = F.ticket_base;
   w.order = F.order;
   w.nBA = F.nBA;
   w.nBC = F.nBC;
@@ -229,12 +231,12 @@ WaveCtl next_ctl() {
   w.mailW = F.mail;
   w.mailB = F.mail + (size_t)F.nblk * BC * F.g.Nj * 3;
   w.spin_limit = 1LL << 21;
-  F.ticket_base += (unsigned)F.nblk;
+  w.skip = nullptr;
   return w;
 }
 
 template <class Op, bool BWD>
-int run_wave(const Op& op) {
+int run_wave(const Op& op, const int* skip = nullptr) {
   Ctx& c = ctx();
   constexpr size_t smem = wave_smem_bytes<Op, BA, BC>();
   static bool attr_set = false;   // once per process (one device per context)
@@ -243,6 +245,7 @@ int run_wave(const Op& op) {
     attr_set = true;
   }
   WaveCtl w = next_ctl();
+  w.skip = skip;
   launch_smem(k_wave<Op, BA, BC, BWD>, F.nblk, wave_threads<BA, BC>(), smem, c.st, op, F.g, w);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
@@ -262,12 +265,37 @@ __device__ inline bool d_cell(const DG& g, long long t, int& a, int& b, int& c) 
   return a < g.Ni && b >= 0 && b < g.Nj;
 }
 
-// pk = zk + bet pk (pcg-sip.f90:241).  A pass of its own: fusing it into
-// the product would recompute pk at all seven stencil points, and on GB300
-// the FP64 issue rate, not HBM, bounds these passes.
-__global__ void k_pk_d(DG g, const double* __restrict__ zk, const double* __restrict__ pko, double* __restrict__ pkn,
-                       const double* __restrict__ scal) {
-  const double bet = scal[4];
+// ---------------------------------------------- batched CG iterations
+// The scalars of a CG iteration are formed by the kernel that needs them,
+// from the previous kernel's block partials, summed in a fixed order that is
+// the same in every block (deterministic).  A one-block check kernel ends
+// the iteration: it records the residual norm and, once the exit test
+// holds (or nsw iterations ran, or the norm is not finite), sets ctl[0];
+// every later kernel of the batch then returns at once.  The host reads
+// ctl once per batch.
+__device__ double block_sum_fixed(const double* __restrict__ part, int n) {
+  __shared__ double sh[kThreads];
+  double v = 0.0;
+  for (int q = threadIdx.x; q < n; q += kThreads) v += part[q];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = kThreads / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// sk = res.z from the backward sweep's partials; bet = sk/s0
+// (pcg-sip.f90:229-233); pk = zk + bet pk (pcg-sip.f90:241)
+__global__ void k_pk_x(DG g, const double* __restrict__ zk, const double* __restrict__ pko, double* __restrict__ pkn,
+                       const double* __restrict__ wpart, int nwp, double* scal, const int* ctl) {
+  if (*(volatile const int*)ctl) return;
+  const double sk = block_sum_fixed(wpart, nwp);
+  const double bet = sk / scal[0];
+  if (blockIdx.x == 0 && threadIdx.x == 0) { scal[1] = sk; scal[4] = bet; }
   D_LOOP(g) {
     int a, b, c;
     if (!d_cell(g, t_, a, b, c)) continue;
@@ -275,13 +303,54 @@ __global__ void k_pk_d(DG g, const double* __restrict__ zk, const double* __rest
   }
 }
 
-// zz = A pk (pcg-sip.f90:253-255; pk is zero outside the interior) and the
-// partial sums of pk.zz (pcg-sip.f90:258-261)
-__global__ void k_spmv_d(DG g, const double* __restrict__ ae, const double* __restrict__ aw,
+// pkapk from the product's partials, alf = sk/pkapk (pcg-sip.f90:261-263);
+// fi += alf pk; res -= alf zz; partial sums |res| (pcg-sip.f90:268-281)
+__global__ void k_update_x(DG g, double* __restrict__ fi, double* __restrict__ res, const double* __restrict__ pk,
+                           const double* __restrict__ zz, const double* __restrict__ pin, double* scal,
+                           double* pout, const int* ctl) {
+  if (*(volatile const int*)ctl) return;
+  const double pkapk = block_sum_fixed(pin, kRedBlocks);
+  const double alf = scal[1] / pkapk;
+  if (blockIdx.x == 0 && threadIdx.x == 0) { scal[2] = pkapk; scal[3] = alf; }
+  double v[1] = {0.0};
+  D_LOOP(g) {
+    int a, b, c;
+    if (!d_cell(g, t_, a, b, c)) continue;
+    fi[t_] = fi[t_] + alf * pk[t_];
+    const double r = res[t_] - alf * zz[t_];
+    res[t_] = r;
+    v[0] += fabs(r);
+  }
+  block_reduce_store<1>(v, pout);
+}
+
+// resl = sum |res| (pcg-sip.f90:283-285), s0 = sk, exit test
+// resl/res0 < resmax (pcg-sip.f90:286-289); target > 0 replaces the test by
+// resl <= target (inner loop of the refinement form)
+__global__ void k_cg_check(const double* __restrict__ part, double* scal, int* ctl, double res0, double resmax,
+                           double target, int nsw) {
+  if (*(volatile const int*)ctl) return;
+  const double resl = block_sum_fixed(part, kRedBlocks);
+  if (threadIdx.x == 0) {
+    scal[5] = resl;
+    scal[0] = scal[1];
+    const int it = ctl[1] + 1;
+    ctl[1] = it;
+    const bool bad = !isfinite(resl);
+    const bool conv = target > 0.0 ? resl <= target : resl / (res0 + CAP_SMALL) < resmax;
+    if (bad) ctl[2] = 1;
+    if (conv && !bad) ctl[3] = 1;
+    if (bad || conv || it >= nsw) ctl[0] = it;
+  }
+}
+
+// zz = A pk with the partial sums of pk.zz (k_spmv_d), skipped once stopped
+__global__ void k_spmv_x(DG g, const double* __restrict__ ae, const double* __restrict__ aw,
                          const double* __restrict__ an, const double* __restrict__ as,
                          const double* __restrict__ at, const double* __restrict__ ab,
                          const double* __restrict__ ap, const double* __restrict__ pk, double* __restrict__ zz,
-                         double* part) {
+                         double* part, const int* ctl) {
+  if (*(volatile const int*)ctl) return;
   double v[1] = {0.0};
   D_LOOP(g) {
     int a, b, c;
@@ -297,22 +366,6 @@ __global__ void k_spmv_d(DG g, const double* __restrict__ ae, const double* __re
     const double r = ap[P] * pP - ae[P] * pE - aw[P] * pW - an[P] * pN - as[P] * pS - at[P] * pT - ab[P] * pB;
     zz[P] = r;
     v[0] += pP * r;
-  }
-  block_reduce_store<1>(v, part);
-}
-
-// fi += alf pk; res -= alf zz; partial sum |res| (pcg-sip.f90:268-281)
-__global__ void k_update_d(DG g, double* __restrict__ fi, double* __restrict__ res, const double* __restrict__ pk,
-                           const double* __restrict__ zz, const double* __restrict__ scal, double* part) {
-  const double alf = scal[3];
-  double v[1] = {0.0};
-  D_LOOP(g) {
-    int a, b, c;
-    if (!d_cell(g, t_, a, b, c)) continue;
-    fi[t_] = fi[t_] + alf * pk[t_];
-    const double r = res[t_] - alf * zz[t_];
-    res[t_] = r;
-    v[0] += fabs(r);
   }
   block_reduce_store<1>(v, part);
 }
@@ -387,8 +440,9 @@ __global__ void k_add_f(DG g, double* __restrict__ x, const float* __restrict__ 
   }
 }
 
-// partial sums of a.b (FP32 products and per-thread sums, FP64 across threads)
-__global__ void k_dot_f(DG g, const float* __restrict__ x, const float* __restrict__ y, double* part) {
+// FP32 inner-loop kernels with fused scalars (same scheme as k_pk_x ...)
+__global__ void k_dot_fx(DG g, const float* __restrict__ x, const float* __restrict__ y, double* part, const int* ctl) {
+  if (*(volatile const int*)ctl) return;
   float acc = 0.0f;
   D_LOOP(g) {
     int a, b, c;
@@ -399,16 +453,17 @@ __global__ void k_dot_f(DG g, const float* __restrict__ x, const float* __restri
   block_reduce_store<1>(v, part);
 }
 
-// pk_new = z + bet pk_old at the cell and its neighbours (FP32 arithmetic is
-// cheap on GB300, so the neighbours' values are recomputed rather than
-// stored), zz = A pk_new, partial sums of pk_new.zz
-__global__ void k_pk_spmv_f(DG g, const float* __restrict__ ae, const float* __restrict__ aw,
-                            const float* __restrict__ an, const float* __restrict__ as,
-                            const float* __restrict__ at, const float* __restrict__ ab,
-                            const float* __restrict__ ap, const float* __restrict__ zk,
-                            const float* __restrict__ pko, float* __restrict__ pkn, float* __restrict__ zz,
-                            const double* __restrict__ scal, double* part) {
-  const float bet = (float)scal[4];
+__global__ void k_pk_spmv_fx(DG g, const float* __restrict__ ae, const float* __restrict__ aw,
+                             const float* __restrict__ an, const float* __restrict__ as,
+                             const float* __restrict__ at, const float* __restrict__ ab,
+                             const float* __restrict__ ap, const float* __restrict__ zk,
+                             const float* __restrict__ pko, float* __restrict__ pkn, float* __restrict__ zz,
+                             const double* __restrict__ pin, double* scal, double* pout, const int* ctl) {
+  if (*(volatile const int*)ctl) return;
+  const double sk = block_sum_fixed(pin, kRedBlocks);
+  const double betd = sk / scal[0];
+  if (blockIdx.x == 0 && threadIdx.x == 0) { scal[1] = sk; scal[4] = betd; }
+  const float bet = (float)betd;
   float acc = 0.0f;
   D_LOOP(g) {
     int a, b, c;
@@ -428,13 +483,17 @@ __global__ void k_pk_spmv_f(DG g, const float* __restrict__ ae, const float* __r
     acc += pP * r;
   }
   double v[1] = {(double)acc};
-  block_reduce_store<1>(v, part);
+  block_reduce_store<1>(v, pout);
 }
 
-// x += alf pk; r -= alf zz; partial sums |r|
-__global__ void k_update_f(DG g, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ pk,
-                           const float* __restrict__ zz, const double* __restrict__ scal, double* part) {
-  const float alf = (float)scal[3];
+__global__ void k_update_fx(DG g, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ pk,
+                            const float* __restrict__ zz, const double* __restrict__ pin, double* scal, double* pout,
+                            const int* ctl) {
+  if (*(volatile const int*)ctl) return;
+  const double pkapk = block_sum_fixed(pin, kRedBlocks);
+  const double alfd = scal[1] / pkapk;
+  if (blockIdx.x == 0 && threadIdx.x == 0) { scal[2] = pkapk; scal[3] = alfd; }
+  const float alf = (float)alfd;
   float acc = 0.0f;
   D_LOOP(g) {
     int a, b, c;
@@ -445,7 +504,7 @@ __global__ void k_update_f(DG g, float* __restrict__ x, float* __restrict__ r, c
     acc += fabsf(rr);
   }
   double v[1] = {(double)acc};
-  block_reduce_store<1>(v, part);
+  block_reduce_store<1>(v, pout);
 }
 
 }  // namespace
@@ -460,7 +519,6 @@ static int check_wave_error() {
     cudaMemset(F.ticket, 0, sizeof(unsigned));
     fill_mail(ctx().st);
     cudaStreamSynchronize(ctx().st);
-    F.ticket_base = 0;
     set_error(h[1] == 1 ? "wavefront: a block waited beyond the spin limit for its predecessor"
                         : "wavefront: block ticket out of range");
     return CAPPGPU_E_SPIN;
@@ -556,45 +614,51 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   launch(k_set_scal, 1, 1, c.st, c.dscal, (double)1.e20f);   // s0 = 1.e20 (default real)
   const SipFwdD fwd = make_fwd(D_RES, D_Z, nullptr);
   const SipBwdD bwd = make_bwd(D_Z, D_RES);
-  int ns = P.nsw[ifi - 1], l;
-  double resl = 0.0, rsm;
-  bool done = false;
+  const int ns = P.nsw[ifi - 1];
+  P.resor[ifi - 1] = res0;   // pcg-sip.f90:185 (l = 1)
+  CAP_CUDA(cudaMemsetAsync(F.ctl, 0, sizeof(int) * 4, c.st));
+  double* const part0 = c.partials;               // product partials
+  double* const part1 = c.partials + kRedBlocks;  // |res| partials
   int cur = 0;
-  for (l = 1; l <= ns; ++l) {
-    if ((rc = run_wave<SipFwdD, false>(fwd))) return rc;
-    if ((rc = run_wave<SipBwdD, true>(bwd))) return rc;
-    launch(k_cg_scalars, 1, 32, c.st, 0, (const double*)F.wpart, F.nblk, c.dscal);
-    double* pko = F.d[cur ? D_PK1 : D_PK0];
-    double* pkn = F.d[cur ? D_PK0 : D_PK1];
-    launch(k_pk_d, grid_for(F.g.size()), kThreads, c.st, F.g, (const double*)F.d[D_Z], (const double*)pko, pkn,
-           (const double*)c.dscal);
-    launch(k_spmv_d, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
-           (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
-           (const double*)F.d[D_AP], (const double*)pkn, F.d[D_ZZ], c.partials);
-    launch(k_cg_scalars, 1, 32, c.st, 1, (const double*)c.partials, kRedBlocks, c.dscal);
-    launch(k_update_d, kRedBlocks, kThreads, c.st, F.g, F.d[D_FI], F.d[D_RES], (const double*)pkn,
-           (const double*)F.d[D_ZZ], (const double*)c.dscal, c.partials);
-    launch(k_cg_scalars, 1, 32, c.st, 2, (const double*)c.partials, kRedBlocks, c.dscal);
-    CAP_CHECK_LAUNCH();
-    cur ^= 1;
-    CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 5, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+  int hctl[4] = {0, 0, 0, 0};
+  for (int launched = 0; launched < ns;) {
+    // a batch of iterations; those after the exit test return at once
+    const int batch = ns - launched < kBatch ? ns - launched : kBatch;
+    for (int q = 0; q < batch; ++q) {
+      if ((rc = run_wave<SipFwdD, false>(fwd, F.ctl))) return rc;
+      if ((rc = run_wave<SipBwdD, true>(bwd, F.ctl))) return rc;
+      double* pko = F.d[cur ? D_PK1 : D_PK0];
+      double* pkn = F.d[cur ? D_PK0 : D_PK1];
+      launch(k_pk_x, grid_for(F.g.size()), kThreads, c.st, F.g, (const double*)F.d[D_Z], (const double*)pko, pkn,
+             (const double*)F.wpart, F.nblk, c.dscal, (const int*)F.ctl);
+      launch(k_spmv_x, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
+             (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
+             (const double*)F.d[D_AP], (const double*)pkn, F.d[D_ZZ], part0, (const int*)F.ctl);
+      launch(k_update_x, kRedBlocks, kThreads, c.st, F.g, F.d[D_FI], F.d[D_RES], (const double*)pkn,
+             (const double*)F.d[D_ZZ], (const double*)part0, c.dscal, part1, (const int*)F.ctl);
+      launch(k_cg_check, 1, kThreads, c.st, (const double*)part1, c.dscal, F.ctl, res0, resmax, 0.0, ns);
+      CAP_CHECK_LAUNCH();
+      cur ^= 1;
+    }
+    launched += batch;
+    CAP_CUDA(cudaMemcpyAsync(hctl, F.ctl, sizeof(hctl), cudaMemcpyDeviceToHost, c.st));
     CAP_CUDA(cudaStreamSynchronize(c.st));
     if ((rc = check_wave_error())) return rc;
-    resl = F.hres[0];
-    if (l == 1) P.resor[ifi - 1] = res0;
-    rsm = resl / (P.resor[ifi - 1] + CAP_SMALL);
-    if (!isfinite(resl)) break;
-    if (rsm < resmax) { done = true; break; }
+    if (hctl[0]) break;
   }
+  CAP_CUDA(cudaMemcpy(F.hres, c.dscal + 5, sizeof(double), cudaMemcpyDeviceToHost));
+  const int l = hctl[1];
+  const double resl = l > 0 ? F.hres[0] : res0;
+  const bool done = hctl[3] != 0;
   if ((rc = from_d(D_FI, fif))) return rc;
   if ((rc = from_d(D_RES, CAP_RES))) return rc;
   if (rep) {
     rep->res0 = res0;
     rep->resl = resl;
-    rep->iters = done ? l : ns;
+    rep->iters = l;
     rep->status = done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
   }
-  if (!isfinite(resl)) {
+  if (hctl[2] || !isfinite(resl)) {
     set_error("linear solver residual is not finite");
     if (rep) rep->status = CAPPGPU_E_NONFINITE;
     return CAPPGPU_E_NONFINITE;
@@ -730,31 +794,40 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     launch(k_set_scal, 1, 1, c.st, c.dscal, (double)1.e20f);
     // reduce the residual far enough for the FP64 test, not below what FP32 holds
     const double target = fmax(0.5 * resmax * res0, 2e-5 * resl);
+    const int budget = ns - total;
+    CAP_CUDA(cudaMemsetAsync(F.ctl, 0, sizeof(int) * 4, c.st));
+    double* const part0 = c.partials;
+    double* const part1 = c.partials + kRedBlocks;
+    double* const part2 = c.partials + 2 * kRedBlocks;
     int cur = 0;
-    for (;;) {
-      if ((rc = run_wave<SipFwdF, false>(fwd))) return rc;
-      if ((rc = run_wave<SipBwdF, true>(bwd))) return rc;
-      launch(k_dot_f, kRedBlocks, kThreads, c.st, g, (const float*)G.e[E_R], (const float*)G.e[E_Z], c.partials);
-      launch(k_cg_scalars, 1, 32, c.st, 0, (const double*)c.partials, kRedBlocks, c.dscal);
-      float* pko = G.e[cur ? E_P1 : E_P0];
-      float* pkn = G.e[cur ? E_P0 : E_P1];
-      launch(k_pk_spmv_f, kRedBlocks, kThreads, c.st, g, (const float*)G.e[E_AE], (const float*)G.e[E_AW],
-             (const float*)G.e[E_AN], (const float*)G.e[E_AS], (const float*)G.e[E_AT], (const float*)G.e[E_AB],
-             (const float*)G.e[E_AP], (const float*)G.e[E_Z], (const float*)pko, pkn, G.e[E_ZZ],
-             (const double*)c.dscal, c.partials);
-      launch(k_cg_scalars, 1, 32, c.st, 1, (const double*)c.partials, kRedBlocks, c.dscal);
-      launch(k_update_f, kRedBlocks, kThreads, c.st, g, G.e[E_X], G.e[E_R], (const float*)pkn,
-             (const float*)G.e[E_ZZ], (const double*)c.dscal, c.partials);
-      launch(k_cg_scalars, 1, 32, c.st, 2, (const double*)c.partials, kRedBlocks, c.dscal);
-      CAP_CHECK_LAUNCH();
-      cur ^= 1;
-      ++total;
-      CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 5, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    int hctl[4] = {0, 0, 0, 0};
+    for (int launched = 0; launched < budget;) {
+      const int batch = budget - launched < kBatch ? budget - launched : kBatch;
+      for (int q = 0; q < batch; ++q) {
+        if ((rc = run_wave<SipFwdF, false>(fwd, F.ctl))) return rc;
+        if ((rc = run_wave<SipBwdF, true>(bwd, F.ctl))) return rc;
+        float* pko = G.e[cur ? E_P1 : E_P0];
+        float* pkn = G.e[cur ? E_P0 : E_P1];
+        launch(k_dot_fx, kRedBlocks, kThreads, c.st, g, (const float*)G.e[E_R], (const float*)G.e[E_Z], part0,
+               (const int*)F.ctl);
+        launch(k_pk_spmv_fx, kRedBlocks, kThreads, c.st, g, (const float*)G.e[E_AE], (const float*)G.e[E_AW],
+               (const float*)G.e[E_AN], (const float*)G.e[E_AS], (const float*)G.e[E_AT], (const float*)G.e[E_AB],
+               (const float*)G.e[E_AP], (const float*)G.e[E_Z], (const float*)pko, pkn, G.e[E_ZZ],
+               (const double*)part0, c.dscal, part1, (const int*)F.ctl);
+        launch(k_update_fx, kRedBlocks, kThreads, c.st, g, G.e[E_X], G.e[E_R], (const float*)pkn,
+               (const float*)G.e[E_ZZ], (const double*)part1, c.dscal, part2, (const int*)F.ctl);
+        launch(k_cg_check, 1, kThreads, c.st, (const double*)part2, c.dscal, F.ctl, res0, resmax, target, budget);
+        CAP_CHECK_LAUNCH();
+        cur ^= 1;
+      }
+      launched += batch;
+      CAP_CUDA(cudaMemcpyAsync(hctl, F.ctl, sizeof(hctl), cudaMemcpyDeviceToHost, c.st));
       CAP_CUDA(cudaStreamSynchronize(c.st));
       if ((rc = check_wave_error())) return rc;
-      const double rin = F.hres[0];
-      if (!isfinite(rin) || rin <= target || total >= ns) break;
+      if (hctl[0]) break;
     }
+    total += hctl[1] ? hctl[1] : budget;
+    if (hctl[2]) { bad = true; break; }
     launch(k_add_f, grid_for(g.size()), kThreads, c.st, g, F.d[D_FI], (const float*)G.e[E_X]);
     CAP_CHECK_LAUNCH();
   }
@@ -791,6 +864,25 @@ int fast_profile_unit(int which, double* bytes) {
     const SipBwdD bwd = make_bwd(D_Z, D_RES);
     *bytes = 6.0 * 8.0 * cells;   // z + 3 factors + res read, z written
     return run_wave<SipBwdD, true>(bwd);
+  }
+  if (which == 7 || which == 8) {   // FP32 substitutions of the refinement form
+    if (!G.ready) {
+      int rc = fast32_setup();
+      if (rc) return rc;
+    }
+    *bytes = 6.0 * 4.0 * cells;   // 5 words read, 1 written, 4 bytes each
+    if (which == 7) {
+      SipFwdF fwd;
+      fwd.map[0] = G.map[E_R];
+      fwd.map[1] = G.map_fq;
+      fwd.z = G.e[E_Z];
+      return run_wave<SipFwdF, false>(fwd);
+    }
+    SipBwdF bwd;
+    bwd.map[0] = G.map[E_Z];
+    bwd.map[1] = G.map_bq;
+    bwd.z = G.e[E_Z];
+    return run_wave<SipBwdF, true>(bwd);
   }
   *bytes = 21.0 * 8.0 * cells;    // 7 coefficients read, 7 factors natural + 7 hyperplane written
   return factor_wave();

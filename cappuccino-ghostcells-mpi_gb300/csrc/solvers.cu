@@ -569,6 +569,10 @@ int profile_unit(int which, double* bytes) {
   double cells = (double)b.count();
   double* zk = c.work[1];
   double* pk = c.work[0];
+  if (which == 7 || which == 8) {
+    if (d.nimm < 4 || d.njmm < 4 || d.nkmm < 4) { set_error("profile unit %d needs 2 interior cells per axis", which); return CAPPGPU_E_ARG; }
+    return fast_profile_unit(which, bytes);
+  }
   if (c.wave_impl == 1 && (which == 0 || which == 1 || which == 6)) return fast_profile_unit(which, bytes);
   switch (which) {
     case 0: {

@@ -43,8 +43,7 @@
 namespace cap {
 
 struct WaveCtl {
-  unsigned* ticket;               // monotonically increasing ticket counter
-  unsigned ticket_base;           // its value when this launch started
+  unsigned* ticket;               // block ticket counter: 0 between launches (the last block resets it)
   const int2* order;              // blocks in topological order
   int nBA, nBC, nblk;
   int* abort;                     // device-wide abort flag
@@ -53,18 +52,20 @@ struct WaveCtl {
   double* mailW;                  // per block: BC x Nj states of its last a-line
   double* mailB;                  // per block: BA x Nj states of its last c-row
   long long spin_limit;
+  const int* skip;                // when non-null and *skip != 0 at launch, every block exits at once
 };
 
 constexpr int kG = 4;        // hyperplanes per TMA copy
 constexpr int kMaxSlots = 8; // copies in flight (per op: Op::kSlots)
-constexpr int kRing = 32;    // planes of staged edge states
+constexpr int kRing = 32;    // planes of staged edge states (a power of two)
 constexpr int kPW = 8;       // edge planes examined per communication pass
 constexpr unsigned long long kSentinel = 0x7FF0DEAD5EA1F00DULL;   // signalling NaN
 // a slot is refilled at the start of the next group, so two slots at least;
 // the ring holds the planes between two updates of the consumed-plane count
 static_assert(kRing >= kG + 3, "edge ring capacity");
 
-__host__ __device__ constexpr int ring_slot(int q) { return (q + kRing) % kRing; }   // valid for q >= -kRing
+__host__ __device__ constexpr int ring_slot(int q) { return q & (kRing - 1); }   // also for q < 0
+static_assert((kRing & (kRing - 1)) == 0, "ring size");
 
 // Shared-memory input slots: per map a box of (BA + 16/esize) x NQ x BC x kG
 // elements (the extra columns let a mirrored block start its copy on a
@@ -105,9 +106,17 @@ struct InView {
   }
 };
 
+// The cell a compute thread works on at the current step.
+struct Cell {
+  long long di;   // hyperplane-layout index
+  int nat;        // 0-based natural index
+  int sr;         // its hyperplane a+b+c
+  int a, c;
+};
+
 template <class St, int BA, int BC>
 struct WaveSmem {
-  St sbuf[2][BC][BA];                      // states of the two latest planes
+  St sbuf[2][BC + 1][BA + 1];              // states of the two latest planes (row 0 and column 0 unused)
   St ringW[kRing][BC];                     // W edge states by plane
   St ringB[kRing][BA];                     // B edge states by plane
   unsigned long long full[kMaxSlots];
@@ -242,12 +251,13 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
     sm.bail = 0;
     for (int k = 0; k < NSLOT; ++k) mbar_init(&sm.full[k], 1);
     mbar_fence_init();
-    unsigned t = atomicAdd(w.ticket, 1u) - w.ticket_base;
+    const unsigned t = atomicAdd(w.ticket, 1u);
+    if (t == (unsigned)w.nblk - 1) atomicExch(w.ticket, 0u);   // every ticket of this launch is taken
     if (t < (unsigned)w.nblk) {
       int2 blk = w.order[t];
       sm.blk[0] = blk.x;
       sm.blk[1] = blk.y;
-      sm.start_ok = 1;
+      sm.start_ok = (w.skip && *(volatile const int*)w.skip) ? 0 : 1;
     } else {   // ticket counter out of step with the host: refuse to run
       sm.blk[0] = sm.blk[1] = 0;
       sm.start_ok = 0;
@@ -406,21 +416,42 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
   double* mW = w.mailW + ((size_t)blk_id * BC + cl) * g.Nj * NS;
   double* mB = w.mailB + ((size_t)blk_id * BA + al) * g.Nj * NS;
   const St sg = line_ok ? op.ghost(g.nat(a, BWD ? g.Nj : -1, c)) : St{};   // j-predecessor of the first cell
+  // per-thread addresses: W, B of the previous plane and this cell's slot,
+  // for both buffer parities
+  // W and B come from the previous plane's buffer inside the block and from
+  // the staged edge rings on its first column / row
+  const St* const rdW0 = al > 0 ? &sm.sbuf[0][cl + 1][al] : nullptr;
+  const St* const rdW1 = al > 0 ? &sm.sbuf[1][cl + 1][al] : nullptr;
+  const St* const rdB0 = cl > 0 ? &sm.sbuf[0][cl][al + 1] : nullptr;
+  const St* const rdB1 = cl > 0 ? &sm.sbuf[1][cl][al + 1] : nullptr;
+  St* const wr0 = &sm.sbuf[0][cl + 1][al + 1];
+  St* const wr1 = &sm.sbuf[1][cl + 1][al + 1];
+  const long long cpa = (long long)c * g.P + a;
+  const int nat_first = g.nat(a, BWD ? g.Nj - 1 : 0, c);
+  Cell x;
+  x.a = a;
+  x.c = c;
   St prevS{};
   double part = 0.0;
-  int gi = 0, ds = 0;
+  int ds = 0;
+  const unsigned char* slot = inbuf;
+  const unsigned char* const slot_end = inbuf + NSLOT * L::slot_bytes;
   for (int s = s0; s <= s1; ++s) {
-    if (named_bar_red_or(1, NC + 32, false)) break;   // plane s-1 computed; inputs of plane s ready
+    if (named_bar_red_or(1, NC + 32, false)) break;   // plane s-1 computed; inputs and halo of plane s ready
     const int bv = s - sfirst;
-    if (line_ok && bv >= 0 && bv < g.Nj) {
-      const int b = BWD ? g.Nj - 1 - bv : bv;
-      const St W = al > 0 ? sm.sbuf[(s - 1) & 1][cl][al - 1] : sm.ringW[ring_slot(s - 1)][cl];
-      const St B = cl > 0 ? sm.sbuf[(s - 1) & 1][cl - 1][al] : sm.ringB[ring_slot(s - 1)][al];
+    if (line_ok && (unsigned)bv < (unsigned)g.Nj) {
+      const bool odd = (s & 1) != 0;   // the previous plane is in buffer 0 when s is odd
+      const int rs = ring_slot(s - 1);
+      const St W = *(al > 0 ? (odd ? rdW0 : rdW1) : &sm.ringW[rs][cl]);
+      const St B = *(cl > 0 ? (odd ? rdB0 : rdB1) : &sm.ringB[rs][al]);
       const St S = bv > 0 ? prevS : sg;
-      in.slot = inbuf + (gi % NSLOT) * L::slot_bytes;
+      x.sr = BWD ? g.S - 1 - s : s;
+      x.di = (long long)x.sr * g.plane + cpa;
+      x.nat = BWD ? nat_first - bv : nat_first + bv;
+      in.slot = slot;
       in.zb = BWD ? kG - 1 - ds : ds;
-      const St out = op.compute(in, g, a, b, c, W, S, B, part);
-      sm.sbuf[s & 1][cl][al] = out;
+      const St out = op.compute(in, g, x, W, S, B, part);
+      *(odd ? wr1 : wr0) = out;
       prevS = out;
       if (edgeE || edgeT) {
         unsigned long long u[NS];
@@ -434,7 +465,11 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
         }
       }
     }
-    if (++ds == kG) { ds = 0; ++gi; }
+    if (++ds == kG) {
+      ds = 0;
+      slot += L::slot_bytes;
+      if (slot == slot_end) slot = inbuf;
+    }
   }
   if (Op::kReduce) {
     const int lane = tid & 31, wid = tid >> 5;
@@ -473,9 +508,9 @@ struct SipFwdD {
   const double* ghost_src;    // natural array of ghost values, or null (zero)
   __device__ St ghost(int nat) const { return ghost_src ? ghost_src[nat] : 0.0; }
   template <class In>
-  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
     const double v = (in.d(0, 0) - in.d(1, 0) * B - in.d(1, 1) * W - in.d(1, 2) * S) * in.d(1, 3);
-    z[g.d(a, b, c)] = v;
+    z[x.di] = v;
     return v;
   }
 };
@@ -495,9 +530,9 @@ struct SipBwdD {
   const double* ghost_src;
   __device__ St ghost(int nat) const { return ghost_src ? ghost_src[nat] : 0.0; }
   template <class In>
-  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double& part) const {
+  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double& part) const {
     const double v = in.d(0, 0) - in.d(1, 0) * S - in.d(1, 1) * W - in.d(1, 2) * B;
-    z[g.d(a, b, c)] = v;
+    z[x.di] = v;
     part += in.d(2, 0) * v;
     return v;
   }
@@ -517,11 +552,10 @@ struct SipBwdFiD {
   const double* ghost_src;    // module res (stale ghost values, as the reference reads them)
   __device__ St ghost(int nat) const { return ghost_src[nat]; }
   template <class In>
-  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
     const double v = in.d(0, 0) - in.d(1, 0) * S - in.d(1, 1) * W - in.d(1, 2) * B;
-    const long long di = g.d(a, b, c);
-    z[di] = v;
-    fi[di] = in.d(2, 0) + v;
+    z[x.di] = v;
+    fi[x.di] = in.d(2, 0) + v;
     return v;
   }
 };
@@ -541,7 +575,7 @@ struct SipFactorD {
   double alfa;
   __device__ St ghost(int nat) const { return St3{bnn[nat], ben[nat], btn[nat]}; }
   template <class In>
-  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
     const double bbv = -in.d(5, 0) / (1.0 + alfa * (B.bn + B.be));
     const double bwv = -in.d(1, 0) / (1.0 + alfa * (W.bn + W.bt));
     const double bsv = -in.d(3, 0) / (1.0 + alfa * (S.be + S.bt));
@@ -552,16 +586,16 @@ struct SipFactorD {
     const double bnv = (-in.d(2, 0) - p1) * bpv;
     const double bev = (-in.d(0, 0) - p2) * bpv;
     const double btv = (-in.d(4, 0) - p3) * bpv;
-    const int nat = g.nat(a, b, c);
+    const int nat = x.nat;
     bbn[nat] = bbv; bwn[nat] = bwv; bsn[nat] = bsv; bpn[nat] = bpv;
     bnn[nat] = bnv; ben[nat] = bev; btn[nat] = btv;
-    fq[g.dq(a, b, c, 0, 4)] = bbv;
-    fq[g.dq(a, b, c, 1, 4)] = bwv;
-    fq[g.dq(a, b, c, 2, 4)] = bsv;
-    fq[g.dq(a, b, c, 3, 4)] = bpv;
-    bq[g.dq(a, b, c, 0, 3)] = bnv;
-    bq[g.dq(a, b, c, 1, 3)] = bev;
-    bq[g.dq(a, b, c, 2, 3)] = btv;
+    fq[g.dqs(x.sr, x.c, x.a, 0, 4)] = bbv;
+    fq[g.dqs(x.sr, x.c, x.a, 1, 4)] = bwv;
+    fq[g.dqs(x.sr, x.c, x.a, 2, 4)] = bsv;
+    fq[g.dqs(x.sr, x.c, x.a, 3, 4)] = bpv;
+    bq[g.dqs(x.sr, x.c, x.a, 0, 3)] = bnv;
+    bq[g.dqs(x.sr, x.c, x.a, 1, 3)] = bev;
+    bq[g.dqs(x.sr, x.c, x.a, 2, 3)] = btv;
     return St3{bnv, bev, btv};
   }
 };
@@ -586,9 +620,9 @@ struct SipFwdF {
   float* z;
   __device__ St ghost(int) const { return 0.0f; }
   template <class In>
-  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
     const float v = (in.f(0, 0) - in.f(1, 0) * B - in.f(1, 1) * W - in.f(1, 2) * S) * in.f(1, 3);
-    z[g.d(a, b, c)] = v;
+    z[x.di] = v;
     return v;
   }
 };
@@ -604,9 +638,9 @@ struct SipBwdF {
   float* z;
   __device__ St ghost(int) const { return 0.0f; }
   template <class In>
-  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
     const float v = in.f(0, 0) - in.f(1, 0) * S - in.f(1, 1) * W - in.f(1, 2) * B;
-    z[g.d(a, b, c)] = v;
+    z[x.di] = v;
     return v;
   }
 };
@@ -625,7 +659,7 @@ struct SipFactorF {
   float alfa;
   __device__ St ghost(int nat) const { return St3f{(float)bnn[nat], (float)ben[nat], (float)btn[nat]}; }
   template <class In>
-  __device__ St compute(const In& in, const DG& g, int a, int b, int c, St W, St S, St B, double&) const {
+  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
     const float bbv = -in.f(5, 0) / (1.0f + alfa * (B.bn + B.be));
     const float bwv = -in.f(1, 0) / (1.0f + alfa * (W.bn + W.bt));
     const float bsv = -in.f(3, 0) / (1.0f + alfa * (S.be + S.bt));
@@ -636,13 +670,13 @@ struct SipFactorF {
     const float bnv = (-in.f(2, 0) - p1) * bpv;
     const float bev = (-in.f(0, 0) - p2) * bpv;
     const float btv = (-in.f(4, 0) - p3) * bpv;
-    fq[g.dq(a, b, c, 0, 4)] = bbv;
-    fq[g.dq(a, b, c, 1, 4)] = bwv;
-    fq[g.dq(a, b, c, 2, 4)] = bsv;
-    fq[g.dq(a, b, c, 3, 4)] = bpv;
-    bq[g.dq(a, b, c, 0, 3)] = bnv;
-    bq[g.dq(a, b, c, 1, 3)] = bev;
-    bq[g.dq(a, b, c, 2, 3)] = btv;
+    fq[g.dqs(x.sr, x.c, x.a, 0, 4)] = bbv;
+    fq[g.dqs(x.sr, x.c, x.a, 1, 4)] = bwv;
+    fq[g.dqs(x.sr, x.c, x.a, 2, 4)] = bsv;
+    fq[g.dqs(x.sr, x.c, x.a, 3, 4)] = bpv;
+    bq[g.dqs(x.sr, x.c, x.a, 0, 3)] = bnv;
+    bq[g.dqs(x.sr, x.c, x.a, 1, 3)] = bev;
+    bq[g.dqs(x.sr, x.c, x.a, 2, 3)] = btv;
     return St3f{bnv, bev, btv};
   }
 };

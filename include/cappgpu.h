@@ -327,8 +327,9 @@ int cappgpu_host_alloc(void** p, int64_t bytes);
 int cappgpu_host_free(void* p);
 /* Time reps runs of one hot-path unit (0 SIP forward sweep, 1 SIP backward
    sweep, 2 7-point product + dot, 3 grad_gauss, 4 fluxuvw east, 5 PISO
-   pressure assembly east, 6 SIP factorisation) on the current state;
-   returns device ms per unit and its algorithmic bytes. */
+   pressure assembly east, 6 SIP factorisation, 7 / 8 FP32 forward / backward
+   sweep of the precision-1 form) on the current state; returns device ms per
+   unit and its algorithmic bytes. */
 int cappgpu_profile_kernel(int which, int reps, double* ms_per_unit, double* algo_bytes);
 
 #ifdef __cplusplus
