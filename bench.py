@@ -327,7 +327,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=N_DEFAULT, help="interior cells per axis")
+    ap.add_argument("--size", dest="n", type=int, default=N_DEFAULT, help="interior cells per axis")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     ws, rank, local = dist_env()
