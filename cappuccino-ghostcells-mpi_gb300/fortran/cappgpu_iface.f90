@@ -45,6 +45,11 @@ module cappgpu
     integer(c_int) function cappgpu_finalize() bind(c, name="cappgpu_finalize")
       import :: c_int
     end function
+    ! 0 = FP64 plain (the reference's arithmetic), 1 = FP32 + FP64 refinement
+    integer(c_int) function cappgpu_precision(mode) bind(c, name="cappgpu_precision")
+      import :: c_int
+      integer(c_int), value :: mode
+    end function
     integer(c_int) function cappgpu_set_field(field, host, n) bind(c, name="cappgpu_set_field")
       import :: c_int, c_double, c_int64_t
       integer(c_int), value :: field
