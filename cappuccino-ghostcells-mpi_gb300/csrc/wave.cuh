@@ -215,18 +215,31 @@ __device__ __forceinline__ int commit_edge(EdgeProbe<St, kPW * E / 32>& P, const
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int x = lane + 32 * r, j = x / E, e = x % E, q = loaded + 1 + j;
-    if (j < n && P.need[r]) {
-      memcpy(&ring[ring_slot(q)][e], P.u[r], sizeof(St));
-      if (mail) {
-        int av, cv, pa, pc;
-        line(e, av, cv, pa, pc);
-        double* m = mail + ((size_t)e * g.Nj + (q - pa - pc)) * NS;
-#pragma unroll
-        for (int k = 0; k < NS; ++k) st_relaxed_b64(m + k, kSentinel);
-      }
-    }
+    if (j < n && P.need[r]) memcpy(&ring[ring_slot(q)][e], P.u[r], sizeof(St));
   }
   return n;
+}
+
+// After the staged planes are published: the mailbox entries they came from
+// get the sentinel back, ready for the next launch (kept out of the
+// published planes' release, which would otherwise wait for these stores).
+template <class St, int E, class LineFn>
+__device__ __forceinline__ void free_edge(const EdgeProbe<St, kPW * E / 32>& P, const DG& g, int lane, int loaded,
+                                          int n, double* mail, LineFn line) {
+  constexpr int NS = state_words<St>();
+  constexpr int R = kPW * E / 32;
+  if (!mail) return;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int x = lane + 32 * r, j = x / E, e = x % E, q = loaded + 1 + j;
+    if (j < n && P.need[r]) {
+      int av, cv, pa, pc;
+      line(e, av, cv, pa, pc);
+      double* m = mail + ((size_t)e * g.Nj + (q - pa - pc)) * NS;
+#pragma unroll
+      for (int k = 0; k < NS; ++k) st_relaxed_b64(m + k, kSentinel);
+    }
+  }
 }
 
 template <class Op, int BA, int BC, bool BWD>
@@ -373,13 +386,15 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
       const int nW = commit_edge<St, BC>(PW, g, lane, loadedW, srcW, sm.ringW, lineW);
       const int nB = commit_edge<St, BA>(PB, g, lane, loadedB, srcB, sm.ringB, lineB);
       if (nW + nB > 0) {
-        loadedW += nW;
-        loadedB += nB;
         __syncwarp();
         if (lane == 0) {
-          if (nW) st_release_cta_shared(&sm.stagedW, (unsigned long long)(unsigned)(loadedW + 2));
-          if (nB) st_release_cta_shared(&sm.stagedB, (unsigned long long)(unsigned)(loadedB + 2));
+          if (nW) st_release_cta_shared(&sm.stagedW, (unsigned long long)(unsigned)(loadedW + nW + 2));
+          if (nB) st_release_cta_shared(&sm.stagedB, (unsigned long long)(unsigned)(loadedB + nB + 2));
         }
+        free_edge<St, BC>(PW, g, lane, loadedW, nW, srcW, lineW);
+        free_edge<St, BA>(PB, g, lane, loadedB, nB, srcB, lineB);
+        loadedW += nW;
+        loadedB += nB;
         idle = 0;
       } else {
         int stop = 0;
@@ -437,7 +452,7 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
   const unsigned char* slot = inbuf;
   const unsigned char* const slot_end = inbuf + NSLOT * L::slot_bytes;
   for (int s = s0; s <= s1; ++s) {
-    if (named_bar_red_or(1, NC + 32, false)) break;   // plane s-1 computed; inputs and halo of plane s ready
+    if (named_bar_red_or(1, NC + 32, false)) break;   // plane s-1 computed; inputs and edge states of plane s ready
     const int bv = s - sfirst;
     if (line_ok && (unsigned)bv < (unsigned)g.Nj) {
       const bool odd = (s & 1) != 0;   // the previous plane is in buffer 0 when s is odd
