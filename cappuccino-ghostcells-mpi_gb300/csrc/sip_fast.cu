@@ -246,7 +246,7 @@ int run_wave(const Op& op, const int* skip = nullptr) {
   }
   WaveCtl w = next_ctl();
   w.skip = skip;
-  launch_smem(k_wave<Op, BA, BC, BWD>, F.nblk, wave_threads<BA, BC>(), smem, c.st, op, F.g, w);
+  launch_smem(k_wave<Op, BA, BC, BWD>, F.nblk, wave_threads<Op, BA, BC>(), smem, c.st, op, F.g, w);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
 }

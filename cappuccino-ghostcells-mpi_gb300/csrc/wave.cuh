@@ -58,7 +58,6 @@ struct WaveCtl {
 constexpr int kG = 4;        // hyperplanes per TMA copy
 constexpr int kMaxSlots = 8; // copies in flight (per op: Op::kSlots)
 constexpr int kRing = 32;    // planes of staged edge states (a power of two)
-constexpr int kPW = 8;       // edge planes examined per communication pass
 constexpr unsigned long long kSentinel = 0x7FF0DEAD5EA1F00DULL;   // signalling NaN
 // a slot is refilled at the start of the next group, so two slots at least;
 // the ring holds the planes between two updates of the consumed-plane count
@@ -128,9 +127,9 @@ struct WaveSmem {
   int bail;                                // any warp gave up
 };
 
-// compute warps (one thread per line) + communication warp + pacing warp
-template <int BA, int BC>
-constexpr int wave_threads() { return BA * BC + 64; }
+// compute warps (one thread per line) + communication warp + pacing warp(s)
+template <class Op, int BA, int BC>
+constexpr int wave_threads() { return BA * BC + 32 + 32 * Op::kPacers; }
 
 template <class Op, int BA, int BC>
 constexpr size_t wave_smem_bytes() {
@@ -160,12 +159,12 @@ struct EdgeProbe {
 };
 
 template <class Op, int E, bool BWD, class LineFn>
-__device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, kPW * E / 32>& P, const Op& op, const DG& g,
+__device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, Op::kPW * E / 32>& P, const Op& op, const DG& g,
                                            int lane, int loaded, int hi, const double* mail, LineFn line) {
   using St = typename Op::St;
   constexpr int NS = state_words<St>();
 #pragma unroll
-  for (int r = 0; r < kPW * E / 32; ++r) {
+  for (int r = 0; r < Op::kPW * E / 32; ++r) {
     const int x = lane + 32 * r, j = x / E, e = x % E, q = loaded + 1 + j;
     int av, cv, pa, pc;
     line(e, av, cv, pa, pc);
@@ -190,7 +189,7 @@ __device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, kPW * E / 
   }
 }
 
-template <class St, int E, class LineFn>
+template <class St, int E, int kPW, class LineFn>
 __device__ __forceinline__ int commit_edge(EdgeProbe<St, kPW * E / 32>& P, const DG& g, int lane, int loaded,
                                            double* mail, St (*ring)[E], LineFn line) {
   constexpr int NS = state_words<St>();
@@ -223,7 +222,7 @@ __device__ __forceinline__ int commit_edge(EdgeProbe<St, kPW * E / 32>& P, const
 // After the staged planes are published: the mailbox entries they came from
 // get the sentinel back, ready for the next launch (kept out of the
 // published planes' release, which would otherwise wait for these stores).
-template <class St, int E, class LineFn>
+template <class St, int E, int kPW, class LineFn>
 __device__ __forceinline__ void free_edge(const EdgeProbe<St, kPW * E / 32>& P, const DG& g, int lane, int loaded,
                                           int n, double* mail, LineFn line) {
   constexpr int NS = state_words<St>();
@@ -243,13 +242,16 @@ __device__ __forceinline__ void free_edge(const EdgeProbe<St, kPW * E / 32>& P, 
 }
 
 template <class Op, int BA, int BC, bool BWD>
-__global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid_constant__ Op op, const DG g, const WaveCtl w) {
+__global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __grid_constant__ Op op, const DG g, const WaveCtl w) {
   using St = typename Op::St;
   using L = WaveLayout<Op, BA, BC>;
   constexpr int NC = BA * BC;
   constexpr int NS = state_words<St>();
   constexpr int NSLOT = Op::kSlots;
+  constexpr int NP = Op::kPacers;        // pacing warps; pacer p checks the steps with (s - s0) % NP == p
+  constexpr int NB = NC + 32 * NP;       // threads in named barrier 1
   static_assert(NC % 32 == 0, "block shape");
+  constexpr int kPW = Op::kPW;           // edge planes examined per communication pass
   static_assert(32 % BC == 0 && (kPW * BC) % 32 == 0 && (kPW * BA) % 32 == 0, "edge staging shape");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((size_t)smem_raw + 127) & ~(size_t)127);
@@ -290,8 +292,9 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
   const int ngroups = (s1 - s0 + kG) / kG;
 
   if (tid >= NC + 32) {
-    // ------------------------------------------------------- pacing warp
-    const int lane = tid - (NC + 32);
+    // ------------------------------------------------------- pacing warps
+    const int lane = (tid - NC) & 31;
+    const int pw = (tid - NC - 32) >> 5;   // this pacer's index
     auto issue = [&](int gq) {   // TMA copy of group gq (planes s0 + gq*kG ...) into its slot
       const int slot = gq % NSLOT, sg = s0 + gq * kG;
       const int alo = BWD ? g.Ni - (ba + 1) * BA : ba * BA;   // first column of the block's lines
@@ -306,14 +309,17 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
         else tma_load4(dst + L::map_off(m), &op.map[m], x0, 0, y0, z0, &sm.full[slot]);
       }
     };
+    // pacer 0 owns the copies (issue, refill, drain); group starts fall on
+    // its steps because kG is a multiple of NP
+    static_assert(kG % NP == 0, "group starts on pacer 0");
     int issued = min(NSLOT, ngroups);
-    if (lane == 0)
+    if (pw == 0 && lane == 0)
       for (int gq = 0; gq < issued; ++gq) issue(gq);
     unsigned long long knownW = 0, knownB = 0;
     int gi = 0, ds = 0;
     for (int s = s0; s <= s1; ++s) {
       int st = 0;
-      if (lane == 0) {
+      if (lane == 0 && (s - s0) % NP == pw) {
         if (ds == 0) {   // the copy of this group of planes has landed
           long long it = 0;
           while (!mbar_test(&sm.full[gi % NSLOT], (unsigned)((gi / NSLOT) & 1))) {
@@ -334,8 +340,8 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
           }
         }
       }
-      if (named_bar_red_or(1, NC + 32, st != 0)) break;   // (only lane 0's flag can be set) the compute warps start step s
-      if (lane == 0 && ds == 0 && gi > 0) {
+      if (named_bar_red_or(1, NB, st != 0)) break;   // (only a pacer's lane 0 can set it) the compute warps start step s
+      if (pw == 0 && lane == 0 && ds == 0 && gi > 0) {
         // step s-1 is complete: the edge rings up to plane s-2 and the slot
         // of the previous group are free
         *(volatile int*)&sm.done = s;
@@ -349,7 +355,7 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
       if (++ds == kG) { ds = 0; ++gi; }
     }
     // the copies in flight land before the block exits
-    if (lane == 0) {
+    if (pw == 0 && lane == 0) {
       for (int gq = max(0, issued - NSLOT); gq < issued; ++gq) {
         long long it = 0;
         while (!mbar_test(&sm.full[gq % NSLOT], (unsigned)((gq / NSLOT) & 1))) {
@@ -383,16 +389,16 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
       const int hiW = min(s1W, limit), hiB = min(s1B, limit);
       probe_edge<Op, BC, BWD>(PW, op, g, lane, loadedW, hiW, srcW, lineW);
       probe_edge<Op, BA, BWD>(PB, op, g, lane, loadedB, hiB, srcB, lineB);
-      const int nW = commit_edge<St, BC>(PW, g, lane, loadedW, srcW, sm.ringW, lineW);
-      const int nB = commit_edge<St, BA>(PB, g, lane, loadedB, srcB, sm.ringB, lineB);
+      const int nW = commit_edge<St, BC, kPW>(PW, g, lane, loadedW, srcW, sm.ringW, lineW);
+      const int nB = commit_edge<St, BA, kPW>(PB, g, lane, loadedB, srcB, sm.ringB, lineB);
       if (nW + nB > 0) {
         __syncwarp();
         if (lane == 0) {
           if (nW) st_release_cta_shared(&sm.stagedW, (unsigned long long)(unsigned)(loadedW + nW + 2));
           if (nB) st_release_cta_shared(&sm.stagedB, (unsigned long long)(unsigned)(loadedB + nB + 2));
         }
-        free_edge<St, BC>(PW, g, lane, loadedW, nW, srcW, lineW);
-        free_edge<St, BA>(PB, g, lane, loadedB, nB, srcB, lineB);
+        free_edge<St, BC, kPW>(PW, g, lane, loadedW, nW, srcW, lineW);
+        free_edge<St, BA, kPW>(PB, g, lane, loadedB, nB, srcB, lineB);
         loadedW += nW;
         loadedB += nB;
         idle = 0;
@@ -452,7 +458,7 @@ __global__ void __launch_bounds__(wave_threads<BA, BC>(), 1) k_wave(const __grid
   const unsigned char* slot = inbuf;
   const unsigned char* const slot_end = inbuf + NSLOT * L::slot_bytes;
   for (int s = s0; s <= s1; ++s) {
-    if (named_bar_red_or(1, NC + 32, false)) break;   // plane s-1 computed; inputs and edge states of plane s ready
+    if (named_bar_red_or(1, NB, false)) break;   // plane s-1 computed; inputs and edge states of plane s ready
     const int bv = s - sfirst;
     if (line_ok && (unsigned)bv < (unsigned)g.Nj) {
       const bool odd = (s & 1) != 0;   // the previous plane is in buffer 0 when s is odd
@@ -516,6 +522,8 @@ struct SipFwdD {
   static constexpr int kMaps = 2;   // r, forward factors (bb, bw, bs, bp)
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 3;
+  static constexpr int kPacers = 1;
+  static constexpr int kPW = 4;   // edge planes polled per communication pass
   __host__ __device__ static constexpr int nq(int m) { return m == 0 ? 1 : 4; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
   CUtensorMap map[kMaps];
@@ -538,6 +546,8 @@ struct SipBwdD {
   static constexpr int kMaps = 3;   // z, backward factors (bn, be, bt), res
   static constexpr bool kReduce = true;
   static constexpr int kSlots = 3;
+  static constexpr int kPacers = 1;
+  static constexpr int kPW = 4;   // edge planes polled per communication pass
   __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
   CUtensorMap map[kMaps];
@@ -559,6 +569,8 @@ struct SipBwdFiD {
   static constexpr int kMaps = 3;   // z, backward factors, fi
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 3;
+  static constexpr int kPacers = 1;
+  static constexpr int kPW = 4;   // edge planes polled per communication pass
   __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
   CUtensorMap map[kMaps];
@@ -581,6 +593,8 @@ struct SipFactorD {
   static constexpr int kMaps = 7;   // ae, aw, an, as, at, ab, ap
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 3;
+  static constexpr int kPacers = 1;
+  static constexpr int kPW = 4;   // edge planes polled per communication pass
   __host__ __device__ static constexpr int nq(int) { return 1; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
   CUtensorMap map[kMaps];
@@ -629,6 +643,8 @@ struct SipFwdF {
   static constexpr int kMaps = 2;   // r, forward factors (bb, bw, bs, bp)
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 6;
+  static constexpr int kPacers = 2;
+  static constexpr int kPW = 8;
   __host__ __device__ static constexpr int nq(int m) { return m == 0 ? 1 : 4; }
   __host__ __device__ static constexpr int esize(int) { return 4; }
   CUtensorMap map[kMaps];
@@ -647,6 +663,8 @@ struct SipBwdF {
   static constexpr int kMaps = 2;   // z, backward factors (bn, be, bt)
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 6;
+  static constexpr int kPacers = 2;
+  static constexpr int kPW = 8;
   __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
   __host__ __device__ static constexpr int esize(int) { return 4; }
   CUtensorMap map[kMaps];
@@ -665,6 +683,8 @@ struct SipFactorF {
   static constexpr int kMaps = 7;   // ae, aw, an, as, at, ab, ap (FP32 copies)
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 4;
+  static constexpr int kPacers = 1;
+  static constexpr int kPW = 8;
   __host__ __device__ static constexpr int nq(int) { return 1; }
   __host__ __device__ static constexpr int esize(int) { return 4; }
   CUtensorMap map[kMaps];
