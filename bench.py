@@ -138,6 +138,11 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+LEARN_STEPS = 20     # PISO steps whose pressure solves are recorded as training pairs
+LEARN_EPOCHS = 20
+LEARN_BLOCK = 64     # training window (cells per axis)
+
+
 def snapshot(lib):
     """Every field and the parameters (outside any timed region)."""
     import cappgpu
@@ -149,6 +154,25 @@ def restore(lib, snap):
     for n, a in fields.items():
         lib.set_field(n, a)
     lib.set_params(params)
+
+
+def result_state(lib):
+    """Velocity, pressure and the continuity residual after a run (host copies)."""
+    p = lib.get_params()
+    return {"u": lib.get_field("u"), "v": lib.get_field("v"), "w": lib.get_field("w"), "p": lib.get_field("p"),
+            "continuity": float(p.sumlocalconterr)}
+
+
+def state_errors(x, ref):
+    """Relative L2 differences of u, v, w, p and the continuity residuals of two runs."""
+    import numpy as np
+    out = {}
+    for k in ("u", "v", "w", "p"):
+        den = float(np.linalg.norm(ref[k]))
+        out[k + "_rel_l2"] = float(np.linalg.norm(x[k] - ref[k])) / den if den else None
+    out["continuity"] = x["continuity"]
+    out["continuity_fp64"] = ref["continuity"]
+    return out
 
 
 def profiled_traffic(n):
@@ -240,6 +264,7 @@ def run_gpu(args, ws, rank, local):
     group.barrier()
     launches = lib.stats().launches - launches0
     st = lib.stats()
+    ref_state = result_state(lib)   # FP64 plain result of the timed steps
     ms = group.max(ms)
     value = ws * args.steps / (ms / 1e3)
 
@@ -275,10 +300,47 @@ def run_gpu(args, ws, rank, local):
     ms32 = group.max(lib.timer_stop())
     st32 = lib.stats()
     lib.precision(0)
+    errs = state_errors(result_state(lib), ref_state)
     fp32 = {"value": ws * args.steps / (ms32 / 1e3), "unit": "steps/s", "ms_per_step": ms32 / args.steps,
             "p_solve_ms": st32.p_solve_ms, "p_iters": st32.p_report.iters,
             "p_rel_residual": st32.p_report.resl / st32.p_report.res0 if st32.p_report.res0 else None,
-            "form": "FP32 SIP-preconditioned CG inside FP64 iterative refinement (exit test on the FP64 residual)"}
+            "form": "FP32 SIP-preconditioned CG inside FP64 iterative refinement (exit test on the FP64 residual)",
+            "errors_vs_fp64": errs}
+
+    # precision mode 2: the refinement form starting from the learned guess.
+    # The net is trained on pairs the solver records during steps of the
+    # refinement form from the same start, then the same timed steps run.
+    restore(lib, snap)
+    t0 = time.perf_counter()
+    lib.learn_reset(2 * LEARN_STEPS, seed=20261203)
+    lib.learn_collect(True)
+    lib.precision(1)
+    lib.piso_steps(LEARN_STEPS)
+    lib.learn_collect(False)
+    t1 = time.perf_counter()
+    loss = lib.learn_train(LEARN_EPOCHS, block=LEARN_BLOCK, lr=1e-3)
+    t2 = time.perf_counter()
+    restore(lib, snap)
+    lib.precision(2)
+    lib.piso_steps(1)   # warm-up of the inference buffers
+    restore(lib, snap)
+    s0 = lib.learn_stats()
+    group.barrier()
+    lib.timer_start()
+    lib.piso_steps(args.steps)
+    msl = group.max(lib.timer_stop())
+    stl = lib.stats()
+    s1 = lib.learn_stats()
+    lib.precision(0)
+    learned = {"value": ws * args.steps / (msl / 1e3), "unit": "steps/s", "ms_per_step": msl / args.steps,
+               "p_solve_ms": stl.p_solve_ms, "p_iters": stl.p_report.iters,
+               "p_rel_residual": stl.p_report.resl / stl.p_report.res0 if stl.p_report.res0 else None,
+               "guesses_kept": s1["guesses"] - s0["guesses"], "guesses_discarded": s1["fallbacks"] - s0["fallbacks"],
+               "train": {"pairs": 2 * LEARN_STEPS, "epochs": LEARN_EPOCHS, "block": LEARN_BLOCK, "loss": loss,
+                         "collect_s": t1 - t0, "train_s": t2 - t1},
+               "form": "as fp32_refined, each pressure solve starting from the learned guess when it lowers the "
+                       "FP64 residual",
+               "errors_vs_fp64": state_errors(result_state(lib), ref_state)}
 
     # roofline of the SIP forward substitution on the current state
     peak, peak_kind = measured_peaks()
@@ -308,6 +370,7 @@ def run_gpu(args, ws, rank, local):
                      "algorithmic_bytes": bytes_fwd, "ms_per_launch": ms_fwd},
         "units": units,
         "fp32_refined": fp32,
+        "fp32_learned": learned,
         "gpu_launches": launches,
         "clocks": clk,
     }

@@ -108,6 +108,13 @@ inline void launch(void (*k)(KArgs...), int grid, int block, cudaStream_t s, Arg
   k<<<grid, block, 0, s>>>(args...);
 }
 
+// launch() with a 2-D or 3-D grid
+template <typename... KArgs, typename... Args>
+inline void launch(void (*k)(KArgs...), dim3 grid, int block, cudaStream_t s, Args... args) {
+  ++ctx().launches;
+  k<<<grid, block, 0, s>>>(args...);
+}
+
 // launch() with dynamic shared memory
 template <typename... KArgs, typename... Args>
 inline void launch_smem(void (*k)(KArgs...), int grid, int block, size_t smem, cudaStream_t s, Args... args) {

@@ -74,6 +74,7 @@ static const char* kFieldNames[CAP_NFIELDS] = {
 
 static void free_all() {
   fast_free();
+  learned_free();
   Ctx& c = ctx();
   for (auto& p : c.f) { if (p) cudaFree(p); p = nullptr; }
   for (auto& p : c.bc) { if (p) cudaFree(p); p = nullptr; }
@@ -269,11 +270,11 @@ int cappgpu_set_option(const char* key, int value) {
 
 // Precision of the pressure solve (pcgsip): 0 = FP64 plain, the reference's
 // arithmetic (default); 1 = FP32 SIP-preconditioned CG inside FP64
-// iterative refinement.
+// iterative refinement; 2 = as 1, starting from the learned initial guess.
 int cappgpu_precision(int mode) {
   CAP_REQUIRE_INIT();
-  if (mode != 0 && mode != 1) {
-    set_error("precision mode %d: 0 (FP64 plain) or 1 (FP32 + FP64 refinement)", mode);
+  if (mode < 0 || mode > 2) {
+    set_error("precision mode %d: 0 (FP64 plain), 1 (FP32 + FP64 refinement) or 2 (1 + learned guess)", mode);
     return CAPPGPU_E_ARG;
   }
   ctx().precision = mode;

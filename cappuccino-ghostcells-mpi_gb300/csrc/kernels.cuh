@@ -22,6 +22,15 @@ int pcgsip_mixed(int fi, int ifi, cappgpu_solve_report* rep);
 int sipsol_fast(int fi, int ifi, cappgpu_solve_report* rep);
 int fast_profile_unit(int which, double* bytes);
 void fast_free();
+// learned initial guess (learned.cu)
+void learned_free();
+int learned_solve_start(int fif, double res0);
+int learned_solve_end(int fif);
+// natural-layout residual r = su - A fi over the interior of an arbitrary
+// field array, written to res, with its L1 norm (solvers.cu)
+int resid_into(const double* fi, double* res, double* l1);
+// z = A p over the interior (p's ghost values included) and (r.z, z.z)
+int spmv_dot2_natural(const double* p, double* z, const double* r, double* out2);
 
 // assembly
 int fluxuvw(int idew, int idns, int idtb, int arvx, int arvy, int arvz, int fif, int acfe, int acfw, int fcf);

@@ -741,6 +741,10 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
   double res0 = 0.0;
   if ((rc = resid_natural(fif, &res0))) return rc;
   P.resor[ifi - 1] = res0;
+  // recording of a training pair; in precision mode 2 the learned guess,
+  // kept only if it lowers the FP64 residual (the exit test below stays
+  // relative to res0)
+  if ((rc = learned_solve_start(fif, res0))) return rc;
   const int cf[8] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_SU};
   for (int q = 0; q < 8; ++q)
     if ((rc = to_d(cf[q], D_AE + q))) return rc;
@@ -832,6 +836,7 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     CAP_CHECK_LAUNCH();
   }
   if ((rc = from_d(D_FI, fif))) return rc;
+  if ((rc = learned_solve_end(fif))) return rc;
   if ((rc = from_d(D_RES, CAP_RES))) return rc;
   if (rep) {
     rep->res0 = res0;

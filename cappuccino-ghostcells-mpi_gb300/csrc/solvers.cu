@@ -221,10 +221,29 @@ int resid_natural(int fif, double* res0) {
   return reduce_fetch(1, res0);
 }
 
+int spmv_dot2_natural(const double* p, double* z, const double* r, double* out2) {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  Box b{3, d.nimm, 3, d.njmm, 3, d.nkmm};
+  launch(k_spmv, kRedBlocks, kThreads, c.st, d, b, coef(), p, z, (double*)nullptr);
+  launch(k_dot, kRedBlocks, kThreads, c.st, d, b, r, (const double*)z, (const double*)z, (const double*)z, c.partials);
+  CAP_CHECK_LAUNCH();
+  return reduce_fetch(2, out2);
+}
+
+int resid_into(const double* fi, double* res, double* l1) {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  Box b{3, d.nimm, 3, d.njmm, 3, d.nkmm};
+  launch(k_resid, kRedBlocks, kThreads, c.st, d, b, coef(), fi, res, c.partials);
+  CAP_CHECK_LAUNCH();
+  return reduce_fetch(1, l1);
+}
+
 int pcgsip(int fif, int ifi, cappgpu_solve_report* rep) {
   Ctx& c = ctx();
   if (c.wave_impl == 1 && c.d.nimm >= 4 && c.d.njmm >= 4 && c.d.nkmm >= 4)
-    return c.precision == 1 ? pcgsip_mixed(fif, ifi, rep) : pcgsip_fast(fif, ifi, rep);
+    return c.precision >= 1 ? pcgsip_mixed(fif, ifi, rep) : pcgsip_fast(fif, ifi, rep);
   const Dims& d = c.d;
   double** F = c.f;
   cappgpu_params& P = c.prm;

@@ -59,6 +59,13 @@ SIGNATURES = {
     "cappgpu_spmv": [_INT, _INT, _DP],
     "cappgpu_spmv_noalloc": [_INT, _INT, _DP],
     "cappgpu_precision": [_INT],
+    "cappgpu_learn_reset": [_INT, ctypes.c_ulonglong],
+    "cappgpu_learn_collect": [_INT],
+    "cappgpu_learn_train": [_INT, _INT, ctypes.c_double, _DP],
+    "cappgpu_learn_params": [ctypes.POINTER(ctypes.c_float), _INT, _INT],
+    "cappgpu_learn_stats": [ctypes.POINTER(_INT), ctypes.POINTER(_INT), ctypes.POINTER(_INT), _DP],
+    "cappgpu_learn_check": [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _INT, _INT, _INT,
+                            ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _DP],
     "cappgpu_fluxuvw": [_INT] * 10,
     "cappgpu_calcuvw": [_REP],
     "cappgpu_piso_assemble_pressure_eq": [_INT] * 12,
@@ -246,6 +253,50 @@ class Library:
     def precision(self, mode):
         """0 = FP64 plain (reference arithmetic), 1 = FP32 preconditioned CG in FP64 refinement."""
         self._check(self.lib.cappgpu_precision(int(mode)), "precision")
+
+    # ------------------------------------------------ learned initial guess
+    def learn_reset(self, max_samples, seed=0):
+        self._check(self.lib.cappgpu_learn_reset(int(max_samples), int(seed)), "learn_reset")
+
+    def learn_collect(self, on=True):
+        self._check(self.lib.cappgpu_learn_collect(1 if on else 0), "learn_collect")
+
+    def learn_train(self, epochs, block=32, lr=1e-3):
+        loss = ctypes.c_double()
+        self._check(self.lib.cappgpu_learn_train(int(epochs), int(block), float(lr), ctypes.byref(loss)), "learn_train")
+        return loss.value
+
+    def learn_params(self, values=None):
+        fp = ctypes.POINTER(ctypes.c_float)
+        n = self.lib.cappgpu_learn_params(ctypes.cast(None, fp), 0, 0)
+        self._check(n, "learn_params")
+        if values is None:
+            out = np.empty(n, np.float32)
+            self._check(self.lib.cappgpu_learn_params(out.ctypes.data_as(fp), n, 0), "learn_params")
+            return out
+        a = np.ascontiguousarray(values, dtype=np.float32)
+        self._check(self.lib.cappgpu_learn_params(a.ctypes.data_as(fp), a.size, 1), "learn_params")
+
+    def learn_stats(self):
+        s, g, f, r = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        self._check(self.lib.cappgpu_learn_stats(ctypes.byref(s), ctypes.byref(g), ctypes.byref(f), ctypes.byref(r)),
+                    "learn_stats")
+        return {"samples": s.value, "guesses": g.value, "fallbacks": f.value, "last_ratio": r.value}
+
+    def learn_check(self, inp, tgt):
+        """One forward + backward pass on a (D, H, W) input/target: output, parameter gradients, loss."""
+        fp = ctypes.POINTER(ctypes.c_float)
+        inp = np.ascontiguousarray(inp, np.float32)
+        tgt = np.ascontiguousarray(tgt, np.float32)
+        D, H, W = inp.shape
+        out = np.empty_like(inp)
+        n = self.lib.cappgpu_learn_params(ctypes.cast(None, fp), 0, 0)
+        grad = np.empty(n, np.float32)
+        loss = ctypes.c_double()
+        self._check(self.lib.cappgpu_learn_check(inp.ctypes.data_as(fp), tgt.ctypes.data_as(fp), D, H, W,
+                                                 out.ctypes.data_as(fp), grad.ctypes.data_as(fp), ctypes.byref(loss)),
+                    "learn_check")
+        return out, grad, loss.value
 
     def spmv(self, pk, zk):
         dot = ctypes.c_double()

@@ -203,6 +203,37 @@ int cappgpu_set_option(const char* key, int value);
    CAPPGPU_E_ARG for other modes. */
 int cappgpu_precision(int mode);
 
+/* ================================================ learned initial guess */
+/* No counterpart in the reference.  A small 3-D convolutional net (four
+   3x3x3 layers of 16 channels, dilations 1,2,4,8, ReLU, then 1x1x1 to one
+   channel; BF16 on the tensor cores, FP32 accumulation and master weights,
+   Adam) predicts the correction of a pressure solve from its initial
+   residual, both normalised by the mean |residual|.  In precision mode 2 the
+   refinement form of cappgpu_pcgsip starts from fi + guess when that lowers
+   the FP64 residual and from fi otherwise; its exit test stays relative to
+   the residual of fi, so the plain solve is judge and fallback.
+   cappgpu_learn_reset     (re)creates the net with seeded weights and room
+                           for max_samples recorded pairs of this grid
+   cappgpu_learn_collect   records (residual, converged correction) pairs in
+                           the pressure solves that follow (precision 1 or 2)
+   cappgpu_learn_train     Adam on random block^3 windows of the pairs,
+                           mean-squared error; *loss = mean loss of the last
+                           epoch
+   cappgpu_learn_params    FP32 parameters out (direction 0) or in (1); with
+                           host == NULL returns the parameter count
+   cappgpu_learn_stats     pairs recorded, guesses kept, guesses discarded,
+                           residual ratio of the last guess
+   cappgpu_learn_check     one forward and backward pass on a D x H x W
+                           input/target from the host (for tests): output,
+                           parameter gradients and loss */
+int cappgpu_learn_reset(int max_samples, unsigned long long seed);
+int cappgpu_learn_collect(int on);
+int cappgpu_learn_train(int epochs, int block, double lr, double* loss);
+int cappgpu_learn_params(float* host, int n, int direction);
+int cappgpu_learn_stats(int* samples, int* guesses, int* fallbacks, double* last_ratio);
+int cappgpu_learn_check(const float* input, const float* target, int D, int H, int W, float* output, float* grad,
+                        double* loss);
+
 /* ======================================================= index maps (a1) */
 /* setind.f90:34-40: li(i)=(i-1)*nj for i=1..ni, lk(k)=(k-1)*nij.  Writes
    the device copies back (tests compare them element-wise). */

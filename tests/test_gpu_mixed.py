@@ -63,4 +63,4 @@ def test_mixed_piso_step_channel(gpu_lib):
 def test_precision_rejects_unknown_mode(gpu_lib):
     gpu_lib.init(8, 8, 8)
     with pytest.raises(cappgpu.CappError):
-        gpu_lib.precision(2)
+        gpu_lib.precision(3)
