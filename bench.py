@@ -138,6 +138,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_peak():
+    """Dense BF16 TFLOP/s (burst: the net's kernels are timed alone)."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        if d.get("bf16_tflops"):
+            return d["bf16_tflops"], "measured"
+    return 1900.0, "fallback"
+
+
 LEARN_STEPS = 20     # PISO steps whose pressure solves are recorded as training pairs
 LEARN_EPOCHS = 20
 LEARN_BLOCK = 64     # training window (cells per axis)
@@ -332,15 +342,65 @@ def run_gpu(args, ws, rank, local):
     stl = lib.stats()
     s1 = lib.learn_stats()
     lib.precision(0)
+    # the net's own kernels: one forward pass on this grid (the guess) and one
+    # training pass (forward + backward) on a 64^3 window, against the
+    # measured dense BF16 peak
+    bf16_peak, bf16_kind = measured_bf16_peak()
+    net = {}
+    for w, name in ((9, "inference"), (10, "train_pass")):
+        m, fl = lib.profile_kernel(w, reps=3)
+        tf = fl / (m / 1e3) / 1e12
+        net[name] = {"ms": m, "gflop": fl / 1e9, "tflops": tf, "frac_of_bf16_peak": tf / bf16_peak}
+    net["bf16_peak_tflops"] = bf16_peak
+    net["peak_source"] = bf16_kind
     learned = {"value": ws * args.steps / (msl / 1e3), "unit": "steps/s", "ms_per_step": msl / args.steps,
                "p_solve_ms": stl.p_solve_ms, "p_iters": stl.p_report.iters,
                "p_rel_residual": stl.p_report.resl / stl.p_report.res0 if stl.p_report.res0 else None,
                "guesses_kept": s1["guesses"] - s0["guesses"], "guesses_discarded": s1["fallbacks"] - s0["fallbacks"],
                "train": {"pairs": 2 * LEARN_STEPS, "epochs": LEARN_EPOCHS, "block": LEARN_BLOCK, "loss": loss,
-                         "collect_s": t1 - t0, "train_s": t2 - t1},
+                         "loss_kind": "residual norm |A d - r|^2/|r|^2 on the window", "collect_s": t1 - t0,
+                         "train_s": t2 - t1},
+               "net": net,
                "form": "as fp32_refined, each pressure solve starting from the learned guess when it lowers the "
                        "FP64 residual",
                "errors_vs_fp64": state_errors(result_state(lib), ref_state)}
+
+    # Arithmetic errors of the two reduced-precision forms.  The reference
+    # solves p to sor = 0.1 only in the first corrector, and where that
+    # solve stops moves the step's result by far more than FP32 rounding
+    # (fp64_first_corrector_spread below: FP64 with the first corrector
+    # solved to the last one's tolerance against the reference's FP64).  So
+    # the three forms are also compared with every corrector solved to the
+    # last one's tolerance (the "tight_correctors" option), untimed.
+    lib.set_option("tight_correctors", 1)
+    tight = {}
+    for mode in (0, 1, 2):
+        restore(lib, snap)
+        lib.precision(mode)
+        lib.piso_steps(args.steps)
+        tight[mode] = result_state(lib)
+    lib.precision(0)
+    # FP64 with every solve 100x tighter: how far the 1e-6 tolerance itself
+    # lets a solution lie from the converged one
+    restore(lib, snap)
+    pr = lib.get_params()
+    sor_p = pr.sor[3]
+    pr.sor[3] = sor_p * 1e-2
+    pr.nsw[3] = max(pr.nsw[3], 4000)
+    lib.set_params(pr)
+    lib.piso_steps(args.steps)
+    tight_fine = result_state(lib)
+    lib.set_option("tight_correctors", 0)
+    restore(lib, snap)
+    precision_check = {
+        "steps": args.steps,
+        "fp64_first_corrector_spread": state_errors(tight[0], ref_state),
+        "fp64_vs_fp64_solved_100x_tighter": state_errors(tight[0], tight_fine),
+        "fp32_refined_vs_fp64": state_errors(tight[1], tight[0]),
+        "fp32_learned_vs_fp64": state_errors(tight[2], tight[0]),
+        "fp32_refined_vs_fp64_solved_100x_tighter": state_errors(tight[1], tight_fine),
+        "note": "every corrector solved to the last one's tolerance in all runs",
+    }
 
     # roofline of the SIP forward substitution on the current state
     peak, peak_kind = measured_peaks()
@@ -371,6 +431,7 @@ def run_gpu(args, ws, rank, local):
         "units": units,
         "fp32_refined": fp32,
         "fp32_learned": learned,
+        "precision_check": precision_check,
         "gpu_launches": launches,
         "clocks": clk,
     }

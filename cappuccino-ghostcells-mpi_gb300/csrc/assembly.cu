@@ -833,7 +833,9 @@ int piso_multiple_correction(cappgpu_solve_report* reps) {
       launch(k_pin, 1, 1, c.st, inpr, F[CAP_AP], F[CAP_AE], F[CAP_AW], F[CAP_AN], F[CAP_AS], F[CAP_AT], F[CAP_AB],
                                F[CAP_SU], F[CAP_P]);
       CAP_CHECK_LAUNCH();
-      if (P.icorr != P.ncorr) P.sor[CAP_IP - 1] = (double)0.1f;   // sor(ip) = 0.1 (default real), :132
+      // sor(ip) = 0.1 (default real) before the last corrector, :132; the
+      // tight_correctors option solves every corrector to reltol
+      if (P.icorr != P.ncorr && !c.tight_correctors) P.sor[CAP_IP - 1] = (double)0.1f;
       else P.sor[CAP_IP - 1] = reltol;
       cappgpu_solve_report prep{};
       CAP_CUDA(cudaEventRecord(c.ev[2], c.st));

@@ -76,6 +76,7 @@ struct Ctx {
   cappgpu_solve_report p_rep{};        // its report
   cudaEvent_t ev[4] = {};
   int wave_impl = 1;                   // 1 persistent wavefront, 0 one launch per hyperplane
+  int tight_correctors = 0;            // 1: every PISO corrector solves p to reltol, not only the last
   int precision = 0;                   // pcgsip: 0 FP64 plain, 1 FP32 preconditioned CG in FP64 refinement
 };
 

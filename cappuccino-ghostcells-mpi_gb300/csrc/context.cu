@@ -264,6 +264,10 @@ int cappgpu_set_option(const char* key, int value) {
   CAP_REQUIRE_INIT();
   if (!key) return CAPPGPU_E_ARG;
   if (strcmp(key, "wave") == 0 && (value == 0 || value == 1)) { ctx().wave_impl = value; return CAPPGPU_OK; }
+  if (strcmp(key, "tight_correctors") == 0 && (value == 0 || value == 1)) {
+    ctx().tight_correctors = value;
+    return CAPPGPU_OK;
+  }
   set_error("unknown option %s=%d", key, value);
   return CAPPGPU_E_ARG;
 }

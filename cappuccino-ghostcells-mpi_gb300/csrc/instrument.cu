@@ -66,7 +66,7 @@ int cappgpu_host_free(void* p) {
 // arrays they write (gradu, su.., ae/aw, f1, be), as the routines do.
 int cappgpu_profile_kernel(int which, int reps, double* ms_per_unit, double* algo_bytes) {
   CAP_REQUIRE_INIT();
-  if (reps < 1 || which < 0 || which > 8) { set_error("profile_kernel: bad arguments"); return CAPPGPU_E_ARG; }
+  if (reps < 1 || which < 0 || which > 10) { set_error("profile_kernel: bad arguments"); return CAPPGPU_E_ARG; }
   Ctx& c = ctx();
   double bytes = 0.0;
   int rc = profile_unit(which, &bytes);   // warm-up

@@ -1,25 +1,37 @@
 // learned.cu -- the learned initial guess of the pressure solve
 // (cappgpu_precision(2); no counterpart in the reference).
 //
-// A small 3-D convolutional net predicts the shape of the correction
-// d = A^-1 r0 of a pressure solve from its initial residual r0 (input
-// normalised by the mean |r0|, target by the mean |d|); the amplitude is
-// fitted at solve time by least squares, alpha = (r0.Ad)/(Ad.Ad), which
-// costs one product with A.  The plain solve always continues from the guess
-// to the same tolerance -- the exit test stays relative to the residual of
-// the solve's own start -- so the solver is both judge and fallback: a guess
-// that does not lower the FP64 residual is discarded.
+// A 3-level 3-D convolutional U-Net predicts the correction d of a pressure
+// solve, A d = r0, from the solve's initial residual r0.  Inputs are
+// normalised by the RMS of r0 and the operator by the mean of its diagonal
+// (r^ = r0/rms, A^ = A/mean(ap)); the net's output d^ is trained to make
+// A^ d^ = r^ on the residual-norm loss |A^ d^ - r^|^2 / |r^|^2, with A^ the
+// 7-point operator of the recorded solve restricted to the training window.
+// At solve time the amplitude of the guess is fitted by least squares,
+// alpha = (r0.Ad)/(Ad.Ad), which costs one product with A.  The plain solve
+// always continues from the guess to the same tolerance -- the exit test
+// stays relative to the residual of the solve's own start -- so the solver
+// is both judge and fallback: a guess that does not lower the FP64 residual
+// is discarded.
 //
-// Net: four 3x3x3 convolutions of 16 channels with dilations 1, 2, 4, 8 and
-// ReLU, then a 1x1x1 convolution to one channel (receptive field 31 cells).
+// Net (channels 16/32/64, 3x3x3 kernels, ReLU, zero padding):
+//   level 1  e1a 1->16, e1b 16->16 ............ d1a 48->16, d1b 16->16, 1x1x1 16->1
+//   level 2  avg-pool 2, e2a 16->32, e2b 32->32 ... d2a 96->32, d2b 32->32, nearest-up 2
+//   level 3  avg-pool 2, e3a 32->64, e3b 64->64, nearest-up 2
+// The decoder's input at each level is the up-sampled coarser output
+// followed by the encoder's output of that level (channel concatenation,
+// written in place by the producing layer).  Grid extents are multiples of 4
+// (the solve's interior is zero-padded up to that).
+//
 // Activations and weights are BF16, accumulation FP32, FP32 master weights,
 // Adam.  Convolutions are implicit GEMMs on the tensor cores (mma.sync
 // m16n8k16): forward and input gradient (the same kernel with flipped,
-// transposed weights) take 16 output voxels x 16 channels per warp and K = 27
-// taps x 16 channels; the weight gradient is a GEMM over voxels per tap,
-// split in chunks and summed in a fixed order.  Training pairs are recorded by
-// the solver itself (cappgpu_learn_collect) and the net is trained on random
-// cubic windows of them (cappgpu_learn_train).
+// transposed weights and the ReLU mask of the layer's output) take 16 voxels
+// x 16 output channels per warp and K = 27 taps x input channels; the weight
+// gradient is a GEMM over voxels per tap, split in chunks and summed in a
+// fixed order.  Training pairs are recorded by the solver itself
+// (cappgpu_learn_collect) and the net is trained on random cubic windows of
+// them (cappgpu_learn_train).
 #include <cuda_bf16.h>
 #include <math.h>
 #include <string.h>
@@ -34,39 +46,52 @@ namespace cap {
 namespace {
 
 typedef __nv_bfloat16 bf16;
-constexpr int kC = 16;                 // channels of the hidden layers
-constexpr int kLayers = 4;             // 3x3x3 layers
-constexpr int kWConv = kC * 27 * kC;   // weights of one 3x3x3 layer, [co][tap][ci]
-constexpr int kParams = kLayers * (kWConv + kC) + kC + 1;
-__host__ __device__ constexpr int offW(int l) { return l * (kWConv + kC); }
-__host__ __device__ constexpr int offB(int l) { return l * (kWConv + kC) + kWConv; }
-constexpr int kOffLastW = kLayers * (kWConv + kC);
-constexpr int kOffLastB = kOffLastW + kC;
-constexpr int kDil[kLayers] = {1, 2, 4, 8};
-constexpr int kChunk = 4096;           // voxels per weight-gradient partial
+
+// ------------------------------------------------------------ the layers
+constexpr int kNL = 10;   // 3x3x3 layers in execution order
+constexpr int kCI[kNL] = {16, 16, 16, 32, 32, 64, 96, 32, 48, 16};   // layer 0: 1 used of 16
+constexpr int kCO[kNL] = {16, 16, 32, 32, 64, 64, 32, 32, 16, 16};
+constexpr int kC1 = 16;   // channels at the output of the last 3x3x3 layer
+constexpr int wsize(int l) { return kCO[l] * 27 * kCI[l]; }
+constexpr int woff(int l) { return l == 0 ? 0 : woff(l - 1) + wsize(l - 1); }                // BF16 weight arrays
+constexpr int offW(int l) { return l == 0 ? 0 : offW(l - 1) + wsize(l - 1) + kCO[l - 1]; }   // parameters
+constexpr int offB(int l) { return offW(l) + wsize(l); }
+constexpr int kWAll = woff(kNL - 1) + wsize(kNL - 1);
+constexpr int kOffLastW = offB(kNL - 1) + kCO[kNL - 1];
+constexpr int kOffLastB = kOffLastW + kC1;
+constexpr int kParams = kOffLastB + 1;
+constexpr int kChunk = 8192;   // voxels per weight-gradient partial
+
+__constant__ int cCI[kNL] = {16, 16, 16, 32, 32, 64, 96, 32, 48, 16};
+__constant__ int cCO[kNL] = {16, 16, 32, 32, 64, 64, 32, 32, 16, 16};
+__constant__ int cWoff[kNL] = {woff(0), woff(1), woff(2), woff(3), woff(4),
+                               woff(5), woff(6), woff(7), woff(8), woff(9)};
+__constant__ int cOffW[kNL] = {offW(0), offW(1), offW(2), offW(3), offW(4),
+                               offW(5), offW(6), offW(7), offW(8), offW(9)};
+
+// activation and gradient buffers of one grid size (level 1: V1 voxels)
+struct Acts {
+  long long V1 = 0;
+  bf16 *a0, *a1, *cat1, *p1, *a3, *cat2, *p2, *a5, *b3, *a7, *x2, *a9, *x1;
+  bf16 *gx1, *ga9, *gcat1, *gx2, *ga7, *gcat2, *gb3, *ga5, *gp2, *ga3, *gp1, *ga1;
+  float *out, *gout, *rhs, *coef, *res;
+  void* base = nullptr;
+};
 
 struct Net {
   bool ready = false, trained = false, collect = false;
   float *p = nullptr, *gp = nullptr, *m = nullptr, *v = nullptr;   // parameters, gradients, Adam moments
-  bf16* wb = nullptr;    // BF16 conv weights [layer][co][tap][ci]
-  bf16* wt = nullptr;    // flipped, transposed [layer][ci][tap][co] (input gradient)
+  bf16* wb = nullptr;    // BF16 conv weights, layer l at woff(l): [co][tap][ci]
+  bf16* wt = nullptr;    // flipped, transposed, layer l at woff(l): [ci][tap][co] (input gradient)
   int adam_t = 0;
-  long long maxV = 0;
-  bf16* act[kLayers + 1] = {};   // act[0] input (16 channels, channel 0 used); act[l+1] output of layer l
-  float* out = nullptr;          // output (1 channel)
-  float* tgt = nullptr;          // training target
-  float* gout = nullptr;         // dL/dout
-  bf16* g[2] = {};               // gradients w.r.t. activations
+  Acts A;
   float* part = nullptr;         // partial sums
   size_t part_n = 0;
-  double* dsum = nullptr;        // device scalars
-  // recorded pairs
+  double* dsum = nullptr;        // device scalars: loss
+  // recorded pairs: [sample][8][sV]: r^, then A^ as xp, xm, yp, ym, zp, zm, diag
   int max_samples = 0, nsamples = 0, next = 0;
   int sD = 0, sH = 0, sW = 0;
-  bf16* srhs = nullptr;          // [max_samples][sV] normalised initial residual
-  float* sdel = nullptr;         // [max_samples][sV] normalised correction
-  double* fi0 = nullptr;         // interior of fi at the start of the solve being recorded
-  int pending = -1;              // slot of the sample whose correction is still to come
+  float* store = nullptr;
   // statistics of the guesses
   int guesses = 0, fallbacks = 0;
   double last_ratio = 0.0;
@@ -75,14 +100,17 @@ struct Net {
 
 Net N;
 
+void acts_free() {
+  cudaFree(N.A.base);
+  N.A = Acts();
+}
+
 void net_free() {
   cudaFree(N.p); cudaFree(N.gp); cudaFree(N.m); cudaFree(N.v);
   cudaFree(N.wb); cudaFree(N.wt);
-  for (auto& a : N.act) cudaFree(a);
-  cudaFree(N.out); cudaFree(N.tgt); cudaFree(N.gout);
-  cudaFree(N.g[0]); cudaFree(N.g[1]);
+  acts_free();
   cudaFree(N.part); cudaFree(N.dsum);
-  cudaFree(N.srhs); cudaFree(N.sdel); cudaFree(N.fi0);
+  cudaFree(N.store);
   N = Net();
 }
 
@@ -99,30 +127,35 @@ __device__ __forceinline__ unsigned pack2(bf16 lo, bf16 hi) {
   return (unsigned)__bfloat16_as_ushort(lo) | ((unsigned)__bfloat16_as_ushort(hi) << 16);
 }
 
-// voxel v of a D x H x W grid (x fastest); neighbour at (dz,dy,dx) or -1
-__device__ __forceinline__ long long nbr(long long v, int dz, int dy, int dx, int D, int H, int W) {
-  const int x = (int)(v % W);
-  const long long r = v / W;
-  const int y = (int)(r % H), z = (int)(r / H);
-  const int zz = z + dz, yy = y + dy, xx = x + dx;
-  if (zz < 0 || zz >= D || yy < 0 || yy >= H || xx < 0 || xx >= W) return -1;
-  return ((long long)zz * H + yy) * W + xx;
+__device__ __forceinline__ bool pos(bf16 x) {
+  const unsigned short u = __bfloat16_as_ushort(x);
+  return u != 0 && (u & 0x8000u) == 0;
 }
 
-__device__ __forceinline__ void tap_off(int tap, int dil, int& dz, int& dy, int& dx) {
-  dz = (tap / 9 - 1) * dil;
-  dy = ((tap / 3) % 3 - 1) * dil;
-  dx = (tap % 3 - 1) * dil;
-}
+// a voxel's coordinates in a D x H x W grid (x fastest)
+struct Vox {
+  int x, y, z;
+  __device__ Vox(int v, int H, int W) {
+    x = v % W;
+    const int r = v / W;
+    y = r % H;
+    z = r / H;
+  }
+  __device__ int nbr(int v, int dz, int dy, int dx, int D, int H, int W) const {
+    const int zz = z + dz, yy = y + dy, xx = x + dx;
+    if ((unsigned)zz >= (unsigned)D || (unsigned)yy >= (unsigned)H || (unsigned)xx >= (unsigned)W) return -1;
+    return v + (dz * H + dy) * W + dx;
+  }
+};
 
-// two channels (c, c+1) of voxel n; with a mask, a channel counts only where
-// the mask activation is positive (ReLU derivative)
-__device__ __forceinline__ unsigned load_pair(const bf16* __restrict__ x, const bf16* __restrict__ mask, long long n,
-                                              int c) {
+// two channels (c, c+1) of voxel n (row pitch ld); with a mask, a channel
+// counts only where the mask (a ReLU output) is positive
+__device__ __forceinline__ unsigned load_pair(const bf16* __restrict__ x, int ld, const bf16* __restrict__ mask,
+                                              int ldm, int n, int c) {
   if (n < 0) return 0u;
-  unsigned u = *reinterpret_cast<const unsigned*>(x + n * kC + c);
+  unsigned u = *reinterpret_cast<const unsigned*>(x + (long long)n * ld + c);
   if (mask) {
-    const unsigned mk = *reinterpret_cast<const unsigned*>(mask + n * kC + c);
+    const unsigned mk = *reinterpret_cast<const unsigned*>(mask + (long long)n * ldm + c);
     const unsigned lo = mk & 0xffffu, hi = mk >> 16;
     if (!(lo != 0u && (lo & 0x8000u) == 0u)) u &= 0xffff0000u;
     if (!(hi != 0u && (hi & 0x8000u) == 0u)) u &= 0x0000ffffu;
@@ -130,127 +163,146 @@ __device__ __forceinline__ unsigned load_pair(const bf16* __restrict__ x, const 
   return u;
 }
 
-// y = act(conv3x3x3(x * [mask > 0], w) + bias): 16 -> 16 channels, dilation
-// dil, zero padding.  One warp: 16 voxels x 16 output channels.
-__global__ void __launch_bounds__(256) k_conv3(const bf16* __restrict__ x, const bf16* __restrict__ w,
-                                               const float* __restrict__ bias, const bf16* __restrict__ mask,
-                                               bf16* __restrict__ y, int D, int H, int W, int dil, int relu) {
-  __shared__ unsigned ws[kWConv / 2];
-  for (int q = threadIdx.x; q < kWConv / 2; q += blockDim.x) ws[q] = reinterpret_cast<const unsigned*>(w)[q];
+// row pitch (32-bit words) of one output channel's weights in shared memory:
+// 27*CI/2 rounded so that the 8 rows a warp reads fall in distinct banks
+__host__ __device__ constexpr int wrow(int CI) { return 27 * CI / 2 + ((4 - (27 * CI / 2) % 32) + 32) % 32; }
+
+// y[:, co0..co0+15] = act(conv3x3x3(x * [mask > 0], w) + bias) for the
+// output-channel slice co0 = 16*blockIdx.y.  x: CI channels at pitch ldx;
+// w: [CO][27][CI]; y at pitch ldy.  One warp: 16 voxels x 16 channels per
+// tile, tiles grid-strided.
+template <int CI>
+__global__ void __launch_bounds__(256) k_conv3(const bf16* __restrict__ x, int ldx, const bf16* __restrict__ w,
+                                               const float* __restrict__ bias, const bf16* __restrict__ mask, int ldm,
+                                               bf16* __restrict__ y, int ldy, int D, int H, int W, int relu) {
+  extern __shared__ unsigned ws[];   // [16][wrow(CI)]
+  constexpr int R = wrow(CI);
+  const int co0 = blockIdx.y * 16;
+  for (int q = threadIdx.x; q < 16 * 27 * CI / 2; q += blockDim.x) {
+    const int co = q / (27 * CI / 2), r = q - co * (27 * CI / 2);
+    ws[co * R + r] = reinterpret_cast<const unsigned*>(w + (size_t)(co0 + co) * 27 * CI)[r];
+  }
   __syncthreads();
-  const long long V = (long long)D * H * W;
+  const int V = D * H * W;
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const long long vb = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 16;
-  if (vb >= V) return;
-  const long long v0 = vb + g, v1 = vb + g + 8;
-  float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-  for (int tap = 0; tap < 27; ++tap) {
-    int dz, dy, dx;
-    tap_off(tap, dil, dz, dy, dx);
-    const long long n0 = v0 < V ? nbr(v0, dz, dy, dx, D, H, W) : -1;
-    const long long n1 = v1 < V ? nbr(v1, dz, dy, dx, D, H, W) : -1;
-    unsigned a[4];
-    a[0] = load_pair(x, mask, n0, t * 2);
-    a[1] = load_pair(x, mask, n1, t * 2);
-    a[2] = load_pair(x, mask, n0, 8 + t * 2);
-    a[3] = load_pair(x, mask, n1, 8 + t * 2);
+  const int ntiles = (V + 15) / 16;
+  for (int tile = blockIdx.x * 8 + (threadIdx.x >> 5); tile < ntiles; tile += gridDim.x * 8) {
+    const int v0 = tile * 16 + g, v1 = v0 + 8;
+    const Vox P0(v0 < V ? v0 : 0, H, W), P1(v1 < V ? v1 : 0, H, W);
+    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    for (int tap = 0; tap < 27; ++tap) {
+      const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+      const int n0 = v0 < V ? P0.nbr(v0, dz, dy, dx, D, H, W) : -1;
+      const int n1 = v1 < V ? P1.nbr(v1, dz, dy, dx, D, H, W) : -1;
+#pragma unroll
+      for (int ks = 0; ks < CI / 16; ++ks) {
+        unsigned a[4];
+        a[0] = load_pair(x, ldx, mask, ldm, n0, ks * 16 + t * 2);
+        a[1] = load_pair(x, ldx, mask, ldm, n1, ks * 16 + t * 2);
+        a[2] = load_pair(x, ldx, mask, ldm, n0, ks * 16 + 8 + t * 2);
+        a[3] = load_pair(x, ldx, mask, ldm, n1, ks * 16 + 8 + t * 2);
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) {
+          const unsigned* wr = ws + (nt * 8 + g) * R + tap * (CI / 2) + ks * 8 + t;
+          const unsigned b[2] = {wr[0], wr[4]};
+          mma16816(acc[nt], a, b);
+        }
+      }
+    }
 #pragma unroll
     for (int nt = 0; nt < 2; ++nt) {
-      const int co = nt * 8 + g;
-      unsigned b[2];
-      b[0] = ws[((co * 27 + tap) * kC + t * 2) / 2];
-      b[1] = ws[((co * 27 + tap) * kC + 8 + t * 2) / 2];
-      mma16816(acc[nt], a, b);
+      const int co = co0 + nt * 8 + t * 2;
+      const float b0 = bias ? bias[co] : 0.f, b1 = bias ? bias[co + 1] : 0.f;
+      float r[4] = {acc[nt][0] + b0, acc[nt][1] + b1, acc[nt][2] + b0, acc[nt][3] + b1};
+      if (relu)
+        for (int q = 0; q < 4; ++q) r[q] = fmaxf(r[q], 0.f);
+      if (v0 < V)
+        *reinterpret_cast<unsigned*>(y + (long long)v0 * ldy + co) = pack2(__float2bfloat16(r[0]), __float2bfloat16(r[1]));
+      if (v1 < V)
+        *reinterpret_cast<unsigned*>(y + (long long)v1 * ldy + co) = pack2(__float2bfloat16(r[2]), __float2bfloat16(r[3]));
     }
-  }
-#pragma unroll
-  for (int nt = 0; nt < 2; ++nt) {
-    const int co = nt * 8 + t * 2;
-    const float b0 = bias ? bias[co] : 0.f, b1 = bias ? bias[co + 1] : 0.f;
-    float r[4] = {acc[nt][0] + b0, acc[nt][1] + b1, acc[nt][2] + b0, acc[nt][3] + b1};
-    if (relu)
-      for (int q = 0; q < 4; ++q) r[q] = fmaxf(r[q], 0.f);
-    if (v0 < V) *reinterpret_cast<unsigned*>(y + v0 * kC + co) = pack2(__float2bfloat16(r[0]), __float2bfloat16(r[1]));
-    if (v1 < V) *reinterpret_cast<unsigned*>(y + v1 * kC + co) = pack2(__float2bfloat16(r[2]), __float2bfloat16(r[3]));
   }
 }
 
-// partial weight gradients of a 3x3x3 layer: for one tap and one chunk of
-// voxels, G[co][ci] = sum_v gy[v][co] [y[v][co] > 0] x[v + off(tap)][ci]
-__global__ void __launch_bounds__(128) k_wgrad3(const bf16* __restrict__ x, const bf16* __restrict__ gy,
-                                                const bf16* __restrict__ y, float* __restrict__ part, int D, int H,
-                                                int W, int dil) {
-  __shared__ float red[4][kC * kC];
-  const long long V = (long long)D * H * W;
-  const int tap = blockIdx.x, ch = blockIdx.y;
-  const long long vs = (long long)ch * kChunk, ve = min(V, vs + kChunk);
+// partial weight gradients of a 3x3x3 layer: for one tap, one chunk of
+// voxels and the output-channel slice co0 = 16*blockIdx.z,
+// G[co][ci] = sum_v gy[v][co] [y[v][co] > 0] x[v + off(tap)][ci]
+template <int CI>
+__global__ void __launch_bounds__(128) k_wgrad3(const bf16* __restrict__ x, int ldx, const bf16* __restrict__ gy,
+                                                int ldg, const bf16* __restrict__ y, int ldy, float* __restrict__ part,
+                                                int CO, int D, int H, int W) {
+  __shared__ float red[4][16 * CI];
+  const int V = D * H * W;
+  const int tap = blockIdx.x, ch = blockIdx.y, co0 = blockIdx.z * 16;
+  const int vs = ch * kChunk, ve = min(V, vs + kChunk);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  int dz, dy, dx;
-  tap_off(tap, dil, dz, dy, dx);
-  auto gm = [&](long long v, int co) -> bf16 {   // masked output gradient
+  const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+  auto gm = [&](int v, int co) -> bf16 {   // masked output gradient
     if (v >= ve) return __float2bfloat16(0.f);
-    const bf16 yy = y[v * kC + co];
-    return __bfloat162float(yy) > 0.f ? gy[v * kC + co] : __float2bfloat16(0.f);
+    return pos(y[(long long)v * ldy + co0 + co]) ? gy[(long long)v * ldg + co0 + co] : __float2bfloat16(0.f);
   };
-  auto xs = [&](long long v, int ci) -> bf16 {   // shifted input
-    if (v >= ve) return __float2bfloat16(0.f);
-    const long long n = nbr(v, dz, dy, dx, D, H, W);
-    return n < 0 ? __float2bfloat16(0.f) : x[n * kC + ci];
+  auto xs = [&](int n, int ci) -> bf16 {   // shifted input
+    return n < 0 ? __float2bfloat16(0.f) : x[(long long)n * ldx + ci];
   };
-  float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-  for (long long vb = vs + warp * 16; vb < ve; vb += 64) {
+  float acc[CI / 8][4];
+#pragma unroll
+  for (int q = 0; q < CI / 8; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+  for (int vb = vs + warp * 16; vb < ve; vb += 64) {
     unsigned a[4];   // A[co][v] (16 x 16)
     a[0] = pack2(gm(vb + t * 2, g), gm(vb + t * 2 + 1, g));
     a[1] = pack2(gm(vb + t * 2, g + 8), gm(vb + t * 2 + 1, g + 8));
     a[2] = pack2(gm(vb + 8 + t * 2, g), gm(vb + 9 + t * 2, g));
     a[3] = pack2(gm(vb + 8 + t * 2, g + 8), gm(vb + 9 + t * 2, g + 8));
+    int n[4];   // shifted voxels of rows 2t, 2t+1, 2t+8, 2t+9 of B
+    const int vv[4] = {vb + t * 2, vb + t * 2 + 1, vb + 8 + t * 2, vb + 9 + t * 2};
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {   // B[v][ci] (16 x 8)
+    for (int q = 0; q < 4; ++q) n[q] = vv[q] < ve ? Vox(vv[q], H, W).nbr(vv[q], dz, dy, dx, D, H, W) : -1;
+#pragma unroll
+    for (int nt = 0; nt < CI / 8; ++nt) {   // B[v][ci] (16 x 8)
       const int ci = nt * 8 + g;
       unsigned b[2];
-      b[0] = pack2(xs(vb + t * 2, ci), xs(vb + t * 2 + 1, ci));
-      b[1] = pack2(xs(vb + 8 + t * 2, ci), xs(vb + 9 + t * 2, ci));
+      b[0] = pack2(xs(n[0], ci), xs(n[1], ci));
+      b[1] = pack2(xs(n[2], ci), xs(n[3], ci));
       mma16816(acc[nt], a, b);
     }
   }
 #pragma unroll
-  for (int nt = 0; nt < 2; ++nt) {
+  for (int nt = 0; nt < CI / 8; ++nt) {
     const int ci = nt * 8 + t * 2;
-    red[warp][g * kC + ci] = acc[nt][0];
-    red[warp][g * kC + ci + 1] = acc[nt][1];
-    red[warp][(g + 8) * kC + ci] = acc[nt][2];
-    red[warp][(g + 8) * kC + ci + 1] = acc[nt][3];
+    red[warp][g * CI + ci] = acc[nt][0];
+    red[warp][g * CI + ci + 1] = acc[nt][1];
+    red[warp][(g + 8) * CI + ci] = acc[nt][2];
+    red[warp][(g + 8) * CI + ci + 1] = acc[nt][3];
   }
   __syncthreads();
-  for (int q = threadIdx.x; q < kC * kC; q += blockDim.x)
-    part[((size_t)ch * 27 + tap) * kC * kC + q] = ((red[0][q] + red[1][q]) + red[2][q]) + red[3][q];
+  for (int q = threadIdx.x; q < 16 * CI; q += blockDim.x)
+    part[(((size_t)ch * 27 + tap) * CO + co0) * CI + q] = ((red[0][q] + red[1][q]) + red[2][q]) + red[3][q];
 }
 
-// gradient of layer l: W[co][tap][ci] = sum over chunks (fixed order)
-__global__ void k_wgrad_sum(const float* __restrict__ part, int nch, float* __restrict__ gw) {
+// gradient of one layer: W[co][tap][ci] = sum over chunks (fixed order)
+__global__ void k_wgrad_sum(const float* __restrict__ part, int nch, int CO, int CI, float* __restrict__ gw) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;   // (tap, co, ci)
-  if (q >= 27 * kC * kC) return;
-  const int tap = q / (kC * kC), co = (q / kC) % kC, ci = q % kC;
+  if (q >= 27 * CO * CI) return;
+  const int tap = q / (CO * CI), co = (q / CI) % CO, ci = q % CI;
   float s = 0.f;
-  for (int c = 0; c < nch; ++c) s += part[((size_t)c * 27 + tap) * kC * kC + co * kC + ci];
-  gw[(co * 27 + tap) * kC + ci] = s;
+  for (int c = 0; c < nch; ++c) s += part[(((size_t)c * 27 + tap) * CO + co) * CI + ci];
+  gw[(co * 27 + tap) * CI + ci] = s;
 }
 
-// bias gradient partials of a 3x3x3 layer: sum_v gy[v][co] [y > 0]
-__global__ void k_bgrad(const bf16* __restrict__ gy, const bf16* __restrict__ y, long long V, float* part) {
+// bias gradient partials of a layer with C outputs: sum_v gy[v][co] [y > 0]
+__global__ void k_bgrad(const bf16* __restrict__ gy, int ldg, const bf16* __restrict__ y, int ldy, int C, int V,
+                        float* part) {
   __shared__ float sh[256];
-  const int co = threadIdx.x & (kC - 1), row = threadIdx.x >> 4;   // 16 rows x 16 channels
+  const int co = threadIdx.x % C, row = threadIdx.x / C, rows = 256 / C;
   float s = 0.f;
-  for (long long v = blockIdx.x * 16LL + row; v < V; v += 16LL * gridDim.x) {
-    const float yy = __bfloat162float(y[v * kC + co]);
-    if (yy > 0.f) s += __bfloat162float(gy[v * kC + co]);
-  }
+  for (int v = blockIdx.x * rows + row; v < V; v += rows * gridDim.x)
+    if (pos(y[(long long)v * ldy + co])) s += __bfloat162float(gy[(long long)v * ldg + co]);
   sh[threadIdx.x] = s;
   __syncthreads();
-  if (threadIdx.x < kC) {
+  if (threadIdx.x < C) {
     float r = 0.f;
-    for (int q = 0; q < 16; ++q) r += sh[q * kC + threadIdx.x];
-    part[blockIdx.x * kC + threadIdx.x] = r;
+    for (int q = 0; q < rows; ++q) r += sh[q * C + threadIdx.x];
+    part[blockIdx.x * C + threadIdx.x] = r;
   }
 }
 
@@ -262,55 +314,165 @@ __global__ void k_sum_cols(const float* __restrict__ part, int rows, int cols, f
   out[c] = s;
 }
 
-// out = b + sum_ci w[ci] x[v][ci] (1x1x1 convolution to one channel)
-__global__ void k_last_fwd(const bf16* __restrict__ x, const float* __restrict__ p, float* __restrict__ out, long long V) {
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-    float s = p[kOffLastB];
-#pragma unroll
-    for (int c = 0; c < kC; ++c) s += p[kOffLastW + c] * __bfloat162float(x[v * kC + c]);
-    out[v] = s;
+// ---------------------------------------------------- pooling, up-sampling
+// child k (0..7) of coarse voxel P on the fine grid H x W (x fastest)
+__device__ __forceinline__ int child(const Vox& P, int k, int H, int W) {
+  return ((2 * P.z + (k >> 2)) * H + 2 * P.y + ((k >> 1) & 1)) * W + 2 * P.x + (k & 1);
+}
+
+// out[v] = mean of the 8 children of v (coarse grid Dc x Hc x Wc), C channels
+__global__ void k_pool(const bf16* __restrict__ in, int ldi, bf16* __restrict__ out, int ldo, int C, int Dc, int Hc,
+                       int Wc) {
+  const int Vc = Dc * Hc * Wc, np = C / 2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (long long)Vc * np;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int v = (int)(q / np), c = (int)(q % np) * 2;
+    const Vox P(v, Hc, Wc);
+    float s0 = 0.f, s1 = 0.f;
+    for (int k = 0; k < 8; ++k) {
+      const __nv_bfloat162 u =
+          *reinterpret_cast<const __nv_bfloat162*>(in + (long long)child(P, k, 2 * Hc, 2 * Wc) * ldi + c);
+      s0 += __low2float(u);
+      s1 += __high2float(u);
+    }
+    *reinterpret_cast<unsigned*>(out + (long long)v * ldo + c) =
+        pack2(__float2bfloat16(s0 * 0.125f), __float2bfloat16(s1 * 0.125f));
   }
 }
 
-// dL/dout of the mean squared error and partial sums of the squared error
-__global__ void k_mse(const float* __restrict__ out, const float* __restrict__ tgt, float* __restrict__ gout, long long V,
-                      double* part) {
-  double v[1] = {0.0};
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < V; q += (long long)gridDim.x * blockDim.x) {
-    const float d = out[q] - tgt[q];
-    gout[q] = 2.f * d / (float)V;
-    v[0] += (double)d * d;
+// gin[child] += gout[parent] / 8 (fine grid 2Dc x 2Hc x 2Wc)
+__global__ void k_pool_bwd_add(const bf16* __restrict__ gout, int ldo, bf16* __restrict__ gin, int ldi, int C, int Dc,
+                               int Hc, int Wc) {
+  const int H = 2 * Hc, W = 2 * Wc, V = 8 * Dc * Hc * Wc, np = C / 2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (long long)V * np;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int f = (int)(q / np), c = (int)(q % np) * 2;
+    const Vox P(f, H, W);
+    const int v = ((P.z >> 1) * Hc + (P.y >> 1)) * Wc + (P.x >> 1);
+    const __nv_bfloat162 go = *reinterpret_cast<const __nv_bfloat162*>(gout + (long long)v * ldo + c);
+    unsigned* gi = reinterpret_cast<unsigned*>(gin + (long long)f * ldi + c);
+    const unsigned cur = *gi;
+    const float lo = __bfloat162float(__ushort_as_bfloat16((unsigned short)(cur & 0xffffu)));
+    const float hi = __bfloat162float(__ushort_as_bfloat16((unsigned short)(cur >> 16)));
+    *gi = pack2(__float2bfloat16(lo + 0.125f * __low2float(go)), __float2bfloat16(hi + 0.125f * __high2float(go)));
   }
-  block_reduce_store<1>(v, part);
+}
+
+// out[child] = in[parent] (nearest), C channels; coarse grid Dc x Hc x Wc
+__global__ void k_up(const bf16* __restrict__ in, int ldi, bf16* __restrict__ out, int ldo, int C, int Dc, int Hc,
+                     int Wc) {
+  const int H = 2 * Hc, W = 2 * Wc, V = 8 * Dc * Hc * Wc, np = C / 2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (long long)V * np;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int f = (int)(q / np), c = (int)(q % np) * 2;
+    const Vox P(f, H, W);
+    const int v = ((P.z >> 1) * Hc + (P.y >> 1)) * Wc + (P.x >> 1);
+    *reinterpret_cast<unsigned*>(out + (long long)f * ldo + c) =
+        *reinterpret_cast<const unsigned*>(in + (long long)v * ldi + c);
+  }
+}
+
+// gin[parent] = sum of gout over the 8 children
+__global__ void k_up_bwd(const bf16* __restrict__ gout, int ldo, bf16* __restrict__ gin, int ldi, int C, int Dc, int Hc,
+                         int Wc) {
+  const int Vc = Dc * Hc * Wc, np = C / 2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (long long)Vc * np;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int v = (int)(q / np), c = (int)(q % np) * 2;
+    const Vox P(v, Hc, Wc);
+    float s0 = 0.f, s1 = 0.f;
+    for (int k = 0; k < 8; ++k) {
+      const __nv_bfloat162 u =
+          *reinterpret_cast<const __nv_bfloat162*>(gout + (long long)child(P, k, 2 * Hc, 2 * Wc) * ldo + c);
+      s0 += __low2float(u);
+      s1 += __high2float(u);
+    }
+    *reinterpret_cast<unsigned*>(gin + (long long)v * ldi + c) = pack2(__float2bfloat16(s0), __float2bfloat16(s1));
+  }
+}
+
+// ------------------------------------------------------- output and loss
+// out = b + sum_ci w[ci] x[v][ci] (1x1x1 convolution to one channel)
+__global__ void k_last_fwd(const bf16* __restrict__ x, const float* __restrict__ p, float* __restrict__ out, int V) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    float s = p[kOffLastB];
+#pragma unroll
+    for (int c = 0; c < kC1; ++c) s += p[kOffLastW + c] * __bfloat162float(x[(long long)v * kC1 + c]);
+    out[v] = s;
+  }
 }
 
 // backward of the 1x1x1 layer: dx[v][ci] = w[ci] gout[v]; partials of
 // dw[ci] = sum gout x and db = sum gout (17 values per block)
 __global__ void k_last_bwd(const bf16* __restrict__ x, const float* __restrict__ gout, const float* __restrict__ p,
-                           bf16* __restrict__ gx, long long V, float* part) {
-  __shared__ float sh[kC + 1][256 / 32];
-  float acc[kC + 1];
-  for (int c = 0; c <= kC; ++c) acc[c] = 0.f;
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+                           bf16* __restrict__ gx, int V, float* part) {
+  __shared__ float sh[kC1 + 1][256 / 32];
+  float acc[kC1 + 1];
+  for (int c = 0; c <= kC1; ++c) acc[c] = 0.f;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
     const float go = gout[v];
 #pragma unroll
-    for (int c = 0; c < kC; ++c) {
-      acc[c] += go * __bfloat162float(x[v * kC + c]);
-      gx[v * kC + c] = __float2bfloat16(p[kOffLastW + c] * go);
+    for (int c = 0; c < kC1; ++c) {
+      acc[c] += go * __bfloat162float(x[(long long)v * kC1 + c]);
+      gx[(long long)v * kC1 + c] = __float2bfloat16(p[kOffLastW + c] * go);
     }
-    acc[kC] += go;
+    acc[kC1] += go;
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int c = 0; c <= kC; ++c) {
+  for (int c = 0; c <= kC1; ++c) {
     float y = acc[c];
     for (int o = 16; o > 0; o >>= 1) y += __shfl_down_sync(0xffffffffu, y, o);
     if (lane == 0) sh[c][wid] = y;
   }
   __syncthreads();
-  if (threadIdx.x <= kC) {
+  if (threadIdx.x <= kC1) {
     float s = 0.f;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[threadIdx.x][w];
-    part[blockIdx.x * (kC + 1) + threadIdx.x] = s;
+    part[blockIdx.x * (kC1 + 1) + threadIdx.x] = s;
+  }
+}
+
+// res = A^ out - rhs with the window operator (coef planes xp, xm, yp, ym,
+// zp, zm, diag of V each; (A d)_v = diag d_v - sum_nb coef_nb d_nb,
+// neighbours outside the window 0); partials of |res|^2 and |rhs|^2
+__global__ void k_resloss(const float* __restrict__ out, const float* __restrict__ rhs, const float* __restrict__ cf,
+                          float* __restrict__ res, int D, int H, int W, double* part) {
+  const int V = D * H * W;
+  double a[2] = {0.0, 0.0};
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const Vox P(v, H, W);
+    float s = cf[6 * (long long)V + v] * out[v];
+    if (P.x + 1 < W) s -= cf[v] * out[v + 1];
+    if (P.x > 0) s -= cf[(long long)V + v] * out[v - 1];
+    if (P.y + 1 < H) s -= cf[2 * (long long)V + v] * out[v + W];
+    if (P.y > 0) s -= cf[3 * (long long)V + v] * out[v - W];
+    if (P.z + 1 < D) s -= cf[4 * (long long)V + v] * out[v + H * W];
+    if (P.z > 0) s -= cf[5 * (long long)V + v] * out[v - H * W];
+    const float r = s - rhs[v];
+    res[v] = r;
+    a[0] += (double)r * r;
+    a[1] += (double)rhs[v] * rhs[v];
+  }
+  block_reduce_store<2>(a, part);
+}
+
+// gout = 2 A^T res / |rhs|^2 (sums[0..1] = |res|^2, |rhs|^2); loss[0] = ratio
+__global__ void k_resloss_grad(const float* __restrict__ res, const float* __restrict__ cf,
+                               const double* __restrict__ sums, float* __restrict__ gout, double* loss, int D, int H,
+                               int W) {
+  const int V = D * H * W;
+  const float sc = sums[1] > 0.0 ? (float)(2.0 / sums[1]) : 0.f;
+  if (blockIdx.x == 0 && threadIdx.x == 0) loss[0] = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const Vox P(v, H, W);
+    float s = cf[6 * (long long)V + v] * res[v];
+    if (P.x + 1 < W) s -= cf[(long long)V + v + 1] * res[v + 1];              // xm of the +x neighbour
+    if (P.x > 0) s -= cf[v - 1] * res[v - 1];                                  // xp of the -x neighbour
+    if (P.y + 1 < H) s -= cf[3 * (long long)V + v + W] * res[v + W];
+    if (P.y > 0) s -= cf[2 * (long long)V + v - W] * res[v - W];
+    if (P.z + 1 < D) s -= cf[5 * (long long)V + v + H * W] * res[v + H * W];
+    if (P.z > 0) s -= cf[4 * (long long)V + v - H * W] * res[v - H * W];
+    gout[v] = sc * s;
   }
 }
 
@@ -330,77 +492,100 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ gp, floa
 // BF16 weights for the forward pass and, flipped and transposed, for the
 // input gradient
 __global__ void k_cast_w(const float* __restrict__ p, bf16* __restrict__ wb, bf16* __restrict__ wt) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;   // (l, co, tap, ci)
-  if (q >= kLayers * kWConv) return;
-  const int l = q / kWConv, r = q % kWConv;
-  const int co = r / (27 * kC), tap = (r / kC) % 27, ci = r % kC;
-  const bf16 w = __float2bfloat16(p[offW(l) + r]);
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= kWAll) return;
+  int l = 0;
+  while (l + 1 < kNL && q >= cWoff[l + 1]) ++l;
+  const int CI = cCI[l], CO = cCO[l], r = q - cWoff[l];
+  const int co = r / (27 * CI), tap = (r / CI) % 27, ci = r % CI;
+  const bf16 w = __float2bfloat16(p[cOffW[l] + r]);
   wb[q] = w;
-  wt[(size_t)l * kWConv + (ci * 27 + (26 - tap)) * kC + co] = w;
+  wt[cWoff[l] + (ci * 27 + (26 - tap)) * CO + co] = w;
 }
 
-// training window: input (channel 0 = normalised residual) and target
-__global__ void k_window(const bf16* __restrict__ srhs, const float* __restrict__ sdel, int sD, int sH, int sW, int z0,
-                         int y0, int x0, int B, bf16* __restrict__ in, float* __restrict__ tgt) {
-  const long long V = (long long)B * B * B;
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(v % B), y = (int)((v / B) % B), z = (int)(v / ((long long)B * B));
+// training window from a recorded pair: input (channel 0 = r^), r^, A^
+__global__ void k_window(const float* __restrict__ smp, int sD, int sH, int sW, int z0, int y0, int x0, int B,
+                         bf16* __restrict__ in, float* __restrict__ rhs, float* __restrict__ cf) {
+  const int V = B * B * B;
+  const long long sV = (long long)sD * sH * sW;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const int x = v % B, y = (v / B) % B, z = v / (B * B);
     const long long s = ((long long)(z + z0) * sH + (y + y0)) * sW + (x + x0);
-    in[v * kC] = srhs[s];
+    const float r = smp[s];
+    in[(long long)v * 16] = __float2bfloat16(r);
 #pragma unroll
-    for (int c = 1; c < kC; ++c) in[v * kC + c] = __float2bfloat16(0.f);
-    tgt[v] = sdel[s];
+    for (int c = 1; c < 16; ++c) in[(long long)v * 16 + c] = __float2bfloat16(0.f);
+    rhs[v] = r;
+#pragma unroll
+    for (int q = 0; q < 7; ++q) cf[(long long)q * V + v] = smp[(1 + q) * sV + s];
   }
 }
 
 // interior of a natural-layout field (k, i, j order: z = k, y = i, x = j)
-__device__ __forceinline__ int nat_of(const Dims& d, long long v, int Ni, int Nj) {
-  const int x = (int)(v % Nj);
-  const long long r = v / Nj;
-  const int y = (int)(r % Ni), z = (int)(r / Ni);
-  return ixk(d, y + 3, x + 3, z + 3);
+__device__ __forceinline__ int nat_of(const Dims& d, int x, int y, int z) { return ixk(d, y + 3, x + 3, z + 3); }
+
+// sums over the interior of r^2 and ap (the scales of a recorded pair and of
+// the net's input)
+__global__ void k_scales(Dims d, const double* __restrict__ r, const double* __restrict__ ap, int Ni, int Nj, int Nk,
+                         double* part) {
+  const int V = Ni * Nj * Nk;
+  double a[2] = {0.0, 0.0};
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const int x = v % Nj, y = (v / Nj) % Ni, z = v / (Nj * Ni);
+    const int n = nat_of(d, x, y, z);
+    a[0] += r[n] * r[n];
+    a[1] += ap[n];
+  }
+  block_reduce_store<2>(a, part);
 }
 
-__global__ void k_rhs_in(Dims d, const double* __restrict__ r, double inv_scale, bf16* __restrict__ in,
-                         bf16* __restrict__ rec, long long V, int Ni, int Nj) {
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-    const bf16 q = __float2bfloat16((float)(r[nat_of(d, v, Ni, Nj)] * inv_scale));
-    if (in) {
-      in[v * kC] = q;
+// a recorded pair: r^ = r0/rms(r0), A^ = A/mean(ap) in window axes
+// (x = j: an, as; y = i: ae, aw; z = k: at, ab)
+__global__ void k_record(Dims d, const double* __restrict__ r, const double* __restrict__ ae,
+                         const double* __restrict__ aw, const double* __restrict__ an, const double* __restrict__ as,
+                         const double* __restrict__ at, const double* __restrict__ ab, const double* __restrict__ ap,
+                         const double* __restrict__ sums, int Ni, int Nj, int Nk, float* __restrict__ smp) {
+  const int V = Ni * Nj * Nk;
+  const double rinv = sums[0] > 0.0 ? 1.0 / sqrt(sums[0] / V) : 0.0;
+  const double ainv = sums[1] != 0.0 ? (double)V / sums[1] : 0.0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const int x = v % Nj, y = (v / Nj) % Ni, z = v / (Nj * Ni);
+    const int n = nat_of(d, x, y, z);
+    smp[v] = (float)(r[n] * rinv);
+    smp[1LL * V + v] = (float)(an[n] * ainv);
+    smp[2LL * V + v] = (float)(as[n] * ainv);
+    smp[3LL * V + v] = (float)(ae[n] * ainv);
+    smp[4LL * V + v] = (float)(aw[n] * ainv);
+    smp[5LL * V + v] = (float)(at[n] * ainv);
+    smp[6LL * V + v] = (float)(ab[n] * ainv);
+    smp[7LL * V + v] = (float)(ap[n] * ainv);
+  }
+}
+
+// the net's input on the padded grid D x H x W (interior Nk x Ni x Nj at the
+// origin, zero elsewhere): channel 0 = r0/rms(r0)
+__global__ void k_rhs_in(Dims d, const double* __restrict__ r, const double* __restrict__ sums, int Ni, int Nj, int Nk,
+                         bf16* __restrict__ in, int D, int H, int W) {
+  const int V = D * H * W;
+  const int Vi = Ni * Nj * Nk;
+  const double rinv = sums[0] > 0.0 ? 1.0 / sqrt(sums[0] / Vi) : 0.0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const int x = v % W, y = (v / W) % H, z = v / (W * H);
+    const float q = (x < Nj && y < Ni && z < Nk) ? (float)(r[nat_of(d, x, y, z)] * rinv) : 0.f;
+    in[(long long)v * 16] = __float2bfloat16(q);
 #pragma unroll
-      for (int c = 1; c < kC; ++c) in[v * kC + c] = __float2bfloat16(0.f);
-    }
-    if (rec) rec[v] = q;
+    for (int c = 1; c < 16; ++c) in[(long long)v * 16 + c] = __float2bfloat16(0.f);
   }
 }
 
-__global__ void k_save_interior(Dims d, const double* __restrict__ fi, double* __restrict__ dst, long long V, int Ni, int Nj) {
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
-    dst[v] = fi[nat_of(d, v, Ni, Nj)];
-}
-
-// the correction of a recorded solve and partial sums of its |.|
-__global__ void k_record_delta(Dims d, const double* __restrict__ fi, const double* __restrict__ fi0,
-                               float* __restrict__ del, long long V, int Ni, int Nj, double* part) {
-  double a[1] = {0.0};
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-    const double x = fi[nat_of(d, v, Ni, Nj)] - fi0[v];
-    del[v] = (float)x;
-    a[0] += fabs(x);
+// the predicted shape on the interior of a natural field (zero elsewhere)
+__global__ void k_shape_nat(Dims d, double* __restrict__ z, const float* __restrict__ out, int Ni, int Nj, int Nk, int H,
+                            int W) {
+  const int Vi = Ni * Nj * Nk;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < Vi; v += gridDim.x * blockDim.x) {
+    const int x = v % Nj, y = (v / Nj) % Ni, zz = v / (Nj * Ni);
+    z[nat_of(d, x, y, zz)] = (double)out[((long long)zz * H + y) * W + x];
   }
-  block_reduce_store<1>(a, part);
-}
-
-__global__ void k_scale_f(float* __restrict__ x, long long V, const double* __restrict__ sum) {
-  const float inv = sum[0] > 0.0 ? (float)((double)V / sum[0]) : 0.f;   // 1 / mean |x|
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
-    x[v] *= inv;
-}
-
-// the predicted shape on the interior of a natural field, zero elsewhere
-__global__ void k_shape_nat(Dims d, double* __restrict__ z, const float* __restrict__ out, long long V, int Ni, int Nj) {
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
-    z[nat_of(d, v, Ni, Nj)] = (double)out[v];
 }
 
 __global__ void k_axpy_nat(int n, double alpha, const double* __restrict__ x, double* __restrict__ y) {
@@ -408,28 +593,70 @@ __global__ void k_axpy_nat(int n, double alpha, const double* __restrict__ x, do
 }
 
 // ------------------------------------------------------------ host side
-int ensure_act(long long V) {
-  if (V <= N.maxV) return CAPPGPU_OK;
-  for (auto& a : N.act) { cudaFree(a); a = nullptr; }
-  cudaFree(N.out); cudaFree(N.tgt); cudaFree(N.gout); cudaFree(N.g[0]); cudaFree(N.g[1]); cudaFree(N.part);
-  N.out = N.tgt = N.gout = nullptr; N.g[0] = N.g[1] = nullptr; N.part = nullptr;
-  N.maxV = 0;
-  const size_t na = (size_t)V * kC * sizeof(bf16);
-  for (auto& a : N.act) CAP_CUDA(cudaMalloc(&a, na));
-  CAP_CUDA(cudaMalloc(&N.g[0], na));
-  CAP_CUDA(cudaMalloc(&N.g[1], na));
-  CAP_CUDA(cudaMalloc(&N.out, V * sizeof(float)));
-  CAP_CUDA(cudaMalloc(&N.tgt, V * sizeof(float)));
-  CAP_CUDA(cudaMalloc(&N.gout, V * sizeof(float)));
-  const long long nch = (V + kChunk - 1) / kChunk;
-  N.part_n = (size_t)nch * 27 * kC * kC + 4096 * (kC + 1);
-  CAP_CUDA(cudaMalloc(&N.part, N.part_n * sizeof(float)));
-  N.maxV = V;
+int round4(int n) { return (n + 3) & ~3; }
+
+// voxel count of the grid layer l runs on, for level-1 count V1
+long long layer_voxels(int l, long long V1) {
+  const int lev[kNL] = {0, 0, 1, 1, 2, 2, 1, 1, 0, 0};
+  return lev[l] == 0 ? V1 : (lev[l] == 1 ? V1 / 8 : V1 / 64);
+}
+
+int ensure_acts(long long V1) {
+  if (V1 <= N.A.V1) return CAPPGPU_OK;
+  acts_free();
+  const long long V2 = V1 / 8, V3 = V1 / 64;
+  struct Item { void** p; long long bytes; };
+  Acts& A = N.A;
+  const long long b = sizeof(bf16);
+  Item items[] = {
+      {(void**)&A.a0, V1 * 16 * b},    {(void**)&A.a1, V1 * 16 * b},   {(void**)&A.cat1, V1 * 48 * b},
+      {(void**)&A.p1, V2 * 16 * b},    {(void**)&A.a3, V2 * 32 * b},   {(void**)&A.cat2, V2 * 96 * b},
+      {(void**)&A.p2, V3 * 32 * b},    {(void**)&A.a5, V3 * 64 * b},   {(void**)&A.b3, V3 * 64 * b},
+      {(void**)&A.a7, V2 * 32 * b},    {(void**)&A.x2, V2 * 32 * b},   {(void**)&A.a9, V1 * 16 * b},
+      {(void**)&A.x1, V1 * 16 * b},    {(void**)&A.gx1, V1 * 16 * b},  {(void**)&A.ga9, V1 * 16 * b},
+      {(void**)&A.gcat1, V1 * 48 * b}, {(void**)&A.gx2, V2 * 32 * b},  {(void**)&A.ga7, V2 * 32 * b},
+      {(void**)&A.gcat2, V2 * 96 * b}, {(void**)&A.gb3, V3 * 64 * b},  {(void**)&A.ga5, V3 * 64 * b},
+      {(void**)&A.gp2, V3 * 32 * b},   {(void**)&A.ga3, V2 * 32 * b},  {(void**)&A.gp1, V2 * 16 * b},
+      {(void**)&A.ga1, V1 * 16 * b},   {(void**)&A.out, V1 * 4},       {(void**)&A.gout, V1 * 4},
+      {(void**)&A.rhs, V1 * 4},        {(void**)&A.coef, 7 * V1 * 4},  {(void**)&A.res, V1 * 4},
+  };
+  long long total = 0;
+  for (auto& it : items) total += (it.bytes + 255) & ~255LL;
+  char* base = nullptr;
+  if (cudaMalloc(&base, total) != cudaSuccess) {
+    set_error("learned guess: out of device memory for %lld voxels", V1);
+    return CAPPGPU_E_NOMEM;
+  }
+  long long o = 0;
+  for (auto& it : items) {
+    *it.p = base + o;
+    o += (it.bytes + 255) & ~255LL;
+  }
+  A.base = base;
+  A.V1 = V1;
+  // partial sums: weight gradients of the largest layer at this size, then
+  // the bias and last-layer partials
+  size_t need = 0;
+  for (int l = 0; l < kNL; ++l) {
+    const size_t n = (size_t)((layer_voxels(l, V1) + kChunk - 1) / kChunk) * 27 * kCO[l] * kCI[l];
+    if (n > need) need = n;
+  }
+  need += 512 * (kC1 + 1) + 256 * 64;
+  if (need > N.part_n) {
+    cudaFree(N.part);
+    N.part = nullptr;
+    if (cudaMalloc(&N.part, need * sizeof(float)) != cudaSuccess) {
+      N.part_n = 0;
+      set_error("learned guess: out of device memory for partial sums");
+      return CAPPGPU_E_NOMEM;
+    }
+    N.part_n = need;
+  }
   return CAPPGPU_OK;
 }
 
 int cast_weights() {
-  launch(k_cast_w, (kLayers * kWConv + 255) / 256, 256, ctx().st, (const float*)N.p, N.wb, N.wt);
+  launch(k_cast_w, (kWAll + 255) / 256, 256, ctx().st, (const float*)N.p, N.wb, N.wt);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
 }
@@ -445,61 +672,148 @@ int init_params(unsigned long long seed) {
     z ^= z >> 31;
     return (float)((double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0);
   };
-  const float a3 = sqrtf(6.f / (27.f * kC)), a1 = sqrtf(3.f / kC);   // He-uniform
-  for (int l = 0; l < kLayers; ++l)
-    for (int q = 0; q < kWConv; ++q) h[offW(l) + q] = a3 * uni();
-  for (int c = 0; c < kC; ++c) h[kOffLastW + c] = a1 * uni() * 0.1f;
+  for (int l = 0; l < kNL; ++l) {
+    const int fan_in = 27 * (l == 0 ? 1 : kCI[l]);
+    const float a = sqrtf(6.f / (float)fan_in);   // He-uniform
+    for (int q = 0; q < wsize(l); ++q) {
+      const int ci = q % kCI[l];
+      h[offW(l) + q] = (l == 0 && ci > 0) ? 0.f : a * uni();
+    }
+  }
+  for (int c = 0; c < kC1; ++c) h[kOffLastW + c] = sqrtf(3.f / kC1) * uni();
   Ctx& c = ctx();
   CAP_CUDA(cudaMemcpyAsync(N.p, h.data(), sizeof(float) * kParams, cudaMemcpyHostToDevice, c.st));
   CAP_CUDA(cudaMemsetAsync(N.m, 0, sizeof(float) * kParams, c.st));
   CAP_CUDA(cudaMemsetAsync(N.v, 0, sizeof(float) * kParams, c.st));
+  CAP_CUDA(cudaStreamSynchronize(c.st));   // h is released on return
   N.adam_t = 0;
   return cast_weights();
 }
 
-// forward pass on act[0] (V voxels, D x H x W)
+constexpr int kConvGrid = 152 * 4;
+
+template <int CI>
+int conv_ci(const bf16* x, int ldx, const bf16* w, int CO, const float* bias, const bf16* mask, int ldm, bf16* y,
+            int ldy, int D, int H, int W, int relu) {
+  const size_t smem = (size_t)16 * wrow(CI) * sizeof(unsigned);
+  CAP_CUDA(cudaFuncSetAttribute(k_conv3<CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int ntiles = (D * H * W + 15) / 16;
+  int gx = (ntiles + 7) / 8;
+  if (gx > kConvGrid) gx = kConvGrid;
+  ++ctx().launches;
+  k_conv3<CI><<<dim3(gx, CO / 16), 256, smem, ctx().st>>>(x, ldx, w, bias, mask, ldm, y, ldy, D, H, W, relu);
+  return CAPPGPU_OK;
+}
+
+// y = relu(conv(x) + b) (forward, mask == null) or the input gradient
+// (mask = the layer's output, w = flipped transposed weights)
+int conv(int CI, const bf16* x, int ldx, const bf16* w, int CO, const float* bias, const bf16* mask, int ldm, bf16* y,
+         int ldy, int D, int H, int W, int relu) {
+  switch (CI) {
+    case 16: return conv_ci<16>(x, ldx, w, CO, bias, mask, ldm, y, ldy, D, H, W, relu);
+    case 32: return conv_ci<32>(x, ldx, w, CO, bias, mask, ldm, y, ldy, D, H, W, relu);
+    case 48: return conv_ci<48>(x, ldx, w, CO, bias, mask, ldm, y, ldy, D, H, W, relu);
+    case 64: return conv_ci<64>(x, ldx, w, CO, bias, mask, ldm, y, ldy, D, H, W, relu);
+    case 96: return conv_ci<96>(x, ldx, w, CO, bias, mask, ldm, y, ldy, D, H, W, relu);
+  }
+  set_error("learned guess: no convolution for %d input channels", CI);
+  return CAPPGPU_E_ARG;
+}
+
+int fwd_layer(int l, const bf16* x, int ldx, bf16* y, int ldy, int D, int H, int W) {
+  return conv(kCI[l], x, ldx, N.wb + woff(l), kCO[l], N.p + offB(l), nullptr, 0, y, ldy, D, H, W, 1);
+}
+
+template <int CI>
+void wgrad_ci(const bf16* x, int ldx, const bf16* gy, int ldg, const bf16* y, int ldy, int CO, int D, int H, int W) {
+  const int nch = (D * H * W + kChunk - 1) / kChunk;
+  launch(k_wgrad3<CI>, dim3(27, nch, CO / 16), 128, ctx().st, x, ldx, gy, ldg, y, ldy, N.part, CO, D, H, W);
+}
+
+// weight and bias gradients of layer l (input x, output y, output gradient
+// gy), then (dx != null) the gradient with respect to its input
+int bwd_layer(int l, const bf16* x, int ldx, const bf16* gy, int ldg, const bf16* y, int ldy, bf16* dx, int lddx,
+              int D, int H, int W) {
+  Ctx& c = ctx();
+  const int CI = kCI[l], CO = kCO[l];
+  const int V = D * H * W;
+  switch (CI) {
+    case 16: wgrad_ci<16>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
+    case 32: wgrad_ci<32>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
+    case 48: wgrad_ci<48>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
+    case 64: wgrad_ci<64>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
+    case 96: wgrad_ci<96>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
+    default: set_error("learned guess: bad layer"); return CAPPGPU_E_ARG;
+  }
+  const int nch = (V + kChunk - 1) / kChunk;
+  launch(k_wgrad_sum, (27 * CO * CI + 255) / 256, 256, c.st, (const float*)N.part, nch, CO, CI, N.gp + offW(l));
+  launch(k_bgrad, 256, 256, c.st, gy, ldg, y, ldy, CO, V, N.part);
+  launch(k_sum_cols, 1, 64, c.st, (const float*)N.part, 256, CO, N.gp + offB(l));
+  CAP_CHECK_LAUNCH();
+  if (dx) return conv(CO, gy, ldg, N.wt + woff(l), CI, nullptr, y, ldy, dx, lddx, D, H, W, 0);
+  return CAPPGPU_OK;
+}
+
+// forward pass on A.a0 (D x H x W, multiples of 4) into A.out
 int forward(int D, int H, int W) {
   Ctx& c = ctx();
-  const long long V = (long long)D * H * W;
-  const int blocks = (int)((V + 127) / 128);   // 8 warps x 16 voxels
-  for (int l = 0; l < kLayers; ++l) {
-    launch(k_conv3, blocks, 256, c.st, (const bf16*)N.act[l], (const bf16*)(N.wb + (size_t)l * kWConv),
-           (const float*)(N.p + offB(l)), (const bf16*)nullptr, N.act[l + 1], D, H, W, kDil[l], 1);
-  }
-  launch(k_last_fwd, grid_for(V), kThreads, c.st, (const bf16*)N.act[kLayers], (const float*)N.p, N.out, V);
+  Acts& A = N.A;
+  const int D2 = D / 2, H2 = H / 2, W2 = W / 2, D3 = D / 4, H3 = H / 4, W3 = W / 4;
+  const long long V = (long long)D * H * W, V2 = V / 8, V3 = V / 64;
+  int rc;
+  if ((rc = fwd_layer(0, A.a0, 16, A.a1, 16, D, H, W))) return rc;
+  if ((rc = fwd_layer(1, A.a1, 16, A.cat1 + 32, 48, D, H, W))) return rc;
+  launch(k_pool, grid_for(V2 * 8), kThreads, c.st, (const bf16*)(A.cat1 + 32), 48, A.p1, 16, 16, D2, H2, W2);
+  if ((rc = fwd_layer(2, A.p1, 16, A.a3, 32, D2, H2, W2))) return rc;
+  if ((rc = fwd_layer(3, A.a3, 32, A.cat2 + 64, 96, D2, H2, W2))) return rc;
+  launch(k_pool, grid_for(V3 * 16), kThreads, c.st, (const bf16*)(A.cat2 + 64), 96, A.p2, 32, 32, D3, H3, W3);
+  if ((rc = fwd_layer(4, A.p2, 32, A.a5, 64, D3, H3, W3))) return rc;
+  if ((rc = fwd_layer(5, A.a5, 64, A.b3, 64, D3, H3, W3))) return rc;
+  launch(k_up, grid_for(V2 * 32), kThreads, c.st, (const bf16*)A.b3, 64, A.cat2, 96, 64, D3, H3, W3);
+  if ((rc = fwd_layer(6, A.cat2, 96, A.a7, 32, D2, H2, W2))) return rc;
+  if ((rc = fwd_layer(7, A.a7, 32, A.x2, 32, D2, H2, W2))) return rc;
+  launch(k_up, grid_for(V * 16), kThreads, c.st, (const bf16*)A.x2, 32, A.cat1, 48, 32, D2, H2, W2);
+  if ((rc = fwd_layer(8, A.cat1, 48, A.a9, 16, D, H, W))) return rc;
+  if ((rc = fwd_layer(9, A.a9, 16, A.x1, 16, D, H, W))) return rc;
+  launch(k_last_fwd, grid_for(V), kThreads, c.st, (const bf16*)A.x1, (const float*)N.p, A.out, (int)V);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
 }
 
-// loss, backward pass into N.gp; loss returned on the device in dsum[0]
+// residual-norm loss of A.out against A.rhs / A.coef (loss in N.dsum[0]),
+// then the backward pass into N.gp
 int backward(int D, int H, int W) {
   Ctx& c = ctx();
-  const long long V = (long long)D * H * W;
-  launch(k_mse, kRedBlocks, kThreads, c.st, (const float*)N.out, (const float*)N.tgt, N.gout, V, c.partials);
+  Acts& A = N.A;
+  const int V = D * H * W;
+  const int D2 = D / 2, H2 = H / 2, W2 = W / 2, D3 = D / 4, H3 = H / 4, W3 = W / 4;
+  const long long V2 = V / 8, V3 = V / 64;
+  launch(k_resloss, kRedBlocks, kThreads, c.st, (const float*)A.out, (const float*)A.rhs, (const float*)A.coef, A.res, D,
+         H, W, c.partials);
   CAP_CHECK_LAUNCH();
-  int rc = finish_reduce(1);
+  int rc = finish_reduce(2);
   if (rc) return rc;
-  CAP_CUDA(cudaMemcpyAsync(N.dsum, c.redout, sizeof(double), cudaMemcpyDeviceToDevice, c.st));
+  launch(k_resloss_grad, grid_for(V), kThreads, c.st, (const float*)A.res, (const float*)A.coef,
+         (const double*)c.redout, A.gout, N.dsum, D, H, W);
   const int lb = 512;
-  launch(k_last_bwd, lb, 256, c.st, (const bf16*)N.act[kLayers], (const float*)N.gout, (const float*)N.p, N.g[0], V,
-         N.part);
-  launch(k_sum_cols, 1, 32, c.st, (const float*)N.part, lb, kC + 1, N.gp + kOffLastW);
-  int cur = 0;
-  const int nch = (int)((V + kChunk - 1) / kChunk);
-  const int blocks = (int)((V + 127) / 128);
-  for (int l = kLayers - 1; l >= 0; --l) {
-    // weight and bias gradients of layer l (input act[l], output act[l+1])
-    launch(k_wgrad3, dim3(27, nch), 128, c.st, (const bf16*)N.act[l], (const bf16*)N.g[cur], (const bf16*)N.act[l + 1],
-           N.part, D, H, W, kDil[l]);
-    launch(k_wgrad_sum, (27 * kC * kC + 255) / 256, 256, c.st, (const float*)N.part, nch, N.gp + offW(l));
-    launch(k_bgrad, 256, 256, c.st, (const bf16*)N.g[cur], (const bf16*)N.act[l + 1], V, N.part);
-    launch(k_sum_cols, 1, 32, c.st, (const float*)N.part, 256, kC, N.gp + offB(l));
-    if (l > 0) {   // gradient with respect to act[l]
-      launch(k_conv3, blocks, 256, c.st, (const bf16*)N.g[cur], (const bf16*)(N.wt + (size_t)l * kWConv),
-             (const float*)nullptr, (const bf16*)N.act[l + 1], N.g[cur ^ 1], D, H, W, kDil[l], 0);
-      cur ^= 1;
-    }
-  }
+  launch(k_last_bwd, lb, 256, c.st, (const bf16*)A.x1, (const float*)A.gout, (const float*)N.p, A.gx1, V, N.part);
+  launch(k_sum_cols, 1, 32, c.st, (const float*)N.part, lb, kC1 + 1, N.gp + kOffLastW);
+  CAP_CHECK_LAUNCH();
+  if ((rc = bwd_layer(9, A.a9, 16, A.gx1, 16, A.x1, 16, A.ga9, 16, D, H, W))) return rc;
+  if ((rc = bwd_layer(8, A.cat1, 48, A.ga9, 16, A.a9, 16, A.gcat1, 48, D, H, W))) return rc;
+  launch(k_up_bwd, grid_for(V2 * 16), kThreads, c.st, (const bf16*)A.gcat1, 48, A.gx2, 32, 32, D2, H2, W2);
+  if ((rc = bwd_layer(7, A.a7, 32, A.gx2, 32, A.x2, 32, A.ga7, 32, D2, H2, W2))) return rc;
+  if ((rc = bwd_layer(6, A.cat2, 96, A.ga7, 32, A.a7, 32, A.gcat2, 96, D2, H2, W2))) return rc;
+  launch(k_up_bwd, grid_for(V3 * 32), kThreads, c.st, (const bf16*)A.gcat2, 96, A.gb3, 64, 64, D3, H3, W3);
+  if ((rc = bwd_layer(5, A.a5, 64, A.gb3, 64, A.b3, 64, A.ga5, 64, D3, H3, W3))) return rc;
+  if ((rc = bwd_layer(4, A.p2, 32, A.ga5, 64, A.a5, 64, A.gp2, 32, D3, H3, W3))) return rc;
+  launch(k_pool_bwd_add, grid_for(V2 * 16), kThreads, c.st, (const bf16*)A.gp2, 32, A.gcat2 + 64, 96, 32, D3, H3, W3);
+  if ((rc = bwd_layer(3, A.a3, 32, A.gcat2 + 64, 96, A.cat2 + 64, 96, A.ga3, 32, D2, H2, W2))) return rc;
+  if ((rc = bwd_layer(2, A.p1, 16, A.ga3, 32, A.a3, 32, A.gp1, 16, D2, H2, W2))) return rc;
+  launch(k_pool_bwd_add, grid_for((long long)V * 8), kThreads, c.st, (const bf16*)A.gp1, 16, A.gcat1 + 32, 48, 16, D2,
+         H2, W2);
+  if ((rc = bwd_layer(1, A.a1, 16, A.gcat1 + 32, 48, A.cat1 + 32, 48, A.ga1, 16, D, H, W))) return rc;
+  if ((rc = bwd_layer(0, A.a0, 16, A.ga1, 16, A.a1, 16, nullptr, 0, D, H, W))) return rc;
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
 }
@@ -512,44 +826,111 @@ int adam_step(float lr) {
   return cast_weights();
 }
 
+// algorithmic FLOPs of one forward pass per level-1 voxel (layer 0 has one
+// input channel) and of the weight and input gradients
+double fwd_flops_per_voxel() {
+  double f = 0.0;
+  for (int l = 0; l < kNL; ++l) {
+    const double vl = (double)layer_voxels(l, 64) / 64.0;
+    f += 2.0 * 27.0 * (l == 0 ? 1 : kCI[l]) * kCO[l] * vl;
+  }
+  return f + 2.0 * kC1;
+}
+
+double bwd_flops_per_voxel() {
+  double f = 0.0;
+  for (int l = 0; l < kNL; ++l) {
+    const double vl = (double)layer_voxels(l, 64) / 64.0;
+    const double ci = l == 0 ? 1 : kCI[l];
+    f += 2.0 * 27.0 * ci * kCO[l] * vl;                 // weight gradient
+    if (l > 0) f += 2.0 * 27.0 * ci * kCO[l] * vl;      // input gradient
+  }
+  return f + 4.0 * kC1;
+}
+
 }  // namespace
 
 void learned_free() { net_free(); }
 
-// Record hooks and the guess, called by the refinement form of pcgsip.
-// At the start of a solve: r0 (module res) and res0 are known.
+// Unit timing (cappgpu_profile_kernel): 9 = one forward pass of the net on
+// this grid (interior padded to multiples of 4) from the module residual;
+// 10 = one forward and backward pass on a 64^3 window (or the grid, if
+// smaller) of the first recorded pair.  *flops = algorithmic FLOPs.
+int learned_profile_unit(int which, double* flops) {
+  if (!N.ready) { set_error("profile unit %d: call cappgpu_learn_reset first", which); return CAPPGPU_E_NOINIT; }
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  const int Ni = d.nimm - 2, Nj = d.njmm - 2, Nk = d.nkmm - 2;
+  int rc;
+  if (which == 9) {
+    const int D = round4(Nk), H = round4(Ni), W = round4(Nj);
+    if ((rc = ensure_acts((long long)D * H * W))) return rc;
+    launch(k_scales, kRedBlocks, kThreads, c.st, d, (const double*)c.f[CAP_RES], (const double*)c.f[CAP_AP], Ni, Nj,
+           Nk, c.partials);
+    CAP_CHECK_LAUNCH();
+    if ((rc = finish_reduce(2))) return rc;
+    launch(k_rhs_in, grid_for((long long)D * H * W), kThreads, c.st, d, (const double*)c.f[CAP_RES],
+           (const double*)c.redout, Ni, Nj, Nk, N.A.a0, D, H, W);
+    CAP_CHECK_LAUNCH();
+    *flops = fwd_flops_per_voxel() * (double)D * H * W;
+    return forward(D, H, W);
+  }
+  if (N.nsamples == 0) { set_error("profile unit 10: no recorded pairs"); return CAPPGPU_E_NOINIT; }
+  const int B = min(64, min(N.sD, min(N.sH, N.sW))) & ~3;
+  if (B < 4) { set_error("profile unit 10: the grid is smaller than 4 cells"); return CAPPGPU_E_ARG; }
+  const int V = B * B * B;
+  if ((rc = ensure_acts(V))) return rc;
+  launch(k_window, grid_for(V), kThreads, c.st, (const float*)N.store, N.sD, N.sH, N.sW, 0, 0, 0, B, N.A.a0, N.A.rhs,
+         N.A.coef);
+  CAP_CHECK_LAUNCH();
+  *flops = (fwd_flops_per_voxel() + bwd_flops_per_voxel()) * (double)V;
+  if ((rc = forward(B, B, B))) return rc;
+  return backward(B, B, B);
+}
+
+// Record hook and the guess, called by the refinement form of pcgsip at the
+// start of a solve: r0 (module res) and res0 are known.
 int learned_solve_start(int fif, double res0) {
   if (!N.ready) return CAPPGPU_OK;
   Ctx& c = ctx();
   const Dims& d = c.d;
   const int Ni = d.nimm - 2, Nj = d.njmm - 2, Nk = d.nkmm - 2;
-  const long long V = (long long)Ni * Nj * Nk;
-  const double scale = res0 / (double)V;   // mean |r0|
-  if (!(scale > 0.0) || !isfinite(scale)) return CAPPGPU_OK;
-  N.pending = -1;
-  if (N.collect && N.max_samples > 0 && N.sD == Nk && N.sH == Ni && N.sW == Nj) {
-    const int slot = N.next;
-    launch(k_rhs_in, grid_for(V), kThreads, c.st, d, (const double*)c.f[CAP_RES], 1.0 / scale, (bf16*)nullptr,
-           N.srhs + (size_t)slot * V, V, Ni, Nj);
-    launch(k_save_interior, grid_for(V), kThreads, c.st, d, (const double*)c.f[fif], N.fi0, V, Ni, Nj);
-    CAP_CHECK_LAUNCH();
-    N.pending = slot;
-  }
-  if (c.precision != 2 || !N.trained) return CAPPGPU_OK;
-  // the guess: fi + scale * net(r0 / scale), kept only if it lowers the FP64 residual
-  int rc = ensure_act(V);
-  if (rc) return rc;
-  launch(k_rhs_in, grid_for(V), kThreads, c.st, d, (const double*)c.f[CAP_RES], 1.0 / scale, N.act[0], (bf16*)nullptr,
-         V, Ni, Nj);
+  const long long Vi = (long long)Ni * Nj * Nk;
+  if (!(res0 > 0.0) || !isfinite(res0)) return CAPPGPU_OK;
+  const bool rec = N.collect && N.max_samples > 0 && N.sD == Nk && N.sH == Ni && N.sW == Nj;
+  const bool guess = c.precision == 2 && N.trained;
+  if (!rec && !guess) return CAPPGPU_OK;
+  launch(k_scales, kRedBlocks, kThreads, c.st, d, (const double*)c.f[CAP_RES], (const double*)c.f[CAP_AP], Ni, Nj, Nk,
+         c.partials);
   CAP_CHECK_LAUNCH();
-  if ((rc = forward(Nk, Ni, Nj))) return rc;
+  int rc = finish_reduce(2);
+  if (rc) return rc;
+  if (rec) {
+    float* smp = N.store + (size_t)N.next * 8 * Vi;
+    launch(k_record, grid_for(Vi), kThreads, c.st, d, (const double*)c.f[CAP_RES], (const double*)c.f[CAP_AE],
+           (const double*)c.f[CAP_AW], (const double*)c.f[CAP_AN], (const double*)c.f[CAP_AS],
+           (const double*)c.f[CAP_AT], (const double*)c.f[CAP_AB], (const double*)c.f[CAP_AP],
+           (const double*)c.redout, Ni, Nj, Nk, smp);
+    CAP_CHECK_LAUNCH();
+    N.next = (N.next + 1) % N.max_samples;
+    if (N.nsamples < N.max_samples) ++N.nsamples;
+  }
+  if (!guess) return CAPPGPU_OK;
+  // the guess: fi + alpha * net(r0 / rms(r0)), kept only if it lowers the
+  // FP64 residual
+  const int D = round4(Nk), H = round4(Ni), W = round4(Nj);
+  if ((rc = ensure_acts((long long)D * H * W))) return rc;
+  launch(k_rhs_in, grid_for((long long)D * H * W), kThreads, c.st, d, (const double*)c.f[CAP_RES],
+         (const double*)c.redout, Ni, Nj, Nk, N.A.a0, D, H, W);
+  CAP_CHECK_LAUNCH();
+  if ((rc = forward(D, H, W))) return rc;
   // amplitude by least squares: alpha = (r0.Ad)/(Ad.Ad)
   double* shape = c.work[4];
   double* ashape = c.work[5];
   double* cand = c.work[2];
   double* rcand = c.work[3];
   CAP_CUDA(cudaMemsetAsync(shape, 0, sizeof(double) * d.nijk, c.st));
-  launch(k_shape_nat, grid_for(V), kThreads, c.st, d, shape, (const float*)N.out, V, Ni, Nj);
+  launch(k_shape_nat, grid_for(Vi), kThreads, c.st, d, shape, (const float*)N.A.out, Ni, Nj, Nk, H, W);
   CAP_CHECK_LAUNCH();
   double dots[2] = {0.0, 0.0};
   if ((rc = spmv_dot2_natural(shape, ashape, c.f[CAP_RES], dots))) return rc;
@@ -574,26 +955,9 @@ int learned_solve_start(int fif, double res0) {
   return CAPPGPU_OK;
 }
 
-// At the end of a solve: the correction of a recorded pair
-int learned_solve_end(int fif) {
-  if (N.pending < 0) return CAPPGPU_OK;
-  Ctx& c = ctx();
-  const Dims& d = c.d;
-  const int Ni = d.nimm - 2, Nj = d.njmm - 2, Nk = d.nkmm - 2;
-  const long long V = (long long)Ni * Nj * Nk;
-  float* del = N.sdel + (size_t)N.pending * V;
-  launch(k_record_delta, kRedBlocks, kThreads, c.st, d, (const double*)c.f[fif], (const double*)N.fi0, del, V, Ni, Nj,
-         c.partials);
-  CAP_CHECK_LAUNCH();
-  int rc = finish_reduce(1);
-  if (rc) return rc;
-  launch(k_scale_f, grid_for(V), kThreads, c.st, del, V, (const double*)c.redout);   // target: the shape
-  CAP_CHECK_LAUNCH();
-  N.next = (N.pending + 1) % N.max_samples;
-  if (N.nsamples < N.max_samples) ++N.nsamples;
-  N.pending = -1;
-  return CAPPGPU_OK;
-}
+// At the end of a solve: nothing to record (the residual-norm loss needs
+// only the solve's initial residual and operator).
+int learned_solve_end(int) { return CAPPGPU_OK; }
 
 }  // namespace cap
 
@@ -614,18 +978,15 @@ int cappgpu_learn_reset(int max_samples, unsigned long long seed) {
   CAP_CUDA(cudaMalloc(&N.gp, sizeof(float) * kParams));
   CAP_CUDA(cudaMalloc(&N.m, sizeof(float) * kParams));
   CAP_CUDA(cudaMalloc(&N.v, sizeof(float) * kParams));
-  CAP_CUDA(cudaMalloc(&N.wb, sizeof(bf16) * kLayers * kWConv));
-  CAP_CUDA(cudaMalloc(&N.wt, sizeof(bf16) * kLayers * kWConv));
+  CAP_CUDA(cudaMalloc(&N.wb, sizeof(bf16) * kWAll));
+  CAP_CUDA(cudaMalloc(&N.wt, sizeof(bf16) * kWAll));
   CAP_CUDA(cudaMalloc(&N.dsum, sizeof(double) * 4));
   CAP_CUDA(cudaMemset(N.gp, 0, sizeof(float) * kParams));
-  if (max_samples > 0) {
-    if (cudaMalloc(&N.srhs, sizeof(bf16) * (size_t)max_samples * V) != cudaSuccess ||
-        cudaMalloc(&N.sdel, sizeof(float) * (size_t)max_samples * V) != cudaSuccess ||
-        cudaMalloc(&N.fi0, sizeof(double) * (size_t)V) != cudaSuccess) {
-      net_free();
-      set_error("learn_reset: out of device memory for %d samples", max_samples);
-      return CAPPGPU_E_NOMEM;
-    }
+  CAP_CUDA(cudaMemset(N.dsum, 0, sizeof(double) * 4));
+  if (max_samples > 0 && cudaMalloc(&N.store, sizeof(float) * 8 * (size_t)max_samples * V) != cudaSuccess) {
+    net_free();
+    set_error("learn_reset: out of device memory for %d samples", max_samples);
+    return CAPPGPU_E_NOMEM;
   }
   N.max_samples = max_samples;
   N.seed = seed;
@@ -647,10 +1008,11 @@ int cappgpu_learn_train(int epochs, int block, double lr, double* loss) {
   CAP_REQUIRE_INIT();
   if (!N.ready || N.nsamples == 0) { set_error("learn_train: no recorded pairs"); return CAPPGPU_E_NOINIT; }
   if (epochs < 1 || block < 4 || !(lr > 0.0)) { set_error("learn_train: bad arguments"); return CAPPGPU_E_ARG; }
+  const int B = min(block, min(N.sD, min(N.sH, N.sW))) & ~3;
+  if (B < 4) { set_error("learn_train: the grid is smaller than 4 cells"); return CAPPGPU_E_ARG; }
   Ctx& c = ctx();
-  const int B = min(block, min(N.sD, min(N.sH, N.sW)));
-  const long long V = (long long)B * B * B;
-  int rc = ensure_act(V);
+  const int V = B * B * B;
+  int rc = ensure_acts(V);
   if (rc) return rc;
   const long long sV = (long long)N.sD * N.sH * N.sW;
   unsigned long long s = N.seed * 0x9e3779b97f4a7c15ULL + 12345;
@@ -665,8 +1027,8 @@ int cappgpu_learn_train(int epochs, int block, double lr, double* loss) {
       const int sidx = (int)rnd((unsigned)N.nsamples);
       const int z0 = (int)rnd((unsigned)(N.sD - B + 1)), y0 = (int)rnd((unsigned)(N.sH - B + 1)),
                 x0 = (int)rnd((unsigned)(N.sW - B + 1));
-      launch(k_window, grid_for(V), kThreads, c.st, (const bf16*)(N.srhs + (size_t)sidx * sV),
-             (const float*)(N.sdel + (size_t)sidx * sV), N.sD, N.sH, N.sW, z0, y0, x0, B, N.act[0], N.tgt);
+      launch(k_window, grid_for(V), kThreads, c.st, (const float*)(N.store + (size_t)sidx * 8 * sV), N.sD, N.sH, N.sW,
+             z0, y0, x0, B, N.A.a0, N.A.rhs, N.A.coef);
       CAP_CHECK_LAUNCH();
       if ((rc = forward(B, B, B))) return rc;
       if ((rc = backward(B, B, B))) return rc;
@@ -674,7 +1036,7 @@ int cappgpu_learn_train(int epochs, int block, double lr, double* loss) {
       double h = 0.0;
       CAP_CUDA(cudaMemcpyAsync(&h, N.dsum, sizeof(double), cudaMemcpyDeviceToHost, c.st));
       CAP_CUDA(cudaStreamSynchronize(c.st));
-      sum += h / (double)V;
+      sum += h;
     }
     last = sum / N.nsamples;
   }
@@ -696,7 +1058,6 @@ int cappgpu_learn_params(float* host, int n, int direction) {
     if (rc) return rc;
     N.trained = true;
     CAP_CUDA(cudaStreamSynchronize(ctx().st));
-    return kParams;
   }
   return kParams;
 }
@@ -710,29 +1071,29 @@ int cappgpu_learn_stats(int* samples, int* guesses, int* fallbacks, double* last
   return CAPPGPU_OK;
 }
 
-int cappgpu_learn_check(const float* input, const float* target, int D, int H, int W, float* output, float* grad,
+int cappgpu_learn_check(const float* rhs, const float* coef, int D, int H, int W, float* output, float* grad,
                         double* loss) {
   CAP_REQUIRE_INIT();
   if (!N.ready) { set_error("learn_check: call cappgpu_learn_reset first"); return CAPPGPU_E_NOINIT; }
-  if (!input || !target || D < 1 || H < 1 || W < 1) { set_error("learn_check: bad arguments"); return CAPPGPU_E_ARG; }
+  if (!rhs || !coef || D < 4 || H < 4 || W < 4 || ((D | H | W) & 3)) {
+    set_error("learn_check: extents must be multiples of 4");
+    return CAPPGPU_E_ARG;
+  }
   Ctx& c = ctx();
   const long long V = (long long)D * H * W;
-  int rc = ensure_act(V);
+  int rc = ensure_acts(V);
   if (rc) return rc;
-  std::vector<bf16> in((size_t)V * kC, __float2bfloat16(0.f));
-  for (long long v = 0; v < V; ++v) in[v * kC] = __float2bfloat16(input[v]);
-  CAP_CUDA(cudaMemcpy(N.act[0], in.data(), sizeof(bf16) * in.size(), cudaMemcpyHostToDevice));
-  CAP_CUDA(cudaMemcpy(N.tgt, target, sizeof(float) * V, cudaMemcpyHostToDevice));
+  std::vector<bf16> in((size_t)V * 16, __float2bfloat16(0.f));
+  for (long long v = 0; v < V; ++v) in[v * 16] = __float2bfloat16(rhs[v]);
+  CAP_CUDA(cudaMemcpy(N.A.a0, in.data(), sizeof(bf16) * in.size(), cudaMemcpyHostToDevice));
+  CAP_CUDA(cudaMemcpy(N.A.rhs, rhs, sizeof(float) * V, cudaMemcpyHostToDevice));
+  CAP_CUDA(cudaMemcpy(N.A.coef, coef, sizeof(float) * 7 * V, cudaMemcpyHostToDevice));
   if ((rc = forward(D, H, W))) return rc;
   if ((rc = backward(D, H, W))) return rc;
   CAP_CUDA(cudaStreamSynchronize(c.st));
-  if (output) CAP_CUDA(cudaMemcpy(output, N.out, sizeof(float) * V, cudaMemcpyDeviceToHost));
+  if (output) CAP_CUDA(cudaMemcpy(output, N.A.out, sizeof(float) * V, cudaMemcpyDeviceToHost));
   if (grad) CAP_CUDA(cudaMemcpy(grad, N.gp, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
-  if (loss) {
-    double h;
-    CAP_CUDA(cudaMemcpy(&h, N.dsum, sizeof(double), cudaMemcpyDeviceToHost));
-    *loss = h / (double)V;
-  }
+  if (loss) CAP_CUDA(cudaMemcpy(loss, N.dsum, sizeof(double), cudaMemcpyDeviceToHost));
   return CAPPGPU_OK;
 }
 

@@ -252,17 +252,22 @@ int run_wave(const Op& op, const int* skip = nullptr) {
 }
 
 // ------------------------------------------------------ vector kernels (D)
-#define D_LOOP(g)                                                                                  \
-  for (long long t_ = blockIdx.x * (long long)blockDim.x + threadIdx.x, n_ = (g).size(); t_ < n_;   \
-       t_ += (long long)gridDim.x * blockDim.x)
-
-__device__ inline bool d_cell(const DG& g, long long t, int& a, int& b, int& c) {
-  long long row = t / g.P;
-  a = (int)(t - row * g.P);
-  int s = (int)(row / g.Nk);
-  c = (int)(row - (long long)s * g.Nk);
-  b = s - a - c;
-  return a < g.Ni && b >= 0 && b < g.Nj;
+// f(t, a, b, c) for every cell of the hyperplane layout.  A row (s, c) of
+// the layout holds the cells a = max(0, s-c-(Nj-1)) .. min(Ni-1, s-c) in
+// consecutive slots; one warp takes a row, its lanes the row's cells, so no
+// thread spends work on the layout's empty slots and the row index is the
+// only division.
+template <class F>
+__device__ __forceinline__ void for_cells(const DG& g, F&& f) {
+  const int lane = threadIdx.x & 31;
+  const int nrow = g.S * g.Nk;
+  const int step = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int row = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); row < nrow; row += step) {
+    const int s = row / g.Nk, c = row - s * g.Nk;
+    const int hi = min(g.Ni - 1, s - c);
+    const long long base = (long long)row * g.P;
+    for (int a = max(0, s - c - (g.Nj - 1)) + lane; a <= hi; a += 32) f(base + a, a, s - a - c, c);
+  }
 }
 
 // ---------------------------------------------- batched CG iterations
@@ -296,11 +301,9 @@ __global__ void k_pk_x(DG g, const double* __restrict__ zk, const double* __rest
   const double sk = block_sum_fixed(wpart, nwp);
   const double bet = sk / scal[0];
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[1] = sk; scal[4] = bet; }
-  D_LOOP(g) {
-    int a, b, c;
-    if (!d_cell(g, t_, a, b, c)) continue;
+  for_cells(g, [&](long long t_, int a, int b, int c) {
     pkn[t_] = zk[t_] + bet * pko[t_];
-  }
+  });
 }
 
 // pkapk from the product's partials, alf = sk/pkapk (pcg-sip.f90:261-263);
@@ -313,14 +316,12 @@ __global__ void k_update_x(DG g, double* __restrict__ fi, double* __restrict__ r
   const double alf = scal[1] / pkapk;
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[2] = pkapk; scal[3] = alf; }
   double v[1] = {0.0};
-  D_LOOP(g) {
-    int a, b, c;
-    if (!d_cell(g, t_, a, b, c)) continue;
+  for_cells(g, [&](long long t_, int a, int b, int c) {
     fi[t_] = fi[t_] + alf * pk[t_];
     const double r = res[t_] - alf * zz[t_];
     res[t_] = r;
     v[0] += fabs(r);
-  }
+  });
   block_reduce_store<1>(v, pout);
 }
 
@@ -352,9 +353,7 @@ __global__ void k_spmv_x(DG g, const double* __restrict__ ae, const double* __re
                          double* part, const int* ctl) {
   if (*(volatile const int*)ctl) return;
   double v[1] = {0.0};
-  D_LOOP(g) {
-    int a, b, c;
-    if (!d_cell(g, t_, a, b, c)) continue;
+  for_cells(g, [&](long long t_, int a, int b, int c) {
     const long long P = t_;
     const double pP = pk[P];
     const double pE = a + 1 < g.Ni ? pk[P + g.plane + 1] : 0.0;
@@ -366,7 +365,7 @@ __global__ void k_spmv_x(DG g, const double* __restrict__ ae, const double* __re
     const double r = ap[P] * pP - ae[P] * pE - aw[P] * pW - an[P] * pN - as[P] * pS - at[P] * pT - ab[P] * pB;
     zz[P] = r;
     v[0] += pP * r;
-  }
+  });
   block_reduce_store<1>(v, part);
 }
 
@@ -401,9 +400,7 @@ __global__ void k_resid_d(DG g, const double* __restrict__ ae, const double* __r
                           const double* __restrict__ fid, const double* __restrict__ fin,
                           double* __restrict__ res, double* part) {
   double v[1] = {0.0};
-  D_LOOP(g) {
-    int a, b, c;
-    if (!d_cell(g, t_, a, b, c)) continue;
+  for_cells(g, [&](long long t_, int a, int b, int c) {
     const long long P = t_;
     const int n = g.nat(a, b, c);
     const double fE = a + 1 < g.Ni ? fid[P + g.plane + 1] : fin[n + g.nj];
@@ -416,7 +413,7 @@ __global__ void k_resid_d(DG g, const double* __restrict__ ae, const double* __r
                      ap[P] * fid[P];
     res[P] = r;
     v[0] += fabs(r);
-  }
+  });
   block_reduce_store<1>(v, part);
 }
 
@@ -424,31 +421,25 @@ __global__ void k_resid_d(DG g, const double* __restrict__ ae, const double* __r
 // ---------------------------------------- FP32 + FP64-refinement kernels
 // D-layout FP64 -> FP32 copy of the cells
 __global__ void k_d_to_f(DG g, const double* __restrict__ src, float* __restrict__ dst) {
-  D_LOOP(g) {
-    int a, b, c;
-    if (!d_cell(g, t_, a, b, c)) continue;
+  for_cells(g, [&](long long t_, int a, int b, int c) {
     dst[t_] = (float)src[t_];
-  }
+  });
 }
 
 // x += dx (the refinement step)
 __global__ void k_add_f(DG g, double* __restrict__ x, const float* __restrict__ dx) {
-  D_LOOP(g) {
-    int a, b, c;
-    if (!d_cell(g, t_, a, b, c)) continue;
+  for_cells(g, [&](long long t_, int a, int b, int c) {
     x[t_] = x[t_] + (double)dx[t_];
-  }
+  });
 }
 
 // FP32 inner-loop kernels with fused scalars (same scheme as k_pk_x ...)
 __global__ void k_dot_fx(DG g, const float* __restrict__ x, const float* __restrict__ y, double* part, const int* ctl) {
   if (*(volatile const int*)ctl) return;
   float acc = 0.0f;
-  D_LOOP(g) {
-    int a, b, c;
-    if (!d_cell(g, t_, a, b, c)) continue;
+  for_cells(g, [&](long long t_, int a, int b, int c) {
     acc += x[t_] * y[t_];
-  }
+  });
   double v[1] = {(double)acc};
   block_reduce_store<1>(v, part);
 }
@@ -465,9 +456,7 @@ __global__ void k_pk_spmv_fx(DG g, const float* __restrict__ ae, const float* __
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[1] = sk; scal[4] = betd; }
   const float bet = (float)betd;
   float acc = 0.0f;
-  D_LOOP(g) {
-    int a, b, c;
-    if (!d_cell(g, t_, a, b, c)) continue;
+  for_cells(g, [&](long long t_, int a, int b, int c) {
     const long long P = t_;
     auto pnew = [&](long long q) { return zk[q] + bet * pko[q]; };
     const float pP = pnew(P);
@@ -481,7 +470,7 @@ __global__ void k_pk_spmv_fx(DG g, const float* __restrict__ ae, const float* __
     pkn[P] = pP;
     zz[P] = r;
     acc += pP * r;
-  }
+  });
   double v[1] = {(double)acc};
   block_reduce_store<1>(v, pout);
 }
@@ -495,14 +484,12 @@ __global__ void k_update_fx(DG g, float* __restrict__ x, float* __restrict__ r, 
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[2] = pkapk; scal[3] = alfd; }
   const float alf = (float)alfd;
   float acc = 0.0f;
-  D_LOOP(g) {
-    int a, b, c;
-    if (!d_cell(g, t_, a, b, c)) continue;
+  for_cells(g, [&](long long t_, int a, int b, int c) {
     x[t_] = x[t_] + alf * pk[t_];
     const float rr = r[t_] - alf * zz[t_];
     r[t_] = rr;
     acc += fabsf(rr);
-  }
+  });
   double v[1] = {(double)acc};
   block_reduce_store<1>(v, pout);
 }

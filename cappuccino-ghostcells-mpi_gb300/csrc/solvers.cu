@@ -588,6 +588,7 @@ int profile_unit(int which, double* bytes) {
   double cells = (double)b.count();
   double* zk = c.work[1];
   double* pk = c.work[0];
+  if (which == 9 || which == 10) return learned_profile_unit(which, bytes);
   if (which == 7 || which == 8) {
     if (d.nimm < 4 || d.njmm < 4 || d.nkmm < 4) { set_error("profile unit %d needs 2 interior cells per axis", which); return CAPPGPU_E_ARG; }
     return fast_profile_unit(which, bytes);

@@ -283,17 +283,21 @@ class Library:
                     "learn_stats")
         return {"samples": s.value, "guesses": g.value, "fallbacks": f.value, "last_ratio": r.value}
 
-    def learn_check(self, inp, tgt):
-        """One forward + backward pass on a (D, H, W) input/target: output, parameter gradients, loss."""
+    def learn_check(self, rhs, coef):
+        """One forward + backward pass of the residual-norm loss on a (D, H, W)
+        normalised residual and its (7, D, H, W) window operator (planes xp, xm,
+        yp, ym, zp, zm, diag): output, parameter gradients, loss."""
         fp = ctypes.POINTER(ctypes.c_float)
-        inp = np.ascontiguousarray(inp, np.float32)
-        tgt = np.ascontiguousarray(tgt, np.float32)
-        D, H, W = inp.shape
-        out = np.empty_like(inp)
+        rhs = np.ascontiguousarray(rhs, np.float32)
+        coef = np.ascontiguousarray(coef, np.float32)
+        D, H, W = rhs.shape
+        if coef.shape != (7, D, H, W):
+            raise ValueError("coef must have shape (7, D, H, W)")
+        out = np.empty_like(rhs)
         n = self.lib.cappgpu_learn_params(ctypes.cast(None, fp), 0, 0)
         grad = np.empty(n, np.float32)
         loss = ctypes.c_double()
-        self._check(self.lib.cappgpu_learn_check(inp.ctypes.data_as(fp), tgt.ctypes.data_as(fp), D, H, W,
+        self._check(self.lib.cappgpu_learn_check(rhs.ctypes.data_as(fp), coef.ctypes.data_as(fp), D, H, W,
                                                  out.ctypes.data_as(fp), grad.ctypes.data_as(fp), ctypes.byref(loss)),
                     "learn_check")
         return out, grad, loss.value

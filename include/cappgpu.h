@@ -190,7 +190,13 @@ int cappgpu_find_intersection_point(const double* p, double* out);
 
 /* Run-time options.  "wave": 1 = SIP factorisation/substitutions of pcgsip
    as persistent hyperplane wavefronts (default), 0 = one kernel launch per
-   hyperplane (the simple form, kept for cross-checks). */
+   hyperplane (the simple form, kept for cross-checks).
+   "tight_correctors": 0 = the reference's tolerances (default: every PISO
+   corrector but the last solves p to sor(ip) = 0.1 only,
+   PISO_multiple_correction.f90:131-135), 1 = every corrector solves to the
+   last one's tolerance.  Where the first corrector stops decides the step's
+   result to well above the arithmetic's precision, so two precision modes
+   are compared with 1; it is not the reference's algorithm. */
 int cappgpu_set_option(const char* key, int value);
 
 /* Precision of the pressure solve (cappgpu_pcgsip and the PISO correctors
@@ -204,34 +210,40 @@ int cappgpu_set_option(const char* key, int value);
 int cappgpu_precision(int mode);
 
 /* ================================================ learned initial guess */
-/* No counterpart in the reference.  A small 3-D convolutional net (four
-   3x3x3 layers of 16 channels, dilations 1,2,4,8, ReLU, then 1x1x1 to one
-   channel; BF16 on the tensor cores, FP32 accumulation and master weights,
-   Adam) predicts the correction of a pressure solve from its initial
-   residual, both normalised by the mean |residual|.  In precision mode 2 the
-   refinement form of cappgpu_pcgsip starts from fi + guess when that lowers
-   the FP64 residual and from fi otherwise; its exit test stays relative to
-   the residual of fi, so the plain solve is judge and fallback.
+/* No counterpart in the reference.  A 3-level 3-D convolutional U-Net
+   (3x3x3 kernels, 16/32/64 channels, average pooling, nearest up-sampling,
+   skip concatenation, ReLU, then 1x1x1 to one channel; BF16 on the tensor
+   cores, FP32 accumulation and master weights, Adam) predicts the
+   correction d of a pressure solve, A d = r0, from its initial residual
+   normalised by its RMS, trained on the residual-norm loss
+   |A^ d - r^|^2/|r^|^2 with the solve's own operator (normalised by the
+   mean diagonal) on random block^3 windows.  In precision mode 2 the
+   refinement form of cappgpu_pcgsip starts from fi + alpha*guess (alpha by
+   least squares) when that lowers the FP64 residual and from fi otherwise;
+   its exit test stays relative to the residual of fi, so the plain solve is
+   judge and fallback.
    cappgpu_learn_reset     (re)creates the net with seeded weights and room
                            for max_samples recorded pairs of this grid
-   cappgpu_learn_collect   records (residual, converged correction) pairs in
-                           the pressure solves that follow (precision 1 or 2)
-   cappgpu_learn_train     Adam on random block^3 windows of the pairs,
-                           mean-squared error; *loss = mean loss of the last
-                           epoch
+   cappgpu_learn_collect   records (initial residual, operator) of the
+                           pressure solves that follow (precision 1 or 2)
+   cappgpu_learn_train     Adam on random block^3 windows of the pairs
+                           (block rounded down to a multiple of 4);
+                           *loss = mean loss of the last epoch
    cappgpu_learn_params    FP32 parameters out (direction 0) or in (1); with
                            host == NULL returns the parameter count
    cappgpu_learn_stats     pairs recorded, guesses kept, guesses discarded,
                            residual ratio of the last guess
    cappgpu_learn_check     one forward and backward pass on a D x H x W
-                           input/target from the host (for tests): output,
+                           normalised residual and its window operator
+                           (7 planes xp, xm, yp, ym, zp, zm, diag; extents
+                           multiples of 4) from the host, for tests: output,
                            parameter gradients and loss */
 int cappgpu_learn_reset(int max_samples, unsigned long long seed);
 int cappgpu_learn_collect(int on);
 int cappgpu_learn_train(int epochs, int block, double lr, double* loss);
 int cappgpu_learn_params(float* host, int n, int direction);
 int cappgpu_learn_stats(int* samples, int* guesses, int* fallbacks, double* last_ratio);
-int cappgpu_learn_check(const float* input, const float* target, int D, int H, int W, float* output, float* grad,
+int cappgpu_learn_check(const float* rhs, const float* coef, int D, int H, int W, float* output, float* grad,
                         double* loss);
 
 /* ======================================================= index maps (a1) */
@@ -359,8 +371,10 @@ int cappgpu_host_free(void* p);
 /* Time reps runs of one hot-path unit (0 SIP forward sweep, 1 SIP backward
    sweep, 2 7-point product + dot, 3 grad_gauss, 4 fluxuvw east, 5 PISO
    pressure assembly east, 6 SIP factorisation, 7 / 8 FP32 forward / backward
-   sweep of the precision-1 form) on the current state; returns device ms per
-   unit and its algorithmic bytes. */
+   sweep of the precision-1 form, 9 forward pass of the learned guess's net
+   on this grid, 10 its forward and backward pass on a 64^3 window of the
+   first recorded pair) on the current state; returns device ms per unit and
+   its algorithmic bytes (units 9 and 10: algorithmic FLOPs). */
 int cappgpu_profile_kernel(int which, int reps, double* ms_per_unit, double* algo_bytes);
 
 #ifdef __cplusplus

@@ -64,3 +64,37 @@ def test_precision_rejects_unknown_mode(gpu_lib):
     gpu_lib.init(8, 8, 8)
     with pytest.raises(cappgpu.CappError):
         gpu_lib.precision(3)
+
+
+def _channel_run(gpu_lib, case, mode, tight, steps=3):
+    gpu_lib.load_case(case)
+    gpu_lib.set_option("tight_correctors", tight)
+    gpu_lib.precision(mode)
+    try:
+        rep = gpu_lib.piso_steps(steps)
+    finally:
+        gpu_lib.precision(0)
+        gpu_lib.set_option("tight_correctors", 0)
+    assert rep.status == 0
+    return {k: gpu_lib.get_field(k) for k in ("u", "v", "w", "p")}
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_mixed_piso_agrees_with_fp64_when_every_corrector_is_converged(gpu_lib):
+    # The reference stops the first corrector's p solve at sor = 0.1, and
+    # where it stops moves the step's result far above FP32 rounding.  With
+    # every corrector solved to the last one's tolerance (1e-6) the FP32 form
+    # must land on the FP64 result within that tolerance's reach.
+    case = cappgpu.cases.channel(N=(24, 20, 28))
+    ref = _channel_run(gpu_lib, case, 0, 0)
+    t64 = _channel_run(gpu_lib, case, 0, 1)
+    t32 = _channel_run(gpu_lib, case, 1, 1)
+    spread = {k: _rel(t64[k], ref[k]) for k in ref}
+    err = {k: _rel(t32[k], t64[k]) for k in ref}
+    print("first-corrector spread", spread, "FP32 form vs FP64", err)
+    for k in ("u", "v", "w"):
+        assert err[k] < 1e-5, (k, err[k])
+    assert err["p"] < 1e-4
