@@ -24,12 +24,15 @@
 // (the solve's interior is zero-padded up to that).
 //
 // Activations and weights are BF16, accumulation FP32, FP32 master weights,
-// Adam.  Convolutions are implicit GEMMs on the tensor cores (mma.sync
-// m16n8k16): forward and input gradient (the same kernel with flipped,
-// transposed weights and the ReLU mask of the layer's output) take 16 voxels
-// x 16 output channels per warp and K = 27 taps x input channels; the weight
-// gradient is a GEMM over voxels per tap, split in chunks and summed in a
-// fixed order.  Training pairs are recorded by the solver itself
+// Adam.  Convolutions are implicit GEMMs on the tensor cores: forward and
+// input gradient (the same kernel with flipped, transposed weights and the
+// ReLU mask of the layer's output) as tcgen05 MMAs into TMEM, 128 voxels x
+// all output channels per CTA and K = 27 taps x input channels
+// (learned_tc.cuh); an mma.sync m16n8k16 form of the same convolution (16
+// voxels x 16 output channels per warp) is kept for cross-checks
+// (cappgpu_set_option("learn_conv", 0)).  The weight gradient is a GEMM
+// over voxels per tap (mma.sync), split in chunks and summed in a fixed
+// order.  Training pairs are recorded by the solver itself
 // (cappgpu_learn_collect) and the net is trained on random cubic windows of
 // them (cappgpu_learn_train).
 #include <cuda_bf16.h>
@@ -40,6 +43,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "learned_tc.cuh"
 
 namespace cap {
 
@@ -88,6 +92,7 @@ struct Net {
   float* part = nullptr;         // partial sums
   size_t part_n = 0;
   double* dsum = nullptr;        // device scalars: loss
+  int* err = nullptr;            // set by a tensor-core convolution whose wait ran out
   // recorded pairs: [sample][8][sV]: r^, then A^ as xp, xm, yp, ym, zp, zm, diag
   int max_samples = 0, nsamples = 0, next = 0;
   int sD = 0, sH = 0, sW = 0;
@@ -109,7 +114,7 @@ void net_free() {
   cudaFree(N.p); cudaFree(N.gp); cudaFree(N.m); cudaFree(N.v);
   cudaFree(N.wb); cudaFree(N.wt);
   acts_free();
-  cudaFree(N.part); cudaFree(N.dsum);
+  cudaFree(N.part); cudaFree(N.dsum); cudaFree(N.err);
   cudaFree(N.store);
   N = Net();
 }
@@ -705,10 +710,49 @@ int conv_ci(const bf16* x, int ldx, const bf16* w, int CO, const float* bias, co
   return CAPPGPU_OK;
 }
 
+// the convolution kernels: 1 = tcgen05 (default), 0 = mma.sync
+int g_conv_impl = 1;
+
+template <int CI, int CO, bool MASK>
+int conv_tc(const bf16* x, int ldx, const bf16* w, const float* bias, const bf16* mask, int ldm, bf16* y, int ldy,
+            int D, int H, int W, int relu) {
+  typedef tc::ConvTC<CI, CO> T;
+  CAP_CUDA(cudaFuncSetAttribute(tc::k_conv3_tc<CI, CO, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize, T::kSmem));
+  const int ntiles = (D * H * W + 127) / 128;
+  // CTAs one SM holds: shared memory, 512 TMEM columns, 16 x 128 threads
+  int per_sm = (228 * 1024) / (T::kSmem + 1024);
+  if (per_sm > 512 / T::kCols) per_sm = 512 / T::kCols;
+  if (per_sm > 16) per_sm = 16;
+  if (per_sm < 1) per_sm = 1;
+  int grid = 152 * per_sm;
+  if (grid > ntiles) grid = ntiles;
+  ++ctx().launches;
+  tc::k_conv3_tc<CI, CO, MASK><<<grid, 128, T::kSmem, ctx().st>>>(x, ldx, w, bias, mask, ldm, y, ldy, D, H, W, relu,
+                                                                   N.err);
+  return CAPPGPU_OK;
+}
+
+// the tensor-core form for the net's (CI, CO) pairs; -1 if there is none
+int conv_tc_any(int CI, const bf16* x, int ldx, const bf16* w, int CO, const float* bias, const bf16* mask, int ldm,
+                bf16* y, int ldy, int D, int H, int W, int relu) {
+#define CAP_TC(ci, co)                                                                                  \
+  if (CI == ci && CO == co)                                                                             \
+    return mask ? conv_tc<ci, co, true>(x, ldx, w, bias, mask, ldm, y, ldy, D, H, W, relu)              \
+                : conv_tc<ci, co, false>(x, ldx, w, bias, mask, ldm, y, ldy, D, H, W, relu);
+  CAP_TC(16, 16) CAP_TC(16, 32) CAP_TC(32, 32) CAP_TC(32, 64) CAP_TC(64, 64) CAP_TC(96, 32) CAP_TC(48, 16)
+  CAP_TC(32, 16) CAP_TC(64, 32) CAP_TC(32, 96) CAP_TC(16, 48)
+#undef CAP_TC
+  return -1;
+}
+
 // y = relu(conv(x) + b) (forward, mask == null) or the input gradient
 // (mask = the layer's output, w = flipped transposed weights)
 int conv(int CI, const bf16* x, int ldx, const bf16* w, int CO, const float* bias, const bf16* mask, int ldm, bf16* y,
          int ldy, int D, int H, int W, int relu) {
+  if (g_conv_impl == 1) {
+    const int rc = conv_tc_any(CI, x, ldx, w, CO, bias, mask, ldm, y, ldy, D, H, W, relu);
+    if (rc >= 0) return rc;
+  }
   switch (CI) {
     case 16: return conv_ci<16>(x, ldx, w, CO, bias, mask, ldm, y, ldy, D, H, W, relu);
     case 32: return conv_ci<32>(x, ldx, w, CO, bias, mask, ldm, y, ldy, D, H, W, relu);
@@ -818,6 +862,19 @@ int backward(int D, int H, int W) {
   return CAPPGPU_OK;
 }
 
+// a tensor-core convolution whose bounded wait ran out (synchronises)
+int check_err() {
+  int h = 0;
+  CAP_CUDA(cudaMemcpyAsync(&h, N.err, sizeof(int), cudaMemcpyDeviceToHost, ctx().st));
+  CAP_CUDA(cudaStreamSynchronize(ctx().st));
+  if (h) {
+    cudaMemsetAsync(N.err, 0, sizeof(int), ctx().st);
+    set_error("learned guess: a tensor-core convolution waited beyond its limit");
+    return CAPPGPU_E_SPIN;
+  }
+  return CAPPGPU_OK;
+}
+
 int adam_step(float lr) {
   ++N.adam_t;
   const float c1 = 1.f - powf(0.9f, (float)N.adam_t), c2 = 1.f - powf(0.999f, (float)N.adam_t);
@@ -851,6 +908,12 @@ double bwd_flops_per_voxel() {
 }  // namespace
 
 void learned_free() { net_free(); }
+
+int learned_set_conv(int impl) {
+  if (impl != 0 && impl != 1) return CAPPGPU_E_ARG;
+  g_conv_impl = impl;
+  return CAPPGPU_OK;
+}
 
 // Unit timing (cappgpu_profile_kernel): 9 = one forward pass of the net on
 // this grid (interior padded to multiples of 4) from the module residual;
@@ -924,6 +987,7 @@ int learned_solve_start(int fif, double res0) {
          (const double*)c.redout, Ni, Nj, Nk, N.A.a0, D, H, W);
   CAP_CHECK_LAUNCH();
   if ((rc = forward(D, H, W))) return rc;
+  if ((rc = check_err())) return rc;
   // amplitude by least squares: alpha = (r0.Ad)/(Ad.Ad)
   double* shape = c.work[4];
   double* ashape = c.work[5];
@@ -981,6 +1045,8 @@ int cappgpu_learn_reset(int max_samples, unsigned long long seed) {
   CAP_CUDA(cudaMalloc(&N.wb, sizeof(bf16) * kWAll));
   CAP_CUDA(cudaMalloc(&N.wt, sizeof(bf16) * kWAll));
   CAP_CUDA(cudaMalloc(&N.dsum, sizeof(double) * 4));
+  CAP_CUDA(cudaMalloc(&N.err, sizeof(int)));
+  CAP_CUDA(cudaMemset(N.err, 0, sizeof(int)));
   CAP_CUDA(cudaMemset(N.gp, 0, sizeof(float) * kParams));
   CAP_CUDA(cudaMemset(N.dsum, 0, sizeof(double) * 4));
   if (max_samples > 0 && cudaMalloc(&N.store, sizeof(float) * 8 * (size_t)max_samples * V) != cudaSuccess) {
@@ -1035,7 +1101,7 @@ int cappgpu_learn_train(int epochs, int block, double lr, double* loss) {
       if ((rc = adam_step((float)lr))) return rc;
       double h = 0.0;
       CAP_CUDA(cudaMemcpyAsync(&h, N.dsum, sizeof(double), cudaMemcpyDeviceToHost, c.st));
-      CAP_CUDA(cudaStreamSynchronize(c.st));
+      if ((rc = check_err())) return rc;
       sum += h;
     }
     last = sum / N.nsamples;
@@ -1090,7 +1156,7 @@ int cappgpu_learn_check(const float* rhs, const float* coef, int D, int H, int W
   CAP_CUDA(cudaMemcpy(N.A.coef, coef, sizeof(float) * 7 * V, cudaMemcpyHostToDevice));
   if ((rc = forward(D, H, W))) return rc;
   if ((rc = backward(D, H, W))) return rc;
-  CAP_CUDA(cudaStreamSynchronize(c.st));
+  if ((rc = check_err())) return rc;
   if (output) CAP_CUDA(cudaMemcpy(output, N.A.out, sizeof(float) * V, cudaMemcpyDeviceToHost));
   if (grad) CAP_CUDA(cudaMemcpy(grad, N.gp, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
   if (loss) CAP_CUDA(cudaMemcpy(loss, N.dsum, sizeof(double), cudaMemcpyDeviceToHost));
