@@ -30,10 +30,16 @@ struct FluxArgs {
   int lcds, lcds4, lluds, lquds, flux_limiter, lsmart, lavl, lmuscl, lumist, lgamma;
 };
 
-__device__ inline double dmin_(double a, double b) { return a < b ? a : b; }
-__device__ inline double dmax_(double a, double b) { return a > b ? a : b; }
+template <typename R>
+__device__ inline R dmin_(R a, R b) { return a < b ? a : b; }
+// square root in the compute type (FP32 form: sqrtf, IEEE-rounded)
+__device__ inline double sqrt_(double x) { return sqrt(x); }
+__device__ inline float sqrt_(float x) { return sqrtf(x); }
+template <typename R>
+__device__ inline R dmax_(R a, R b) { return a > b ? a : b; }
 
 // fluxuvw-overrelaxed-correction.f90:121-637 for one face inp
+template <typename R>
 __global__ void k_fluxuvw_faces(Dims d, Box b, FluxArgs A) {
   BOX_LOOP(b) {
     int i, j, k;
@@ -41,129 +47,129 @@ __global__ void k_fluxuvw_faces(Dims d, Box b, FluxArgs A) {
     int inp = ixk(d, i, j, k);
     int ine = inp + A.idew, inw = inp - A.idew, ins = inp - A.idns, inb = inp - A.idtb;
     int inee = inp + 2 * A.idew, inbs = inb - A.idns;
-    double fxe = A.fif[inp], fxp = 1.0 - fxe;
-    double fxpw = A.fif[inw], fxw = 1.0 - fxpw;
-    double fxee = A.fif[ine], fxew = 1.0 - fxee;
-    double xpn = A.xc[ine] - A.xc[inp], ypn = A.yc[ine] - A.yc[inp], zpn = A.zc[ine] - A.zc[inp];
-    double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
-    double arx = A.arvx[inp], ary = A.arvy[inp], arz = A.arvz[inp];
-    double are = sqrt(arx * arx + ary * ary + arz * arz);
-    const double costn = 1.0;  // orthogonal correction (:178)
-    double vole = xpn * arx + ypn * ary + zpn * arz;
-    double d1x = costn, d1y = costn, d1z = costn;
-    double d2x = xpn * costn, d2y = ypn * costn, d2z = zpn * costn;
-    double game = (A.vis[inp] * fxp + A.vis[ine] * fxe);
-    double xf = 0.25 * (A.x[inp] + A.x[ins] + A.x[inb] + A.x[inbs]);
-    double yf = 0.25 * (A.y[inp] + A.y[ins] + A.y[inb] + A.y[inbs]);
-    double zf = 0.25 * (A.z[inp] + A.z[ins] + A.z[inb] + A.z[inbs]);
-    double xi = A.xc[inp] * fxp + A.xc[ine] * fxe;
-    double yi = A.yc[inp] * fxp + A.yc[ine] * fxe;
-    double zi = A.zc[inp] * fxp + A.zc[ine] * fxe;
+    R fxe = R(A.fif[inp]), fxp = R(1.0) - fxe;
+    R fxpw = R(A.fif[inw]), fxw = R(1.0) - fxpw;
+    R fxee = R(A.fif[ine]), fxew = R(1.0) - fxee;
+    R xpn = R(A.xc[ine]) - R(A.xc[inp]), ypn = R(A.yc[ine]) - R(A.yc[inp]), zpn = R(A.zc[ine]) - R(A.zc[inp]);
+    R dpn = sqrt_(xpn * xpn + ypn * ypn + zpn * zpn);
+    R arx = R(A.arvx[inp]), ary = R(A.arvy[inp]), arz = R(A.arvz[inp]);
+    R are = sqrt_(arx * arx + ary * ary + arz * arz);
+    const R costn = R(1.0);  // orthogonal correction (:178)
+    R vole = xpn * arx + ypn * ary + zpn * arz;
+    R d1x = costn, d1y = costn, d1z = costn;
+    R d2x = xpn * costn, d2y = ypn * costn, d2z = zpn * costn;
+    R game = (R(A.vis[inp]) * fxp + R(A.vis[ine]) * fxe);
+    R xf = R(0.25) * (R(A.x[inp]) + R(A.x[ins]) + R(A.x[inb]) + R(A.x[inbs]));
+    R yf = R(0.25) * (R(A.y[inp]) + R(A.y[ins]) + R(A.y[inb]) + R(A.y[inbs]));
+    R zf = R(0.25) * (R(A.z[inp]) + R(A.z[ins]) + R(A.z[inb]) + R(A.z[inbs]));
+    R xi = R(A.xc[inp]) * fxp + R(A.xc[ine]) * fxe;
+    R yi = R(A.yc[inp]) * fxp + R(A.yc[ine]) * fxe;
+    R zi = R(A.zc[inp]) * fxp + R(A.zc[ine]) * fxe;
     const double *u = A.u, *v = A.v, *w = A.w;
-    double duxi = A.gux[inp] * fxp + A.gux[ine] * fxe;
-    double duyi = A.guy[inp] * fxp + A.guy[ine] * fxe;
-    double duzi = A.guz[inp] * fxp + A.guz[ine] * fxe;
-    double du = u[ine] - u[inp] - duxi * d2x - duyi * d2y - duzi * d2z;
-    double duxii = duxi * d1x + arx / vole * du;
-    double duyii = duyi * d1y + ary / vole * du;
-    double duzii = duzi * d1z + arz / vole * du;
-    double dvxi = A.gvx[inp] * fxp + A.gvx[ine] * fxe;
-    double dvyi = A.gvy[inp] * fxp + A.gvy[ine] * fxe;
-    double dvzi = A.gvz[inp] * fxp + A.gvz[ine] * fxe;
-    double dv = v[ine] - v[inp] - dvxi * d2x - dvyi * d2y - dvzi * d2z;
-    double dvxii = dvxi * d1x + arx / vole * dv;
-    double dvyii = dvyi * d1y + ary / vole * dv;
-    double dvzii = dvzi * d1z + arz / vole * dv;
-    double dwxi = A.gwx[inp] * fxp + A.gwx[ine] * fxe;
-    double dwyi = A.gwy[inp] * fxp + A.gwy[ine] * fxe;
-    double dwzi = A.gwz[inp] * fxp + A.gwz[ine] * fxe;
-    double dw = w[ine] - w[inp] - dwxi * d2x - dwyi * d2y - dwzi * d2z;
-    double dwxii = dwxi * d1x + arx / vole * dw;
-    double dwyii = dwyi * d1y + ary / vole * dw;
-    double dwzii = dwzi * d1z + arz / vole * dw;
-    double fdue = game * ((duxii + duxii) * arx + (duyii + dvxii) * ary + (duzii + dwxii) * arz);
-    double fdve = game * ((duyii + dvxii) * arx + (dvyii + dvyii) * ary + (dvzii + dwyii) * arz);
-    double fdwe = game * ((duzii + dwxii) * arx + (dwyii + dvzii) * ary + (dwzii + dwzii) * arz);
-    double gad = game * are / dpn;
-    double fdui = gad * (duxi * xpn + duyi * ypn + duzi * zpn);
-    double fdvi = gad * (dvxi * xpn + dvyi * ypn + dvzi * zpn);
-    double fdwi = gad * (dwxi * xpn + dwyi * ypn + dwzi * zpn);
-    double de = gad;
-    double flcf = A.fcf[inp];
-    double ce = dmin_(flcf, A.zero);
-    double cp = dmax_(flcf, A.zero);
+    R duxi = R(A.gux[inp]) * fxp + R(A.gux[ine]) * fxe;
+    R duyi = R(A.guy[inp]) * fxp + R(A.guy[ine]) * fxe;
+    R duzi = R(A.guz[inp]) * fxp + R(A.guz[ine]) * fxe;
+    R du = R(u[ine]) - R(u[inp]) - duxi * d2x - duyi * d2y - duzi * d2z;
+    R duxii = duxi * d1x + arx / vole * du;
+    R duyii = duyi * d1y + ary / vole * du;
+    R duzii = duzi * d1z + arz / vole * du;
+    R dvxi = R(A.gvx[inp]) * fxp + R(A.gvx[ine]) * fxe;
+    R dvyi = R(A.gvy[inp]) * fxp + R(A.gvy[ine]) * fxe;
+    R dvzi = R(A.gvz[inp]) * fxp + R(A.gvz[ine]) * fxe;
+    R dv = R(v[ine]) - R(v[inp]) - dvxi * d2x - dvyi * d2y - dvzi * d2z;
+    R dvxii = dvxi * d1x + arx / vole * dv;
+    R dvyii = dvyi * d1y + ary / vole * dv;
+    R dvzii = dvzi * d1z + arz / vole * dv;
+    R dwxi = R(A.gwx[inp]) * fxp + R(A.gwx[ine]) * fxe;
+    R dwyi = R(A.gwy[inp]) * fxp + R(A.gwy[ine]) * fxe;
+    R dwzi = R(A.gwz[inp]) * fxp + R(A.gwz[ine]) * fxe;
+    R dw = R(w[ine]) - R(w[inp]) - dwxi * d2x - dwyi * d2y - dwzi * d2z;
+    R dwxii = dwxi * d1x + arx / vole * dw;
+    R dwyii = dwyi * d1y + ary / vole * dw;
+    R dwzii = dwzi * d1z + arz / vole * dw;
+    R fdue = game * ((duxii + duxii) * arx + (duyii + dvxii) * ary + (duzii + dwxii) * arz);
+    R fdve = game * ((duyii + dvxii) * arx + (dvyii + dvyii) * ary + (dvzii + dwyii) * arz);
+    R fdwe = game * ((duzii + dwxii) * arx + (dwyii + dvzii) * ary + (dwzii + dwzii) * arz);
+    R gad = game * are / dpn;
+    R fdui = gad * (duxi * xpn + duyi * ypn + duzi * zpn);
+    R fdvi = gad * (dvxi * xpn + dvyi * ypn + dvzi * zpn);
+    R fdwi = gad * (dwxi * xpn + dwyi * ypn + dwzi * zpn);
+    R de = gad;
+    R flcf = R(A.fcf[inp]);
+    R ce = dmin_(flcf, R(A.zero));
+    R cp = dmax_(flcf, R(A.zero));
     A.acfe[inp] = de - ce;
     A.acfw[ine] = de + cp;
-    double fuuds = cp * u[inp] + ce * u[ine];
-    double fvuds = cp * v[inp] + ce * v[ine];
-    double fwuds = cp * w[inp] + ce * w[ine];
-    double fuhigh = 0.0, fvhigh = 0.0, fwhigh = 0.0;
+    R fuuds = cp * R(u[inp]) + ce * R(u[ine]);
+    R fvuds = cp * R(v[inp]) + ce * R(v[ine]);
+    R fwuds = cp * R(w[inp]) + ce * R(w[ine]);
+    R fuhigh = R(0.0), fvhigh = R(0.0), fwhigh = R(0.0);
     if (A.lcds) {
-      double ue = u[inp] * fxp + u[ine] * fxe + (duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi));
-      double ve = v[inp] * fxp + v[ine] * fxe + (dvxi * (xf - xi) + dvyi * (yf - yi) + dvzi * (zf - zi));
-      double we = w[inp] * fxp + w[ine] * fxe + (dwxi * (xf - xi) + dwyi * (yf - yi) + dwzi * (zf - zi));
+      R ue = R(u[inp]) * fxp + R(u[ine]) * fxe + (duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi));
+      R ve = R(v[inp]) * fxp + R(v[ine]) * fxe + (dvxi * (xf - xi) + dvyi * (yf - yi) + dvzi * (zf - zi));
+      R we = R(w[inp]) * fxp + R(w[ine]) * fxe + (dwxi * (xf - xi) + dwyi * (yf - yi) + dwzi * (zf - zi));
       fuhigh = flcf * ue; fvhigh = flcf * ve; fwhigh = flcf * we;
     }
     if (A.lcds4 && (A.idew == d.nj || A.idew == 1)) {
-      double ue = 1.0 / 48.0 * (27.0 * u[inp] + 27.0 * u[ine] - 3.0 * u[inw] - 3.0 * u[inee]);
-      double ve = 1.0 / 48.0 * (27.0 * v[inp] + 27.0 * v[ine] - 3.0 * v[inw] - 3.0 * v[inee]);
-      double we = 1.0 / 48.0 * (27.0 * w[inp] + 27.0 * w[ine] - 3.0 * w[inw] - 3.0 * w[inee]);
+      R ue = R(1.0) / R(48.0) * (R(27.0) * R(u[inp]) + R(27.0) * R(u[ine]) - R(3.0) * R(u[inw]) - R(3.0) * R(u[inee]));
+      R ve = R(1.0) / R(48.0) * (R(27.0) * R(v[inp]) + R(27.0) * R(v[ine]) - R(3.0) * R(v[inw]) - R(3.0) * R(v[inee]));
+      R we = R(1.0) / R(48.0) * (R(27.0) * R(w[inp]) + R(27.0) * R(w[ine]) - R(3.0) * R(w[inw]) - R(3.0) * R(w[inee]));
       fuhigh = flcf * ue; fvhigh = flcf * ve; fwhigh = flcf * we;
     }
     if (A.lluds) {
-      double dxc = xf - A.xc[inp], dyc = yf - A.yc[inp], dzc = zf - A.zc[inp];
-      double dxe = A.xc[ine] - xf, dye = A.yc[ine] - yf, dze = A.zc[ine] - zf;
-      double dfidx_u = A.gud[inw] * fxw + A.gud[inp] * fxpw;
-      double dfidy_u = A.gvd[inw] * fxw + A.gvd[inp] * fxpw;
-      double dfidz_u = A.gwd[inw] * fxw + A.gwd[inp] * fxpw;
-      double dfidx_u1 = A.gud[inee] * fxee + A.gud[ine] * fxew;
-      double dfidy_u1 = A.gvd[inee] * fxee + A.gvd[ine] * fxew;
-      double dfidz_u1 = A.gwd[inee] * fxee + A.gwd[ine] * fxew;
-      fuhigh = ce * (u[ine] + dxe * dfidx_u1) + cp * (u[inp] + dxc * dfidx_u);
-      fvhigh = ce * (v[ine] + dye * dfidy_u1) + cp * (v[inp] + dyc * dfidy_u);
-      fwhigh = ce * (w[ine] + dze * dfidz_u1) + cp * (w[inp] + dzc * dfidz_u);
+      R dxc = xf - R(A.xc[inp]), dyc = yf - R(A.yc[inp]), dzc = zf - R(A.zc[inp]);
+      R dxe = R(A.xc[ine]) - xf, dye = R(A.yc[ine]) - yf, dze = R(A.zc[ine]) - zf;
+      R dfidx_u = R(A.gud[inw]) * fxw + R(A.gud[inp]) * fxpw;
+      R dfidy_u = R(A.gvd[inw]) * fxw + R(A.gvd[inp]) * fxpw;
+      R dfidz_u = R(A.gwd[inw]) * fxw + R(A.gwd[inp]) * fxpw;
+      R dfidx_u1 = R(A.gud[inee]) * fxee + R(A.gud[ine]) * fxew;
+      R dfidy_u1 = R(A.gvd[inee]) * fxee + R(A.gvd[ine]) * fxew;
+      R dfidz_u1 = R(A.gwd[inee]) * fxee + R(A.gwd[ine]) * fxew;
+      fuhigh = ce * (R(u[ine]) + dxe * dfidx_u1) + cp * (R(u[inp]) + dxc * dfidx_u);
+      fvhigh = ce * (R(v[ine]) + dye * dfidy_u1) + cp * (R(v[inp]) + dyc * dfidy_u);
+      fwhigh = ce * (R(w[ine]) + dze * dfidz_u1) + cp * (R(w[inp]) + dzc * dfidz_u);
     }
     if (A.lquds && k > 2 && k < d.nk - 1 && j > 2 && j < d.nj - 1 && i > 2 && i < d.ni - 1) {
-      double fm = A.fif[inp - A.idew], f0 = A.fif[inp], fpl = A.fif[inp + A.idew];
-      double g11 = ((2 - fm) * (f0 * f0)) / (1 + f0 - fm);
-      double g12 = ((1 - f0) * ((1 - fm) * (1 - fm))) / (1 + f0 - fm);
-      double g21 = ((1 + fpl) * ((1 - f0) * (1 - f0))) / (1 + fpl - f0);
-      double g22 = ((fpl * fpl) * f0) / (1 + fpl - f0);
-      fuhigh = ce * (g21 * u[inp] + (1 - g21 + g22) * u[ine] - g22 * u[inee]) +
-               cp * (g11 * u[ine] + (1 - g11 + g12) * u[inp] - g12 * u[inw]);
-      fvhigh = ce * (g21 * v[inp] + (1 - g21 + g22) * v[ine] - g22 * v[inee]) +
-               cp * (g11 * v[ine] + (1 - g11 + g12) * v[inp] - g12 * v[inw]);
-      fwhigh = ce * (g21 * w[inp] + (1 - g21 + g22) * w[ine] - g22 * w[inee]) +
-               cp * (g11 * w[ine] + (1 - g11 + g12) * w[inp] - g12 * w[inw]);
+      R fm = R(A.fif[inp - A.idew]), f0 = R(A.fif[inp]), fpl = R(A.fif[inp + A.idew]);
+      R g11 = ((2 - fm) * (f0 * f0)) / (1 + f0 - fm);
+      R g12 = ((1 - f0) * ((1 - fm) * (1 - fm))) / (1 + f0 - fm);
+      R g21 = ((1 + fpl) * ((1 - f0) * (1 - f0))) / (1 + fpl - f0);
+      R g22 = ((fpl * fpl) * f0) / (1 + fpl - f0);
+      fuhigh = ce * (g21 * R(u[inp]) + (1 - g21 + g22) * R(u[ine]) - g22 * R(u[inee])) +
+               cp * (g11 * R(u[ine]) + (1 - g11 + g12) * R(u[inp]) - g12 * R(u[inw]));
+      fvhigh = ce * (g21 * R(v[inp]) + (1 - g21 + g22) * R(v[ine]) - g22 * R(v[inee])) +
+               cp * (g11 * R(v[ine]) + (1 - g11 + g12) * R(v[inp]) - g12 * R(v[inw]));
+      fwhigh = ce * (g21 * R(w[inp]) + (1 - g21 + g22) * R(w[ine]) - g22 * R(w[inee])) +
+               cp * (g11 * R(w[ine]) + (1 - g11 + g12) * R(w[inp]) - g12 * R(w[inw]));
     }
     if (A.flux_limiter) {
-      double rr[6];
-      rr[0] = (2 * A.gux[inp] * xpn + 2 * A.guy[inp] * ypn + 2 * A.guz[inp] * zpn) / (u[ine] - u[inp]) - 1.0;
-      rr[1] = (2 * A.gvx[inp] * xpn + 2 * A.gvy[inp] * ypn + 2 * A.gvz[inp] * zpn) / (v[ine] - v[inp]) - 1.0;
-      rr[2] = (2 * A.gwx[inp] * xpn + 2 * A.gwy[inp] * ypn + 2 * A.gwz[inp] * zpn) / (w[ine] - w[inp]) - 1.0;
-      rr[3] = (2 * A.gux[ine] * xpn + 2 * A.guy[ine] * ypn + 2 * A.guz[ine] * zpn) / (u[inp] - u[ine]) - 1.0;
-      rr[4] = (2 * A.gvx[ine] * xpn + 2 * A.gvy[ine] * ypn + 2 * A.gvz[ine] * zpn) / (v[inp] - v[ine]) - 1.0;
-      rr[5] = (2 * A.gwx[ine] * xpn + 2 * A.gwy[ine] * ypn + 2 * A.gwz[ine] * zpn) / (w[inp] - w[ine]) - 1.0;
-      double psi[6] = {0, 0, 0, 0, 0, 0};
+      R rr[6];
+      rr[0] = (2 * R(A.gux[inp]) * xpn + 2 * R(A.guy[inp]) * ypn + 2 * R(A.guz[inp]) * zpn) / (R(u[ine]) - R(u[inp])) - R(1.0);
+      rr[1] = (2 * R(A.gvx[inp]) * xpn + 2 * R(A.gvy[inp]) * ypn + 2 * R(A.gvz[inp]) * zpn) / (R(v[ine]) - R(v[inp])) - R(1.0);
+      rr[2] = (2 * R(A.gwx[inp]) * xpn + 2 * R(A.gwy[inp]) * ypn + 2 * R(A.gwz[inp]) * zpn) / (R(w[ine]) - R(w[inp])) - R(1.0);
+      rr[3] = (2 * R(A.gux[ine]) * xpn + 2 * R(A.guy[ine]) * ypn + 2 * R(A.guz[ine]) * zpn) / (R(u[inp]) - R(u[ine])) - R(1.0);
+      rr[4] = (2 * R(A.gvx[ine]) * xpn + 2 * R(A.gvy[ine]) * ypn + 2 * R(A.gvz[ine]) * zpn) / (R(v[inp]) - R(v[ine])) - R(1.0);
+      rr[5] = (2 * R(A.gwx[ine]) * xpn + 2 * R(A.gwy[ine]) * ypn + 2 * R(A.gwz[ine]) * zpn) / (R(w[inp]) - R(w[ine])) - R(1.0);
+      R psi[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
       for (int q = 0; q < 6; ++q) {
-        double r = rr[q];
-        if (A.lsmart) psi[q] = dmax_(0.0, dmin_(dmin_(2.0 * r, 0.75 * r + 0.25), 4.0));
-        if (A.lavl) psi[q] = dmax_(0.0, dmin_(dmin_(1.5 * r, 0.75 * r + 0.25), 2.5));
-        if (A.lmuscl) psi[q] = dmax_(0.0, dmin_(dmin_(2.0 * r, 0.5 * r + 0.5), 2.0));
-        if (A.lumist) psi[q] = dmax_(0.0, dmin_(dmin_(dmin_(2.0 * r, 0.75 * r + 0.25), 0.25 * r + 0.75), 2.0));
-        if (A.lgamma) psi[q] = dmax_(0.0, dmin_(r, 2.0 * r / (r + 1.0)));
+        R r = rr[q];
+        if (A.lsmart) psi[q] = dmax_(R(0.0), dmin_(dmin_(R(2.0) * r, R(0.75) * r + R(0.25)), R(4.0)));
+        if (A.lavl) psi[q] = dmax_(R(0.0), dmin_(dmin_(R(1.5) * r, R(0.75) * r + R(0.25)), R(2.5)));
+        if (A.lmuscl) psi[q] = dmax_(R(0.0), dmin_(dmin_(R(2.0) * r, R(0.5) * r + R(0.5)), R(2.0)));
+        if (A.lumist) psi[q] = dmax_(R(0.0), dmin_(dmin_(dmin_(R(2.0) * r, R(0.75) * r + R(0.25)), R(0.25) * r + R(0.75)), R(2.0)));
+        if (A.lgamma) psi[q] = dmax_(R(0.0), dmin_(r, R(2.0) * r / (r + R(1.0))));
       }
-      fuhigh = ce * (u[ine] + fxe * psi[3] * (u[inp] - u[ine])) + cp * (u[inp] + fxp * psi[0] * (u[ine] - u[inp]));
-      fvhigh = ce * (v[ine] + fxe * psi[4] * (v[inp] - v[ine])) + cp * (v[inp] + fxp * psi[1] * (v[ine] - v[inp]));
-      fwhigh = ce * (w[ine] + fxe * psi[5] * (w[inp] - w[ine])) + cp * (w[inp] + fxp * psi[2] * (w[ine] - w[inp]));
+      fuhigh = ce * (R(u[ine]) + fxe * psi[3] * (R(u[inp]) - R(u[ine]))) + cp * (R(u[inp]) + fxp * psi[0] * (R(u[ine]) - R(u[inp])));
+      fvhigh = ce * (R(v[ine]) + fxe * psi[4] * (R(v[inp]) - R(v[ine]))) + cp * (R(v[inp]) + fxp * psi[1] * (R(v[ine]) - R(v[inp])));
+      fwhigh = ce * (R(w[ine]) + fxe * psi[5] * (R(w[inp]) - R(w[ine]))) + cp * (R(w[inp]) + fxp * psi[2] * (R(w[ine]) - R(w[inp])));
     }
-    A.su[inp] = A.su[inp] + A.gam * (fuuds - fuhigh) + fdue - fdui;
-    A.sv[inp] = A.sv[inp] + A.gam * (fvuds - fvhigh) + fdve - fdvi;
-    A.sw[inp] = A.sw[inp] + A.gam * (fwuds - fwhigh) + fdwe - fdwi;
-    A.bp[ine] = -A.gam * (fuuds - fuhigh) - fdue + fdui;
-    A.bt[ine] = -A.gam * (fvuds - fvhigh) - fdve + fdvi;
-    A.bb[ine] = -A.gam * (fwuds - fwhigh) - fdwe + fdwi;
+    A.su[inp] = R(A.su[inp]) + R(A.gam) * (fuuds - fuhigh) + fdue - fdui;
+    A.sv[inp] = R(A.sv[inp]) + R(A.gam) * (fvuds - fvhigh) + fdve - fdvi;
+    A.sw[inp] = R(A.sw[inp]) + R(A.gam) * (fwuds - fwhigh) + fdwe - fdwi;
+    A.bp[ine] = -R(A.gam) * (fuuds - fuhigh) - fdue + fdui;
+    A.bt[ine] = -R(A.gam) * (fvuds - fvhigh) - fdve + fdvi;
+    A.bb[ine] = -R(A.gam) * (fwuds - fwhigh) - fdwe + fdwi;
   }
 }
 
@@ -208,7 +214,11 @@ int fluxuvw(int idew, int idns, int idtb, int arvx, int arvy, int arvz, int fif,
              F[CAP_SU], F[CAP_SV], F[CAP_SW], F[CAP_BP], F[CAP_BT], F[CAP_BB],
              P.gds[CAP_IU - 1], P.zero, idew, idns, idtb,
              P.lcds, P.lcds4, P.lluds, P.lquds, P.flux_limiter, P.lsmart, P.lavl, P.lmuscl, P.lumist, P.lgamma};
-  launch(k_fluxuvw_faces, grid_for(b.count()), kThreads, c.st, d, b, A);
+  // precision modes 1-2 assemble in FP32 arithmetic (FP64 storage)
+  if (c.fp32(4))
+    launch(k_fluxuvw_faces<float>, grid_for(b.count()), kThreads, c.st, d, b, A);
+  else
+    launch(k_fluxuvw_faces<double>, grid_for(b.count()), kThreads, c.st, d, b, A);
   Box b2{2, d.nimm, 2, d.njmm, 2, d.nkmm};
   launch(k_add_staged, grid_for(b2.count()), kThreads, c.st, d, b2, idew, F[CAP_SU], F[CAP_SV], F[CAP_SW], F[CAP_BP],
                                                             F[CAP_BT], F[CAP_BB]);
@@ -429,60 +439,61 @@ struct PeqArgs {
 };
 
 // PISO_assemble_pressure_eq.f90:48-237 for one face
+template <typename R>
 __global__ void k_piso_peq_faces(Dims d, Box b, PeqArgs A) {
   BOX_LOOP(b) {
     int i, j, k;
     b.at(t_, i, j, k);
     int inp = ixk(d, i, j, k);
     int ine = inp + A.idew, ins = inp - A.idns, inb = inp - A.idtb, inbs = inb - A.idns;
-    double fxe = A.fif[inp], fxp = 1.0 - fxe;
-    double xf = 0.25 * (A.x[inp] + A.x[ins] + A.x[inb] + A.x[inbs]);
-    double yf = 0.25 * (A.y[inp] + A.y[ins] + A.y[inb] + A.y[inbs]);
-    double zf = 0.25 * (A.z[inp] + A.z[ins] + A.z[inb] + A.z[inbs]);
-    double xi = A.xc[inp] * fxp + A.xc[ine] * fxe;
-    double yi = A.yc[inp] * fxp + A.yc[ine] * fxe;
-    double zi = A.zc[inp] * fxp + A.zc[ine] * fxe;
-    double xpn = A.xc[ine] - A.xc[inp], ypn = A.yc[ine] - A.yc[inp], zpn = A.zc[ine] - A.zc[inp];
-    double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
-    double ixi1 = xpn / dpn, ixi2 = ypn / dpn, ixi3 = zpn / dpn;
-    double arx = A.arvx[inp], ary = A.arvy[inp], arz = A.arvz[inp];
-    double are = sqrt(arx * arx + ary * ary + arz * arz);
-    double vole = xpn * arx + ypn * ary + zpn * arz;
-    double nxx = arx / are, nyy = ary / are, nzz = arz / are;
-    double costheta = nxx * ixi1 + nyy * ixi2 + nzz * ixi3;
-    double costn = costheta;
-    double d1x = costn, d1y = costn, d1z = costn;
-    double d2x = xpn * costn, d2y = ypn * costn, d2z = zpn * costn;
-    double dene = A.den[inp] * fxp + A.den[ine] * fxe;
-    double game = dene * (fxp * A.vol[inp] * A.apu[inp] + fxe * A.vol[ine] * A.apu[ine]);
-    double acf = game * are / dpn;
+    R fxe = R(A.fif[inp]), fxp = R(1.0) - fxe;
+    R xf = R(0.25) * (R(A.x[inp]) + R(A.x[ins]) + R(A.x[inb]) + R(A.x[inbs]));
+    R yf = R(0.25) * (R(A.y[inp]) + R(A.y[ins]) + R(A.y[inb]) + R(A.y[inbs]));
+    R zf = R(0.25) * (R(A.z[inp]) + R(A.z[ins]) + R(A.z[inb]) + R(A.z[inbs]));
+    R xi = R(A.xc[inp]) * fxp + R(A.xc[ine]) * fxe;
+    R yi = R(A.yc[inp]) * fxp + R(A.yc[ine]) * fxe;
+    R zi = R(A.zc[inp]) * fxp + R(A.zc[ine]) * fxe;
+    R xpn = R(A.xc[ine]) - R(A.xc[inp]), ypn = R(A.yc[ine]) - R(A.yc[inp]), zpn = R(A.zc[ine]) - R(A.zc[inp]);
+    R dpn = sqrt_(xpn * xpn + ypn * ypn + zpn * zpn);
+    R ixi1 = xpn / dpn, ixi2 = ypn / dpn, ixi3 = zpn / dpn;
+    R arx = R(A.arvx[inp]), ary = R(A.arvy[inp]), arz = R(A.arvz[inp]);
+    R are = sqrt_(arx * arx + ary * ary + arz * arz);
+    R vole = xpn * arx + ypn * ary + zpn * arz;
+    R nxx = arx / are, nyy = ary / are, nzz = arz / are;
+    R costheta = nxx * ixi1 + nyy * ixi2 + nzz * ixi3;
+    R costn = costheta;
+    R d1x = costn, d1y = costn, d1z = costn;
+    R d2x = xpn * costn, d2y = ypn * costn, d2z = zpn * costn;
+    R dene = R(A.den[inp]) * fxp + R(A.den[ine]) * fxe;
+    R game = dene * (fxp * R(A.vol[inp]) * R(A.apu[inp]) + fxe * R(A.vol[ine]) * R(A.apu[ine]));
+    R acf = game * are / dpn;
     A.acfe[inp] = acf;
     A.acfw[ine] = acf;
     if (A.ipc > 0) {
-      double dfixi = A.gpx[inp] * fxp + A.gpx[ine] * fxe;
-      double dfiyi = A.gpy[inp] * fxp + A.gpy[ine] * fxe;
-      double dfizi = A.gpz[inp] * fxp + A.gpz[ine] * fxe;
-      double dp = A.p[ine] - A.p[inp] - (dfixi * d2x + dfiyi * d2y + dfizi * d2z);
-      double dfixii = dfixi * d1x + arx / vole * dp;
-      double dfiyii = dfiyi * d1y + ary / vole * dp;
-      double dfizii = dfizi * d1z + arz / vole * dp;
-      double fdfie = game * (dfixii * arx + dfiyii * ary + dfizii * arz);
-      double fdfii = game * are / dpn * (dfixi * xpn + dfiyi * ypn + dfizi * zpn);
-      double suadd = fdfie - fdfii;
-      A.su[inp] = A.su[inp] + suadd;
+      R dfixi = R(A.gpx[inp]) * fxp + R(A.gpx[ine]) * fxe;
+      R dfiyi = R(A.gpy[inp]) * fxp + R(A.gpy[ine]) * fxe;
+      R dfizi = R(A.gpz[inp]) * fxp + R(A.gpz[ine]) * fxe;
+      R dp = R(A.p[ine]) - R(A.p[inp]) - (dfixi * d2x + dfiyi * d2y + dfizi * d2z);
+      R dfixii = dfixi * d1x + arx / vole * dp;
+      R dfiyii = dfiyi * d1y + ary / vole * dp;
+      R dfizii = dfizi * d1z + arz / vole * dp;
+      R fdfie = game * (dfixii * arx + dfiyii * ary + dfizii * arz);
+      R fdfii = game * are / dpn * (dfixi * xpn + dfiyi * ypn + dfizi * zpn);
+      R suadd = fdfie - fdfii;
+      A.su[inp] = R(A.su[inp]) + suadd;
       A.bp[inp] = suadd;
-      double duxi = A.gux[inp] * fxp + A.gux[ine] * fxe;
-      double duyi = A.guy[inp] * fxp + A.guy[ine] * fxe;
-      double duzi = A.guz[inp] * fxp + A.guz[ine] * fxe;
-      double ui = A.u[inp] * fxp + A.u[ine] * fxe + duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi);
-      duxi = A.gvx[inp] * fxp + A.gvx[ine] * fxe;
-      duyi = A.gvy[inp] * fxp + A.gvy[ine] * fxe;
-      duzi = A.gvz[inp] * fxp + A.gvz[ine] * fxe;
-      double vi = A.v[inp] * fxp + A.v[ine] * fxe + duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi);
-      duxi = A.gwx[inp] * fxp + A.gwx[ine] * fxe;
-      duyi = A.gwy[inp] * fxp + A.gwy[ine] * fxe;
-      duzi = A.gwz[inp] * fxp + A.gwz[ine] * fxe;
-      double wi = A.w[inp] * fxp + A.w[ine] * fxe + duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi);
+      R duxi = R(A.gux[inp]) * fxp + R(A.gux[ine]) * fxe;
+      R duyi = R(A.guy[inp]) * fxp + R(A.guy[ine]) * fxe;
+      R duzi = R(A.guz[inp]) * fxp + R(A.guz[ine]) * fxe;
+      R ui = R(A.u[inp]) * fxp + R(A.u[ine]) * fxe + duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi);
+      duxi = R(A.gvx[inp]) * fxp + R(A.gvx[ine]) * fxe;
+      duyi = R(A.gvy[inp]) * fxp + R(A.gvy[ine]) * fxe;
+      duzi = R(A.gvz[inp]) * fxp + R(A.gvz[ine]) * fxe;
+      R vi = R(A.v[inp]) * fxp + R(A.v[ine]) * fxe + duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi);
+      duxi = R(A.gwx[inp]) * fxp + R(A.gwx[ine]) * fxe;
+      duyi = R(A.gwy[inp]) * fxp + R(A.gwy[ine]) * fxe;
+      duzi = R(A.gwz[inp]) * fxp + R(A.gwz[ine]) * fxe;
+      R wi = R(A.w[inp]) * fxp + R(A.w[ine]) * fxe + duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi);
       A.fcf[inp] = dene * (ui * arx + vi * ary + wi * arz);
     }
   }
@@ -511,7 +522,10 @@ int piso_assemble(int idew, int idns, int idtb, int arvx, int arvy, int arvz, in
             F[CAP_GRADW_X], F[CAP_GRADW_Y], F[CAP_GRADW_Z], F[CAP_GRADP_X], F[CAP_GRADP_Y], F[CAP_GRADP_Z],
             idew, idns, idtb, ipc};
   Box b{2, d.nimm, 2, d.njmm, 2, d.nkmm};
-  launch(k_piso_peq_faces, grid_for(b.count()), kThreads, c.st, d, b, A);
+  if (c.fp32(4))
+    launch(k_piso_peq_faces<float>, grid_for(b.count()), kThreads, c.st, d, b, A);
+  else
+    launch(k_piso_peq_faces<double>, grid_for(b.count()), kThreads, c.st, d, b, A);
   CAP_CHECK_LAUNCH();
   if (ipc > 0) {
     Box bi{3, d.nimm, 3, d.njmm, 3, d.nkmm};

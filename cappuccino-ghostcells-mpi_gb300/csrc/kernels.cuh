@@ -20,6 +20,7 @@ int dpcg(int fi, int ifi, cappgpu_solve_report* rep);
 int pcgsip_fast(int fi, int ifi, cappgpu_solve_report* rep);
 int pcgsip_mixed(int fi, int ifi, cappgpu_solve_report* rep);
 int sipsol_fast(int fi, int ifi, cappgpu_solve_report* rep);
+int sipsol_mixed(int fi, int ifi, cappgpu_solve_report* rep);
 int fast_profile_unit(int which, double* bytes);
 void fast_free();
 // learned initial guess (learned.cu)

@@ -706,6 +706,88 @@ int sipsol_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   return done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
 }
 
+// sipsol in the FP32 + FP64-refinement form (precision modes 1-2): each
+// sweep forms the residual su - A fi and its L1 norm in FP64 (sipsol.f90:
+// 60-69), runs the forward and backward SIP substitutions on it in FP32
+// with the FP32 factors (sipsol.f90:28-50, 70-92) and adds the correction
+// to fi in FP64; the exit test is the reference's (sipsol.f90:77, 96).  The
+// sweeps are iterative refinement with SIP as the inner solver; ghost
+// neighbours of the correction are zero.
+int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
+  Ctx& c = ctx();
+  cappgpu_params& P = c.prm;
+  int rc = fast_setup();
+  if (rc) return rc;
+  if ((rc = fast32_setup())) return rc;
+  CAP_CUDA(cudaMemsetAsync(F.flags, 0, sizeof(int) * 2, c.st));
+  const int cf[8] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_SU};
+  for (int q = 0; q < 8; ++q)
+    if ((rc = to_d(cf[q], D_AE + q))) return rc;
+  if ((rc = to_d(fif, D_FI))) return rc;
+  const DG& g = F.g;
+  for (int q = 0; q < 7; ++q)
+    launch(k_d_to_f, grid_for(g.size()), kThreads, c.st, g, (const double*)F.d[D_AE + q], G.e[E_AE + q]);
+  CAP_CHECK_LAUNCH();
+  {   // FP32 SIP factorisation
+    SipFactorF op;
+    for (int q = 0; q < 7; ++q) op.map[q] = G.map[E_AE + q];
+    op.bnn = c.f[CAP_BN];
+    op.ben = c.f[CAP_BE];
+    op.btn = c.f[CAP_BT];
+    op.fq = G.fq;
+    op.bq = G.bq;
+    op.alfa = (float)P.alfa;
+    if ((rc = run_wave<SipFactorF, false>(op))) return rc;
+  }
+  SipFwdF fwd;
+  fwd.map[0] = G.map[E_R];
+  fwd.map[1] = G.map_fq;
+  fwd.z = G.e[E_Z];
+  SipBwdF bwd;
+  bwd.map[0] = G.map[E_Z];
+  bwd.map[1] = G.map_bq;
+  bwd.z = G.e[E_Z];
+  const int ns = P.nsw[ifi - 1];
+  double res1 = 0.0, rsm = 0.0;
+  int n;
+  bool done = false;
+  for (n = 1; n <= ns; ++n) {
+    launch(k_resid_d, kRedBlocks, kThreads, c.st, g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
+           (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
+           (const double*)F.d[D_AP], (const double*)F.d[D_SU], (const double*)F.d[D_FI], (const double*)c.f[fif],
+           F.d[D_RES], c.partials);
+    launch(k_cg_scalars, 1, 32, c.st, 3, (const double*)c.partials, kRedBlocks, c.dscal);
+    launch(k_d_to_f, grid_for(g.size()), kThreads, c.st, g, (const double*)F.d[D_RES], G.e[E_R]);
+    CAP_CHECK_LAUNCH();
+    if ((rc = run_wave<SipFwdF, false>(fwd))) return rc;
+    if ((rc = run_wave<SipBwdF, true>(bwd))) return rc;
+    launch(k_add_f, grid_for(g.size()), kThreads, c.st, g, F.d[D_FI], (const float*)G.e[E_Z]);
+    CAP_CHECK_LAUNCH();
+    CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 6, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    CAP_CUDA(cudaStreamSynchronize(c.st));
+    if ((rc = check_wave_error())) return rc;
+    res1 = F.hres[0];
+    if (n == 1) P.resor[ifi - 1] = res1;
+    rsm = res1 / (P.resor[ifi - 1] + CAP_SMALL);
+    if (!isfinite(res1)) break;
+    if (rsm < P.sor[ifi - 1]) { done = true; break; }
+  }
+  if ((rc = from_d(D_FI, fif))) return rc;
+  if ((rc = from_d(D_RES, CAP_RES))) return rc;
+  if (rep) {
+    rep->res0 = P.resor[ifi - 1];
+    rep->resl = res1;
+    rep->iters = done ? n : ns;
+    rep->status = done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+  }
+  if (!isfinite(res1)) {
+    set_error("linear solver residual is not finite");
+    if (rep) rep->status = CAPPGPU_E_NONFINITE;
+    return CAPPGPU_E_NONFINITE;
+  }
+  return done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+}
+
 // pcgsip in the FP32 + FP64-refinement form (cappgpu_precision(1)).
 // Outer loop in FP64: r = su - A fi over the interior with the reference's
 // residual (pcg-sip.f90:150-165) and its exit test resl/res0 < sor(ifi)

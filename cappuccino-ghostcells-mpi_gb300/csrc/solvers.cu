@@ -180,7 +180,8 @@ static int finish_status(double resl, bool done, cappgpu_solve_report* rep) {
 // sipsol.f90:3-106
 int sipsol(int fif, int ifi, cappgpu_solve_report* rep) {
   Ctx& c = ctx();
-  if (c.wave_impl == 1 && c.d.nimm >= 4 && c.d.njmm >= 4 && c.d.nkmm >= 4) return sipsol_fast(fif, ifi, rep);
+  if (c.wave_impl == 1 && c.d.nimm >= 4 && c.d.njmm >= 4 && c.d.nkmm >= 4)
+    return c.fp32(2) ? sipsol_mixed(fif, ifi, rep) : sipsol_fast(fif, ifi, rep);
   const Dims& d = c.d;
   double** F = c.f;
   cappgpu_params& P = c.prm;
@@ -243,7 +244,7 @@ int resid_into(const double* fi, double* res, double* l1) {
 int pcgsip(int fif, int ifi, cappgpu_solve_report* rep) {
   Ctx& c = ctx();
   if (c.wave_impl == 1 && c.d.nimm >= 4 && c.d.njmm >= 4 && c.d.nkmm >= 4)
-    return c.precision >= 1 ? pcgsip_mixed(fif, ifi, rep) : pcgsip_fast(fif, ifi, rep);
+    return c.fp32(1) ? pcgsip_mixed(fif, ifi, rep) : pcgsip_fast(fif, ifi, rep);
   const Dims& d = c.d;
   double** F = c.f;
   cappgpu_params& P = c.prm;

@@ -177,6 +177,7 @@ int ghost_update() {
 // south face (from j-1), own east/north/top faces.  The gather below adds
 // the same rounded terms in the same order, so every element -- ghost and
 // padding cells included -- is bit-identical.
+template <typename R>
 __global__ void k_grad_gauss(Dims d, const double* __restrict__ u, const double* __restrict__ fx,
                              const double* __restrict__ fy, const double* __restrict__ fz,
                              const double* __restrict__ a1x, const double* __restrict__ a1y,
@@ -195,38 +196,38 @@ __global__ void k_grad_gauss(Dims d, const double* __restrict__ u, const double*
     auto inF = [&](int ii, int jj, int kk) {
       return kk >= 2 && kk <= d.nkm && ii >= 2 && ii <= d.nimm && jj >= 2 && jj <= d.njmm;
     };
-    double gx = 0.0, gy = 0.0, gz = 0.0;
+    R gx = R(0.0), gy = R(0.0), gz = R(0.0);
     if (inF(i, j, k - 1)) {  // bottom face: this cell is 'int' of inp = p - nij
       int q = p - d.nij;
-      double ut = u[p] * fz[q] + u[q] * (1.0 - fz[q]);
-      gx = gx - (ut * a3x[q]);
-      gy = gy - (ut * a3y[q]);
-      gz = gz - (ut * a3z[q]);
+      R ut = R(u[p]) * R(fz[q]) + R(u[q]) * (R(1.0) - R(fz[q]));
+      gx = gx - (ut * R(a3x[q]));
+      gy = gy - (ut * R(a3y[q]));
+      gz = gz - (ut * R(a3z[q]));
     }
     if (inF(i - 1, j, k)) {  // west face: this cell is 'ine' of inp = p - nj
       int q = p - d.nj;
-      double ue = u[p] * fx[q] + u[q] * (1.0 - fx[q]);
-      gx = gx - (ue * a1x[q]);
-      gy = gy - (ue * a1y[q]);
-      gz = gz - (ue * a1z[q]);
+      R ue = R(u[p]) * R(fx[q]) + R(u[q]) * (R(1.0) - R(fx[q]));
+      gx = gx - (ue * R(a1x[q]));
+      gy = gy - (ue * R(a1y[q]));
+      gz = gz - (ue * R(a1z[q]));
     }
     if (inF(i, j - 1, k)) {  // south face: this cell is 'inn' of inp = p - 1
       int q = p - 1;
-      double un = u[p] * fy[q] + u[q] * (1.0 - fy[q]);
-      gx = gx - (un * a2x[q]);
-      gy = gy - (un * a2y[q]);
-      gz = gz - (un * a2z[q]);
+      R un = R(u[p]) * R(fy[q]) + R(u[q]) * (R(1.0) - R(fy[q]));
+      gx = gx - (un * R(a2x[q]));
+      gy = gy - (un * R(a2y[q]));
+      gz = gz - (un * R(a2z[q]));
     }
     if (inF(i, j, k)) {  // own east, north, top faces
-      double ue = u[p + d.nj] * fx[p] + u[p] * (1.0 - fx[p]);
-      double un = u[p + 1] * fy[p] + u[p] * (1.0 - fy[p]);
-      double ut = u[p + d.nij] * fz[p] + u[p] * (1.0 - fz[p]);
-      gx = gx + (ue * a1x[p] + un * a2x[p] + ut * a3x[p]);
-      gy = gy + (ue * a1y[p] + un * a2y[p] + ut * a3y[p]);
-      gz = gz + (ue * a1z[p] + un * a2z[p] + ut * a3z[p]);
+      R ue = R(u[p + d.nj]) * R(fx[p]) + R(u[p]) * (R(1.0) - R(fx[p]));
+      R un = R(u[p + 1]) * R(fy[p]) + R(u[p]) * (R(1.0) - R(fy[p]));
+      R ut = R(u[p + d.nij]) * R(fz[p]) + R(u[p]) * (R(1.0) - R(fz[p]));
+      gx = gx + (ue * R(a1x[p]) + un * R(a2x[p]) + ut * R(a3x[p]));
+      gy = gy + (ue * R(a1y[p]) + un * R(a2y[p]) + ut * R(a3y[p]));
+      gz = gz + (ue * R(a1z[p]) + un * R(a2z[p]) + ut * R(a3z[p]));
     }
     if (k >= 2 && k <= d.nkm && i >= 3 && i <= d.nimm && j >= 3 && j <= d.njmm) {
-      double volr = 1.0 / vol[p];
+      R volr = R(1.0) / R(vol[p]);
       gx = gx * volr;
       gy = gy * volr;
       gz = gz * volr;
@@ -240,7 +241,11 @@ __global__ void k_grad_gauss(Dims d, const double* __restrict__ u, const double*
 int grad_gauss(int uf, int dxf, int dyf, int dzf) {
   Ctx& c = ctx();
   double** F = c.f;
-  launch(k_grad_gauss, grid_for(c.d.nijk), kThreads, c.st, 
+  // precision modes 1-2: velocity gradients (inputs of the coefficient
+  // assembly) in FP32 arithmetic; the pressure gradient of the velocity
+  // correction stays FP64
+  auto k = (c.fp32(8) && uf != CAP_P) ? k_grad_gauss<float> : k_grad_gauss<double>;
+  launch(k, grid_for(c.d.nijk), kThreads, c.st,
       c.d, F[uf], F[CAP_FX], F[CAP_FY], F[CAP_FZ], F[CAP_AR1X], F[CAP_AR1Y], F[CAP_AR1Z], F[CAP_AR2X],
       F[CAP_AR2Y], F[CAP_AR2Z], F[CAP_AR3X], F[CAP_AR3Y], F[CAP_AR3Z], F[CAP_VOL], F[dxf], F[dyf], F[dzf]);
   CAP_CHECK_LAUNCH();
@@ -397,7 +402,7 @@ int cappgpu_grad_gauss_h(const double* u, double* dudx, double* dudy, double* du
   double** F = c.f;
   double *du = c.work[4], *gx = c.work[5], *gy = c.work[6], *gz = c.work[7];
   CAP_CUDA(cudaMemcpyAsync(du, u, nb, cudaMemcpyHostToDevice, c.st));
-  cap::launch(k_grad_gauss, cap::grid_for(c.d.nijk), cap::kThreads, c.st, 
+  cap::launch(k_grad_gauss<double>, cap::grid_for(c.d.nijk), cap::kThreads, c.st,
       c.d, du, F[CAP_FX], F[CAP_FY], F[CAP_FZ], F[CAP_AR1X], F[CAP_AR1Y], F[CAP_AR1Z], F[CAP_AR2X],
       F[CAP_AR2Y], F[CAP_AR2Z], F[CAP_AR3X], F[CAP_AR3Y], F[CAP_AR3Z], F[CAP_VOL], gx, gy, gz);
   CAP_CHECK_LAUNCH();

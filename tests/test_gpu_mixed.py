@@ -68,6 +68,12 @@ def test_precision_rejects_unknown_mode(gpu_lib):
 
 def _channel_run(gpu_lib, case, mode, tight, steps=3):
     gpu_lib.load_case(case)
+    if tight:   # the momentum solves to 1e-9 too (sor 1e-3 and 20 sweeps otherwise)
+        pr = gpu_lib.get_params()
+        for q in range(3):
+            pr.sor[q] = 1e-9
+            pr.nsw[q] = 400
+        gpu_lib.set_params(pr)
     gpu_lib.set_option("tight_correctors", tight)
     gpu_lib.precision(mode)
     try:
@@ -84,10 +90,12 @@ def _rel(a, b):
 
 
 def test_mixed_piso_agrees_with_fp64_when_every_corrector_is_converged(gpu_lib):
-    # The reference stops the first corrector's p solve at sor = 0.1, and
-    # where it stops moves the step's result far above FP32 rounding.  With
-    # every corrector solved to the last one's tolerance (1e-6) the FP32 form
-    # must land on the FP64 result within that tolerance's reach.
+    # The reference stops the first corrector's p solve at sor = 0.1 and the
+    # momentum solves at 1e-3, and where they stop moves the step's result
+    # far above FP32 rounding.  With every corrector solved to the last one's
+    # tolerance (1e-6) and the momentum solves to 1e-9, the FP32 form (FP32
+    # assembly, SIP factors and sweeps) must land on the FP64 result within
+    # that tolerance's reach.
     case = cappgpu.cases.channel(N=(24, 20, 28))
     ref = _channel_run(gpu_lib, case, 0, 0)
     t64 = _channel_run(gpu_lib, case, 0, 1)
@@ -98,3 +106,29 @@ def test_mixed_piso_agrees_with_fp64_when_every_corrector_is_converged(gpu_lib):
     for k in ("u", "v", "w"):
         assert err[k] < 1e-5, (k, err[k])
     assert err["p"] < 1e-4
+
+
+@pytest.mark.parametrize("dims,sor", [((14, 13, 12), 1e-6), ((40, 37, 35), 1e-4)])
+def test_mixed_sipsol_meets_fp64_exit_test(gpu_lib, oracle_mod, dims, sor):
+    """sipsol in precision mode 1: FP64 residual and exit test, FP32 SIP
+    factorisation and substitutions."""
+    st = _state(oracle_mod, dims, 4, sor)
+    # the reference's forward recurrence reads the ghost layers of res; start
+    # both forms from a clean res so that the FP64 form converges too
+    st.set_field("res", np.zeros_like(st.field("res")))
+    push(gpu_lib, st)
+    gpu_lib.precision(0)
+    r64 = gpu_lib.sipsol("p", IP)
+    p64 = gpu_lib.get_field("p")
+    push(gpu_lib, st)
+    gpu_lib.precision(1)
+    try:
+        r32 = gpu_lib.sipsol("p", IP)
+    finally:
+        gpu_lib.precision(0)
+    p32 = gpu_lib.get_field("p")
+    assert r32.status == 0 and r64.status == 0
+    assert r32.res0 == pytest.approx(r64.res0, rel=1e-12)   # the first sweep's FP64 residual
+    assert r32.resl / r32.res0 < sor
+    assert abs(r32.iters - r64.iters) <= max(2, r64.iters // 10)
+    assert np.linalg.norm(p32 - p64) <= 1e3 * sor * np.linalg.norm(p64)
