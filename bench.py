@@ -459,6 +459,34 @@ def run_gpu(args, ws, rank, local):
         print(json.dumps(out), flush=True)
 
 
+def run_profile(args):
+    """Small fixed workloads for ncu captures (no bench line): one PISO step
+    of the channel in FP64 or in the FP32 form after one warm-up step, or
+    the learned guess's net (one forward pass on the grid, one training pass
+    on a 64^3 window of a recorded pair)."""
+    import cappgpu
+    lib = cappgpu.Library()
+    lib.load_case(make_case(args.n))
+    out = {"profile": args.profile, "size": args.n}
+    if args.profile in ("step64", "step32"):
+        lib.precision(0 if args.profile == "step64" else 1)
+        lib.piso_steps(1)
+        lib.timer_start()
+        lib.piso_steps(1)
+        out["ms"] = lib.timer_stop()
+    else:
+        lib.precision(1)
+        lib.learn_reset(2, seed=1)
+        lib.learn_collect(True)
+        lib.piso_steps(1)
+        lib.learn_collect(False)
+        for w, name in ((9, "inference"), (10, "train_pass")):
+            m, fl = lib.profile_kernel(w, reps=1)
+            out[name] = {"ms": m, "tflops": fl / (m / 1e3) / 1e12}
+    lib.finalize()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -467,7 +495,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", dest="n", type=int, default=N_DEFAULT, help="interior cells per axis")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", choices=["step64", "step32", "net"],
+                    help="run a small fixed workload for an ncu capture instead of the bench")
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     ws, rank, local = dist_env()
     if ws > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)

@@ -45,10 +45,39 @@ module cappgpu
     integer(c_int) function cappgpu_finalize() bind(c, name="cappgpu_finalize")
       import :: c_int
     end function
-    ! 0 = FP64 plain (the reference's arithmetic), 1 = FP32 + FP64 refinement
+    ! 0 = FP64 plain (the reference's arithmetic), 1 = FP32 + FP64 refinement,
+    ! 2 = 1 + the learned initial guess of the pressure solve
     integer(c_int) function cappgpu_precision(mode) bind(c, name="cappgpu_precision")
       import :: c_int
       integer(c_int), value :: mode
+    end function
+    ! key: NUL-terminated, e.g. "fp32_parts"//c_null_char
+    integer(c_int) function cappgpu_set_option(key, val) bind(c, name="cappgpu_set_option")
+      import :: c_int, c_char
+      character(kind=c_char), intent(in) :: key(*)
+      integer(c_int), value :: val
+    end function
+    ! learned initial guess: record pairs, train, report
+    integer(c_int) function cappgpu_learn_reset(max_samples, seed) bind(c, name="cappgpu_learn_reset")
+      import :: c_int, c_long_long
+      integer(c_int), value :: max_samples
+      integer(c_long_long), value :: seed
+    end function
+    integer(c_int) function cappgpu_learn_collect(on) bind(c, name="cappgpu_learn_collect")
+      import :: c_int
+      integer(c_int), value :: on
+    end function
+    integer(c_int) function cappgpu_learn_train(epochs, block, lr, loss) bind(c, name="cappgpu_learn_train")
+      import :: c_int, c_double
+      integer(c_int), value :: epochs, block
+      real(c_double), value :: lr
+      real(c_double), intent(out) :: loss
+    end function
+    integer(c_int) function cappgpu_learn_stats(samples, guesses, fallbacks, last_ratio) &
+        bind(c, name="cappgpu_learn_stats")
+      import :: c_int, c_double
+      integer(c_int), intent(out) :: samples, guesses, fallbacks
+      real(c_double), intent(out) :: last_ratio
     end function
     integer(c_int) function cappgpu_set_field(field, host, n) bind(c, name="cappgpu_set_field")
       import :: c_int, c_double, c_int64_t

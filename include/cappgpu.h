@@ -196,17 +196,29 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    PISO_multiple_correction.f90:131-135), 1 = every corrector solves to the
    last one's tolerance.  Where the first corrector stops decides the step's
    result to well above the arithmetic's precision, so two precision modes
-   are compared with 1; it is not the reference's algorithm. */
+   are compared with 1; it is not the reference's algorithm.
+   "fp32_parts": bitmask of the parts that run in FP32 in precision modes
+   1-2 (default 15): 1 the pressure solve (pcgsip), 2 the momentum solves
+   (sipsol), 4 the coefficient assembly (fluxuvw, PISO pressure assembly),
+   8 the velocity gradients (grad_gauss of u, v, w).
+   "learn_conv": convolutions of the learned guess's net, 1 = tcgen05
+   (default), 0 = mma.sync (kept for cross-checks). */
 int cappgpu_set_option(const char* key, int value);
 
-/* Precision of the pressure solve (cappgpu_pcgsip and the PISO correctors
-   that call it).  0 = FP64 plain, the reference's arithmetic (default).
-   1 = the SIP factors and both substitutions in FP32 inside conjugate
-   gradients in FP32, wrapped in FP64 iterative refinement: the exit test is
-   the reference's (L1 norm of the FP64 residual su - A fi over res0 below
-   sor(ifi)), the iterates are not the reference's.  Replaces the
-   reference's fixed FP64 arithmetic (pcg-sip.f90:3-200); returns
-   CAPPGPU_E_ARG for other modes. */
+/* Arithmetic of the step.  0 = FP64 plain, the reference's arithmetic
+   (default).  1 = FP32 inside FP64 iterative refinement:
+   - pcgsip: the SIP factors and both substitutions in FP32 inside conjugate
+     gradients in FP32, wrapped in an FP64 refinement loop whose exit test
+     is the reference's (L1 norm of the FP64 residual su - A fi over res0
+     below sor(ifi), pcg-sip.f90:283-289);
+   - sipsol: FP64 residual and exit test per sweep (sipsol.f90:60-69, 96),
+     FP32 factors and substitutions, FP64 update of fi;
+   - coefficient assembly (fluxuvw, PISO pressure assembly) and the velocity
+     gradients in FP32 arithmetic with FP64 storage;
+   residuals, norms, dot products, the flux and velocity corrections, the
+   pressure gradient and the continuity error stay FP64.  The iterates are
+   not the reference's.  2 = mode 1 with the learned initial guess of the
+   pressure solve (below).  Returns CAPPGPU_E_ARG for other modes. */
 int cappgpu_precision(int mode);
 
 /* ================================================ learned initial guess */
