@@ -272,7 +272,7 @@ int cappgpu_set_option(const char* key, int value) {
     ctx().fp32_parts = value;
     return CAPPGPU_OK;
   }
-  if (strcmp(key, "learn_conv") == 0 && (value == 0 || value == 1)) return learned_set_conv(value);
+  if (strcmp(key, "learn_conv") == 0 && value >= 0 && value <= 2) return learned_set_conv(value);
   if (strcmp(key, "tight_correctors") == 0 && (value == 0 || value == 1)) {
     ctx().tight_correctors = value;
     return CAPPGPU_OK;

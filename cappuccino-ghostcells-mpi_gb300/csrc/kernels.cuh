@@ -34,6 +34,8 @@ int learned_set_conv(int impl);
 int resid_into(const double* fi, double* res, double* l1);
 // z = A p over the interior (p's ghost values included) and (r.z, z.z)
 int spmv_dot2_natural(const double* p, double* z, const double* r, double* out2);
+// (a1.b1, a2.b2) over the interior (natural layout)
+int dot2_natural(const double* a1, const double* b1, const double* a2, const double* b2, double* out2);
 
 // assembly
 int fluxuvw(int idew, int idns, int idtb, int arvx, int arvy, int arvz, int fif, int acfe, int acfw, int fcf);

@@ -7,8 +7,9 @@
 // (r^ = r0/rms, A^ = A/mean(ap)); the net's output d^ is trained to make
 // A^ d^ = r^ on the residual-norm loss |A^ d^ - r^|^2 / |r^|^2, with A^ the
 // 7-point operator of the recorded solve restricted to the training window.
-// At solve time the amplitude of the guess is fitted by least squares,
-// alpha = (r0.Ad)/(Ad.Ad), which costs one product with A.  The plain solve
+// At solve time the amplitude and the level of the guess, fi + alpha d +
+// beta over the interior, come from a Galerkin projection onto span{d, 1}
+// (two products with A): the energy-norm error of CG's start cannot grow.  The plain solve
 // always continues from the guess to the same tolerance -- the exit test
 // stays relative to the residual of the solve's own start -- so the solver
 // is both judge and fallback: a guess that does not lower the FP64 residual
@@ -99,7 +100,7 @@ struct Net {
   float* store = nullptr;
   // statistics of the guesses
   int guesses = 0, fallbacks = 0;
-  double last_ratio = 0.0;
+  double last_ratio = 0.0, last_alpha = 0.0, last_beta = 0.0;
   unsigned long long seed = 0;
 };
 
@@ -593,6 +594,15 @@ __global__ void k_shape_nat(Dims d, double* __restrict__ z, const float* __restr
   }
 }
 
+// 1 on the interior of a natural field (the rest left as it is)
+__global__ void k_ones_nat(Dims d, double* __restrict__ z, int Ni, int Nj, int Nk) {
+  const int Vi = Ni * Nj * Nk;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < Vi; v += gridDim.x * blockDim.x) {
+    const int x = v % Nj, y = (v / Nj) % Ni, zz = v / (Nj * Ni);
+    z[nat_of(d, x, y, zz)] = 1.0;
+  }
+}
+
 __global__ void k_axpy_nat(int n, double alpha, const double* __restrict__ x, double* __restrict__ y) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) y[q] = y[q] + alpha * x[q];
 }
@@ -710,7 +720,8 @@ int conv_ci(const bf16* x, int ldx, const bf16* w, int CO, const float* bias, co
   return CAPPGPU_OK;
 }
 
-// the convolution kernels: 1 = tcgen05 (default), 0 = mma.sync
+// the convolution kernels: 1 = tcgen05, halo tiles where they fit (default),
+// 2 = tcgen05 per-tap gathers only, 0 = mma.sync
 int g_conv_impl = 1;
 
 template <int CI, int CO, bool MASK>
@@ -732,13 +743,41 @@ int conv_tc(const bf16* x, int ldx, const bf16* w, const float* bias, const bf16
   return CAPPGPU_OK;
 }
 
-// the tensor-core form for the net's (CI, CO) pairs; -1 if there is none
+template <int CI, int CO, bool MASK>
+int conv_halo(const bf16* x, int ldx, const bf16* w, const float* bias, const bf16* mask, int ldm, bf16* y, int ldy,
+              int D, int H, int W, int relu) {
+  typedef tc::HaloTC<CI, CO> T;
+  CAP_CUDA(cudaFuncSetAttribute(tc::k_conv3_halo<CI, CO, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                T::kSmem));
+  const int ntiles = ((W + 7) / 8) * ((H + 15) / 16) * D;
+  int per_sm = (228 * 1024) / (T::kSmem + 1024);
+  if (per_sm > 512 / T::kCols) per_sm = 512 / T::kCols;
+  if (per_sm > 16) per_sm = 16;
+  if (per_sm < 1) per_sm = 1;
+  int grid = 152 * per_sm;
+  if (grid > ntiles) grid = ntiles;
+  ++ctx().launches;
+  tc::k_conv3_halo<CI, CO, MASK><<<grid, 128, T::kSmem, ctx().st>>>(x, ldx, w, bias, mask, ldm, y, ldy, D, H, W,
+                                                                     relu, N.err);
+  return CAPPGPU_OK;
+}
+
+// the tensor-core form for the net's (CI, CO) pairs: the halo-tile kernel
+// where all 27 taps' weights fit in shared memory beside the halo (unless
+// impl 2 asks for the per-tap kernel), else the per-tap kernel (d2a 96->32
+// and e3b 64->64: two half-width halo launches of one CTA per SM each were
+// slower); -1 if there is none
 int conv_tc_any(int CI, const bf16* x, int ldx, const bf16* w, int CO, const float* bias, const bf16* mask, int ldm,
                 bf16* y, int ldy, int D, int H, int W, int relu) {
+  const bool halo = g_conv_impl == 1;
 #define CAP_TC(ci, co)                                                                                  \
-  if (CI == ci && CO == co)                                                                             \
+  if (CI == ci && CO == co) {                                                                           \
+    if (tc::HaloTC<ci, co>::kFits && halo)                                                              \
+      return mask ? conv_halo<ci, co, true>(x, ldx, w, bias, mask, ldm, y, ldy, D, H, W, relu)          \
+                  : conv_halo<ci, co, false>(x, ldx, w, bias, mask, ldm, y, ldy, D, H, W, relu);        \
     return mask ? conv_tc<ci, co, true>(x, ldx, w, bias, mask, ldm, y, ldy, D, H, W, relu)              \
-                : conv_tc<ci, co, false>(x, ldx, w, bias, mask, ldm, y, ldy, D, H, W, relu);
+                : conv_tc<ci, co, false>(x, ldx, w, bias, mask, ldm, y, ldy, D, H, W, relu);            \
+  }
   CAP_TC(16, 16) CAP_TC(16, 32) CAP_TC(32, 32) CAP_TC(32, 64) CAP_TC(64, 64) CAP_TC(96, 32) CAP_TC(48, 16)
   CAP_TC(32, 16) CAP_TC(64, 32) CAP_TC(32, 96) CAP_TC(16, 48)
 #undef CAP_TC
@@ -749,7 +788,7 @@ int conv_tc_any(int CI, const bf16* x, int ldx, const bf16* w, int CO, const flo
 // (mask = the layer's output, w = flipped transposed weights)
 int conv(int CI, const bf16* x, int ldx, const bf16* w, int CO, const float* bias, const bf16* mask, int ldm, bf16* y,
          int ldy, int D, int H, int W, int relu) {
-  if (g_conv_impl == 1) {
+  if (g_conv_impl >= 1) {
     const int rc = conv_tc_any(CI, x, ldx, w, CO, bias, mask, ldm, y, ldy, D, H, W, relu);
     if (rc >= 0) return rc;
   }
@@ -910,7 +949,7 @@ double bwd_flops_per_voxel() {
 void learned_free() { net_free(); }
 
 int learned_set_conv(int impl) {
-  if (impl != 0 && impl != 1) return CAPPGPU_E_ARG;
+  if (impl < 0 || impl > 2) return CAPPGPU_E_ARG;
   g_conv_impl = impl;
   return CAPPGPU_OK;
 }
@@ -988,23 +1027,48 @@ int learned_solve_start(int fif, double res0) {
   CAP_CHECK_LAUNCH();
   if ((rc = forward(D, H, W))) return rc;
   if ((rc = check_err())) return rc;
-  // amplitude by least squares: alpha = (r0.Ad)/(Ad.Ad)
+  // amplitude and level of the guess, fi + alpha d + beta (beta on the
+  // interior), by Galerkin projection onto span{d, 1}: the pair that
+  // minimises the error in the energy norm of A, the norm CG minimises, so
+  // the guess cannot start CG from a larger energy error (a residual
+  // least-squares fit can: it weights the high frequencies, and on a
+  // Neumann system pinned at one cell it left smooth error that cost CG
+  // 2.4x the iterations of the plain solve).  A is symmetric apart from the
+  // pinned row.
   double* shape = c.work[4];
   double* ashape = c.work[5];
+  double* one = c.work[6];
+  double* aone = c.work[7];
   double* cand = c.work[2];
   double* rcand = c.work[3];
   CAP_CUDA(cudaMemsetAsync(shape, 0, sizeof(double) * d.nijk, c.st));
+  CAP_CUDA(cudaMemsetAsync(one, 0, sizeof(double) * d.nijk, c.st));
   launch(k_shape_nat, grid_for(Vi), kThreads, c.st, d, shape, (const float*)N.A.out, Ni, Nj, Nk, H, W);
+  launch(k_ones_nat, grid_for(Vi), kThreads, c.st, d, one, Ni, Nj, Nk);
   CAP_CHECK_LAUNCH();
-  double dots[2] = {0.0, 0.0};
-  if ((rc = spmv_dot2_natural(shape, ashape, c.f[CAP_RES], dots))) return rc;
-  if (!(dots[1] > 0.0) || !isfinite(dots[0] / dots[1])) {
+  double t[2], g1[2], g2[2], rr[2];
+  if ((rc = spmv_dot2_natural(shape, ashape, c.f[CAP_RES], t))) return rc;   // Ad
+  if ((rc = spmv_dot2_natural(one, aone, c.f[CAP_RES], t))) return rc;       // A1
+  if ((rc = dot2_natural(shape, ashape, shape, aone, g1))) return rc;         // d.Ad, d.A1
+  if ((rc = dot2_natural(one, ashape, one, aone, g2))) return rc;             // 1.Ad, 1.A1
+  if ((rc = dot2_natural(shape, c.f[CAP_RES], one, c.f[CAP_RES], rr))) return rc;   // d.r0, 1.r0
+  double alpha = 0.0, beta = 0.0;
+  const double det = g1[0] * g2[1] - g1[1] * g2[0];
+  if (g2[1] > 0.0 && fabs(det) > 1e-12 * fabs(g1[0] * g2[1])) {
+    alpha = (rr[0] * g2[1] - g1[1] * rr[1]) / det;
+    beta = (g1[0] * rr[1] - g2[0] * rr[0]) / det;
+  } else if (g1[0] > 0.0) {
+    alpha = rr[0] / g1[0];
+  }
+  N.last_alpha = alpha;
+  N.last_beta = beta;
+  if (!isfinite(alpha) || !isfinite(beta) || (alpha == 0.0 && beta == 0.0)) {
     ++N.fallbacks;
     return CAPPGPU_OK;
   }
-  const double alpha = dots[0] / dots[1];
   CAP_CUDA(cudaMemcpyAsync(cand, c.f[fif], sizeof(double) * d.nijk, cudaMemcpyDeviceToDevice, c.st));
   launch(k_axpy_nat, grid_for(d.nijk), kThreads, c.st, d.nijk, alpha, (const double*)shape, cand);
+  launch(k_axpy_nat, grid_for(d.nijk), kThreads, c.st, d.nijk, beta, (const double*)one, cand);
   CAP_CHECK_LAUNCH();
   double res1 = 0.0;
   if ((rc = resid_into(cand, rcand, &res1))) return rc;
@@ -1134,6 +1198,13 @@ int cappgpu_learn_stats(int* samples, int* guesses, int* fallbacks, double* last
   if (guesses) *guesses = N.guesses;
   if (fallbacks) *fallbacks = N.fallbacks;
   if (last_ratio) *last_ratio = N.last_ratio;
+  return CAPPGPU_OK;
+}
+
+int cappgpu_learn_fit(double* alpha, double* beta) {
+  CAP_REQUIRE_INIT();
+  if (alpha) *alpha = N.last_alpha;
+  if (beta) *beta = N.last_beta;
   return CAPPGPU_OK;
 }
 

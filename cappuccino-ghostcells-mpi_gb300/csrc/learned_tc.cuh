@@ -272,3 +272,144 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const bf16* __restrict__ x, in
 
 }  // namespace tc
 }  // namespace cap
+
+namespace cap {
+namespace tc {
+
+// Halo-tile form.  An output tile is 8 (x) x 16 (y) voxels of one z-plane
+// (M = 128 rows, row r = (x = r % 8, y = r / 8)).  The CTA stages the tile's
+// input halo, 10 x 18 x 3 voxels, once: each 8-channel group is a plane of
+// 540 rows of 16 bytes, row (hz*18 + hy)*10 + hx.  For tap (dz, dy, dx) the
+// A operand is that plane read from row ((1+dz)*18 + 1+dy)*10 + 1+dx on:
+// 8 consecutive rows (x) form a core matrix, row groups (y) are 10 rows =
+// 160 B apart (stride-dimension offset) and the two 8-channel halves of a
+// 16-channel K step are one plane apart (leading-dimension offset), so a tap
+// costs only a descriptor.  All 27 taps' weights stay in shared memory for
+// the CTA's life.  One elected thread issues the tile's 27 x CI/16 MMAs.
+template <int CI, int CO>
+struct HaloTC {
+  static constexpr int HX = 10, HY = 18, HZ = 3, HV = HX * HY * HZ;
+  static constexpr int NC = CI / 8;                      // 8-channel groups
+  static constexpr int kPlane = HV * 16;                 // bytes of one group's plane
+  static constexpr int kA = (NC * kPlane + 1023) & ~1023;
+  static constexpr int kB = (27 * CO * CI * 2 + 1023) & ~1023;
+  static constexpr int kSboB = CI / 8 * 128;
+  static constexpr int kCols = pow2_cols(CO);
+  static constexpr int kSmemUse = kA + kB + 1024 + 64;
+  static constexpr int kSmemTmem = kCols * (228 * 1024 / 512);
+  static constexpr int kSmem = kSmemUse > kSmemTmem ? kSmemUse : kSmemTmem;
+  static constexpr bool kFits = kSmem <= 220 * 1024;
+  static_assert(CI % 16 == 0 && CO % 16 == 0 && CO <= 256, "tile shape");
+};
+
+template <int CI, int CO, bool MASK>
+__global__ void __launch_bounds__(128) k_conv3_halo(const bf16* __restrict__ x, int ldx, const bf16* __restrict__ w,
+                                                    const float* __restrict__ bias, const bf16* __restrict__ mask,
+                                                    int ldm, bf16* __restrict__ y, int ldy, int D, int H, int W,
+                                                    int relu, int* err) {
+  typedef HaloTC<CI, CO> T;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((unsigned long long)smem_raw + 1023) & ~1023ull);
+  unsigned char* A = smem;
+  unsigned char* B = smem + T::kA;
+  unsigned long long* bar = (unsigned long long*)(B + T::kB);
+  unsigned* tslot = (unsigned*)(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_fence_init();
+  }
+  if (warp == 0) tmem_alloc(tslot, T::kCols);
+  // the weights of all taps, K-major per tap
+  for (int q = tid; q < 27 * CO * T::NC; q += 128) {
+    const int tap = q / (CO * T::NC), r = q - tap * (CO * T::NC);
+    const int co = r / T::NC, kc = r - co * T::NC;
+    const uint4 u = *reinterpret_cast<const uint4*>(w + ((size_t)co * 27 + tap) * CI + kc * 8);
+    *reinterpret_cast<uint4*>(B + tap * (CO * CI * 2) + (co >> 3) * T::kSboB + kc * 128 + (co & 7) * 16) = u;
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = *tslot;
+  constexpr unsigned idesc = idesc_bf16(128, CO);
+  const int ntx = (W + 7) / 8, nty = (H + 15) / 16;
+  const int ntiles = ntx * nty * D;
+  unsigned phase = 0u;
+  bool bad = false;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int tx = tile % ntx, ty = (tile / ntx) % nty, z0 = tile / (ntx * nty);
+    const int x0 = tx * 8, y0 = ty * 16;
+    // input halo, zero outside the grid
+    for (int q = tid; q < T::HV * T::NC; q += 128) {
+      const int hv = q / T::NC, kc = q - hv * T::NC;
+      const int hx = hv % T::HX, hy = (hv / T::HX) % T::HY, hz = hv / (T::HX * T::HY);
+      const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
+      uint4 u = make_uint4(0u, 0u, 0u, 0u);
+      if ((unsigned)gx < (unsigned)W && (unsigned)gy < (unsigned)H && (unsigned)gz < (unsigned)D) {
+        const long long n = ((long long)gz * H + gy) * W + gx;
+        u = *reinterpret_cast<const uint4*>(x + n * ldx + kc * 8);
+        if (MASK) u = mask8(u, *reinterpret_cast<const uint4*>(mask + n * ldm + kc * 8));
+      }
+      *reinterpret_cast<uint4*>(A + kc * T::kPlane + hv * 16) = u;
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const unsigned a0 = smem_u32(A), b0 = smem_u32(B);
+      for (int tap = 0; tap < 27; ++tap) {
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+        const unsigned row = (unsigned)(((1 + dz) * T::HY + 1 + dy) * T::HX + 1 + dx);
+#pragma unroll
+        for (int ks = 0; ks < CI / 16; ++ks)
+          mma_bf16(tmem, smem_desc(a0 + 2 * ks * T::kPlane + row * 16, T::kPlane, T::HX * 16),
+                   smem_desc(b0 + tap * (CO * CI * 2) + ks * 256, 128, T::kSboB), idesc, (tap | ks) != 0);
+      }
+      mma_commit(&bar[0]);
+    }
+    if (!bad && !mbar_wait_bounded(&bar[0], phase)) bad = true;
+    phase ^= 1u;
+    tc_fence_after();
+    const int ox = x0 + (tid & 7), oy = y0 + (tid >> 3);
+    const bool valid = ox < W && oy < H;
+    const long long v = ((long long)z0 * H + oy) * W + ox;
+    const unsigned trow = tmem + ((unsigned)(warp * 32) << 16);
+#pragma unroll
+    for (int c0 = 0; c0 < CO; c0 += 16) {
+      float acc[16];
+      tmem_ld16(trow + c0, acc);
+      tmem_wait_ld();
+      if (valid) {
+        unsigned pk[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          float a = acc[2 * q], b = acc[2 * q + 1];
+          if (bias) {
+            a += bias[c0 + 2 * q];
+            b += bias[c0 + 2 * q + 1];
+          }
+          if (relu) {
+            a = fmaxf(a, 0.f);
+            b = fmaxf(b, 0.f);
+          }
+          const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+          pk[q] = *reinterpret_cast<const unsigned*>(&h);
+        }
+        uint4* dst = reinterpret_cast<uint4*>(y + v * ldy + c0);
+        dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+      }
+    }
+    tc_fence_before();
+    if (__syncthreads_or(bad)) break;
+  }
+  if (bad && tid == 0) atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, T::kCols);
+}
+
+}  // namespace tc
+}  // namespace cap

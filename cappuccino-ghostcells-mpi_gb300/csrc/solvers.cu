@@ -232,6 +232,15 @@ int spmv_dot2_natural(const double* p, double* z, const double* r, double* out2)
   return reduce_fetch(2, out2);
 }
 
+int dot2_natural(const double* a1, const double* b1, const double* a2, const double* b2, double* out2) {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  Box b{3, d.nimm, 3, d.njmm, 3, d.nkmm};
+  launch(k_dot, kRedBlocks, kThreads, c.st, d, b, a1, b1, a2, b2, c.partials);
+  CAP_CHECK_LAUNCH();
+  return reduce_fetch(2, out2);
+}
+
 int resid_into(const double* fi, double* res, double* l1) {
   Ctx& c = ctx();
   const Dims& d = c.d;

@@ -64,6 +64,7 @@ SIGNATURES = {
     "cappgpu_learn_train": [_INT, _INT, ctypes.c_double, _DP],
     "cappgpu_learn_params": [ctypes.POINTER(ctypes.c_float), _INT, _INT],
     "cappgpu_learn_stats": [ctypes.POINTER(_INT), ctypes.POINTER(_INT), ctypes.POINTER(_INT), _DP],
+    "cappgpu_learn_fit": [_DP, _DP],
     "cappgpu_learn_check": [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _INT, _INT, _INT,
                             ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _DP],
     "cappgpu_fluxuvw": [_INT] * 10,
@@ -281,7 +282,10 @@ class Library:
         s, g, f, r = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
         self._check(self.lib.cappgpu_learn_stats(ctypes.byref(s), ctypes.byref(g), ctypes.byref(f), ctypes.byref(r)),
                     "learn_stats")
-        return {"samples": s.value, "guesses": g.value, "fallbacks": f.value, "last_ratio": r.value}
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.cappgpu_learn_fit(ctypes.byref(a), ctypes.byref(b)), "learn_fit")
+        return {"samples": s.value, "guesses": g.value, "fallbacks": f.value, "last_ratio": r.value,
+                "last_alpha": a.value, "last_beta": b.value}
 
     def learn_check(self, rhs, coef):
         """One forward + backward pass of the residual-norm loss on a (D, H, W)

@@ -258,6 +258,9 @@ int cappgpu_learn_collect(int on);
 int cappgpu_learn_train(int epochs, int block, double lr, double* loss);
 int cappgpu_learn_params(float* host, int n, int direction);
 int cappgpu_learn_stats(int* samples, int* guesses, int* fallbacks, double* last_ratio);
+/* Amplitude alpha and level beta of the last guess (fi + alpha d + beta on
+   the interior, Galerkin projection onto span{d, 1}). */
+int cappgpu_learn_fit(double* alpha, double* beta);
 int cappgpu_learn_check(const float* rhs, const float* coef, int D, int H, int W, float* output, float* grad,
                         double* loss);
 

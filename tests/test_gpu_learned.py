@@ -28,11 +28,14 @@ def _check(gpu_lib, impl, rhs, coef):
         gpu_lib.set_option("learn_conv", 0)
 
 
-@pytest.mark.parametrize("dims", [(8, 12, 16), (16, 16, 20), (4, 12, 20)])
-def test_tensor_core_convolutions_match_mma_sync(gpu_lib, dims):
-    """tcgen05 implicit GEMMs (forward and input gradient) against the
-    mma.sync kernels on the same weights and data; the extents include a
-    voxel count that is not a multiple of the 128-voxel tile."""
+@pytest.mark.parametrize("impl", [1, 2])
+@pytest.mark.parametrize("dims", [(8, 12, 16), (16, 16, 20), (4, 12, 20), (8, 36, 20)])
+def test_tensor_core_convolutions_match_mma_sync(gpu_lib, dims, impl):
+    """tcgen05 implicit GEMMs (forward and input gradient; impl 1 halo tiles
+    where the weights fit, impl 2 per-tap gathers) against the mma.sync
+    kernels on the same weights and data; the extents include voxel counts
+    that are not multiples of the 128-voxel tile and x/y extents that are
+    not multiples of the 8 x 16 halo tile."""
     import learned_oracle as lo
     gpu_lib.init(12, 12, 12)
     gpu_lib.learn_reset(0, seed=7)
@@ -40,7 +43,7 @@ def test_tensor_core_convolutions_match_mma_sync(gpu_lib, dims):
     rhs = rng.standard_normal(dims).astype(np.float32)
     coef = _window_operator(rng, dims)
     out0, grad0, loss0 = _check(gpu_lib, 0, rhs, coef)
-    out1, grad1, loss1 = _check(gpu_lib, 1, rhs, coef)
+    out1, grad1, loss1 = _check(gpu_lib, impl, rhs, coef)
     assert np.all(np.isfinite(out1)) and np.all(np.isfinite(grad1))
     assert _rel(out1, out0) < 1e-2
     assert abs(loss1 - loss0) <= 1e-2 * loss0
@@ -48,7 +51,7 @@ def test_tensor_core_convolutions_match_mma_sync(gpu_lib, dims):
         assert _rel(grad1[sl], grad0[sl]) < 5e-2, name
 
 
-@pytest.mark.parametrize("impl", [0, 1])
+@pytest.mark.parametrize("impl", [0, 1, 2])
 @pytest.mark.parametrize("dims", [(8, 12, 16), (16, 16, 20)])
 def test_forward_and_gradients_match_cpu_oracle(gpu_lib, dims, impl):
     pytest.importorskip("torch")
