@@ -77,6 +77,7 @@ struct Ctx {
   cudaEvent_t ev[4] = {};
   int wave_impl = 1;                   // 1 persistent wavefront, 0 one launch per hyperplane
   int tight_correctors = 0;            // 1: every PISO corrector solves p to reltol, not only the last
+  int cg_batch = 4;                    // CG iterations launched between two host reads of the exit test
   int inner_drop = 4;                  // FP32 inner CG stops at 10^-inner_drop of the outer residual
   int fp32_parts = 15;                 // parts in FP32 in precision modes 1-2: 1 p solve, 2 sipsol,
                                        // 4 coefficient assembly, 8 velocity gradients

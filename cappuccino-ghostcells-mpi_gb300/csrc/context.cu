@@ -264,6 +264,10 @@ int cappgpu_set_option(const char* key, int value) {
   CAP_REQUIRE_INIT();
   if (!key) return CAPPGPU_E_ARG;
   if (strcmp(key, "wave") == 0 && (value == 0 || value == 1)) { ctx().wave_impl = value; return CAPPGPU_OK; }
+  if (strcmp(key, "cg_batch") == 0 && value >= 1 && value <= 64) {
+    ctx().cg_batch = value;
+    return CAPPGPU_OK;
+  }
   if (strcmp(key, "inner_drop") == 0 && value >= 1 && value <= 9) {
     ctx().inner_drop = value;
     return CAPPGPU_OK;

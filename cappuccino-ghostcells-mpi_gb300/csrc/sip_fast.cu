@@ -24,7 +24,6 @@ namespace cap {
 namespace {
 
 constexpr int BA = 16, BC = 8;   // lines per wavefront block (a x c)
-constexpr int kBatch = 4;        // CG iterations launched between two host reads of the exit test
 
 enum DBuf { D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_SU, D_RES, D_FI, D_Z, D_ZZ, D_PK0, D_PK1, D_NBUF };
 
@@ -46,6 +45,7 @@ struct Fast {
   double* mail = nullptr;     // edge mailboxes (sentinel when empty)
   size_t mail_n = 0;
   double* hres = nullptr;     // pinned host copy of the residual norm
+  int* hstat = nullptr;       // pinned host copies: [0..3] ctl, [4..5] flags
 };
 
 Fast F;
@@ -83,6 +83,7 @@ void fast_release() {
   if (F.flags) cudaFree(F.flags);
   if (F.wpart) cudaFree(F.wpart);
   if (F.hres) cudaFreeHost(F.hres);
+  if (F.hstat) cudaFreeHost(F.hstat);
   F = Fast();
 }
 
@@ -187,6 +188,7 @@ int fast_setup() {
   CAP_CUDA(cudaMemset(F.flags, 0, sizeof(int) * 2));
   CAP_CUDA(cudaMalloc(&F.wpart, sizeof(double) * F.nblk));
   CAP_CUDA(cudaMallocHost(&F.hres, sizeof(double) * 4));
+  CAP_CUDA(cudaMallocHost(&F.hstat, sizeof(int) * 8));
   CAP_CUDA(cudaMalloc(&F.ctl, sizeof(int) * 4));
   CAP_CUDA(cudaMemset(F.ctl, 0, sizeof(int) * 4));
   CAP_CUDA(cudaStreamSynchronize(c.st));
@@ -498,9 +500,7 @@ __global__ void k_update_fx(DG g, float* __restrict__ x, float* __restrict__ r, 
 
 void fast_free() { fast_release(); }
 
-static int check_wave_error() {
-  int h[2];
-  CAP_CUDA(cudaMemcpy(h, F.flags, sizeof(h), cudaMemcpyDeviceToHost));
+static int wave_error_reset(const int* h) {
   if (h[1] != 0) {
     cudaMemset(F.flags, 0, sizeof(int) * 2);
     cudaMemset(F.ticket, 0, sizeof(unsigned));
@@ -511,6 +511,15 @@ static int check_wave_error() {
     return CAPPGPU_E_SPIN;
   }
   return CAPPGPU_OK;
+}
+
+// One host round trip per check: the wavefront flags join the copies the
+// caller queued (into F.hres / F.hstat), then the stream is synchronised.
+static int sync_status() {
+  Ctx& c = ctx();
+  CAP_CUDA(cudaMemcpyAsync(F.hstat + 4, F.flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, c.st));
+  CAP_CUDA(cudaStreamSynchronize(c.st));
+  return wave_error_reset(F.hstat + 4);
 }
 
 // SIP factorisation as a persistent wavefront (coefficients already in the
@@ -610,7 +619,7 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   int hctl[4] = {0, 0, 0, 0};
   for (int launched = 0; launched < ns;) {
     // a batch of iterations; those after the exit test return at once
-    const int batch = ns - launched < kBatch ? ns - launched : kBatch;
+    const int batch = ns - launched < c.cg_batch ? ns - launched : c.cg_batch;
     for (int q = 0; q < batch; ++q) {
       if ((rc = run_wave<SipFwdD, false>(fwd, F.ctl))) return rc;
       if ((rc = run_wave<SipBwdD, true>(bwd, F.ctl))) return rc;
@@ -628,9 +637,9 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
       cur ^= 1;
     }
     launched += batch;
-    CAP_CUDA(cudaMemcpyAsync(hctl, F.ctl, sizeof(hctl), cudaMemcpyDeviceToHost, c.st));
-    CAP_CUDA(cudaStreamSynchronize(c.st));
-    if ((rc = check_wave_error())) return rc;
+    CAP_CUDA(cudaMemcpyAsync(F.hstat, F.ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.st));
+    if ((rc = sync_status())) return rc;
+    for (int q = 0; q < 4; ++q) hctl[q] = F.hstat[q];
     if (hctl[0]) break;
   }
   CAP_CUDA(cudaMemcpy(F.hres, c.dscal + 5, sizeof(double), cudaMemcpyDeviceToHost));
@@ -682,8 +691,7 @@ int sipsol_fast(int fif, int ifi, cappgpu_solve_report* rep) {
     if ((rc = run_wave<SipFwdD, false>(fwd))) return rc;
     if ((rc = run_wave<SipBwdFiD, true>(bwd))) return rc;
     CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 6, sizeof(double), cudaMemcpyDeviceToHost, c.st));
-    CAP_CUDA(cudaStreamSynchronize(c.st));
-    if ((rc = check_wave_error())) return rc;
+    if ((rc = sync_status())) return rc;
     res1 = F.hres[0];
     if (n == 1) P.resor[ifi - 1] = res1;
     rsm = res1 / (P.resor[ifi - 1] + CAP_SMALL);
@@ -764,8 +772,7 @@ int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     launch(k_add_f, grid_for(g.size()), kThreads, c.st, g, F.d[D_FI], (const float*)G.e[E_Z]);
     CAP_CHECK_LAUNCH();
     CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 6, sizeof(double), cudaMemcpyDeviceToHost, c.st));
-    CAP_CUDA(cudaStreamSynchronize(c.st));
-    if ((rc = check_wave_error())) return rc;
+    if ((rc = sync_status())) return rc;
     res1 = F.hres[0];
     if (n == 1) P.resor[ifi - 1] = res1;
     rsm = res1 / (P.resor[ifi - 1] + CAP_SMALL);
@@ -878,7 +885,7 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     int cur = 0;
     int hctl[4] = {0, 0, 0, 0};
     for (int launched = 0; launched < budget;) {
-      const int batch = budget - launched < kBatch ? budget - launched : kBatch;
+      const int batch = budget - launched < c.cg_batch ? budget - launched : c.cg_batch;
       for (int q = 0; q < batch; ++q) {
         if ((rc = run_wave<SipFwdF, false>(fwd, F.ctl))) return rc;
         if ((rc = run_wave<SipBwdF, true>(bwd, F.ctl))) return rc;
@@ -897,9 +904,9 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
         cur ^= 1;
       }
       launched += batch;
-      CAP_CUDA(cudaMemcpyAsync(hctl, F.ctl, sizeof(hctl), cudaMemcpyDeviceToHost, c.st));
-      CAP_CUDA(cudaStreamSynchronize(c.st));
-      if ((rc = check_wave_error())) return rc;
+      CAP_CUDA(cudaMemcpyAsync(F.hstat, F.ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.st));
+      if ((rc = sync_status())) return rc;
+      for (int q = 0; q < 4; ++q) hctl[q] = F.hstat[q];
       if (hctl[0]) break;
     }
     total += hctl[1] ? hctl[1] : budget;

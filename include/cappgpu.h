@@ -201,6 +201,9 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    1-2 (default 15): 1 the pressure solve (pcgsip), 2 the momentum solves
    (sipsol), 4 the coefficient assembly (fluxuvw, PISO pressure assembly),
    8 the velocity gradients (grad_gauss of u, v, w).
+   "cg_batch": conjugate-gradient iterations of pcgsip launched between two
+   host reads of the device-side exit test (1..64, default 4; surplus
+   iterations after the exit return at once).
    "inner_drop": in precision modes 1-2 the FP32 conjugate-gradient loop of
    pcgsip stops once its residual has dropped by 10^-inner_drop (1..9,
    default 4) and restarts from the FP64 residual.
