@@ -253,7 +253,9 @@ def channel(N=(128, 128, 128), beta=2.0, seed=DEFAULT_SEED, L=(2 * math.pi, math
     (update_values_at_ghostcells.f90); tanh wall stretching beta = 2;
     nu = 1/180; Poiseuille u = 1.5 (1 - z^2) plus a seeded uniform
     perturbation of 10% of the centreline velocity on u, v, w; PISO with 2
-    correctors, fixed CFL 0.5 (CourantNo.h:58-64)."""
+    correctors, fixed CFL 0.5 (CourantNo.h:58-64); Smagorinsky LES
+    (lles, lcal(ivis): calc_vis_les.f90, whose coefficient is 0.17 with Van
+    Driest damping, the strain from find_strain_rate.f90)."""
     N3 = tuple(N) if not np.isscalar(N) else (N, N, N)
     ni, nj, nk, g = build_grid(*channel_nodes(N3, L, beta))
     p = _base_params()
@@ -262,7 +264,8 @@ def channel(N=(128, 128, 128), beta=2.0, seed=DEFAULT_SEED, L=(2 * math.pi, math
     # (the SIP preconditioner is not symmetric); 0.5 converges (about 140
     # iterations at 128^3).  Same code path, different module value.
     p.update(viscos=1.0 / 180.0, ltransient=1, bdf=1, btime=0.0, periodic=1, ncorr=2, npcor=1,
-             conumfix=1, conumfixvalue=0.5, timestep=1e-3, alfa=0.5)
+             conumfix=1, conumfixvalue=0.5, timestep=1e-3, alfa=0.5, lles=1)
+    p["lcal"][IVIS - 1] = 1
     p["sor"][IU - 1] = p["sor"][IV - 1] = p["sor"][IW - 1] = 1e-3
     p["nsw"][IU - 1] = p["nsw"][IV - 1] = p["nsw"][IW - 1] = 20
     p["sor"][IP - 1] = 1e-6

@@ -35,6 +35,17 @@ static int shift_time_levels() {
   return CAPPGPU_OK;
 }
 
+// main.f90:205: the SGS viscosity of the LES model after the pressure-
+// velocity coupling; the strain is formed here (the reference forms it in
+// calcscm, which this path does not run)
+static int les_viscosity() {
+  const cappgpu_params& P = ctx().prm;
+  if (!P.lcal[CAP_IVIS - 1] || !P.lles) return CAPPGPU_OK;
+  int rc = find_strain_rate();
+  if (rc) return rc;
+  return calc_vis_les();
+}
+
 int piso_steps(int nsteps, cappgpu_solve_report* last) {
   Ctx& c = ctx();
   int rc = check_top_wall_index();
@@ -55,6 +66,7 @@ int piso_steps(int nsteps, cappgpu_solve_report* last) {
     if (rc < 0) return rc;
     agg |= rc;
     if (last) *last = reps[nrep - 1];
+    if ((rc = les_viscosity())) return rc;    // main.f90:205
   }
   return agg;
 }
@@ -77,6 +89,7 @@ int simple_iters(int niters, cappgpu_solve_report* last) {
     if (rc < 0) return rc;
     agg |= rc;
     if (last) *last = reps[nrep - 1];
+    if ((rc = les_viscosity())) return rc;    // main.f90:205
   }
   return agg;
 }

@@ -51,5 +51,8 @@ int calcp(cappgpu_solve_report* reps);
 int outbc();
 int courant();
 int continuity_errors();
+// LES sub-grid viscosity (les.cu)
+int find_strain_rate();
+int calc_vis_les();
 
 }  // namespace cap

@@ -65,6 +65,8 @@ SIGNATURES = {
     "cappgpu_learn_params": [ctypes.POINTER(ctypes.c_float), _INT, _INT],
     "cappgpu_learn_stats": [ctypes.POINTER(_INT), ctypes.POINTER(_INT), ctypes.POINTER(_INT), _DP],
     "cappgpu_learn_fit": [_DP, _DP],
+    "cappgpu_find_strain_rate": [],
+    "cappgpu_calc_vis_les": [],
     "cappgpu_learn_check": [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _INT, _INT, _INT,
                             ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _DP],
     "cappgpu_fluxuvw": [_INT] * 10,
@@ -351,6 +353,12 @@ class Library:
 
     def courant(self):
         self._check(self.lib.cappgpu_courant(), "courant")
+
+    def find_strain_rate(self):
+        self._check(self.lib.cappgpu_find_strain_rate(), "find_strain_rate")
+
+    def calc_vis_les(self):
+        self._check(self.lib.cappgpu_calc_vis_les(), "calc_vis_les")
 
     def continuity_errors(self):
         self._check(self.lib.cappgpu_continuity_errors(), "continuity_errors")

@@ -267,6 +267,18 @@ int cappgpu_learn_fit(double* alpha, double* beta);
 int cappgpu_learn_check(const float* rhs, const float* coef, int D, int H, int W, float* output, float* grad,
                         double* loss);
 
+/* ================================================= LES sub-grid viscosity */
+/* find_strain_rate.f90:20-79 (gauss branch): Green-Gauss gradients of u, v,
+   w into the module gradients, then strain = sqrt(2 s_ij s_ij) on
+   k=2..nkm, i=3..nimm, j=3..njmm (the vorticity invariant is not kept). */
+int cappgpu_find_strain_rate(void);
+/* calc_vis_les.f90:38-249: Smagorinsky viscosity with Van Driest damping
+   into vis (same box, under-relaxed by urf(ivis)), then the wall-function
+   viscosity of the bottom and top ghost layers.  The step drivers call both
+   after the pressure-velocity coupling when lcal(ivis) and lles are set
+   (main.f90:205). */
+int cappgpu_calc_vis_les(void);
+
 /* ======================================================= index maps (a1) */
 /* setind.f90:34-40: li(i)=(i-1)*nj for i=1..ni, lk(k)=(k-1)*nij.  Writes
    the device copies back (tests compare them element-wise). */

@@ -85,6 +85,9 @@ void cap_outbc(cap_state* s);
 void cap_correct_boundary_conditions(cap_state* s);
 void cap_courant(cap_state* s);
 void cap_continuity_errors(cap_state* s);
+/* find_strain_rate.f90:20-79 (gauss branch), calc_vis_les.f90:38-249 */
+void cap_find_strain_rate(cap_state* s);
+void cap_calc_vis_les(cap_state* s);
 int cap_piso_steps(cap_state* s, int nsteps, cappgpu_solve_report* last);
 int cap_simple_iters(cap_state* s, int niters, cappgpu_solve_report* last);
 

@@ -58,6 +58,8 @@ _SIGS = {
     "cap_correct_boundary_conditions": ([_VP], None),
     "cap_courant": ([_VP], None),
     "cap_continuity_errors": ([_VP], None),
+    "cap_find_strain_rate": ([_VP], None),
+    "cap_calc_vis_les": ([_VP], None),
     "cap_piso_steps": ([_VP, _INT, _REP], _INT),
     "cap_simple_iters": ([_VP, _INT, _REP], _INT),
 }
@@ -233,6 +235,12 @@ class State:
 
     def continuity_errors(self):
         self.L.cap_continuity_errors(self.ptr)
+
+    def find_strain_rate(self):
+        self.L.cap_find_strain_rate(self.ptr)
+
+    def calc_vis_les(self):
+        self.L.cap_calc_vis_les(self.ptr)
 
     def piso_steps(self, n):
         rep = SolveReport()

@@ -890,6 +890,99 @@ int cap_calcp(cap_state* s, cappgpu_solve_report* reps) {
 }
 
 /* ------------------------------------------------------------ drivers */
+/* ------------------------------------------------------------------- LES */
+/* find_strain_rate.f90:20-79, gauss branch: Green-Gauss gradients of u, v,
+   w into the module gradients (:27-31), then |S| = sqrt(2 s_ij s_ij) over
+   k = 2..nkm, i = 3..nimm, j = 3..njmm (:33-76).  The vorticity invariant
+   of :77 is not kept (nothing on this path reads it). */
+void cap_find_strain_rate(cap_state* s) {
+  cap_grad_gauss(s, CAP_U, CAP_GRADU_X, CAP_GRADU_Y, CAP_GRADU_Z);
+  cap_grad_gauss(s, CAP_V, CAP_GRADV_X, CAP_GRADV_Y, CAP_GRADV_Z);
+  cap_grad_gauss(s, CAP_W, CAP_GRADW_X, CAP_GRADW_Y, CAP_GRADW_Z);
+  const double *gux = s->f[CAP_GRADU_X], *guy = s->f[CAP_GRADU_Y], *guz = s->f[CAP_GRADU_Z];
+  const double *gvx = s->f[CAP_GRADV_X], *gvy = s->f[CAP_GRADV_Y], *gvz = s->f[CAP_GRADV_Z];
+  const double *gwx = s->f[CAP_GRADW_X], *gwy = s->f[CAP_GRADW_Y], *gwz = s->f[CAP_GRADW_Z];
+  double* strain = s->f[CAP_STRAIN];
+  for (int k = 2; k <= s->nkm; ++k)
+    for (int i = 3; i <= s->nimm; ++i)
+      for (int j = 3; j <= s->njmm; ++j) {
+        const int inp = IXK(i, j, k);
+        const double s11 = gux[inp];
+        const double s12 = 0.5 * (guy[inp] + gvx[inp]);
+        const double s13 = 0.5 * (guz[inp] + gwx[inp]);
+        const double s22 = gvy[inp];
+        const double s23 = 0.5 * (gvz[inp] + gwy[inp]);
+        const double s33 = gwz[inp];
+        strain[inp] = sqrt(2 * (s11 * s11 + s22 * s22 + s33 * s33 + 2 * (s12 * s12 + s13 * s13 + s23 * s23)));
+      }
+}
+
+/* calc_vis_les.f90:38-249: Smagorinsky viscosity with the Van Driest and
+   Schumann limits over k = 2..nkm, i = 3..nimm, j = 3..njmm (:42-73; the
+   coefficient is the 0.17 assigned last at :66, C_delta the
+   default-real 0.158, 1/3 the default-real 1./3.), under-relaxed by
+   urf(ivis); then the wall-function viscosity of the bottom and top ghost
+   layers (:80-246; dnw dotted with the integer extents nx,ny,nz and the
+   top wall at lk(nimm), as calcuvw does). */
+void cap_calc_vis_les(cap_state* s) {
+  const cappgpu_params* P = &s->prm;
+  const double *u = s->f[CAP_U], *v = s->f[CAP_V], *w = s->f[CAP_W];
+  const double *wd = s->f[CAP_WALLDIST], *vol = s->f[CAP_VOL], *strain = s->f[CAP_STRAIN], *den = s->f[CAP_DEN];
+  double* vis = s->f[CAP_VIS];
+  const double viscos = P->viscos, cappa = P->cappa, urf = P->urf[CAP_IVIS - 1];
+  const double c_delta = (double)0.158f, c_les = (double)0.17f, third = (double)(1.f / 3.f);
+  for (int k = 2; k <= s->nkm; ++k)
+    for (int i = 3; i <= s->nimm; ++i)
+      for (int j = 3; j <= s->njmm; ++j) {
+        const int inp = IXK(i, j, k);
+        const double visold = vis[inp];
+        const double wldist = wd[inp];
+        const double uref = sqrt(u[inp] * u[inp] + v[inp] * v[inp] + w[inp] * w[inp]);
+        const double utau = sqrt(viscos * uref / wldist);
+        const double zplus = wldist * utau / viscos;
+        const double l = dmin(c_les * pow(vol[inp], third), cappa / c_delta * wldist) * (1. - exp(-zplus / 26.0));
+        const double vis_smag = l * l * strain[inp] * den[inp];
+        double vnew = vis_smag + viscos;
+        vnew = urf * vnew + (1. - urf) * visold;
+        vis[inp] = vnew;
+      }
+  const double *xc = s->f[CAP_XC], *yc = s->f[CAP_YC], *zc = s->f[CAP_ZC], *fz = s->f[CAP_FZ];
+  const double *a3x = s->f[CAP_AR3X], *a3y = s->f[CAP_AR3Y], *a3z = s->f[CAP_AR3Z];
+  const double nxi = (double)s->ni, nyi = (double)s->nj, nzi = (double)s->nk;
+  for (int top = 0; top < 2; ++top)
+    for (int i = 3; i <= s->nimm; ++i)
+      for (int j = 3; j <= s->njmm; ++j) {
+        int inbc, ingc, iface;
+        double fxp, fxe;
+        if (!top) {
+          inbc = IXK(i, j, 3); ingc = inbc - s->nij; iface = ingc;
+          fxp = fz[ingc]; fxe = 1.0 - fxp;
+        } else {
+          inbc = IXK(i, j, s->nimm); ingc = inbc + s->nij; iface = inbc;
+          fxp = 1.0 - fz[inbc]; fxe = 1.0 - fxp;
+        }
+        const double gzx = xc[inbc] * fxp + xc[ingc] * fxe;
+        const double gzy = yc[inbc] * fxp + yc[ingc] * fxe;
+        const double gzz = zc[inbc] * fxp + zc[ingc] * fxe;
+        const double are = sqrt(a3x[iface] * a3x[iface] + a3y[iface] * a3y[iface] + a3z[iface] * a3z[iface]);
+        const double nxf = a3x[iface] / are, nyf = a3y[iface] / are, nzf = a3z[iface] / are;
+        const double vnp = u[inbc] * nxf + v[inbc] * nyf + w[inbc] * nzf;
+        double xtp = u[inbc] - vnp * nxf, ytp = v[inbc] - vnp * nyf, ztp = w[inbc] - vnp * nzf;
+        const double vtp = sqrt(xtp * xtp + ytp * ytp + ztp * ztp);
+        xtp = xtp / vtp;
+        ytp = ytp / vtp;
+        ztp = ztp / vtp;
+        const double ut2 = fabs(u[inbc] * xtp + v[inbc] * ytp + w[inbc] * ztp);
+        const double dnw = fabs((xc[inbc] - gzx) * nxi + (yc[inbc] - gzy) * nyi + (zc[inbc] - gzz) * nzi);
+        const double tau = viscos * ut2 / dnw;
+        const double utau = sqrt(tau / P->densit);
+        const double ypl = P->densit * utau * dnw / viscos;
+        double viscw = P->zero;
+        if (ypl > (double)11.61f) viscw = ypl * viscos * cappa / log(P->elog * ypl);
+        vis[ingc] = dmax(viscos, viscw);
+      }
+}
+
 /* main.f90:140-207 with maxit = 1 iteration per time step (transient PISO).
    The reference's residual-normalised convergence test (main.f90:218-237)
    uses snorin, which only bcin sets for inlet cases; the drivers here run
@@ -918,6 +1011,12 @@ int cap_piso_steps(cap_state* s, int nsteps, cappgpu_solve_report* last) {
     if (r < 0) return r;
     rc |= r;
     if (last) *last = reps[P->ncorr * P->npcor - 1];
+    /* main.f90:205; the strain is formed here (the reference forms it in
+       calcscm, which this path does not run) */
+    if (P->lcal[CAP_IVIS - 1] && P->lles) {
+      cap_find_strain_rate(s);
+      cap_calc_vis_les(s);
+    }
   }
   return rc;
 }
@@ -937,6 +1036,10 @@ int cap_simple_iters(cap_state* s, int niters, cappgpu_solve_report* last) {
     if (r < 0) return r;
     rc |= r;
     if (last) *last = reps[P->ncorr * P->npcor - 1];
+    if (P->lcal[CAP_IVIS - 1] && P->lles) {   /* main.f90:205 */
+      cap_find_strain_rate(s);
+      cap_calc_vis_les(s);
+    }
   }
   return rc;
 }

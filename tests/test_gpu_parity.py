@@ -359,6 +359,36 @@ def test_simple_iters_parity(gpu_lib, oracle_mod):
     compare(gpu_lib, st, rtol=RTOL, names=["u", "v", "w", "p", "f1", "f2", "f3"])
 
 
+def test_les_viscosity_parity(gpu_lib, oracle_mod):
+    """find_strain_rate + calc_vis_les (LES path, main.f90:205): gradients and
+    strain bit-exact; the viscosity (pow, exp, log of CUDA against the
+    oracle's libm) and the wall-function ghost values to 1e-13."""
+    case, st = state(oracle_mod, "channel")
+    p = st.params
+    p.lles = 1
+    p.lcal[cappgpu.params.IVIS - 1] = 1
+    p.urf[cappgpu.params.IVIS - 1] = 0.7   # the under-relaxation of :69 takes part
+    # a viscosity field to relax from, and strain-bearing velocities
+    rng = np.random.default_rng(21)
+    v0 = st.field("vis") * (1 + 0.1 * rng.random(st.field("vis").size))
+    st.set_field("vis", v0)
+    run_both(gpu_lib, st, lambda s: (s.find_strain_rate(), s.calc_vis_les()))
+    grads = [f"grad{c}_{x}" for c in "uvw" for x in "xyz"]
+    compare(gpu_lib, st, exact=grads + ["strain"], names=grads + ["strain"])
+    compare(gpu_lib, st, rtol=1e-13, names=["vis"])
+    g = case.view(gpu_lib.get_field("vis"))
+    assert np.all(g[2:-2, 2:-2, 2:-2] >= p.viscos * (1 - 1e-12))
+
+
+def test_les_piso_steps_parity(gpu_lib, oracle_mod):
+    case, st = state(oracle_mod, "channel")
+    st.params.lles = 1
+    st.params.lcal[cappgpu.params.IVIS - 1] = 1
+    rg, ro = run_both(gpu_lib, st, lambda s: s.piso_steps(3))
+    assert rg.iters == ro.iters
+    compare(gpu_lib, st, rtol=RTOL, names=["u", "v", "w", "p", "f1", "f2", "f3", "vis", "strain"])
+
+
 def test_top_wall_index_guard(gpu_lib, oracle_mod):
     """calcuvw.f90:254 addresses the top wall with lk(nimm); a grid with
     ni > nk would put it outside the array: refused, not run."""
