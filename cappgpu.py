@@ -19,6 +19,7 @@ _pkg = sys.modules["cappgpu._pkg"]
 
 params = _pkg.params
 cases = _pkg.cases
+fortio = _pkg.fortio
 build = _pkg.build
 Library = _pkg.Library
 CappError = _pkg.CappError

@@ -8,8 +8,9 @@ Layout:
   native.py  ctypes binding mirroring the reference routine interface
   params.py  ctypes mirrors of the ABI structures, field/BC identifiers
   cases.py   seeded synthetic grids and cases of the benchmarked shapes
+  fortio.py  the reference's grid and restart file formats
 """
-from . import params, cases  # noqa: F401
+from . import params, cases, fortio  # noqa: F401
 from .params import FIELD, FIELD_NAMES, BC_NAMES, Params, SolveReport, SOLVER  # noqa: F401
 from .build import build, LIB  # noqa: F401
 from .native import Library, CappError, load_library, SIGNATURES  # noqa: F401
