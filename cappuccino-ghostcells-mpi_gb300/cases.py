@@ -255,7 +255,10 @@ def channel(N=(128, 128, 128), beta=2.0, seed=DEFAULT_SEED, L=(2 * math.pi, math
     perturbation of 10% of the centreline velocity on u, v, w; PISO with 2
     correctors, fixed CFL 0.5 (CourantNo.h:58-64); Smagorinsky LES
     (lles, lcal(ivis): calc_vis_les.f90, whose coefficient is 0.17 with Van
-    Driest damping, the strain from find_strain_rate.f90)."""
+    Driest damping, the strain from find_strain_rate.f90); constant mass
+    flux at the bulk velocity uin = 1 of the Poiseuille profile
+    (const_massflux_correction.f90, the source gradpcmf*vol of
+    calcuvw.f90:78)."""
     N3 = tuple(N) if not np.isscalar(N) else (N, N, N)
     ni, nj, nk, g = build_grid(*channel_nodes(N3, L, beta))
     p = _base_params()
@@ -264,7 +267,7 @@ def channel(N=(128, 128, 128), beta=2.0, seed=DEFAULT_SEED, L=(2 * math.pi, math
     # (the SIP preconditioner is not symmetric); 0.5 converges (about 140
     # iterations at 128^3).  Same code path, different module value.
     p.update(viscos=1.0 / 180.0, ltransient=1, bdf=1, btime=0.0, periodic=1, ncorr=2, npcor=1,
-             conumfix=1, conumfixvalue=0.5, timestep=1e-3, alfa=0.5, lles=1)
+             conumfix=1, conumfixvalue=0.5, timestep=1e-3, alfa=0.5, lles=1, const_mflux=1, uin=1.0)
     p["lcal"][IVIS - 1] = 1
     p["sor"][IU - 1] = p["sor"][IV - 1] = p["sor"][IW - 1] = 1e-3
     p["nsw"][IU - 1] = p["nsw"][IV - 1] = p["nsw"][IW - 1] = 20

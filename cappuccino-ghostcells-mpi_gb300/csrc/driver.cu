@@ -67,6 +67,7 @@ int piso_steps(int nsteps, cappgpu_solve_report* last) {
     agg |= rc;
     if (last) *last = reps[nrep - 1];
     if ((rc = les_viscosity())) return rc;    // main.f90:205
+    if (c.prm.ltransient && c.prm.const_mflux && (rc = const_massflux_correction())) return rc;   // main.f90:252
   }
   return agg;
 }

@@ -54,5 +54,7 @@ int continuity_errors();
 // LES sub-grid viscosity (les.cu)
 int find_strain_rate();
 int calc_vis_les();
+// constant mass-flux forcing (mflux.cu)
+int const_massflux_correction();
 
 }  // namespace cap

@@ -67,6 +67,7 @@ SIGNATURES = {
     "cappgpu_learn_fit": [_DP, _DP],
     "cappgpu_find_strain_rate": [],
     "cappgpu_calc_vis_les": [],
+    "cappgpu_const_massflux_correction": [],
     "cappgpu_learn_check": [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _INT, _INT, _INT,
                             ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _DP],
     "cappgpu_fluxuvw": [_INT] * 10,
@@ -359,6 +360,9 @@ class Library:
 
     def calc_vis_les(self):
         self._check(self.lib.cappgpu_calc_vis_les(), "calc_vis_les")
+
+    def const_massflux_correction(self):
+        self._check(self.lib.cappgpu_const_massflux_correction(), "const_massflux_correction")
 
     def continuity_errors(self):
         self._check(self.lib.cappgpu_continuity_errors(), "continuity_errors")

@@ -278,6 +278,12 @@ int cappgpu_find_strain_rate(void);
    after the pressure-velocity coupling when lcal(ivis) and lles are set
    (main.f90:205). */
 int cappgpu_calc_vis_les(void);
+/* const_massflux_correction.f90:1-22: the volume-weighted averages of u and
+   apu (fieldManipulation.f90:10-44), the pressure-gradient increment that
+   restores the bulk velocity uin, u += apu * increment (whole array),
+   gradpcmf += increment.  cappgpu_piso_steps runs it at the end of every
+   step when ltransient and const_mflux are set (main.f90:252). */
+int cappgpu_const_massflux_correction(void);
 
 /* ======================================================= index maps (a1) */
 /* setind.f90:34-40: li(i)=(i-1)*nj for i=1..ni, lk(k)=(k-1)*nij.  Writes

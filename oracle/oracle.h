@@ -88,6 +88,8 @@ void cap_continuity_errors(cap_state* s);
 /* find_strain_rate.f90:20-79 (gauss branch), calc_vis_les.f90:38-249 */
 void cap_find_strain_rate(cap_state* s);
 void cap_calc_vis_les(cap_state* s);
+/* const_massflux_correction.f90:1-22 */
+void cap_const_massflux_correction(cap_state* s);
 int cap_piso_steps(cap_state* s, int nsteps, cappgpu_solve_report* last);
 int cap_simple_iters(cap_state* s, int niters, cappgpu_solve_report* last);
 

@@ -60,6 +60,7 @@ _SIGS = {
     "cap_continuity_errors": ([_VP], None),
     "cap_find_strain_rate": ([_VP], None),
     "cap_calc_vis_les": ([_VP], None),
+    "cap_const_massflux_correction": ([_VP], None),
     "cap_piso_steps": ([_VP, _INT, _REP], _INT),
     "cap_simple_iters": ([_VP, _INT, _REP], _INT),
 }
@@ -241,6 +242,9 @@ class State:
 
     def calc_vis_les(self):
         self.L.cap_calc_vis_les(self.ptr)
+
+    def const_massflux_correction(self):
+        self.L.cap_const_massflux_correction(self.ptr)
 
     def piso_steps(self, n):
         rep = SolveReport()

@@ -890,6 +890,33 @@ int cap_calcp(cap_state* s, cappgpu_solve_report* reps) {
 }
 
 /* ------------------------------------------------------------ drivers */
+/* --------------------------------------------------- constant mass flux */
+/* const_massflux_correction.f90:1-22 (included at main.f90:252 at the end
+   of a transient step): volume-weighted averages of U and APU over
+   k = 2..nkm, i = 3..nimm, j = 3..njmm (fieldManipulation.f90:10-44, summed
+   in loop order), the pressure-gradient increment that restores the bulk
+   velocity magUbar = uin (init.f90:356), applied to the whole U array. */
+void cap_const_massflux_correction(cap_state* s) {
+  cappgpu_params* P = &s->prm;
+  const double *vol = s->f[CAP_VOL], *apu = s->f[CAP_APU];
+  double* u = s->f[CAP_U];
+  double su = 0.0, sa = 0.0, sv = 0.0;
+  for (int k = 2; k <= s->nkm; ++k)
+    for (int i = 3; i <= s->nimm; ++i)
+      for (int j = 3; j <= s->njmm; ++j) {
+        const int inp = IXK(i, j, k);
+        sv = sv + vol[inp];
+        su = su + vol[inp] * u[inp];
+        sa = sa + vol[inp] * apu[inp];
+      }
+  const double mag_ubar_star = su / sv;
+  const double rua = sa / sv;
+  const double dgrad = (P->uin - mag_ubar_star) / rua;
+  const double flow_direction = 1.0;
+  for (int q = 0; q < s->nijk; ++q) u[q] = u[q] + flow_direction * apu[q] * dgrad;
+  P->gradpcmf = P->gradpcmf + dgrad;
+}
+
 /* ------------------------------------------------------------------- LES */
 /* find_strain_rate.f90:20-79, gauss branch: Green-Gauss gradients of u, v,
    w into the module gradients (:27-31), then |S| = sqrt(2 s_ij s_ij) over
@@ -1017,6 +1044,7 @@ int cap_piso_steps(cap_state* s, int nsteps, cappgpu_solve_report* last) {
       cap_find_strain_rate(s);
       cap_calc_vis_les(s);
     }
+    if (P->ltransient && P->const_mflux) cap_const_massflux_correction(s);   /* main.f90:252 */
   }
   return rc;
 }

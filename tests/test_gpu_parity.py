@@ -389,6 +389,25 @@ def test_les_piso_steps_parity(gpu_lib, oracle_mod):
     compare(gpu_lib, st, rtol=RTOL, names=["u", "v", "w", "p", "f1", "f2", "f3", "vis", "strain"])
 
 
+def test_const_massflux_correction_parity(gpu_lib, oracle_mod):
+    case, st = state(oracle_mod, "channel")
+    rng = np.random.default_rng(5)
+    st.set_field("apu", 0.01 + 0.01 * rng.random(st.field("apu").size))
+    st.params.uin = 1.3
+    st.params.gradpcmf = 0.2
+    run_both(gpu_lib, st, lambda s: s.const_massflux_correction())
+    compare(gpu_lib, st, rtol=1e-13, names=["u"])
+    g = gpu_lib.get_params().gradpcmf
+    assert abs(g - st.params.gradpcmf) <= 1e-12 * abs(st.params.gradpcmf)
+    # the bulk velocity is restored (to the rounding of the sums)
+    v = case.view
+    vol = v(st.field("vol"))[1:-1, 2:-2, 2:-2]
+    u = v(gpu_lib.get_field("u"))[1:-1, 2:-2, 2:-2]
+    a = v(st.field("apu"))[1:-1, 2:-2, 2:-2]
+    ubar = (vol * u).sum() / vol.sum()
+    assert abs(ubar - 1.3) < 1e-12
+
+
 def test_top_wall_index_guard(gpu_lib, oracle_mod):
     """calcuvw.f90:254 addresses the top wall with lk(nimm); a grid with
     ni > nk would put it outside the array: refused, not run."""
