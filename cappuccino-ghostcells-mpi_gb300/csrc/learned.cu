@@ -813,6 +813,33 @@ void wgrad_ci(const bf16* x, int ldx, const bf16* gy, int ldg, const bf16* y, in
   launch(k_wgrad3<CI>, dim3(27, nch, CO / 16), 128, ctx().st, x, ldx, gy, ldg, y, ldy, N.part, CO, D, H, W);
 }
 
+// tcgen05 weight gradient on halo tiles; returns the number of chunks
+template <int CI, int CO>
+int wgrad_halo(const bf16* x, int ldx, const bf16* gy, int ldg, const bf16* y, int ldy, int D, int H, int W) {
+  typedef tc::WgradTC<CI, CO> T;
+  CAP_CUDA(cudaFuncSetAttribute(tc::k_wgrad_halo<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, T::kSmem));
+  const int ntiles = ((W + 7) / 8) * ((H + 15) / 16) * D;
+  // 16 tiles per chunk, fewer chunks if the partial sums would not fit
+  const long long cap = (long long)(N.part_n / ((size_t)27 * CO * CI));
+  int per = 16;
+  while ((ntiles + per - 1) / per > cap) per *= 2;
+  const int nch = (ntiles + per - 1) / per;
+  const int ngroups = (27 + T::kTG - 1) / T::kTG;
+  ++ctx().launches;
+  tc::k_wgrad_halo<CI, CO><<<dim3(ngroups, nch), 128, T::kSmem, ctx().st>>>(x, ldx, gy, ldg, y, ldy, N.part, D, H,
+                                                                             W, per, N.err);
+  return nch;
+}
+
+int wgrad_any_halo(int CI, int CO, const bf16* x, int ldx, const bf16* gy, int ldg, const bf16* y, int ldy, int D,
+                   int H, int W) {
+#define CAP_WG(ci, co) \
+  if (CI == ci && CO == co) return wgrad_halo<ci, co>(x, ldx, gy, ldg, y, ldy, D, H, W);
+  CAP_WG(16, 16) CAP_WG(16, 32) CAP_WG(32, 32) CAP_WG(32, 64) CAP_WG(64, 64) CAP_WG(96, 32) CAP_WG(48, 16)
+#undef CAP_WG
+  return -1;
+}
+
 // weight and bias gradients of layer l (input x, output y, output gradient
 // gy), then (dx != null) the gradient with respect to its input
 int bwd_layer(int l, const bf16* x, int ldx, const bf16* gy, int ldg, const bf16* y, int ldy, bf16* dx, int lddx,
@@ -820,15 +847,19 @@ int bwd_layer(int l, const bf16* x, int ldx, const bf16* gy, int ldg, const bf16
   Ctx& c = ctx();
   const int CI = kCI[l], CO = kCO[l];
   const int V = D * H * W;
-  switch (CI) {
-    case 16: wgrad_ci<16>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
-    case 32: wgrad_ci<32>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
-    case 48: wgrad_ci<48>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
-    case 64: wgrad_ci<64>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
-    case 96: wgrad_ci<96>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
-    default: set_error("learned guess: bad layer"); return CAPPGPU_E_ARG;
+  int nch = -1;
+  if (g_conv_impl == 1) nch = wgrad_any_halo(CI, CO, x, ldx, gy, ldg, y, ldy, D, H, W);
+  if (nch < 0) {
+    switch (CI) {
+      case 16: wgrad_ci<16>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
+      case 32: wgrad_ci<32>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
+      case 48: wgrad_ci<48>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
+      case 64: wgrad_ci<64>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
+      case 96: wgrad_ci<96>(x, ldx, gy, ldg, y, ldy, CO, D, H, W); break;
+      default: set_error("learned guess: bad layer"); return CAPPGPU_E_ARG;
+    }
+    nch = (V + kChunk - 1) / kChunk;
   }
-  const int nch = (V + kChunk - 1) / kChunk;
   launch(k_wgrad_sum, (27 * CO * CI + 255) / 256, 256, c.st, (const float*)N.part, nch, CO, CI, N.gp + offW(l));
   launch(k_bgrad, 256, 256, c.st, gy, ldg, y, ldy, CO, V, N.part);
   launch(k_sum_cols, 1, 64, c.st, (const float*)N.part, 256, CO, N.gp + offB(l));

@@ -413,3 +413,155 @@ __global__ void __launch_bounds__(128) k_conv3_halo(const bf16* __restrict__ x, 
 
 }  // namespace tc
 }  // namespace cap
+
+namespace cap {
+namespace tc {
+
+// Weight gradient on the halo tile: for the taps t of a group and the
+// tiles of a chunk, G_t[co][ci] += sum over the tile's voxels v of
+// gm[v][co] x[v + off(t)][ci], gm = gy masked by the layer's ReLU output.
+// Both operands are MN-major in shared memory (the 16-byte rows run along
+// the channels, consecutive rows along the voxels = K).  Without swizzling
+// the leading-dimension offset is the step between core matrices along K
+// and the stride-dimension offset the step along M/N, for either major: A
+// is the tile's 128 rows of gm, one 2 KB plane per 8 output channels,
+// padded with zero planes to M = 128 (leading offset 128 B between 8-voxel
+// groups, stride offset 2 KB between channel groups); B is the input halo of
+// the forward kernel read from the tap's shifted row (leading offset 160 B
+// = one tile row, stride offset one plane).  The group's taps accumulate side by side
+// in TMEM (CI columns each); the CTA writes its partial sums for the
+// chunk, summed over chunks in a fixed order afterwards.
+template <int CI, int CO>
+struct WgradTC {
+  static constexpr int NC = CI / 8, NG = CO / 8;
+  static constexpr int kPlaneB = HaloTC<CI, 16>::kPlane;   // 540 rows of 16 B
+  static constexpr int kB = (NC * kPlaneB + 1023) & ~1023;
+  static constexpr int kPlaneA = 128 * 16;
+  static constexpr int kA = 16 * kPlaneA;                  // M = 128
+  static constexpr int kTG = (256 / CI) < 27 ? (256 / CI) : 27;   // taps per group
+  static constexpr int kCols = pow2_cols(kTG * CI);
+  static constexpr int kSmemUse = kB + kA + 1024 + 64;
+  static constexpr int kSmemTmem = kCols * (228 * 1024 / 512);
+  static constexpr int kSmem = kSmemUse > kSmemTmem ? kSmemUse : kSmemTmem;
+  static_assert(CI % 16 == 0 && CO % 8 == 0 && CO <= 128, "tile shape");
+};
+
+// instruction descriptor, both operands MN-major (bits 15, 16 = 1)
+__host__ __device__ constexpr unsigned idesc_bf16_mn(int M, int N) { return idesc_bf16(M, N) | (1u << 15) | (1u << 16); }
+
+template <int CI, int CO>
+__global__ void __launch_bounds__(128) k_wgrad_halo(const bf16* __restrict__ x, int ldx, const bf16* __restrict__ gy,
+                                                    int ldg, const bf16* __restrict__ y, int ldy,
+                                                    float* __restrict__ part, int D, int H, int W, int tiles_per_chunk,
+                                                    int* err) {
+  typedef WgradTC<CI, CO> T;
+  typedef HaloTC<CI, 16> Hl;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((unsigned long long)smem_raw + 1023) & ~1023ull);
+  unsigned char* B = smem;              // halo planes (B first: an overrun lands in A)
+  unsigned char* A = smem + T::kB;      // gm planes
+  unsigned long long* bar = (unsigned long long*)(A + T::kA);
+  unsigned* tslot = (unsigned*)(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tap0 = blockIdx.x * T::kTG;
+  const int ntap = 27 - tap0 < T::kTG ? 27 - tap0 : T::kTG;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_fence_init();
+  }
+  if (warp == 0) tmem_alloc(tslot, T::kCols);
+  // the padding planes of A (output channels CO..127) stay zero
+  for (int q = tid; q < (16 - T::NG) * T::kPlaneA / 16; q += 128)
+    reinterpret_cast<uint4*>(A + T::NG * T::kPlaneA)[q] = make_uint4(0u, 0u, 0u, 0u);
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = *tslot;
+  constexpr unsigned idesc = idesc_bf16_mn(128, CI);
+  const int ntx = (W + 7) / 8, nty = (H + 15) / 16;
+  const int ntiles = ntx * nty * D;
+  const int t_begin = blockIdx.y * tiles_per_chunk;
+  const int t_end = t_begin + tiles_per_chunk < ntiles ? t_begin + tiles_per_chunk : ntiles;
+  unsigned phase = 0u;
+  bool bad = false, first = true;
+  for (int tile = t_begin; tile < t_end; ++tile) {
+    const int tx = tile % ntx, ty = (tile / ntx) % nty, z0 = tile / (ntx * nty);
+    const int x0 = tx * 8, y0 = ty * 16;
+    for (int q = tid; q < Hl::HV * T::NC; q += 128) {   // input halo, zero outside the grid
+      const int hv = q / T::NC, kc = q - hv * T::NC;
+      const int hx = hv % Hl::HX, hy = (hv / Hl::HX) % Hl::HY, hz = hv / (Hl::HX * Hl::HY);
+      const int gx = x0 - 1 + hx, gyy = y0 - 1 + hy, gz = z0 - 1 + hz;
+      uint4 u = make_uint4(0u, 0u, 0u, 0u);
+      if ((unsigned)gx < (unsigned)W && (unsigned)gyy < (unsigned)H && (unsigned)gz < (unsigned)D)
+        u = *reinterpret_cast<const uint4*>(x + (((long long)gz * H + gyy) * W + gx) * ldx + kc * 8);
+      *reinterpret_cast<uint4*>(B + kc * T::kPlaneB + hv * 16) = u;
+    }
+    {   // the tile's masked output gradient, row = tid (x = tid % 8, y = tid / 8)
+      const int ox = x0 + (tid & 7), oy = y0 + (tid >> 3);
+      const bool valid = ox < W && oy < H;
+      const long long v = ((long long)z0 * H + oy) * W + ox;
+#pragma unroll
+      for (int kc = 0; kc < T::NG; ++kc) {
+        uint4 u = make_uint4(0u, 0u, 0u, 0u);
+        if (valid)
+          u = mask8(*reinterpret_cast<const uint4*>(gy + v * ldg + kc * 8),
+                    *reinterpret_cast<const uint4*>(y + v * ldy + kc * 8));
+        *reinterpret_cast<uint4*>(A + kc * T::kPlaneA + tid * 16) = u;
+      }
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const unsigned a0 = smem_u32(A), b0 = smem_u32(B);
+      for (int j = 0; j < ntap; ++j) {
+        const int tap = tap0 + j;
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+        const unsigned row = (unsigned)(((1 + dz) * Hl::HY + 1 + dy) * Hl::HX + 1 + dx);
+#pragma unroll
+        for (int ks = 0; ks < 8; ++ks)
+          mma_bf16(tmem + (unsigned)(j * CI), smem_desc(a0 + ks * 256, 128, T::kPlaneA),
+                   smem_desc(b0 + row * 16 + ks * 320, Hl::HX * 16, T::kPlaneB), idesc, (!first || ks) ? 1 : 0);
+      }
+      mma_commit(&bar[0]);
+    }
+    if (!bad && !mbar_wait_bounded(&bar[0], phase)) bad = true;
+    phase ^= 1u;
+    first = false;
+    tc_fence_before();
+    if (__syncthreads_or(bad)) break;
+    tc_fence_after();
+  }
+  // partial sums of the chunk: lane co, CI columns per tap
+  if (t_begin < t_end && !bad && warp * 32 < CO) {
+    const int co = warp * 32 + (tid & 31);
+    const unsigned trow = tmem + ((unsigned)(warp * 32) << 16);
+    for (int j = 0; j < ntap; ++j) {
+#pragma unroll
+      for (int c0 = 0; c0 < CI; c0 += 16) {
+        float acc[16];
+        tmem_ld16(trow + (unsigned)(j * CI + c0), acc);
+        tmem_wait_ld();
+        if (co < CO) {
+          float* dst = part + (((size_t)blockIdx.y * 27 + tap0 + j) * CO + co) * CI + c0;
+#pragma unroll
+          for (int q = 0; q < 16; ++q) dst[q] = acc[q];
+        }
+      }
+    }
+  } else if (t_begin >= t_end && warp * 32 < CO) {   // an empty chunk adds nothing
+    const int co = warp * 32 + (tid & 31);
+    if (co < CO)
+      for (int j = 0; j < ntap; ++j)
+        for (int c = 0; c < CI; ++c) part[(((size_t)blockIdx.y * 27 + tap0 + j) * CO + co) * CI + c] = 0.f;
+  }
+  if (bad && tid == 0) atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, T::kCols);
+}
+
+}  // namespace tc
+}  // namespace cap
