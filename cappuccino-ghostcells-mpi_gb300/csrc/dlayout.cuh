@@ -14,6 +14,10 @@
 // row of doubles or floats start on a 16-byte boundary, which the
 // tensor-memory-access (TMA) copies of the wavefront require.
 //
+// In row order -- rows (s,c) by s, then c; cells of a row by a -- the cells
+// form one compact sequence; chunk q of 32 consecutive cells starts at the
+// cell recorded in chunk[q] (the vector kernels walk it).
+//
 // Factors with several components per cell use the component-major variant
 //     Dc(a,b,c,q) = ((s*Nk + c)*NQ + q)*P + a
 // so that one component of a row of cells is contiguous.
@@ -27,6 +31,9 @@ struct DG {
   int P;               // row pitch (Ni rounded up to a multiple of 4)
   int nj, nij;         // natural strides
   long long plane;     // Nk*P
+  long long ncell;     // Ni*Nj*Nk
+  int nchunk;          // ceil(ncell / 32)
+  const int4* chunk;   // (s, c, a) of the first cell of each 32-cell chunk
   __host__ __device__ long long d(int a, int b, int c) const {
     return (long long)(a + b + c) * plane + (long long)c * P + a;
   }
@@ -53,6 +60,9 @@ inline DG make_dg(const Dims& d) {
   g.nj = d.nj;
   g.nij = d.nij;
   g.plane = (long long)g.Nk * g.P;
+  g.ncell = (long long)g.Ni * g.Nj * g.Nk;
+  g.nchunk = (int)((g.ncell + 31) / 32);
+  g.chunk = nullptr;
   return g;
 }
 

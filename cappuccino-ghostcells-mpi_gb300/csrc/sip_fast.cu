@@ -38,6 +38,7 @@ struct Fast {
   CUtensorMap map_fq, map_bq;
   int nBA = 0, nBC = 0, nblk = 0;
   int2* order = nullptr;
+  int4* chunk = nullptr;      // compact-order chunk starts (DG::chunk)
   unsigned* ticket = nullptr;
   int* flags = nullptr;       // [0] abort, [1] err
   int* ctl = nullptr;         // iteration control: [0] stop at iteration, [1] iterations, [2] non-finite, [3] converged
@@ -77,6 +78,7 @@ void fast_release() {
   if (F.fq) cudaFree(F.fq);
   if (F.bq) cudaFree(F.bq);
   if (F.order) cudaFree(F.order);
+  if (F.chunk) cudaFree(F.chunk);
   if (F.mail) cudaFree(F.mail);
   if (F.ticket) cudaFree(F.ticket);
   if (F.ctl) cudaFree(F.ctl);
@@ -179,6 +181,26 @@ int fast_setup() {
     }
   CAP_CUDA(cudaMalloc(&F.order, sizeof(int2) * F.nblk));
   CAP_CUDA(cudaMemcpy(F.order, ord.data(), sizeof(int2) * F.nblk, cudaMemcpyHostToDevice));
+  {
+    // start (s, c, a) of every 32-cell chunk of the compact cell order
+    const DG& g = F.g;
+    std::vector<int4> ch((size_t)g.nchunk);
+    long long t = 0;
+    const int mmax = g.Ni + g.Nj - 2;
+    for (int s = 0; s < g.S; ++s)
+      for (int cc = 0; cc < g.Nk; ++cc) {
+        const int m = s - cc;
+        if (m < 0 || m > mmax) continue;
+        const int lo = m - (g.Nj - 1) > 0 ? m - (g.Nj - 1) : 0, hi = m < g.Ni - 1 ? m : g.Ni - 1;
+        for (long long q = (t + 31) / 32; q * 32 < t + (hi - lo + 1); ++q)
+          ch[(size_t)q] = make_int4(s, cc, lo + (int)(q * 32 - t), 0);
+        t += hi - lo + 1;
+      }
+    if (t != g.ncell) { fast_release(); set_error("hyperplane layout: cell count mismatch"); return CAPPGPU_E_ARG; }
+    CAP_CUDA(cudaMalloc(&F.chunk, sizeof(int4) * ch.size()));
+    CAP_CUDA(cudaMemcpy(F.chunk, ch.data(), sizeof(int4) * ch.size(), cudaMemcpyHostToDevice));
+    F.g.chunk = F.chunk;
+  }
   F.mail_n = (size_t)F.nblk * (BA + BC) * F.g.Nj * 3;   // up to 3 doubles per state
   CAP_CUDA(cudaMalloc(&F.mail, F.mail_n * sizeof(double)));
   fill_mail(c.st);
@@ -254,13 +276,68 @@ int run_wave(const Op& op, const int* skip = nullptr) {
 }
 
 // ------------------------------------------------------ vector kernels (D)
-// f(t, a, b, c) for every cell of the hyperplane layout.  A row (s, c) of
-// the layout holds the cells a = max(0, s-c-(Nj-1)) .. min(Ni-1, s-c) in
-// consecutive slots; one warp takes a row, its lanes the row's cells, so no
-// thread spends work on the layout's empty slots and the row index is the
-// only division.
-template <class F>
+// f(t, a, b, c) for every cell of the hyperplane layout, in the compact cell
+// order of dlayout.cuh: a warp takes U consecutive 32-cell chunks per pass,
+// lane L of chunk q the L-th cell after the chunk's recorded start, found by
+// walking along the rows (integer work only; a row ends at
+// a = min(Ni-1, s-c), the next non-empty row follows in closed form).  Every
+// lane owns a cell (the row-per-warp loop this replaces left a fifth of the
+// lanes idle at 128^3, and each FP64 warp instruction occupies its
+// sub-partition whatever the active lanes), and the U chunks' loads are in
+// flight together.
+__device__ __forceinline__ void walk_cells(const DG& g, int& s, int& c, int& a, int n) {
+  const int mmax = g.Ni + g.Nj - 2;
+  int m = s - c;
+  int hi = min(g.Ni - 1, m);
+  a += n;
+  while (a > hi) {
+    const int over = a - hi - 1;
+    ++c;
+    if (c >= g.Nk || c > s) {
+      ++s;
+      c = max(0, s - mmax);
+    }
+    m = s - c;
+    hi = min(g.Ni - 1, m);
+    a = max(0, m - (g.Nj - 1)) + over;
+  }
+}
+
+template <int U = 2, class F>
 __device__ __forceinline__ void for_cells(const DG& g, F&& f) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int q0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * U; q0 < g.nchunk; q0 += nw * U) {
+    long long t[U];
+    int A[U], B[U], C[U];
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int q = q0 + u;
+      ok[u] = q < g.nchunk && (long long)q * 32 + lane < g.ncell;
+      if (ok[u]) {
+        const int4 e = g.chunk[q];
+        int s = e.x, c = e.y, a = e.z;
+        walk_cells(g, s, c, a, lane);
+        t[u] = ((long long)s * g.Nk + c) * g.P + a;
+        A[u] = a;
+        B[u] = s - a - c;
+        C[u] = c;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (ok[u]) f(t[u], A[u], B[u], C[u]);
+  }
+}
+
+// The same over rows: one warp takes a row (s, c), its lanes the row's cells
+// a = max(0, s-c-(Nj-1)) .. min(Ni-1, s-c).  Idle lanes at row ends, but all
+// of a warp's loads fall in one row of every array; the FP32 kernels with
+// many neighbour loads per cell (k_pk_spmv_fx) or little work per cell
+// (k_dot_fx) measured faster this way than with the compact walk.
+template <class F>
+__device__ __forceinline__ void for_rows(const DG& g, F&& f) {
   const int lane = threadIdx.x & 31;
   const int nrow = g.S * g.Nk;
   const int step = (int)((gridDim.x * blockDim.x) >> 5);
@@ -295,13 +372,39 @@ __device__ double block_sum_fixed(const double* __restrict__ part, int n) {
   return r;
 }
 
+// a sum of block partials and a scalar formed from it by one thread, for
+// the many-block vector kernels: one warp sums (lane-strided, then a shuffle
+// tree), so the block issues few FP64 instructions -- on GB300 each holds its
+// sub-partition for 64 cycles whatever the active lanes, and an FP64
+// division per thread of every block cost more than the vector pass itself.
+// The one-block check kernel keeps the 256-thread tree above, which is
+// faster there.
+template <class Fn>
+__device__ double2 block_scalar2(const double* __restrict__ part, int n, Fn fn) {
+  __shared__ double sh[2];
+  if (threadIdx.x < 32) {
+    double v = 0.0;
+    for (int q = threadIdx.x; q < n; q += 32) v += part[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) {
+      sh[0] = v;
+      sh[1] = fn(v);
+    }
+  }
+  __syncthreads();
+  const double2 r = make_double2(sh[0], sh[1]);
+  __syncthreads();
+  return r;
+}
+
 // sk = res.z from the backward sweep's partials; bet = sk/s0
 // (pcg-sip.f90:229-233); pk = zk + bet pk (pcg-sip.f90:241)
 __global__ void k_pk_x(DG g, const double* __restrict__ zk, const double* __restrict__ pko, double* __restrict__ pkn,
                        const double* __restrict__ wpart, int nwp, double* scal, const int* ctl) {
   if (*(volatile const int*)ctl) return;
-  const double sk = block_sum_fixed(wpart, nwp);
-  const double bet = sk / scal[0];
+  const double2 sb = block_scalar2(wpart, nwp, [&](double v) { return v / scal[0]; });
+  const double sk = sb.x, bet = sb.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[1] = sk; scal[4] = bet; }
   for_cells(g, [&](long long t_, int a, int b, int c) {
     pkn[t_] = zk[t_] + bet * pko[t_];
@@ -314,8 +417,8 @@ __global__ void k_update_x(DG g, double* __restrict__ fi, double* __restrict__ r
                            const double* __restrict__ zz, const double* __restrict__ pin, double* scal,
                            double* pout, const int* ctl) {
   if (*(volatile const int*)ctl) return;
-  const double pkapk = block_sum_fixed(pin, kRedBlocks);
-  const double alf = scal[1] / pkapk;
+  const double2 sa = block_scalar2(pin, kRedBlocks, [&](double v) { return scal[1] / v; });
+  const double pkapk = sa.x, alf = sa.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[2] = pkapk; scal[3] = alf; }
   double v[1] = {0.0};
   for_cells(g, [&](long long t_, int a, int b, int c) {
@@ -423,14 +526,14 @@ __global__ void k_resid_d(DG g, const double* __restrict__ ae, const double* __r
 // ---------------------------------------- FP32 + FP64-refinement kernels
 // D-layout FP64 -> FP32 copy of the cells
 __global__ void k_d_to_f(DG g, const double* __restrict__ src, float* __restrict__ dst) {
-  for_cells(g, [&](long long t_, int a, int b, int c) {
+  for_cells<4>(g, [&](long long t_, int a, int b, int c) {
     dst[t_] = (float)src[t_];
   });
 }
 
 // x += dx (the refinement step)
 __global__ void k_add_f(DG g, double* __restrict__ x, const float* __restrict__ dx) {
-  for_cells(g, [&](long long t_, int a, int b, int c) {
+  for_cells<4>(g, [&](long long t_, int a, int b, int c) {
     x[t_] = x[t_] + (double)dx[t_];
   });
 }
@@ -439,7 +542,7 @@ __global__ void k_add_f(DG g, double* __restrict__ x, const float* __restrict__ 
 __global__ void k_dot_fx(DG g, const float* __restrict__ x, const float* __restrict__ y, double* part, const int* ctl) {
   if (*(volatile const int*)ctl) return;
   float acc = 0.0f;
-  for_cells(g, [&](long long t_, int a, int b, int c) {
+  for_rows(g, [&](long long t_, int a, int b, int c) {
     acc += x[t_] * y[t_];
   });
   double v[1] = {(double)acc};
@@ -453,12 +556,12 @@ __global__ void k_pk_spmv_fx(DG g, const float* __restrict__ ae, const float* __
                              const float* __restrict__ pko, float* __restrict__ pkn, float* __restrict__ zz,
                              const double* __restrict__ pin, double* scal, double* pout, const int* ctl) {
   if (*(volatile const int*)ctl) return;
-  const double sk = block_sum_fixed(pin, kRedBlocks);
-  const double betd = sk / scal[0];
+  const double2 sb = block_scalar2(pin, kRedBlocks, [&](double v) { return v / scal[0]; });
+  const double sk = sb.x, betd = sb.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[1] = sk; scal[4] = betd; }
   const float bet = (float)betd;
   float acc = 0.0f;
-  for_cells(g, [&](long long t_, int a, int b, int c) {
+  for_rows(g, [&](long long t_, int a, int b, int c) {
     const long long P = t_;
     auto pnew = [&](long long q) { return zk[q] + bet * pko[q]; };
     const float pP = pnew(P);
@@ -481,12 +584,12 @@ __global__ void k_update_fx(DG g, float* __restrict__ x, float* __restrict__ r, 
                             const float* __restrict__ zz, const double* __restrict__ pin, double* scal, double* pout,
                             const int* ctl) {
   if (*(volatile const int*)ctl) return;
-  const double pkapk = block_sum_fixed(pin, kRedBlocks);
-  const double alfd = scal[1] / pkapk;
+  const double2 sa = block_scalar2(pin, kRedBlocks, [&](double v) { return scal[1] / v; });
+  const double pkapk = sa.x, alfd = sa.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[2] = pkapk; scal[3] = alfd; }
   const float alf = (float)alfd;
   float acc = 0.0f;
-  for_cells(g, [&](long long t_, int a, int b, int c) {
+  for_cells<4>(g, [&](long long t_, int a, int b, int c) {
     x[t_] = x[t_] + alf * pk[t_];
     const float rr = r[t_] - alf * zz[t_];
     r[t_] = rr;
@@ -625,7 +728,7 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
       if ((rc = run_wave<SipBwdD, true>(bwd, F.ctl))) return rc;
       double* pko = F.d[cur ? D_PK1 : D_PK0];
       double* pkn = F.d[cur ? D_PK0 : D_PK1];
-      launch(k_pk_x, grid_for(F.g.size()), kThreads, c.st, F.g, (const double*)F.d[D_Z], (const double*)pko, pkn,
+      launch(k_pk_x, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_Z], (const double*)pko, pkn,
              (const double*)F.wpart, F.nblk, c.dscal, (const int*)F.ctl);
       launch(k_spmv_x, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
              (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
@@ -734,7 +837,7 @@ int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
   if ((rc = to_d(fif, D_FI))) return rc;
   const DG& g = F.g;
   for (int q = 0; q < 7; ++q)
-    launch(k_d_to_f, grid_for(g.size()), kThreads, c.st, g, (const double*)F.d[D_AE + q], G.e[E_AE + q]);
+    launch(k_d_to_f, grid_for(g.ncell / 4), kThreads, c.st, g, (const double*)F.d[D_AE + q], G.e[E_AE + q]);
   CAP_CHECK_LAUNCH();
   {   // FP32 SIP factorisation
     SipFactorF op;
@@ -765,11 +868,11 @@ int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
            (const double*)F.d[D_AP], (const double*)F.d[D_SU], (const double*)F.d[D_FI], (const double*)c.f[fif],
            F.d[D_RES], c.partials);
     launch(k_cg_scalars, 1, 32, c.st, 3, (const double*)c.partials, kRedBlocks, c.dscal);
-    launch(k_d_to_f, grid_for(g.size()), kThreads, c.st, g, (const double*)F.d[D_RES], G.e[E_R]);
+    launch(k_d_to_f, grid_for(g.ncell / 4), kThreads, c.st, g, (const double*)F.d[D_RES], G.e[E_R]);
     CAP_CHECK_LAUNCH();
     if ((rc = run_wave<SipFwdF, false>(fwd))) return rc;
     if ((rc = run_wave<SipBwdF, true>(bwd))) return rc;
-    launch(k_add_f, grid_for(g.size()), kThreads, c.st, g, F.d[D_FI], (const float*)G.e[E_Z]);
+    launch(k_add_f, grid_for(g.ncell / 4), kThreads, c.st, g, F.d[D_FI], (const float*)G.e[E_Z]);
     CAP_CHECK_LAUNCH();
     CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 6, sizeof(double), cudaMemcpyDeviceToHost, c.st));
     if ((rc = sync_status())) return rc;
@@ -827,7 +930,7 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
   if ((rc = to_d(fif, D_FI))) return rc;
   const DG& g = F.g;
   for (int q = 0; q < 7; ++q)
-    launch(k_d_to_f, grid_for(g.size()), kThreads, c.st, g, (const double*)F.d[D_AE + q], G.e[E_AE + q]);
+    launch(k_d_to_f, grid_for(g.ncell / 4), kThreads, c.st, g, (const double*)F.d[D_AE + q], G.e[E_AE + q]);
   CAP_CHECK_LAUNCH();
   {   // FP32 SIP factorisation
     SipFactorF op;
@@ -867,7 +970,7 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     if (resl / (res0 + CAP_SMALL) < resmax) { done = true; break; }
     if (total >= ns) break;
     // inner FP32 conjugate gradients on A d = r, d = 0
-    launch(k_d_to_f, grid_for(g.size()), kThreads, c.st, g, (const double*)F.d[D_RES], G.e[E_R]);
+    launch(k_d_to_f, grid_for(g.ncell / 4), kThreads, c.st, g, (const double*)F.d[D_RES], G.e[E_R]);
     CAP_CHECK_LAUNCH();
     CAP_CUDA(cudaMemsetAsync(G.e[E_X], 0, nf, c.st));
     CAP_CUDA(cudaMemsetAsync(G.e[E_P0], 0, nf, c.st));
@@ -911,7 +1014,7 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     }
     total += hctl[1] ? hctl[1] : budget;
     if (hctl[2]) { bad = true; break; }
-    launch(k_add_f, grid_for(g.size()), kThreads, c.st, g, F.d[D_FI], (const float*)G.e[E_X]);
+    launch(k_add_f, grid_for(g.ncell / 4), kThreads, c.st, g, F.d[D_FI], (const float*)G.e[E_X]);
     CAP_CHECK_LAUNCH();
   }
   if ((rc = from_d(D_FI, fif))) return rc;
