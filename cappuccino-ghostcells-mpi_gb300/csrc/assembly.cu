@@ -38,9 +38,132 @@ __device__ inline float sqrt_(float x) { return sqrtf(x); }
 template <typename R>
 __device__ inline R dmax_(R a, R b) { return a > b ? a : b; }
 
-// fluxuvw-overrelaxed-correction.f90:121-637 for one face inp
-template <typename R>
-__global__ void k_fluxuvw_faces(Dims d, Box b, FluxArgs A) {
+// ------------------------------------------------ per-face geometry cache
+// The face kernels of the momentum and pressure assembly spend most of
+// their FP64 work on quantities of the grid alone: the distance of the two
+// cell centres and the face area (two square roots), the unit normal, the
+// centre-line unit vector and their cosine, area/volume ratios and the
+// offset of the face centre from the interpolation point (ten divisions).
+// GB300 runs FP64 divisions and square roots slowly, and these values do
+// not change between time steps, so the FP64 forms read them from arrays
+// built once per grid (rebuilt when a geometry field is written).  Each
+// array holds the very expression the reference evaluates per face, with
+// the same operation order, so the cached forms give the same bits.
+enum GeoQ { GQ_XPN, GQ_YPN, GQ_ZPN, GQ_DPN, GQ_ARE, GQ_COSTN, GQ_AVX, GQ_AVY, GQ_AVZ, GQ_DXF, GQ_DYF, GQ_DZF, GQ_N };
+
+struct FaceGeoPtrs {
+  const double* q[GQ_N];
+};
+
+struct FaceGeoCache {
+  double* buf[3] = {};
+  unsigned long long gen[3] = {0, 0, 0};
+  int nijk = 0;
+};
+FaceGeoCache g_fg;
+
+void facegeo_free() {
+  for (auto& p : g_fg.buf) { if (p) cudaFree(p); p = nullptr; }
+  g_fg = FaceGeoCache();
+}
+
+// PISO_assemble_pressure_eq.f90:60-120 / fluxuvw-overrelaxed-correction.f90:
+// 135-205: the geometric part of one face
+__global__ void k_face_geo(Dims d, Box b, int idew, int idns, int idtb, const double* __restrict__ arvx,
+                           const double* __restrict__ arvy, const double* __restrict__ arvz,
+                           const double* __restrict__ fif, const double* __restrict__ x,
+                           const double* __restrict__ y, const double* __restrict__ z,
+                           const double* __restrict__ xc, const double* __restrict__ yc,
+                           const double* __restrict__ zc, double* __restrict__ out) {
+  const size_t n = (size_t)d.nijk;
+  BOX_LOOP(b) {
+    int i, j, k;
+    b.at(t_, i, j, k);
+    const int inp = ixk(d, i, j, k);
+    const int ine = inp + idew, ins = inp - idns, inb = inp - idtb, inbs = inb - idns;
+    const double fxe = fif[inp], fxp = 1.0 - fxe;
+    const double xf = 0.25 * (x[inp] + x[ins] + x[inb] + x[inbs]);
+    const double yf = 0.25 * (y[inp] + y[ins] + y[inb] + y[inbs]);
+    const double zf = 0.25 * (z[inp] + z[ins] + z[inb] + z[inbs]);
+    const double xi = xc[inp] * fxp + xc[ine] * fxe;
+    const double yi = yc[inp] * fxp + yc[ine] * fxe;
+    const double zi = zc[inp] * fxp + zc[ine] * fxe;
+    const double xpn = xc[ine] - xc[inp], ypn = yc[ine] - yc[inp], zpn = zc[ine] - zc[inp];
+    const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    const double ixi1 = xpn / dpn, ixi2 = ypn / dpn, ixi3 = zpn / dpn;
+    const double arx = arvx[inp], ary = arvy[inp], arz = arvz[inp];
+    const double are = sqrt(arx * arx + ary * ary + arz * arz);
+    const double vole = xpn * arx + ypn * ary + zpn * arz;
+    const double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+    const double costheta = nxx * ixi1 + nyy * ixi2 + nzz * ixi3;
+    out[GQ_XPN * n + inp] = xpn;
+    out[GQ_YPN * n + inp] = ypn;
+    out[GQ_ZPN * n + inp] = zpn;
+    out[GQ_DPN * n + inp] = dpn;
+    out[GQ_ARE * n + inp] = are;
+    out[GQ_COSTN * n + inp] = costheta;
+    out[GQ_AVX * n + inp] = arx / vole;
+    out[GQ_AVY * n + inp] = ary / vole;
+    out[GQ_AVZ * n + inp] = arz / vole;
+    out[GQ_DXF * n + inp] = xf - xi;
+    out[GQ_DYF * n + inp] = yf - yi;
+    out[GQ_DZF * n + inp] = zf - zi;
+  }
+}
+
+// The cache of the face direction given by the arguments, built if stale;
+// false when the arguments are not one of the grid's three face sets (the
+// caller then evaluates the geometry itself).
+static int face_geo(int idew, int idns, int idtb, int arvx, int arvy, int arvz, int fif, FaceGeoPtrs* out,
+                    bool* ok) {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  *ok = false;
+  int dir = -1;
+  if (idew == d.nj && idns == 1 && idtb == d.nij && arvx == CAP_AR1X && arvy == CAP_AR1Y && arvz == CAP_AR1Z &&
+      fif == CAP_FX)
+    dir = 0;
+  else if (idew == 1 && idns == d.nij && idtb == d.nj && arvx == CAP_AR2X && arvy == CAP_AR2Y &&
+           arvz == CAP_AR2Z && fif == CAP_FY)
+    dir = 1;
+  else if (idew == d.nij && idns == d.nj && idtb == 1 && arvx == CAP_AR3X && arvy == CAP_AR3Y &&
+           arvz == CAP_AR3Z && fif == CAP_FZ)
+    dir = 2;
+  if (dir < 0 || !c.face_geo) return CAPPGPU_OK;
+  const size_t n = (size_t)d.nijk;
+  if (g_fg.nijk != d.nijk) {
+    facegeo_free();
+    g_fg.nijk = d.nijk;
+  }
+  if (!g_fg.buf[dir]) {
+    if (cudaMalloc(&g_fg.buf[dir], GQ_N * n * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      g_fg.buf[dir] = nullptr;
+      return CAPPGPU_OK;   // no room: evaluate per call
+    }
+    CAP_CUDA(cudaMemsetAsync(g_fg.buf[dir], 0, GQ_N * n * sizeof(double), c.st));
+    g_fg.gen[dir] = 0;
+  }
+  if (g_fg.gen[dir] != c.geo_gen) {
+    double** F = c.f;
+    // every face any caller visits: the pressure equation's box
+    Box b{2, d.nimm, 2, d.njmm, 2, d.nkmm};
+    launch(k_face_geo, grid_for(b.count()), kThreads, c.st, d, b, idew, idns, idtb, (const double*)F[arvx],
+           (const double*)F[arvy], (const double*)F[arvz], (const double*)F[fif], (const double*)F[CAP_X],
+           (const double*)F[CAP_Y], (const double*)F[CAP_Z], (const double*)F[CAP_XC], (const double*)F[CAP_YC],
+           (const double*)F[CAP_ZC], g_fg.buf[dir]);
+    CAP_CHECK_LAUNCH();
+    g_fg.gen[dir] = c.geo_gen;
+  }
+  for (int q = 0; q < GQ_N; ++q) out->q[q] = g_fg.buf[dir] + q * n;
+  *ok = true;
+  return CAPPGPU_OK;
+}
+
+// fluxuvw-overrelaxed-correction.f90:121-637 for one face inp; GEO: the
+// geometric terms come from the per-face cache (FP64 form only)
+template <typename R, bool GEO>
+__global__ void k_fluxuvw_faces(Dims d, Box b, FluxArgs A, FaceGeoPtrs G) {
   BOX_LOOP(b) {
     int i, j, k;
     b.at(t_, i, j, k);
@@ -50,43 +173,53 @@ __global__ void k_fluxuvw_faces(Dims d, Box b, FluxArgs A) {
     R fxe = R(A.fif[inp]), fxp = R(1.0) - fxe;
     R fxpw = R(A.fif[inw]), fxw = R(1.0) - fxpw;
     R fxee = R(A.fif[ine]), fxew = R(1.0) - fxee;
-    R xpn = R(A.xc[ine]) - R(A.xc[inp]), ypn = R(A.yc[ine]) - R(A.yc[inp]), zpn = R(A.zc[ine]) - R(A.zc[inp]);
-    R dpn = sqrt_(xpn * xpn + ypn * ypn + zpn * zpn);
     R arx = R(A.arvx[inp]), ary = R(A.arvy[inp]), arz = R(A.arvz[inp]);
-    R are = sqrt_(arx * arx + ary * ary + arz * arz);
+    R xpn, ypn, zpn, dpn, are, avx, avy, avz, dxf, dyf, dzf;
+    if constexpr (GEO) {
+      xpn = G.q[GQ_XPN][inp]; ypn = G.q[GQ_YPN][inp]; zpn = G.q[GQ_ZPN][inp];
+      dpn = G.q[GQ_DPN][inp]; are = G.q[GQ_ARE][inp];
+      avx = G.q[GQ_AVX][inp]; avy = G.q[GQ_AVY][inp]; avz = G.q[GQ_AVZ][inp];
+      dxf = G.q[GQ_DXF][inp]; dyf = G.q[GQ_DYF][inp]; dzf = G.q[GQ_DZF][inp];
+    } else {
+      xpn = R(A.xc[ine]) - R(A.xc[inp]); ypn = R(A.yc[ine]) - R(A.yc[inp]); zpn = R(A.zc[ine]) - R(A.zc[inp]);
+      dpn = sqrt_(xpn * xpn + ypn * ypn + zpn * zpn);
+      are = sqrt_(arx * arx + ary * ary + arz * arz);
+      R vole = xpn * arx + ypn * ary + zpn * arz;
+      avx = arx / vole; avy = ary / vole; avz = arz / vole;
+      R xf = R(0.25) * (R(A.x[inp]) + R(A.x[ins]) + R(A.x[inb]) + R(A.x[inbs]));
+      R yf = R(0.25) * (R(A.y[inp]) + R(A.y[ins]) + R(A.y[inb]) + R(A.y[inbs]));
+      R zf = R(0.25) * (R(A.z[inp]) + R(A.z[ins]) + R(A.z[inb]) + R(A.z[inbs]));
+      R xi = R(A.xc[inp]) * fxp + R(A.xc[ine]) * fxe;
+      R yi = R(A.yc[inp]) * fxp + R(A.yc[ine]) * fxe;
+      R zi = R(A.zc[inp]) * fxp + R(A.zc[ine]) * fxe;
+      dxf = xf - xi; dyf = yf - yi; dzf = zf - zi;
+    }
     const R costn = R(1.0);  // orthogonal correction (:178)
-    R vole = xpn * arx + ypn * ary + zpn * arz;
     R d1x = costn, d1y = costn, d1z = costn;
     R d2x = xpn * costn, d2y = ypn * costn, d2z = zpn * costn;
     R game = (R(A.vis[inp]) * fxp + R(A.vis[ine]) * fxe);
-    R xf = R(0.25) * (R(A.x[inp]) + R(A.x[ins]) + R(A.x[inb]) + R(A.x[inbs]));
-    R yf = R(0.25) * (R(A.y[inp]) + R(A.y[ins]) + R(A.y[inb]) + R(A.y[inbs]));
-    R zf = R(0.25) * (R(A.z[inp]) + R(A.z[ins]) + R(A.z[inb]) + R(A.z[inbs]));
-    R xi = R(A.xc[inp]) * fxp + R(A.xc[ine]) * fxe;
-    R yi = R(A.yc[inp]) * fxp + R(A.yc[ine]) * fxe;
-    R zi = R(A.zc[inp]) * fxp + R(A.zc[ine]) * fxe;
     const double *u = A.u, *v = A.v, *w = A.w;
     R duxi = R(A.gux[inp]) * fxp + R(A.gux[ine]) * fxe;
     R duyi = R(A.guy[inp]) * fxp + R(A.guy[ine]) * fxe;
     R duzi = R(A.guz[inp]) * fxp + R(A.guz[ine]) * fxe;
     R du = R(u[ine]) - R(u[inp]) - duxi * d2x - duyi * d2y - duzi * d2z;
-    R duxii = duxi * d1x + arx / vole * du;
-    R duyii = duyi * d1y + ary / vole * du;
-    R duzii = duzi * d1z + arz / vole * du;
+    R duxii = duxi * d1x + avx * du;
+    R duyii = duyi * d1y + avy * du;
+    R duzii = duzi * d1z + avz * du;
     R dvxi = R(A.gvx[inp]) * fxp + R(A.gvx[ine]) * fxe;
     R dvyi = R(A.gvy[inp]) * fxp + R(A.gvy[ine]) * fxe;
     R dvzi = R(A.gvz[inp]) * fxp + R(A.gvz[ine]) * fxe;
     R dv = R(v[ine]) - R(v[inp]) - dvxi * d2x - dvyi * d2y - dvzi * d2z;
-    R dvxii = dvxi * d1x + arx / vole * dv;
-    R dvyii = dvyi * d1y + ary / vole * dv;
-    R dvzii = dvzi * d1z + arz / vole * dv;
+    R dvxii = dvxi * d1x + avx * dv;
+    R dvyii = dvyi * d1y + avy * dv;
+    R dvzii = dvzi * d1z + avz * dv;
     R dwxi = R(A.gwx[inp]) * fxp + R(A.gwx[ine]) * fxe;
     R dwyi = R(A.gwy[inp]) * fxp + R(A.gwy[ine]) * fxe;
     R dwzi = R(A.gwz[inp]) * fxp + R(A.gwz[ine]) * fxe;
     R dw = R(w[ine]) - R(w[inp]) - dwxi * d2x - dwyi * d2y - dwzi * d2z;
-    R dwxii = dwxi * d1x + arx / vole * dw;
-    R dwyii = dwyi * d1y + ary / vole * dw;
-    R dwzii = dwzi * d1z + arz / vole * dw;
+    R dwxii = dwxi * d1x + avx * dw;
+    R dwyii = dwyi * d1y + avy * dw;
+    R dwzii = dwzi * d1z + avz * dw;
     R fdue = game * ((duxii + duxii) * arx + (duyii + dvxii) * ary + (duzii + dwxii) * arz);
     R fdve = game * ((duyii + dvxii) * arx + (dvyii + dvyii) * ary + (dvzii + dwyii) * arz);
     R fdwe = game * ((duzii + dwxii) * arx + (dwyii + dvzii) * ary + (dwzii + dwzii) * arz);
@@ -105,9 +238,9 @@ __global__ void k_fluxuvw_faces(Dims d, Box b, FluxArgs A) {
     R fwuds = cp * R(w[inp]) + ce * R(w[ine]);
     R fuhigh = R(0.0), fvhigh = R(0.0), fwhigh = R(0.0);
     if (A.lcds) {
-      R ue = R(u[inp]) * fxp + R(u[ine]) * fxe + (duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi));
-      R ve = R(v[inp]) * fxp + R(v[ine]) * fxe + (dvxi * (xf - xi) + dvyi * (yf - yi) + dvzi * (zf - zi));
-      R we = R(w[inp]) * fxp + R(w[ine]) * fxe + (dwxi * (xf - xi) + dwyi * (yf - yi) + dwzi * (zf - zi));
+      R ue = R(u[inp]) * fxp + R(u[ine]) * fxe + (duxi * dxf + duyi * dyf + duzi * dzf);
+      R ve = R(v[inp]) * fxp + R(v[ine]) * fxe + (dvxi * dxf + dvyi * dyf + dvzi * dzf);
+      R we = R(w[inp]) * fxp + R(w[ine]) * fxe + (dwxi * dxf + dwyi * dyf + dwzi * dzf);
       fuhigh = flcf * ue; fvhigh = flcf * ve; fwhigh = flcf * we;
     }
     if (A.lcds4 && (A.idew == d.nj || A.idew == 1)) {
@@ -117,6 +250,9 @@ __global__ void k_fluxuvw_faces(Dims d, Box b, FluxArgs A) {
       fuhigh = flcf * ue; fvhigh = flcf * ve; fwhigh = flcf * we;
     }
     if (A.lluds) {
+      R xf = R(0.25) * (R(A.x[inp]) + R(A.x[ins]) + R(A.x[inb]) + R(A.x[inbs]));
+      R yf = R(0.25) * (R(A.y[inp]) + R(A.y[ins]) + R(A.y[inb]) + R(A.y[inbs]));
+      R zf = R(0.25) * (R(A.z[inp]) + R(A.z[ins]) + R(A.z[inb]) + R(A.z[inbs]));
       R dxc = xf - R(A.xc[inp]), dyc = yf - R(A.yc[inp]), dzc = zf - R(A.zc[inp]);
       R dxe = R(A.xc[ine]) - xf, dye = R(A.yc[ine]) - yf, dze = R(A.zc[ine]) - zf;
       R dfidx_u = R(A.gud[inw]) * fxw + R(A.gud[inp]) * fxpw;
@@ -215,10 +351,18 @@ int fluxuvw(int idew, int idns, int idtb, int arvx, int arvy, int arvz, int fif,
              P.gds[CAP_IU - 1], P.zero, idew, idns, idtb,
              P.lcds, P.lcds4, P.lluds, P.lquds, P.flux_limiter, P.lsmart, P.lavl, P.lmuscl, P.lumist, P.lgamma};
   // precision modes 1-2 assemble in FP32 arithmetic (FP64 storage)
-  if (c.fp32(4))
-    launch(k_fluxuvw_faces<float>, grid_for(b.count()), kThreads, c.st, d, b, A);
-  else
-    launch(k_fluxuvw_faces<double>, grid_for(b.count()), kThreads, c.st, d, b, A);
+  FaceGeoPtrs G{};
+  bool geo = false;
+  if (c.fp32(4)) {
+    launch(k_fluxuvw_faces<float, false>, grid_for(b.count()), kThreads, c.st, d, b, A, G);
+  } else {
+    int rc = face_geo(idew, idns, idtb, arvx, arvy, arvz, fif, &G, &geo);
+    if (rc) return rc;
+    if (geo)
+      launch(k_fluxuvw_faces<double, true>, grid_for(b.count()), kThreads, c.st, d, b, A, G);
+    else
+      launch(k_fluxuvw_faces<double, false>, grid_for(b.count()), kThreads, c.st, d, b, A, G);
+  }
   Box b2{2, d.nimm, 2, d.njmm, 2, d.nkmm};
   launch(k_add_staged, grid_for(b2.count()), kThreads, c.st, d, b2, idew, F[CAP_SU], F[CAP_SV], F[CAP_SW], F[CAP_BP],
                                                             F[CAP_BT], F[CAP_BB]);
@@ -438,30 +582,41 @@ struct PeqArgs {
   int idew, idns, idtb, ipc;
 };
 
-// PISO_assemble_pressure_eq.f90:48-237 for one face
-template <typename R>
-__global__ void k_piso_peq_faces(Dims d, Box b, PeqArgs A) {
+// PISO_assemble_pressure_eq.f90:48-237 for one face; GEO: the geometric
+// terms come from the per-face cache (FP64 form only)
+template <typename R, bool GEO>
+__global__ void k_piso_peq_faces(Dims d, Box b, PeqArgs A, FaceGeoPtrs G) {
   BOX_LOOP(b) {
     int i, j, k;
     b.at(t_, i, j, k);
     int inp = ixk(d, i, j, k);
-    int ine = inp + A.idew, ins = inp - A.idns, inb = inp - A.idtb, inbs = inb - A.idns;
+    int ine = inp + A.idew;
     R fxe = R(A.fif[inp]), fxp = R(1.0) - fxe;
-    R xf = R(0.25) * (R(A.x[inp]) + R(A.x[ins]) + R(A.x[inb]) + R(A.x[inbs]));
-    R yf = R(0.25) * (R(A.y[inp]) + R(A.y[ins]) + R(A.y[inb]) + R(A.y[inbs]));
-    R zf = R(0.25) * (R(A.z[inp]) + R(A.z[ins]) + R(A.z[inb]) + R(A.z[inbs]));
-    R xi = R(A.xc[inp]) * fxp + R(A.xc[ine]) * fxe;
-    R yi = R(A.yc[inp]) * fxp + R(A.yc[ine]) * fxe;
-    R zi = R(A.zc[inp]) * fxp + R(A.zc[ine]) * fxe;
-    R xpn = R(A.xc[ine]) - R(A.xc[inp]), ypn = R(A.yc[ine]) - R(A.yc[inp]), zpn = R(A.zc[ine]) - R(A.zc[inp]);
-    R dpn = sqrt_(xpn * xpn + ypn * ypn + zpn * zpn);
-    R ixi1 = xpn / dpn, ixi2 = ypn / dpn, ixi3 = zpn / dpn;
     R arx = R(A.arvx[inp]), ary = R(A.arvy[inp]), arz = R(A.arvz[inp]);
-    R are = sqrt_(arx * arx + ary * ary + arz * arz);
-    R vole = xpn * arx + ypn * ary + zpn * arz;
-    R nxx = arx / are, nyy = ary / are, nzz = arz / are;
-    R costheta = nxx * ixi1 + nyy * ixi2 + nzz * ixi3;
-    R costn = costheta;
+    R xpn, ypn, zpn, dpn, are, costn, avx, avy, avz, dxf, dyf, dzf;
+    if constexpr (GEO) {
+      xpn = G.q[GQ_XPN][inp]; ypn = G.q[GQ_YPN][inp]; zpn = G.q[GQ_ZPN][inp];
+      dpn = G.q[GQ_DPN][inp]; are = G.q[GQ_ARE][inp]; costn = G.q[GQ_COSTN][inp];
+      avx = G.q[GQ_AVX][inp]; avy = G.q[GQ_AVY][inp]; avz = G.q[GQ_AVZ][inp];
+      dxf = G.q[GQ_DXF][inp]; dyf = G.q[GQ_DYF][inp]; dzf = G.q[GQ_DZF][inp];
+    } else {
+      int ins = inp - A.idns, inb = inp - A.idtb, inbs = inb - A.idns;
+      R xf = R(0.25) * (R(A.x[inp]) + R(A.x[ins]) + R(A.x[inb]) + R(A.x[inbs]));
+      R yf = R(0.25) * (R(A.y[inp]) + R(A.y[ins]) + R(A.y[inb]) + R(A.y[inbs]));
+      R zf = R(0.25) * (R(A.z[inp]) + R(A.z[ins]) + R(A.z[inb]) + R(A.z[inbs]));
+      R xi = R(A.xc[inp]) * fxp + R(A.xc[ine]) * fxe;
+      R yi = R(A.yc[inp]) * fxp + R(A.yc[ine]) * fxe;
+      R zi = R(A.zc[inp]) * fxp + R(A.zc[ine]) * fxe;
+      xpn = R(A.xc[ine]) - R(A.xc[inp]); ypn = R(A.yc[ine]) - R(A.yc[inp]); zpn = R(A.zc[ine]) - R(A.zc[inp]);
+      dpn = sqrt_(xpn * xpn + ypn * ypn + zpn * zpn);
+      R ixi1 = xpn / dpn, ixi2 = ypn / dpn, ixi3 = zpn / dpn;
+      are = sqrt_(arx * arx + ary * ary + arz * arz);
+      R vole = xpn * arx + ypn * ary + zpn * arz;
+      R nxx = arx / are, nyy = ary / are, nzz = arz / are;
+      costn = nxx * ixi1 + nyy * ixi2 + nzz * ixi3;
+      avx = arx / vole; avy = ary / vole; avz = arz / vole;
+      dxf = xf - xi; dyf = yf - yi; dzf = zf - zi;
+    }
     R d1x = costn, d1y = costn, d1z = costn;
     R d2x = xpn * costn, d2y = ypn * costn, d2z = zpn * costn;
     R dene = R(A.den[inp]) * fxp + R(A.den[ine]) * fxe;
@@ -474,26 +629,26 @@ __global__ void k_piso_peq_faces(Dims d, Box b, PeqArgs A) {
       R dfiyi = R(A.gpy[inp]) * fxp + R(A.gpy[ine]) * fxe;
       R dfizi = R(A.gpz[inp]) * fxp + R(A.gpz[ine]) * fxe;
       R dp = R(A.p[ine]) - R(A.p[inp]) - (dfixi * d2x + dfiyi * d2y + dfizi * d2z);
-      R dfixii = dfixi * d1x + arx / vole * dp;
-      R dfiyii = dfiyi * d1y + ary / vole * dp;
-      R dfizii = dfizi * d1z + arz / vole * dp;
+      R dfixii = dfixi * d1x + avx * dp;
+      R dfiyii = dfiyi * d1y + avy * dp;
+      R dfizii = dfizi * d1z + avz * dp;
       R fdfie = game * (dfixii * arx + dfiyii * ary + dfizii * arz);
-      R fdfii = game * are / dpn * (dfixi * xpn + dfiyi * ypn + dfizi * zpn);
+      R fdfii = acf * (dfixi * xpn + dfiyi * ypn + dfizi * zpn);   // game*are/dpn*(...)
       R suadd = fdfie - fdfii;
       A.su[inp] = R(A.su[inp]) + suadd;
       A.bp[inp] = suadd;
       R duxi = R(A.gux[inp]) * fxp + R(A.gux[ine]) * fxe;
       R duyi = R(A.guy[inp]) * fxp + R(A.guy[ine]) * fxe;
       R duzi = R(A.guz[inp]) * fxp + R(A.guz[ine]) * fxe;
-      R ui = R(A.u[inp]) * fxp + R(A.u[ine]) * fxe + duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi);
+      R ui = R(A.u[inp]) * fxp + R(A.u[ine]) * fxe + duxi * dxf + duyi * dyf + duzi * dzf;
       duxi = R(A.gvx[inp]) * fxp + R(A.gvx[ine]) * fxe;
       duyi = R(A.gvy[inp]) * fxp + R(A.gvy[ine]) * fxe;
       duzi = R(A.gvz[inp]) * fxp + R(A.gvz[ine]) * fxe;
-      R vi = R(A.v[inp]) * fxp + R(A.v[ine]) * fxe + duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi);
+      R vi = R(A.v[inp]) * fxp + R(A.v[ine]) * fxe + duxi * dxf + duyi * dyf + duzi * dzf;
       duxi = R(A.gwx[inp]) * fxp + R(A.gwx[ine]) * fxe;
       duyi = R(A.gwy[inp]) * fxp + R(A.gwy[ine]) * fxe;
       duzi = R(A.gwz[inp]) * fxp + R(A.gwz[ine]) * fxe;
-      R wi = R(A.w[inp]) * fxp + R(A.w[ine]) * fxe + duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi);
+      R wi = R(A.w[inp]) * fxp + R(A.w[ine]) * fxe + duxi * dxf + duyi * dyf + duzi * dzf;
       A.fcf[inp] = dene * (ui * arx + vi * ary + wi * arz);
     }
   }
@@ -522,10 +677,18 @@ int piso_assemble(int idew, int idns, int idtb, int arvx, int arvy, int arvz, in
             F[CAP_GRADW_X], F[CAP_GRADW_Y], F[CAP_GRADW_Z], F[CAP_GRADP_X], F[CAP_GRADP_Y], F[CAP_GRADP_Z],
             idew, idns, idtb, ipc};
   Box b{2, d.nimm, 2, d.njmm, 2, d.nkmm};
-  if (c.fp32(4))
-    launch(k_piso_peq_faces<float>, grid_for(b.count()), kThreads, c.st, d, b, A);
-  else
-    launch(k_piso_peq_faces<double>, grid_for(b.count()), kThreads, c.st, d, b, A);
+  FaceGeoPtrs G{};
+  bool geo = false;
+  if (c.fp32(4)) {
+    launch(k_piso_peq_faces<float, false>, grid_for(b.count()), kThreads, c.st, d, b, A, G);
+  } else {
+    int rc = face_geo(idew, idns, idtb, arvx, arvy, arvz, fif, &G, &geo);
+    if (rc) return rc;
+    if (geo)
+      launch(k_piso_peq_faces<double, true>, grid_for(b.count()), kThreads, c.st, d, b, A, G);
+    else
+      launch(k_piso_peq_faces<double, false>, grid_for(b.count()), kThreads, c.st, d, b, A, G);
+  }
   CAP_CHECK_LAUNCH();
   if (ipc > 0) {
     Box bi{3, d.nimm, 3, d.njmm, 3, d.nkmm};

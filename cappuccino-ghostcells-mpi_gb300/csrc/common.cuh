@@ -76,6 +76,7 @@ struct Ctx {
   cappgpu_solve_report p_rep{};        // its report
   cudaEvent_t ev[4] = {};
   int wave_impl = 1;                   // 1 persistent wavefront, 0 one launch per hyperplane
+  int face_geo = 1;                    // 1: FP64 face kernels read the per-face geometry cache
   int tight_correctors = 0;            // 1: every PISO corrector solves p to reltol, not only the last
   int cg_batch = 4;                    // CG iterations launched between two host reads of the exit test
   int inner_drop = 4;                  // FP32 inner CG stops at 10^-inner_drop of the outer residual
@@ -83,10 +84,15 @@ struct Ctx {
                                        // 4 coefficient assembly, 8 velocity gradients
   bool fp32(int part) const { return precision >= 1 && (fp32_parts & part) != 0; }
   int precision = 0;                   // pcgsip: 0 FP64 plain, 1 FP32 preconditioned CG in FP64 refinement
+  unsigned long long geo_gen = 1;      // bumped whenever a grid-geometry field may have changed
 };
 
 Ctx& ctx();
 void set_error(const char* fmt, ...);
+// record a write into field q: a write into a grid-geometry field (nodes,
+// centres, face areas, interpolation factors) invalidates the per-face
+// geometry derived from it
+void note_write(int q);
 int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 
 #define CAP_CUDA(call)                                                     \

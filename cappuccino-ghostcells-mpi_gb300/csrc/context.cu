@@ -72,9 +72,23 @@ static const char* kFieldNames[CAP_NFIELDS] = {
     "gradu_x", "gradu_y", "gradu_z", "gradv_x", "gradv_y", "gradv_z",
     "gradw_x", "gradw_y", "gradw_z", "gradp_x", "gradp_y", "gradp_z"};
 
+void note_write(int q) {
+  switch (q) {
+    case CAP_X: case CAP_Y: case CAP_Z: case CAP_XC: case CAP_YC: case CAP_ZC:
+    case CAP_FX: case CAP_FY: case CAP_FZ:
+    case CAP_AR1X: case CAP_AR1Y: case CAP_AR1Z: case CAP_AR2X: case CAP_AR2Y: case CAP_AR2Z:
+    case CAP_AR3X: case CAP_AR3Y: case CAP_AR3Z:
+      ++ctx().geo_gen;
+      break;
+    default:
+      break;
+  }
+}
+
 static void free_all() {
   fast_free();
   learned_free();
+  facegeo_free();
   Ctx& c = ctx();
   for (auto& p : c.f) { if (p) cudaFree(p); p = nullptr; }
   for (auto& p : c.bc) { if (p) cudaFree(p); p = nullptr; }
@@ -187,6 +201,7 @@ int cappgpu_set_field(int field, const double* host, int64_t n) {
     set_error("set_field: bad field %d or size %lld (nijk=%d)", field, (long long)n, c.d.nijk);
     return CAPPGPU_E_ARG;
   }
+  note_write(field);
   CAP_CUDA(cudaMemcpyAsync(c.f[field], host, sizeof(double) * n, cudaMemcpyHostToDevice, c.st));
   CAP_CUDA(cudaStreamSynchronize(c.st));
   return CAPPGPU_OK;
@@ -277,6 +292,11 @@ int cappgpu_set_option(const char* key, int value) {
     return CAPPGPU_OK;
   }
   if (strcmp(key, "learn_conv") == 0 && value >= 0 && value <= 2) return learned_set_conv(value);
+  if (strcmp(key, "face_geo") == 0 && (value == 0 || value == 1)) {
+    ctx().face_geo = value;
+    if (!value) facegeo_free();
+    return CAPPGPU_OK;
+  }
   if (strcmp(key, "tight_correctors") == 0 && (value == 0 || value == 1)) {
     ctx().tight_correctors = value;
     return CAPPGPU_OK;

@@ -100,6 +100,7 @@ int cappgpu_build_geometry(int orient) {
   Box be{1, d.nim, 2, d.njm, 2, d.nkm};
   Box bn{2, d.nim, 1, d.njm, 2, d.nkm};
   Box bt{2, d.nim, 2, d.njm, 1, d.nkm};
+  ++c.geo_gen;
   launch(k_face_areas, grid_for(be.count()), kThreads, c.st, d, be, 1, d.nij, 1.0, c.f[CAP_X], c.f[CAP_Y],
                                                             c.f[CAP_Z], c.f[CAP_AR1X], c.f[CAP_AR1Y], c.f[CAP_AR1Z]);
   launch(k_face_areas, grid_for(bn.count()), kThreads, c.st, d, bn, d.nj, d.nij, s23, c.f[CAP_X], c.f[CAP_Y],

@@ -520,6 +520,7 @@ static int solve_h(int solver, double* fi, int ifi) {
   size_t nb = sizeof(double) * c.d.nijk;
   for (int q : ins)
     if (c.host_reg[q]) CAP_CUDA(cudaMemcpyAsync(c.f[q], c.host_reg[q], nb, cudaMemcpyHostToDevice, c.st));
+  note_write(fid);
   CAP_CUDA(cudaMemcpyAsync(c.f[fid], fi, nb, cudaMemcpyHostToDevice, c.st));
   cappgpu_solve_report rep;
   int rc = solve(solver, fid, ifi, &rep);

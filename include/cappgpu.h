@@ -201,6 +201,12 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    1-2 (default 15): 1 the pressure solve (pcgsip), 2 the momentum solves
    (sipsol), 4 the coefficient assembly (fluxuvw, PISO pressure assembly),
    8 the velocity gradients (grad_gauss of u, v, w).
+   "face_geo": 1 = the FP64 face kernels of fluxuvw and the PISO pressure
+   assembly read the geometric part of each face (centre distance, face
+   area, cosine of the non-orthogonality, area/volume ratios, face-centre
+   offsets) from arrays built once per grid, rebuilt after any write into a
+   geometry field (default; 36 arrays of nijk doubles); 0 = evaluate it on
+   every call.  Both give the same bits.
    "cg_batch": conjugate-gradient iterations of pcgsip launched between two
    host reads of the device-side exit test (1..64, default 4; surplus
    iterations after the exit return at once).

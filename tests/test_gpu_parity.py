@@ -268,6 +268,42 @@ def test_piso_assemble_bit_exact(gpu_lib, oracle_mod, ipc, d):
 
 
 @pytest.mark.parametrize("d", [0, 1, 2])
+def test_face_kernels_without_geometry_cache_bit_exact(gpu_lib, oracle_mod, d):
+    """Option face_geo 0: the FP64 face kernels evaluate the geometric part
+    of each face on every call instead of reading the per-face cache (the
+    tests above run the cached form); both match the oracle bit for bit."""
+    case, st = assembly_state(oracle_mod, "skewed", 45 + d)
+    st.params.gds[0] = 0.9
+    a = dir_args(case, d)
+    bp = ["be", "bn", "bt"][d]
+    push(gpu_lib, st)
+    gpu_lib.set_option("face_geo", 0)
+    for s in (gpu_lib, st):
+        s.fluxuvw(*a)
+        s.piso_assemble_pressure_eq(*a, 1, bp)
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+def test_face_geometry_cache_follows_grid_writes(gpu_lib, oracle_mod):
+    """Writing a geometry field after the per-face cache was built (cell
+    centres and face areas moved by set_field) rebuilds it: the next
+    assembly matches the oracle on the new grid bit for bit."""
+    case, st = assembly_state(oracle_mod, "skewed", 48)
+    a = dir_args(case, 0)
+    run_both(gpu_lib, st, lambda s: s.piso_assemble_pressure_eq(*a, 1, "be"))
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+    rng = np.random.default_rng(3)
+    for n in ("xc", "yc", "ar1x"):
+        v = st.field(n) * (1.0 + 1e-3 * rng.standard_normal(st.nijk))
+        st.set_field(n, v)
+        gpu_lib.set_field(n, v)
+    for s in (gpu_lib, st):
+        s.piso_assemble_pressure_eq(*a, 1, "be")
+        s.fluxuvw(*a)
+    compare(gpu_lib, st, exact=FIELD_NAMES)
+
+
+@pytest.mark.parametrize("d", [0, 1, 2])
 def test_assemble_pressure_eq_bit_exact(gpu_lib, oracle_mod, d):
     case, st = assembly_state(oracle_mod, "skewed", 50 + d)
     a = dir_args(case, d)
