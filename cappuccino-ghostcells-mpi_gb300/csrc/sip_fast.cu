@@ -17,6 +17,7 @@
 #include "common.cuh"
 #include "dlayout.cuh"
 #include "kernels.cuh"
+#include "lanewave.cuh"
 #include "wave.cuh"
 
 namespace cap {
@@ -61,6 +62,14 @@ struct Fast32 {
   float* bq = nullptr;   // backward factors, 3 components
   CUtensorMap map[E_NBUF];
   CUtensorMap map_fq, map_bq;
+  // warp-tile substitution engine (lanewave.cuh)
+  CUtensorMap lmap_r, lmap_z, lmap_fq, lmap_bq;   // boxes of one tile
+  int lnA = 0, lnC = 0, lntile = 0, lnt = 0;
+  int2* lorder = nullptr;
+  unsigned* lticket = nullptr;
+  float* lmailW = nullptr;
+  float* lmailB = nullptr;
+  size_t lmail_n = 0;   // floats in lmailW + lmailB
 };
 
 Fast32 G;
@@ -69,6 +78,9 @@ void fast32_release() {
   for (auto& p : G.e) { if (p) cudaFree(p); p = nullptr; }
   if (G.fq) cudaFree(G.fq);
   if (G.bq) cudaFree(G.bq);
+  if (G.lorder) cudaFree(G.lorder);
+  if (G.lticket) cudaFree(G.lticket);
+  if (G.lmailW) cudaFree(G.lmailW);   // lmailB lies in the same allocation
   G = Fast32();
 }
 
@@ -97,6 +109,16 @@ void fill_mail(cudaStream_t st) {
   launch(k_fill_u64, grid_for((long long)F.mail_n), kThreads, st, (unsigned long long*)F.mail, F.mail_n, kSentinel);
 }
 
+__global__ void k_fill_u32(unsigned* p, size_t n, unsigned v) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) p[t] = v;
+}
+
+// the warp-tile engine's mailboxes hold the sentinel between launches
+void fill_lane_mail(cudaStream_t st) {
+  if (G.lmailW)
+    launch(k_fill_u32, grid_for((long long)G.lmail_n), kThreads, st, (unsigned*)G.lmailW, G.lmail_n, kSentinelF);
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -114,9 +136,10 @@ EncodeTiledFn encode_tiled() {
 }
 
 // Tensor map of a hyperplane-layout array of esize-byte elements with NQ
-// components per cell: dims (P, [NQ,] Nk, S), box (BA + 16/esize, [NQ,] BC, kG),
-// zero fill outside.
-int make_map(CUtensorMap* m, void* ptr, int nq, int esize) {
+// components per cell: dims (P, [NQ,] Nk, S), box (bw, [NQ,] rows, planes),
+// zero fill outside.  The wavefront of wave.cuh copies boxes of
+// (BA + 16/esize, [NQ,] BC, kG).
+int make_map_box(CUtensorMap* m, void* ptr, int nq, int esize, int bwid, int rows, int planes) {
   EncodeTiledFn enc = encode_tiled();
   if (!enc) { set_error("cuTensorMapEncodeTiled is not available"); return CAPPGPU_E_CUDA; }
   const DG& g = F.g;
@@ -124,23 +147,27 @@ int make_map(CUtensorMap* m, void* ptr, int nq, int esize) {
   cuuint64_t dims[4], strides[3];
   cuuint32_t box[4], estr[4] = {1, 1, 1, 1};
   cuuint32_t rank;
-  const cuuint32_t bw = (cuuint32_t)(BA + 16 / esize);
+  const cuuint32_t bw = (cuuint32_t)bwid;
   if (nq == 1) {
     rank = 3;
     dims[0] = (cuuint64_t)g.P; dims[1] = (cuuint64_t)g.Nk; dims[2] = (cuuint64_t)g.S;
     strides[0] = (cuuint64_t)g.P * es; strides[1] = (cuuint64_t)g.P * g.Nk * es;
-    box[0] = bw; box[1] = BC; box[2] = kG;
+    box[0] = bw; box[1] = (cuuint32_t)rows; box[2] = (cuuint32_t)planes;
   } else {
     rank = 4;
     dims[0] = (cuuint64_t)g.P; dims[1] = (cuuint64_t)nq; dims[2] = (cuuint64_t)g.Nk; dims[3] = (cuuint64_t)g.S;
     strides[0] = (cuuint64_t)g.P * es; strides[1] = (cuuint64_t)g.P * nq * es; strides[2] = (cuuint64_t)g.P * nq * g.Nk * es;
-    box[0] = bw; box[1] = (cuuint32_t)nq; box[2] = BC; box[3] = kG;
+    box[0] = bw; box[1] = (cuuint32_t)nq; box[2] = (cuuint32_t)rows; box[3] = (cuuint32_t)planes;
   }
   CUresult r = enc(m, esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, ptr, dims,
                    strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed"); return CAPPGPU_E_CUDA; }
   return CAPPGPU_OK;
+}
+
+int make_map(CUtensorMap* m, void* ptr, int nq, int esize) {
+  return make_map_box(m, ptr, nq, esize, BA + 16 / esize, BC, kG);
 }
 
 int fast_setup() {
@@ -237,7 +264,41 @@ int fast32_setup() {
   for (int q = 0; q < E_NBUF && !rc; ++q) rc = make_map(&G.map[q], G.e[q], 1, 4);
   if (!rc) rc = make_map(&G.map_fq, G.fq, 4, 4);
   if (!rc) rc = make_map(&G.map_bq, G.bq, 3, 4);
+  // the warp-tile engine: tile boxes, topological tile order, mailboxes
+  const int lbw = kLW + 4;
+  if (!rc) rc = make_map_box(&G.lmap_r, G.e[E_R], 1, 4, lbw, kCW, kLG);
+  if (!rc) rc = make_map_box(&G.lmap_z, G.e[E_Z], 1, 4, lbw, kCW, kLG);
+  if (!rc) rc = make_map_box(&G.lmap_fq, G.fq, 4, 4, lbw, kCW, kLG);
+  if (!rc) rc = make_map_box(&G.lmap_bq, G.bq, 3, 4, lbw, kCW, kLG);
   if (rc) { fast32_release(); return rc; }
+  {
+    const DG& g = F.g;
+    G.lnA = (g.Ni + kLW - 1) / kLW;
+    G.lnC = (g.Nk + kCW - 1) / kCW;
+    G.lntile = G.lnA * G.lnC;
+    G.lnt = (kLW - 1) + (kCW - 1) + g.Nj;
+    std::vector<int2> ord;
+    ord.reserve(G.lntile);
+    for (int dsum = 0; dsum <= G.lnA + G.lnC - 2; ++dsum)
+      for (int cc = 0; cc < G.lnC; ++cc) {
+        const int aa = dsum - cc;
+        if (aa >= 0 && aa < G.lnA) ord.push_back(make_int2(aa, cc));
+      }
+    const size_t nW = (size_t)G.lntile * G.lnt * kCW, nB = (size_t)G.lntile * G.lnt * kLW;
+    G.lmail_n = nW + nB;
+    if (cudaMalloc(&G.lorder, sizeof(int2) * G.lntile) != cudaSuccess ||
+        cudaMalloc(&G.lticket, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&G.lmailW, sizeof(float) * G.lmail_n) != cudaSuccess) {
+      fast32_release();
+      set_error("out of device memory");
+      return CAPPGPU_E_NOMEM;
+    }
+    G.lmailB = G.lmailW + nW;
+    CAP_CUDA(cudaMemcpy(G.lorder, ord.data(), sizeof(int2) * G.lntile, cudaMemcpyHostToDevice));
+    CAP_CUDA(cudaMemset(G.lticket, 0, sizeof(unsigned)));
+    fill_lane_mail(c.st);
+    CAP_CUDA(cudaStreamSynchronize(c.st));
+  }
   G.ready = true;
   return CAPPGPU_OK;
 }
@@ -273,6 +334,70 @@ int run_wave(const Op& op, const int* skip = nullptr) {
   launch_smem(k_wave<Op, BA, BC, BWD>, F.nblk, wave_threads<Op, BA, BC>(), smem, c.st, op, F.g, w);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
+}
+
+LaneCtl lane_ctl(const int* skip) {
+  LaneCtl w;
+  w.ticket = G.lticket;
+  w.order = G.lorder;
+  w.nA = G.lnA;
+  w.nC = G.lnC;
+  w.ntile = G.lntile;
+  w.nt = G.lnt;
+  w.abort = F.flags;
+  w.err = F.flags + 1;
+  w.mailW = G.lmailW;
+  w.mailB = G.lmailB;
+  w.spin_limit = 1LL << 21;
+  w.skip = skip;
+  return w;
+}
+
+template <class Op, bool BWD>
+int run_lane(const Op& op, const int* skip) {
+  Ctx& c = ctx();
+  constexpr size_t smem = LaneLayout<Op>::smem;
+  static bool attr_set = false;   // once per process (one device per context)
+  if (!attr_set) {
+    CAP_CUDA(cudaFuncSetAttribute(k_lane_wave<Op, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  launch_smem(k_lane_wave<Op, BWD>, G.lntile, 64, smem, c.st, op, F.g, lane_ctl(skip));
+  CAP_CHECK_LAUNCH();
+  return CAPPGPU_OK;
+}
+
+// The FP32 substitutions z = M^-1 r of the refinement form: the wavefront of
+// wave.cuh (default) or the warp-tile engine of lanewave.cuh (option
+// lane_wave = 1; the same bits, faster only on the largest grids).
+int fp32_forward(const int* skip) {
+  if (ctx().lane_wave) {
+    LaneFwdF op;
+    op.map[0] = G.lmap_r;
+    op.map[1] = G.lmap_fq;
+    op.z = G.e[E_Z];
+    return run_lane<LaneFwdF, false>(op, skip);
+  }
+  SipFwdF fwd;
+  fwd.map[0] = G.map[E_R];
+  fwd.map[1] = G.map_fq;
+  fwd.z = G.e[E_Z];
+  return run_wave<SipFwdF, false>(fwd, skip);
+}
+
+int fp32_backward(const int* skip) {
+  if (ctx().lane_wave) {
+    LaneBwdF op;
+    op.map[0] = G.lmap_z;
+    op.map[1] = G.lmap_bq;
+    op.z = G.e[E_Z];
+    return run_lane<LaneBwdF, true>(op, skip);
+  }
+  SipBwdF bwd;
+  bwd.map[0] = G.map[E_Z];
+  bwd.map[1] = G.map_bq;
+  bwd.z = G.e[E_Z];
+  return run_wave<SipBwdF, true>(bwd, skip);
 }
 
 // ------------------------------------------------------ vector kernels (D)
@@ -607,7 +732,9 @@ static int wave_error_reset(const int* h) {
   if (h[1] != 0) {
     cudaMemset(F.flags, 0, sizeof(int) * 2);
     cudaMemset(F.ticket, 0, sizeof(unsigned));
+    if (G.lticket) cudaMemset(G.lticket, 0, sizeof(unsigned));
     fill_mail(ctx().st);
+    fill_lane_mail(ctx().st);
     cudaStreamSynchronize(ctx().st);
     set_error(h[1] == 1 ? "wavefront: a block waited beyond the spin limit for its predecessor"
                         : "wavefront: block ticket out of range");
@@ -850,14 +977,6 @@ int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     op.alfa = (float)P.alfa;
     if ((rc = run_wave<SipFactorF, false>(op))) return rc;
   }
-  SipFwdF fwd;
-  fwd.map[0] = G.map[E_R];
-  fwd.map[1] = G.map_fq;
-  fwd.z = G.e[E_Z];
-  SipBwdF bwd;
-  bwd.map[0] = G.map[E_Z];
-  bwd.map[1] = G.map_bq;
-  bwd.z = G.e[E_Z];
   const int ns = P.nsw[ifi - 1];
   double res1 = 0.0, rsm = 0.0;
   int n;
@@ -870,8 +989,8 @@ int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     launch(k_cg_scalars, 1, 32, c.st, 3, (const double*)c.partials, kRedBlocks, c.dscal);
     launch(k_d_to_f, grid_for(g.ncell / 4), kThreads, c.st, g, (const double*)F.d[D_RES], G.e[E_R]);
     CAP_CHECK_LAUNCH();
-    if ((rc = run_wave<SipFwdF, false>(fwd))) return rc;
-    if ((rc = run_wave<SipBwdF, true>(bwd))) return rc;
+    if ((rc = fp32_forward(nullptr))) return rc;
+    if ((rc = fp32_backward(nullptr))) return rc;
     launch(k_add_f, grid_for(g.ncell / 4), kThreads, c.st, g, F.d[D_FI], (const float*)G.e[E_Z]);
     CAP_CHECK_LAUNCH();
     CAP_CUDA(cudaMemcpyAsync(F.hres, c.dscal + 6, sizeof(double), cudaMemcpyDeviceToHost, c.st));
@@ -943,14 +1062,6 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     op.alfa = (float)P.alfa;
     if ((rc = run_wave<SipFactorF, false>(op))) return rc;
   }
-  SipFwdF fwd;
-  fwd.map[0] = G.map[E_R];
-  fwd.map[1] = G.map_fq;
-  fwd.z = G.e[E_Z];
-  SipBwdF bwd;
-  bwd.map[0] = G.map[E_Z];
-  bwd.map[1] = G.map_bq;
-  bwd.z = G.e[E_Z];
   const size_t nf = sizeof(float) * (size_t)g.size();
   int total = 0;
   double resl = res0;
@@ -990,8 +1101,8 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     for (int launched = 0; launched < budget;) {
       const int batch = budget - launched < c.cg_batch ? budget - launched : c.cg_batch;
       for (int q = 0; q < batch; ++q) {
-        if ((rc = run_wave<SipFwdF, false>(fwd, F.ctl))) return rc;
-        if ((rc = run_wave<SipBwdF, true>(bwd, F.ctl))) return rc;
+        if ((rc = fp32_forward(F.ctl))) return rc;
+        if ((rc = fp32_backward(F.ctl))) return rc;
         float* pko = G.e[cur ? E_P1 : E_P0];
         float* pkn = G.e[cur ? E_P0 : E_P1];
         launch(k_dot_fx, kRedBlocks, kThreads, c.st, g, (const float*)G.e[E_R], (const float*)G.e[E_Z], part0,
@@ -1058,18 +1169,7 @@ int fast_profile_unit(int which, double* bytes) {
       if (rc) return rc;
     }
     *bytes = 6.0 * 4.0 * cells;   // 5 words read, 1 written, 4 bytes each
-    if (which == 7) {
-      SipFwdF fwd;
-      fwd.map[0] = G.map[E_R];
-      fwd.map[1] = G.map_fq;
-      fwd.z = G.e[E_Z];
-      return run_wave<SipFwdF, false>(fwd);
-    }
-    SipBwdF bwd;
-    bwd.map[0] = G.map[E_Z];
-    bwd.map[1] = G.map_bq;
-    bwd.z = G.e[E_Z];
-    return run_wave<SipBwdF, true>(bwd);
+    return which == 7 ? fp32_forward(nullptr) : fp32_backward(nullptr);
   }
   *bytes = 21.0 * 8.0 * cells;    // 7 coefficients read, 7 factors natural + 7 hyperplane written
   return factor_wave();

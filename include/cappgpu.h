@@ -201,6 +201,11 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    1-2 (default 15): 1 the pressure solve (pcgsip), 2 the momentum solves
    (sipsol), 4 the coefficient assembly (fluxuvw, PISO pressure assembly),
    8 the velocity gradients (grad_gauss of u, v, w).
+   "lane_wave": engine of the FP32 SIP substitutions of precision modes 1-2:
+   0 = the persistent hyperplane wavefront, one thread per line (default);
+   1 = one warp per tile of 32 x 8 lines, neighbours by shuffles and
+   registers, no barrier per hyperplane.  Both give the same bits; on GB300
+   1 is slower at 128^3 (192 vs 152 us per forward sweep) and level at 256^3.
    "face_geo": 1 = the FP64 face kernels of fluxuvw and the PISO pressure
    assembly read the geometric part of each face (centre distance, face
    area, cosine of the non-orthogonality, area/volume ratios, face-centre
