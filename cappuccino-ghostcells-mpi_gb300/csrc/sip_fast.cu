@@ -456,6 +456,37 @@ __device__ __forceinline__ void for_cells(const DG& g, F&& f) {
   }
 }
 
+// The cells of one pass of the compact walk, for kernels written in two
+// phases -- every load of the pass first, then the arithmetic and the
+// stores -- so that a warp has U chunks of loads in flight whatever the
+// compiler assumes about aliasing between the loads and the stores.
+template <int U>
+struct CellPass {
+  long long t[U];
+  int a[U], b[U], c[U];
+  bool ok[U];
+};
+
+template <int U>
+__device__ __forceinline__ void pass_cells(const DG& g, int q0, int lane, CellPass<U>& P) {
+  int4 e[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int q = q0 + u;
+    P.ok[u] = q < g.nchunk && (long long)q * 32 + lane < g.ncell;
+    e[u] = P.ok[u] ? g.chunk[q] : make_int4(0, 0, 0, 0);
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    int s = e[u].x, c = e[u].y, a = e[u].z;
+    if (P.ok[u]) walk_cells(g, s, c, a, lane);
+    P.t[u] = ((long long)s * g.Nk + c) * g.P + a;
+    P.a[u] = a;
+    P.b[u] = s - a - c;
+    P.c[u] = c;
+  }
+}
+
 // The same over rows: one warp takes a row (s, c), its lanes the row's cells
 // a = max(0, s-c-(Nj-1)) .. min(Ni-1, s-c).  Idle lanes at row ends, but all
 // of a warp's loads fall in one row of every array; the FP32 kernels with
@@ -666,15 +697,29 @@ __global__ void k_add_f(DG g, double* __restrict__ x, const float* __restrict__ 
 // FP32 inner-loop kernels with fused scalars (same scheme as k_pk_x ...)
 __global__ void k_dot_fx(DG g, const float* __restrict__ x, const float* __restrict__ y, double* part, const int* ctl) {
   if (*(volatile const int*)ctl) return;
+  constexpr int U = 4;
+  const int lane = threadIdx.x & 31, nw = (int)((gridDim.x * blockDim.x) >> 5);
   float acc = 0.0f;
-  for_rows(g, [&](long long t_, int a, int b, int c) {
-    acc += x[t_] * y[t_];
-  });
+  for (int q0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * U; q0 < g.nchunk; q0 += nw * U) {
+    CellPass<U> P;
+    pass_cells<U>(g, q0, lane, P);
+    float xv[U], yv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      xv[u] = P.ok[u] ? x[P.t[u]] : 0.0f;
+      yv[u] = P.ok[u] ? y[P.t[u]] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (P.ok[u]) acc += xv[u] * yv[u];
+  }
   double v[1] = {(double)acc};
   block_reduce_store<1>(v, part);
 }
 
-__global__ void k_pk_spmv_fx(DG g, const float* __restrict__ ae, const float* __restrict__ aw,
+// pk = zk + beta pk (pcg-sip.f90:241) at the cell and its six neighbours,
+// zz = A pk (pcg-sip.f90:247-257), partial sums pk.zz
+__global__ void __launch_bounds__(kThreads, 4) k_pk_spmv_fx(DG g, const float* __restrict__ ae, const float* __restrict__ aw,
                              const float* __restrict__ an, const float* __restrict__ as,
                              const float* __restrict__ at, const float* __restrict__ ab,
                              const float* __restrict__ ap, const float* __restrict__ zk,
@@ -685,26 +730,54 @@ __global__ void k_pk_spmv_fx(DG g, const float* __restrict__ ae, const float* __
   const double sk = sb.x, betd = sb.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[1] = sk; scal[4] = betd; }
   const float bet = (float)betd;
+  constexpr int U = 1;
+  const int lane = threadIdx.x & 31, nw = (int)((gridDim.x * blockDim.x) >> 5);
   float acc = 0.0f;
-  for_rows(g, [&](long long t_, int a, int b, int c) {
-    const long long P = t_;
-    auto pnew = [&](long long q) { return zk[q] + bet * pko[q]; };
-    const float pP = pnew(P);
-    const float pE = a + 1 < g.Ni ? pnew(P + g.plane + 1) : 0.0f;
-    const float pW = a > 0 ? pnew(P - g.plane - 1) : 0.0f;
-    const float pN = b + 1 < g.Nj ? pnew(P + g.plane) : 0.0f;
-    const float pS = b > 0 ? pnew(P - g.plane) : 0.0f;
-    const float pT = c + 1 < g.Nk ? pnew(P + g.plane + g.P) : 0.0f;
-    const float pB = c > 0 ? pnew(P - g.plane - g.P) : 0.0f;
-    const float r = ap[P] * pP - ae[P] * pE - aw[P] * pW - an[P] * pN - as[P] * pS - at[P] * pT - ab[P] * pB;
-    pkn[P] = pP;
-    zz[P] = r;
-    acc += pP * r;
-  });
+  for (int q0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * U; q0 < g.nchunk; q0 += nw * U) {
+    CellPass<U> P;
+    pass_cells<U>(g, q0, lane, P);
+    // neighbour offsets and existence: P, E, W, N, S, T, B
+    float zv[U][7], pv[U][7], cf[U][7];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long t = P.t[u];
+      const int a = P.a[u], b = P.b[u], c = P.c[u];
+      const long long off[7] = {0, g.plane + 1, -g.plane - 1, g.plane, -g.plane, g.plane + g.P, -g.plane - g.P};
+      const bool ex[7] = {true, a + 1 < g.Ni, a > 0, b + 1 < g.Nj, b > 0, c + 1 < g.Nk, c > 0};
+#pragma unroll
+      for (int k = 0; k < 7; ++k) {
+        const bool l = P.ok[u] && ex[k];
+        zv[u][k] = l ? zk[t + off[k]] : 0.0f;
+        pv[u][k] = l ? pko[t + off[k]] : 0.0f;
+      }
+      const float* const cs[7] = {ap, ae, aw, an, as, at, ab};
+#pragma unroll
+      for (int k = 0; k < 7; ++k) cf[u][k] = P.ok[u] ? cs[k][t] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (!P.ok[u]) continue;
+      float p[7];
+#pragma unroll
+      for (int k = 0; k < 7; ++k) p[k] = zv[u][k] + bet * pv[u][k];
+      // a missing neighbour contributes zero, as its pk is zero
+      const int a = P.a[u], b = P.b[u], c = P.c[u];
+      const float pE = a + 1 < g.Ni ? p[1] : 0.0f, pW = a > 0 ? p[2] : 0.0f;
+      const float pN = b + 1 < g.Nj ? p[3] : 0.0f, pS = b > 0 ? p[4] : 0.0f;
+      const float pT = c + 1 < g.Nk ? p[5] : 0.0f, pB = c > 0 ? p[6] : 0.0f;
+      const float r = cf[u][0] * p[0] - cf[u][1] * pE - cf[u][2] * pW - cf[u][3] * pN - cf[u][4] * pS -
+                      cf[u][5] * pT - cf[u][6] * pB;
+      pkn[P.t[u]] = p[0];
+      zz[P.t[u]] = r;
+      acc += p[0] * r;
+    }
+  }
   double v[1] = {(double)acc};
   block_reduce_store<1>(v, pout);
 }
 
+// alf from the partials; x += alf pk; r -= alf zz; partial sums |r|
+// (pcg-sip.f90:261-281)
 __global__ void k_update_fx(DG g, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ pk,
                             const float* __restrict__ zz, const double* __restrict__ pin, double* scal, double* pout,
                             const int* ctl) {
@@ -713,13 +786,30 @@ __global__ void k_update_fx(DG g, float* __restrict__ x, float* __restrict__ r, 
   const double pkapk = sa.x, alfd = sa.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[2] = pkapk; scal[3] = alfd; }
   const float alf = (float)alfd;
+  constexpr int U = 4;
+  const int lane = threadIdx.x & 31, nw = (int)((gridDim.x * blockDim.x) >> 5);
   float acc = 0.0f;
-  for_cells<4>(g, [&](long long t_, int a, int b, int c) {
-    x[t_] = x[t_] + alf * pk[t_];
-    const float rr = r[t_] - alf * zz[t_];
-    r[t_] = rr;
-    acc += fabsf(rr);
-  });
+  for (int q0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * U; q0 < g.nchunk; q0 += nw * U) {
+    CellPass<U> P;
+    pass_cells<U>(g, q0, lane, P);
+    float xv[U], rv[U], pv[U], zv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long t = P.t[u];
+      xv[u] = P.ok[u] ? x[t] : 0.0f;
+      rv[u] = P.ok[u] ? r[t] : 0.0f;
+      pv[u] = P.ok[u] ? pk[t] : 0.0f;
+      zv[u] = P.ok[u] ? zz[t] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (!P.ok[u]) continue;
+      x[P.t[u]] = xv[u] + alf * pv[u];
+      const float rr = rv[u] - alf * zv[u];
+      r[P.t[u]] = rr;
+      acc += fabsf(rr);
+    }
+  }
   double v[1] = {(double)acc};
   block_reduce_store<1>(v, pout);
 }
