@@ -298,7 +298,7 @@ def run_gpu(args, ws, rank, local):
             lib.set_field(n, host[n])
         lib.piso_steps(1)
         for n in names:
-            host[n][:] = lib.get_field(n)
+            lib.get_field(n, out=host[n])
     e2e_ms = group.max(lib.timer_stop())
     lib.free_pinned()
     nbytes = len(names) * lib.nijk * 8

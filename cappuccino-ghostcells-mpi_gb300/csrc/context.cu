@@ -77,7 +77,7 @@ void note_write(int q) {
     case CAP_X: case CAP_Y: case CAP_Z: case CAP_XC: case CAP_YC: case CAP_ZC:
     case CAP_FX: case CAP_FY: case CAP_FZ:
     case CAP_AR1X: case CAP_AR1Y: case CAP_AR1Z: case CAP_AR2X: case CAP_AR2Y: case CAP_AR2Z:
-    case CAP_AR3X: case CAP_AR3Y: case CAP_AR3Z:
+    case CAP_AR3X: case CAP_AR3Y: case CAP_AR3Z: case CAP_VOL:
       ++ctx().geo_gen;
       break;
     default:
@@ -89,6 +89,7 @@ static void free_all() {
   fast_free();
   learned_free();
   facegeo_free();
+  volr_free();
   Ctx& c = ctx();
   for (auto& p : c.f) { if (p) cudaFree(p); p = nullptr; }
   for (auto& p : c.bc) { if (p) cudaFree(p); p = nullptr; }
@@ -298,7 +299,10 @@ int cappgpu_set_option(const char* key, int value) {
   }
   if (strcmp(key, "face_geo") == 0 && (value == 0 || value == 1)) {
     ctx().face_geo = value;
-    if (!value) facegeo_free();
+    if (!value) {
+      facegeo_free();
+      volr_free();
+    }
     return CAPPGPU_OK;
   }
   if (strcmp(key, "tight_correctors") == 0 && (value == 0 || value == 1)) {

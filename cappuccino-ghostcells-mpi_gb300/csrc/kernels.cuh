@@ -23,8 +23,10 @@ int sipsol_fast(int fi, int ifi, cappgpu_solve_report* rep);
 int sipsol_mixed(int fi, int ifi, cappgpu_solve_report* rep);
 int fast_profile_unit(int which, double* bytes);
 void fast_free();
-// per-face geometry cache of the FP64 face kernels (assembly.cu)
+// per-face geometry cache of the FP64 face kernels (assembly.cu) and the
+// 1/vol cache of the FP64 gradient (stencil.cu)
 void facegeo_free();
+void volr_free();
 // learned initial guess (learned.cu)
 void learned_free();
 int learned_solve_start(int fif, double res0);

@@ -177,7 +177,7 @@ int ghost_update() {
 // south face (from j-1), own east/north/top faces.  The gather below adds
 // the same rounded terms in the same order, so every element -- ghost and
 // padding cells included -- is bit-identical.
-template <typename R>
+template <typename R, bool VR>
 __global__ void k_grad_gauss(Dims d, const double* __restrict__ u, const double* __restrict__ fx,
                              const double* __restrict__ fy, const double* __restrict__ fz,
                              const double* __restrict__ a1x, const double* __restrict__ a1y,
@@ -185,7 +185,8 @@ __global__ void k_grad_gauss(Dims d, const double* __restrict__ u, const double*
                              const double* __restrict__ a2y, const double* __restrict__ a2z,
                              const double* __restrict__ a3x, const double* __restrict__ a3y,
                              const double* __restrict__ a3z, const double* __restrict__ vol,
-                             double* __restrict__ dx, double* __restrict__ dy, double* __restrict__ dz) {
+                             const double* __restrict__ volr_c, double* __restrict__ dx, double* __restrict__ dy,
+                             double* __restrict__ dz) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < d.nijk; t += (long long)gridDim.x * blockDim.x) {
     int p = (int)t;
     int k = p / d.nij + 1;
@@ -227,7 +228,9 @@ __global__ void k_grad_gauss(Dims d, const double* __restrict__ u, const double*
       gz = gz + (ue * R(a1z[p]) + un * R(a2z[p]) + ut * R(a3z[p]));
     }
     if (k >= 2 && k <= d.nkm && i >= 3 && i <= d.nimm && j >= 3 && j <= d.njmm) {
-      R volr = R(1.0) / R(vol[p]);
+      R volr;
+      if constexpr (VR) volr = R(volr_c[p]);   // the same 1/vol, evaluated once per grid
+      else volr = R(1.0) / R(vol[p]);
       gx = gx * volr;
       gy = gy * volr;
       gz = gz * volr;
@@ -238,16 +241,57 @@ __global__ void k_grad_gauss(Dims d, const double* __restrict__ u, const double*
   }
 }
 
+// 1/vol of every cell for the FP64 gradient (an FP64 division per cell and
+// call otherwise), rebuilt after a write into a geometry field or vol
+namespace {
+double* g_volr = nullptr;
+unsigned long long g_volr_gen = 0;
+int g_volr_n = 0;
+
+__global__ void k_recip(long long n, const double* __restrict__ v, double* __restrict__ r) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    r[t] = 1.0 / v[t];
+}
+}  // namespace
+
+void volr_free() {
+  if (g_volr) cudaFree(g_volr);
+  g_volr = nullptr;
+  g_volr_gen = 0;
+  g_volr_n = 0;
+}
+
+static const double* volr_cache() {
+  Ctx& c = ctx();
+  if (!c.face_geo) return nullptr;
+  if (g_volr_n != c.d.nijk) {
+    volr_free();
+    if (cudaMalloc(&g_volr, sizeof(double) * c.d.nijk) != cudaSuccess) {
+      cudaGetLastError();
+      g_volr = nullptr;
+      return nullptr;   // no room: divide per call
+    }
+    g_volr_n = c.d.nijk;
+  }
+  if (g_volr_gen != c.geo_gen) {
+    launch(k_recip, grid_for(c.d.nijk), kThreads, c.st, (long long)c.d.nijk, (const double*)c.f[CAP_VOL], g_volr);
+    g_volr_gen = c.geo_gen;
+  }
+  return g_volr;
+}
+
 int grad_gauss(int uf, int dxf, int dyf, int dzf) {
   Ctx& c = ctx();
   double** F = c.f;
   // precision modes 1-2: velocity gradients (inputs of the coefficient
   // assembly) in FP32 arithmetic; the pressure gradient of the velocity
   // correction stays FP64
-  auto k = (c.fp32(8) && uf != CAP_P) ? k_grad_gauss<float> : k_grad_gauss<double>;
+  const bool f32 = c.fp32(8) && uf != CAP_P;
+  const double* vr = f32 ? nullptr : volr_cache();
+  auto k = f32 ? k_grad_gauss<float, false> : vr ? k_grad_gauss<double, true> : k_grad_gauss<double, false>;
   launch(k, grid_for(c.d.nijk), kThreads, c.st,
       c.d, F[uf], F[CAP_FX], F[CAP_FY], F[CAP_FZ], F[CAP_AR1X], F[CAP_AR1Y], F[CAP_AR1Z], F[CAP_AR2X],
-      F[CAP_AR2Y], F[CAP_AR2Z], F[CAP_AR3X], F[CAP_AR3Y], F[CAP_AR3Z], F[CAP_VOL], F[dxf], F[dyf], F[dzf]);
+      F[CAP_AR2Y], F[CAP_AR2Z], F[CAP_AR3X], F[CAP_AR3Y], F[CAP_AR3Z], F[CAP_VOL], vr, F[dxf], F[dyf], F[dzf]);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
 }
@@ -402,9 +446,11 @@ int cappgpu_grad_gauss_h(const double* u, double* dudx, double* dudy, double* du
   double** F = c.f;
   double *du = c.work[4], *gx = c.work[5], *gy = c.work[6], *gz = c.work[7];
   CAP_CUDA(cudaMemcpyAsync(du, u, nb, cudaMemcpyHostToDevice, c.st));
-  cap::launch(k_grad_gauss<double>, cap::grid_for(c.d.nijk), cap::kThreads, c.st,
-      c.d, du, F[CAP_FX], F[CAP_FY], F[CAP_FZ], F[CAP_AR1X], F[CAP_AR1Y], F[CAP_AR1Z], F[CAP_AR2X],
-      F[CAP_AR2Y], F[CAP_AR2Z], F[CAP_AR3X], F[CAP_AR3Y], F[CAP_AR3Z], F[CAP_VOL], gx, gy, gz);
+  const double* vr = cap::volr_cache();
+  cap::launch(vr ? cap::k_grad_gauss<double, true> : cap::k_grad_gauss<double, false>, cap::grid_for(c.d.nijk),
+      cap::kThreads, c.st, c.d, (const double*)du, F[CAP_FX], F[CAP_FY], F[CAP_FZ], F[CAP_AR1X], F[CAP_AR1Y],
+      F[CAP_AR1Z], F[CAP_AR2X], F[CAP_AR2Y], F[CAP_AR2Z], F[CAP_AR3X], F[CAP_AR3Y], F[CAP_AR3Z], F[CAP_VOL], vr, gx,
+      gy, gz);
   CAP_CHECK_LAUNCH();
   CAP_CUDA(cudaMemcpyAsync(dudx, gx, nb, cudaMemcpyDeviceToHost, c.st));
   CAP_CUDA(cudaMemcpyAsync(dudy, gy, nb, cudaMemcpyDeviceToHost, c.st));

@@ -162,10 +162,15 @@ class Library:
         a = np.ascontiguousarray(arr, dtype=np.float64)
         self._check(self.lib.cappgpu_set_field(fid(name), _dp(a), a.size), f"set_field({name})")
 
-    def get_field(self, name):
-        a = np.empty(self.nijk, np.float64)
-        self._check(self.lib.cappgpu_get_field(fid(name), _dp(a), a.size), f"get_field({name})")
-        return a
+    def get_field(self, name, out=None):
+        """The field as a new array, or copied into `out` (a contiguous
+        float64 array of nijk elements, e.g. one from pinned())."""
+        if out is None:
+            out = np.empty(self.nijk, np.float64)
+        elif out.dtype != np.float64 or out.size != self.nijk or not out.flags.c_contiguous:
+            raise ValueError(f"get_field({name}): out must be a contiguous float64 array of {self.nijk}")
+        self._check(self.lib.cappgpu_get_field(fid(name), _dp(out), out.size), f"get_field({name})")
+        return out
 
     def set_bc(self, face, codes):
         a = np.ascontiguousarray(codes, dtype=np.int32)

@@ -209,9 +209,10 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    "face_geo": 1 = the FP64 face kernels of fluxuvw and the PISO pressure
    assembly read the geometric part of each face (centre distance, face
    area, cosine of the non-orthogonality, area/volume ratios, face-centre
-   offsets) from arrays built once per grid, rebuilt after any write into a
-   geometry field (default; 36 arrays of nijk doubles); 0 = evaluate it on
-   every call.  Both give the same bits.
+   offsets), and the FP64 Gauss gradient 1/vol, from arrays built once per
+   grid, rebuilt after any write into a geometry field or vol (default; 37
+   arrays of nijk doubles); 0 = evaluate them on every call.  Both give the
+   same bits.
    "cg_batch": conjugate-gradient iterations of pcgsip launched between two
    host reads of the device-side exit test (1..64, default 4; surplus
    iterations after the exit return at once).

@@ -76,6 +76,22 @@ def test_index_maps(gpu_lib):
     assert gpu_lib.lib.cappgpu_ijkpr() == (3 - 1) * ni * nj + (4 - 1) * nj + 5   # setind.f90:56
 
 
+def test_get_field_into_pinned_buffer(gpu_lib):
+    """get_field(out=...) copies straight into a caller's array (the
+    end-to-end bench reads its fields into page-locked buffers)."""
+    gpu_lib.init(9, 8, 7)
+    x = np.random.default_rng(1).standard_normal(9 * 8 * 7)
+    gpu_lib.set_field("u", x)
+    buf = gpu_lib.pinned(x.size)
+    try:
+        assert gpu_lib.get_field("u", out=buf) is buf
+        np.testing.assert_array_equal(buf, x)
+        with pytest.raises(ValueError):
+            gpu_lib.get_field("u", out=np.empty(3))
+    finally:
+        gpu_lib.free_pinned()
+
+
 # --------------------------------------------------------------- ghost cells
 
 @pytest.mark.parametrize("periodic", [0, 1])
@@ -270,8 +286,9 @@ def test_piso_assemble_bit_exact(gpu_lib, oracle_mod, ipc, d):
 @pytest.mark.parametrize("d", [0, 1, 2])
 def test_face_kernels_without_geometry_cache_bit_exact(gpu_lib, oracle_mod, d):
     """Option face_geo 0: the FP64 face kernels evaluate the geometric part
-    of each face on every call instead of reading the per-face cache (the
-    tests above run the cached form); both match the oracle bit for bit."""
+    of each face, and the gradient 1/vol, on every call instead of reading
+    the caches (the tests above run the cached form); both match the
+    oracle bit for bit."""
     case, st = assembly_state(oracle_mod, "skewed", 45 + d)
     st.params.gds[0] = 0.9
     a = dir_args(case, d)
@@ -281,25 +298,28 @@ def test_face_kernels_without_geometry_cache_bit_exact(gpu_lib, oracle_mod, d):
     for s in (gpu_lib, st):
         s.fluxuvw(*a)
         s.piso_assemble_pressure_eq(*a, 1, bp)
+        s.grad_gauss("v", "gradv_x", "gradv_y", "gradv_z")
     compare(gpu_lib, st, exact=FIELD_NAMES)
 
 
 def test_face_geometry_cache_follows_grid_writes(gpu_lib, oracle_mod):
-    """Writing a geometry field after the per-face cache was built (cell
-    centres and face areas moved by set_field) rebuilds it: the next
-    assembly matches the oracle on the new grid bit for bit."""
+    """Writing a geometry field after the caches were built (cell centres,
+    face areas and volumes moved by set_field) rebuilds them: the next
+    assembly and gradient match the oracle on the new grid bit for bit."""
     case, st = assembly_state(oracle_mod, "skewed", 48)
     a = dir_args(case, 0)
-    run_both(gpu_lib, st, lambda s: s.piso_assemble_pressure_eq(*a, 1, "be"))
+    grad = ("u", "gradu_x", "gradu_y", "gradu_z")
+    run_both(gpu_lib, st, lambda s: (s.piso_assemble_pressure_eq(*a, 1, "be"), s.grad_gauss(*grad)))
     compare(gpu_lib, st, exact=FIELD_NAMES)
     rng = np.random.default_rng(3)
-    for n in ("xc", "yc", "ar1x"):
+    for n in ("xc", "yc", "ar1x", "vol"):
         v = st.field(n) * (1.0 + 1e-3 * rng.standard_normal(st.nijk))
         st.set_field(n, v)
         gpu_lib.set_field(n, v)
     for s in (gpu_lib, st):
         s.piso_assemble_pressure_eq(*a, 1, "be")
         s.fluxuvw(*a)
+        s.grad_gauss(*grad)
     compare(gpu_lib, st, exact=FIELD_NAMES)
 
 
