@@ -179,6 +179,7 @@ def _base_params():
              ipr=3, jpr=3, kpr=3, ncorr=1, npcor=1, icorr=0, ipcorr=0, bdf=0, cn=0,
              lcds=1, lluds=0, lquds=0, lsmart=0, lavl=0, lmuscl=0, lumist=0, lgamma=0, lcds4=0,
              flux_limiter=0, const_mflux=0, lbuoy=0, boussinesq=0, lout=0, ltransient=0, lles=0,
+             low=0, loe=0, los=0, lon=0, lob=0, lot=0,
              periodic=0, conumfix=0, isol_p=SOLVER["cgstab_sip"], piso_solver=SOLVER["pcgsip"])
     for q in (IU, IV, IW, IP):
         p["lcal"][q - 1] = 1

@@ -7,6 +7,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <vector>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -1274,12 +1276,137 @@ int calcp(cappgpu_solve_report* reps) {
   return agg;
 }
 
-// outbc.f90:31: returns at once unless an outlet exists (lout).  Outlet
-// mass-flux rescaling is not part of the configured cases.
+// ------------------------------------------------------------------ outbc
+// outbc.f90:3-318.  With an outlet (lout), the mass flux through every
+// outlet face (code 2) of the face sets flagged low..lot is formed --
+// den(ghost) times u(interior) dotted with ar1x,ar1y,ar1z of the ghost for
+// all six sets, as the reference writes it -- and summed in the routine's
+// loop order; then each outlet ghost takes the interior velocity times
+// fac = flowin/(flow+small), its flux is scaled by fac, and te, ed, vis, t
+// are copied from the interior (vart, con, utt, vtt, wtt have no field
+// here).  The face lists are built on the host in the reference's loop
+// order, the fluxes are formed on the device and the flow is summed on the
+// host in that order, so fac carries the reference's rounding.  Each face
+// set is its own launch, in order: the corner ghosts that two sets share
+// take the later set's values, and a later set may read an earlier set's
+// ghost as its interior neighbour, as in the reference's sequence.  Face
+// sets: 0 W, 1 E, 2 S, 3 N, 4 B, 5 T.
+namespace {
+struct OutbcBuf {
+  int3* ent = nullptr;     // per face: ghost inp, interior inh, index of its flux
+  double* val = nullptr;   // per face: its flux
+  size_t cap = 0;
+};
+OutbcBuf g_ob;
+
+__global__ void k_outbc_flux(int n, const int3* __restrict__ e, const double* __restrict__ den,
+                             const double* __restrict__ a1x, const double* __restrict__ a1y,
+                             const double* __restrict__ a1z, const double* __restrict__ u,
+                             const double* __restrict__ v, const double* __restrict__ w, double* __restrict__ f,
+                             double* __restrict__ val) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int3 q = e[t];
+    const double fl = den[q.x] * (a1x[q.x] * u[q.y] + a1y[q.x] * v[q.y] + a1z[q.x] * w[q.y]);
+    f[q.z] = fl;
+    val[t] = fl;
+  }
+}
+
+__global__ void k_outbc_scale(int n, const int3* __restrict__ e, double fac, double* u, double* v, double* w,
+                              double* f, double* te, double* ed, double* vis, double* tt) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int3 q = e[t];
+    u[q.x] = u[q.y] * fac;
+    v[q.x] = v[q.y] * fac;
+    w[q.x] = w[q.y] * fac;
+    f[q.z] = f[q.z] * fac;
+    te[q.x] = te[q.y];
+    ed[q.x] = ed[q.y];
+    vis[q.x] = vis[q.y];
+    tt[q.x] = tt[q.y];
+  }
+}
+}  // namespace
+
+void outbc_free() {
+  if (g_ob.ent) cudaFree(g_ob.ent);
+  if (g_ob.val) cudaFree(g_ob.val);
+  g_ob = OutbcBuf();
+}
+
 int outbc() {
-  if (!ctx().prm.lout) return CAPPGPU_OK;
-  set_error("outbc: outlet boundaries (lout) are not supported by this build");
-  return CAPPGPU_E_ARG;
+  Ctx& c = ctx();
+  const cappgpu_params& P = c.prm;
+  if (!P.lout) return CAPPGPU_OK;   // outbc.f90:31
+  const Dims& d = c.d;
+  double** F = c.f;
+  const int on[6] = {P.low, P.loe, P.los, P.lon, P.lob, P.lot};
+  const int bcf[6] = {CAP_LBW, CAP_LBE, CAP_LBS, CAP_LBN, CAP_LBB, CAP_LBT};
+  const int ff[6] = {CAP_F1, CAP_F1, CAP_F2, CAP_F2, CAP_F3, CAP_F3};
+  std::vector<int3> ent;
+  size_t start[7];
+  for (int set = 0; set < 6; ++set) {
+    start[set] = ent.size();
+    if (!on[set]) continue;
+    const int len = set < 2 ? d.njk : set < 4 ? d.nik : d.nij;
+    std::vector<int> code((size_t)len);
+    CAP_CUDA(cudaMemcpyAsync(code.data(), c.bc[bcf[set]], sizeof(int) * len, cudaMemcpyDeviceToHost, c.st));
+    CAP_CUDA(cudaStreamSynchronize(c.st));
+    // outer x inner loops: k,j (W/E); k,i (S/N); i,j (B/T)
+    const int o_hi = set < 4 ? d.nkm : d.nim;
+    const int i_hi = (set == 2 || set == 3) ? d.nim : d.njm;
+    for (int o = 2; o <= o_hi; ++o)
+      for (int q = 2; q <= i_hi; ++q) {
+        int inp, inbc, inh, at;
+        switch (set) {
+          case 0: inp = ixk(d, 2, q, o); inbc = (q - 1) * d.nk + o; inh = inp + d.nj; at = inp; break;
+          case 1: inp = ixk(d, d.nim, q, o); inbc = (q - 1) * d.nk + o; inh = inp - d.nj; at = inh; break;
+          case 2: inp = ixk(d, q, 2, o); inbc = (q - 1) * d.nk + o; inh = inp + 1; at = inp; break;
+          case 3: inp = ixk(d, q, d.njm, o); inbc = (q - 1) * d.nk + o; inh = inp - 1; at = inh; break;
+          case 4: inp = ixk(d, o, q, 2); inbc = (o - 1) * d.nj + q; inh = inp + d.nij; at = inp; break;
+          default: inp = ixk(d, o, q, d.nkm); inbc = (o - 1) * d.nj + q; inh = inp - d.nij; at = inh; break;
+        }
+        if (code[(size_t)inbc - 1] == 2) ent.push_back(make_int3(inp, inh, at));
+      }
+  }
+  start[6] = ent.size();
+  const size_t n = ent.size();
+  if (n > g_ob.cap) {
+    outbc_free();
+    if (cudaMalloc(&g_ob.ent, sizeof(int3) * n) != cudaSuccess || cudaMalloc(&g_ob.val, sizeof(double) * n) != cudaSuccess) {
+      outbc_free();
+      set_error("outbc: out of device memory");
+      return CAPPGPU_E_NOMEM;
+    }
+    g_ob.cap = n;
+  }
+  double flow = 0.0;
+  std::vector<double> val(n);
+  if (n) {
+    CAP_CUDA(cudaMemcpyAsync(g_ob.ent, ent.data(), sizeof(int3) * n, cudaMemcpyHostToDevice, c.st));
+    for (int set = 0; set < 6; ++set) {
+      const int m = (int)(start[set + 1] - start[set]);
+      if (m)
+        launch(k_outbc_flux, grid_for(m), kThreads, c.st, m, (const int3*)g_ob.ent + start[set],
+               (const double*)F[CAP_DEN], (const double*)F[CAP_AR1X], (const double*)F[CAP_AR1Y],
+               (const double*)F[CAP_AR1Z], (const double*)F[CAP_U], (const double*)F[CAP_V], (const double*)F[CAP_W],
+               F[ff[set]], g_ob.val + start[set]);
+    }
+    CAP_CHECK_LAUNCH();
+    CAP_CUDA(cudaMemcpyAsync(val.data(), g_ob.val, sizeof(double) * n, cudaMemcpyDeviceToHost, c.st));
+    CAP_CUDA(cudaStreamSynchronize(c.st));
+    for (int set = 0; set < 6; ++set)   // flow in the routine's order: minus W/S/B, plus E/N/T
+      for (size_t e = start[set]; e < start[set + 1]; ++e) flow = (set & 1) ? flow + val[e] : flow - val[e];
+  }
+  const double fac = P.flowin / (flow + CAP_SMALL);   // outbc.f90:147
+  for (int set = 0; set < 6; ++set) {
+    const int m = (int)(start[set + 1] - start[set]);
+    if (m)
+      launch(k_outbc_scale, grid_for(m), kThreads, c.st, m, (const int3*)g_ob.ent + start[set], fac, F[CAP_U],
+             F[CAP_V], F[CAP_W], F[ff[set]], F[CAP_TE], F[CAP_ED], F[CAP_VIS], F[CAP_T]);
+  }
+  CAP_CHECK_LAUNCH();
+  return CAPPGPU_OK;
 }
 
 }  // namespace cap

@@ -90,6 +90,7 @@ static void free_all() {
   learned_free();
   facegeo_free();
   volr_free();
+  outbc_free();
   Ctx& c = ctx();
   for (auto& p : c.f) { if (p) cudaFree(p); p = nullptr; }
   for (auto& p : c.bc) { if (p) cudaFree(p); p = nullptr; }

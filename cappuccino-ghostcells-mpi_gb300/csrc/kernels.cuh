@@ -27,6 +27,8 @@ void fast_free();
 // 1/vol cache of the FP64 gradient (stencil.cu)
 void facegeo_free();
 void volr_free();
+// outlet face lists of outbc (assembly.cu)
+void outbc_free();
 // learned initial guess (learned.cu)
 void learned_free();
 int learned_solve_start(int fif, double res0);

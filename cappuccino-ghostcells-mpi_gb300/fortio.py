@@ -95,7 +95,8 @@ def write_grid(path, case, source=None, low=False, loe=False, los=False, lon=Fal
 def read_grid(path):
     """A Case with the grid file's dimensions, geometry and BC codes (the
     solver parameters are the defaults; set them before use).  The boundary
-    logicals and flags go to case.meta."""
+    logicals and flags go to case.meta; the outlet logicals low..lot and
+    lout also to case.params, where outbc reads them."""
     from .cases import Case, _base_params, _common_fields
     with open(path, "rb") as f:
         ni, nj, nk = struct.unpack("<3i", _read_record(f))
@@ -120,8 +121,10 @@ def read_grid(path):
     case = Case("grid", ni, nj, nk, fields=fields, params=_base_params())
     case.bc = bc
     _common_fields(case, nijk)
-    case.meta.update(dict(zip(("low", "loe", "los", "lon", "lob", "lot", "lout"), (bool(v) for v in flags[:7]))),
+    names = ("low", "loe", "los", "lon", "lob", "lot", "lout")
+    case.meta.update(dict(zip(names, (bool(v) for v in flags[:7]))),
                      lthermbc=flags[7], lconbc=flags[8], grid_file=str(path))
+    case.params.update(dict(zip(names, (int(bool(v)) for v in flags[:7]))))   # outbc reads them
     return case
 
 

@@ -357,6 +357,9 @@ class Library:
     def correct_boundary_conditions(self):
         self._check(self.lib.cappgpu_correct_boundary_conditions(), "correctBoundaryConditions")
 
+    def outbc(self):
+        self._check(self.lib.cappgpu_outbc(), "outbc")
+
     def courant(self):
         self._check(self.lib.cappgpu_courant(), "courant")
 

@@ -71,6 +71,8 @@ class Params(ctypes.Structure):
         ("conumfix", ctypes.c_int),
         ("isol_p", ctypes.c_int),
         ("piso_solver", ctypes.c_int),
+        ("low", ctypes.c_int), ("loe", ctypes.c_int), ("los", ctypes.c_int),
+        ("lon", ctypes.c_int), ("lob", ctypes.c_int), ("lot", ctypes.c_int),
         ("pad_", ctypes.c_int),
     ]
 

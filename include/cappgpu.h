@@ -126,6 +126,8 @@ typedef struct cappgpu_params {
   int    conumfix;
   int    isol_p;                    /* calcp p' solver, calcp...f90:22 (5)  */
   int    piso_solver;               /* PISO p solver, PISO_multiple_correction.f90:138-142 (4 = pcgsip) */
+  int    low, loe, los, lon, lob, lot;   /* outlet faces present, read with the
+                                       grid (read_grid.f90:140); outbc    */
   int    pad_;
 } cappgpu_params;
 
@@ -388,7 +390,10 @@ int cappgpu_fluxmass(int idew, int idns, int idtb, int arvx, int arvy, int arvz,
                      int fif, int acfe, int acfw, int fcf);
 /* calcp (SIMPLE), calcp-multiple_correction_SIMPLE.f90:3-238 */
 int cappgpu_calcp(cappgpu_solve_report* rep);
-/* outbc, outbc.f90:3-318 */
+/* outbc, outbc.f90:3-318: with lout, rescales the outlet faces (code 2)
+   of the face sets flagged low..lot so that their mass flow equals
+   flowin.  The flow is summed in the routine's loop order (on the host,
+   from the device-formed face fluxes), so the result is bit-exact. */
 int cappgpu_outbc(void);
 /* correctBoundaryConditions, correctBoundaryConditions.f90:1-86 */
 int cappgpu_correct_boundary_conditions(void);

@@ -231,6 +231,9 @@ class State:
     def correct_boundary_conditions(self):
         self.L.cap_correct_boundary_conditions(self.ptr)
 
+    def outbc(self):
+        self.L.cap_outbc(self.ptr)
+
     def courant(self):
         self.L.cap_courant(self.ptr)
 

@@ -750,36 +750,61 @@ double cap_fluxmc(cap_state* s, int inp, int idew, int idns, int idtb, int fiff)
          dppnnr;
 }
 
-/* outbc.f90:3-318: only acts when an outlet exists (lout); the configs of
-   this build have none, and for them the routine returns at :31. */
-void cap_outbc(cap_state* s) {
-  if (!s->prm.lout) return;
-  /* Outlet mass-flux rescaling for outlet faces is not exercised by the
-     configured cases; restated only for the west/east faces that an
-     inflow/outflow case would use. */
-  cappgpu_params* P = &s->prm;
-  double *f1 = s->f[CAP_F1], *u = s->f[CAP_U], *v = s->f[CAP_V], *w = s->f[CAP_W];
+/* outbc.f90:3-318: with an outlet (lout), the mass flux through the outlet
+   faces (code 2) of every face set whose flag low..lot is set is formed --
+   den(ghost) times u(interior) dotted with ar1x,ar1y,ar1z of the ghost for
+   all six sets, as the reference writes it -- and summed in the routine's
+   loop order (flow: minus on west/south/bottom, plus on east/north/top);
+   then every outlet ghost takes the interior velocity times
+   fac = flowin/(flow+small), its flux is scaled by fac, and te, ed, vis, t
+   are copied from the interior (vart, con, utt, vtt, wtt have no field
+   here).  Face sets: 0 W, 1 E, 2 S, 3 N, 4 B, 5 T. */
+static void outbc_set(cap_state* s, int set, int pass, double fac, double* flow) {
+  const cappgpu_params* P = &s->prm;
+  const int on[6] = {P->low, P->loe, P->los, P->lon, P->lob, P->lot};
+  if (!on[set]) return;
+  static const int bcf[6] = {CAP_LBW, CAP_LBE, CAP_LBS, CAP_LBN, CAP_LBB, CAP_LBT};
+  static const int ff[6] = {CAP_F1, CAP_F1, CAP_F2, CAP_F2, CAP_F3, CAP_F3};
+  double *u = s->f[CAP_U], *v = s->f[CAP_V], *w = s->f[CAP_W], *f = s->f[ff[set]];
+  double *te = s->f[CAP_TE], *ed = s->f[CAP_ED], *vis = s->f[CAP_VIS], *t = s->f[CAP_T];
   const double *den = s->f[CAP_DEN], *a1x = s->f[CAP_AR1X], *a1y = s->f[CAP_AR1Y], *a1z = s->f[CAP_AR1Z];
+  /* outer x inner loop ranges: k,j (W/E); k,i (S/N); i,j (B/T) */
+  const int o_hi = set < 4 ? s->nkm : s->nim;
+  const int i_hi = (set == 2 || set == 3) ? s->nim : s->njm;
+  for (int o = 2; o <= o_hi; ++o)
+    for (int q = 2; q <= i_hi; ++q) {
+      int inp, inbc, inh, at;
+      switch (set) {
+        case 0: inp = IXK(2, q, o); inbc = (q - 1) * s->nk + o; inh = inp + s->nj; at = inp; break;
+        case 1: inp = IXK(s->nim, q, o); inbc = (q - 1) * s->nk + o; inh = inp - s->nj; at = inh; break;
+        case 2: inp = IXK(q, 2, o); inbc = (q - 1) * s->nk + o; inh = inp + 1; at = inp; break;
+        case 3: inp = IXK(q, s->njm, o); inbc = (q - 1) * s->nk + o; inh = inp - 1; at = inh; break;
+        case 4: inp = IXK(o, q, 2); inbc = (o - 1) * s->nj + q; inh = inp + s->nij; at = inp; break;
+        default: inp = IXK(o, q, s->nkm); inbc = (o - 1) * s->nj + q; inh = inp - s->nij; at = inh; break;
+      }
+      if (s->bc[bcf[set]][inbc - 1] != 2) continue;
+      if (pass == 0) {
+        f[at] = den[inp] * (a1x[inp] * u[inh] + a1y[inp] * v[inh] + a1z[inp] * w[inh]);
+        *flow = (set & 1) ? *flow + f[at] : *flow - f[at];
+      } else {
+        u[inp] = u[inh] * fac;
+        v[inp] = v[inh] * fac;
+        w[inp] = w[inh] * fac;
+        f[at] = f[at] * fac;
+        te[inp] = te[inh];
+        ed[inp] = ed[inh];
+        vis[inp] = vis[inh];
+        t[inp] = t[inh];
+      }
+    }
+}
+
+void cap_outbc(cap_state* s) {
+  if (!s->prm.lout) return;   /* outbc.f90:31 */
   double flow = 0.0;
-  for (int k = 2; k <= s->nkm; ++k)
-    for (int j = 2; j <= s->njm; ++j) {
-      int inp = IXK(s->nim, j, k), inbc = (j - 1) * s->nk + k;
-      if (s->bc[CAP_LBE][inbc - 1] == 2) {
-        int inh = inp - s->nj;
-        f1[inh] = den[inp] * (a1x[inp] * u[inh] + a1y[inp] * v[inh] + a1z[inp] * w[inh]);
-        flow = flow + f1[inh];
-      }
-    }
-  double fac = P->flowin / (flow + SMALL);
-  for (int k = 2; k <= s->nkm; ++k)
-    for (int j = 2; j <= s->njm; ++j) {
-      int inp = IXK(s->nim, j, k), inbc = (j - 1) * s->nk + k;
-      if (s->bc[CAP_LBE][inbc - 1] == 2) {
-        int inh = inp - s->nj;
-        u[inp] = u[inh] * fac; v[inp] = v[inh] * fac; w[inp] = w[inh] * fac;
-        f1[inh] = f1[inh] * fac;
-      }
-    }
+  for (int set = 0; set < 6; ++set) outbc_set(s, set, 0, 0.0, &flow);
+  const double fac = s->prm.flowin / (flow + SMALL);   /* :147 */
+  for (int set = 0; set < 6; ++set) outbc_set(s, set, 1, fac, &flow);
 }
 
 /* correctBoundaryConditions.f90:1-86 (periodic copies into the padding

@@ -167,3 +167,43 @@ def test_simple_iterations_run(oracle_mod):
         assert np.all(np.isfinite(st.field(n))), n
     # the lid drives a flow
     assert np.abs(st.field("u")).max() > 1e-3
+
+
+def test_outbc_restores_the_inflow(oracle_mod):
+    """outbc.f90: after the rescale the flux through the outlet faces sums
+    to flowin, and an outlet ghost holds the interior velocity times
+    fac = flowin/flow, with te copied from the interior."""
+    case = cappgpu.cases.cavity(N=(6, 5, 7))
+    st = oracle_mod.State.from_case(case, geometry_orient=1)
+    with_fluxes(case, st)
+    rng = np.random.default_rng(8)
+    for n in ("u", "v", "w", "te", "ed", "vis", "t", "den"):
+        st.set_field(n, rng.uniform(0.5, 1.5, st.nijk))
+    ni, nj, nk = st.dims
+    st.bc("lbe")[:] = 2
+    st.bc("lbt")[:] = 2
+    st.params.update(dict(lout=1, loe=1, lot=1, flowin=0.7))
+    v = lambda n: case.view(st.field(n)).copy()
+    u0, te0 = v("u"), v("te")
+    st.outbc()
+    f1, f3, u, te = v("f1"), v("f3"), v("u"), v("te")
+    # east fluxes sit at i = nim-1, top fluxes at k = nkm-1 (0-based ni-3, nk-3)
+    flow = f1[1:nk - 1, ni - 3, 1:nj - 1].sum() + f3[nk - 3, 1:ni - 1, 1:nj - 1].sum()
+    assert flow == pytest.approx(0.7, rel=1e-12)
+    # an east ghost away from the top set: u(nim) = u(nim-1) * fac
+    k, j = 2, 2
+    fac = u[k, ni - 2, j] / u0[k, ni - 3, j]
+    assert u[k + 1, ni - 2, j] == pytest.approx(u0[k + 1, ni - 3, j] * fac, rel=1e-14)
+    assert te[k, ni - 2, j] == te0[k, ni - 3, j]
+
+
+def test_outbc_without_outlet_is_a_no_op(oracle_mod):
+    case = cappgpu.cases.cavity(N=(5, 4, 6))
+    st = oracle_mod.State.from_case(case)
+    with_fluxes(case, st)
+    st.bc("lbe")[:] = 2
+    st.params.update(dict(lout=0, loe=1, flowin=0.7))
+    before = {n: st.field(n).copy() for n in ("u", "f1")}
+    st.outbc()
+    for n, a in before.items():
+        np.testing.assert_array_equal(st.field(n), a)
