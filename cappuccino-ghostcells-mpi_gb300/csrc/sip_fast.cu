@@ -555,16 +555,29 @@ __device__ double2 block_scalar2(const double* __restrict__ part, int n, Fn fn) 
 }
 
 // sk = res.z from the backward sweep's partials; bet = sk/s0
-// (pcg-sip.f90:229-233); pk = zk + bet pk (pcg-sip.f90:241)
+// (pcg-sip.f90:229-233); pk = zk + bet pk (pcg-sip.f90:241).  Two-phase
+// passes of U chunks (see CellPass).
 __global__ void k_pk_x(DG g, const double* __restrict__ zk, const double* __restrict__ pko, double* __restrict__ pkn,
                        const double* __restrict__ wpart, int nwp, double* scal, const int* ctl) {
   if (*(volatile const int*)ctl) return;
   const double2 sb = block_scalar2(wpart, nwp, [&](double v) { return v / scal[0]; });
   const double sk = sb.x, bet = sb.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[1] = sk; scal[4] = bet; }
-  for_cells(g, [&](long long t_, int a, int b, int c) {
-    pkn[t_] = zk[t_] + bet * pko[t_];
-  });
+  constexpr int U = 4;
+  const int lane = threadIdx.x & 31, nw = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int q0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * U; q0 < g.nchunk; q0 += nw * U) {
+    CellPass<U> P;
+    pass_cells<U>(g, q0, lane, P);
+    double zv[U], pv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      zv[u] = P.ok[u] ? zk[P.t[u]] : 0.0;
+      pv[u] = P.ok[u] ? pko[P.t[u]] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (P.ok[u]) pkn[P.t[u]] = zv[u] + bet * pv[u];
+  }
 }
 
 // pkapk from the product's partials, alf = sk/pkapk (pcg-sip.f90:261-263);
@@ -576,13 +589,30 @@ __global__ void k_update_x(DG g, double* __restrict__ fi, double* __restrict__ r
   const double2 sa = block_scalar2(pin, kRedBlocks, [&](double v) { return scal[1] / v; });
   const double pkapk = sa.x, alf = sa.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[2] = pkapk; scal[3] = alf; }
+  constexpr int U = 4;
+  const int lane = threadIdx.x & 31, nw = (int)((gridDim.x * blockDim.x) >> 5);
   double v[1] = {0.0};
-  for_cells(g, [&](long long t_, int a, int b, int c) {
-    fi[t_] = fi[t_] + alf * pk[t_];
-    const double r = res[t_] - alf * zz[t_];
-    res[t_] = r;
-    v[0] += fabs(r);
-  });
+  for (int q0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * U; q0 < g.nchunk; q0 += nw * U) {
+    CellPass<U> P;
+    pass_cells<U>(g, q0, lane, P);
+    double fv[U], rv[U], pv[U], zv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long t = P.t[u];
+      fv[u] = P.ok[u] ? fi[t] : 0.0;
+      rv[u] = P.ok[u] ? res[t] : 0.0;
+      pv[u] = P.ok[u] ? pk[t] : 0.0;
+      zv[u] = P.ok[u] ? zz[t] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (!P.ok[u]) continue;
+      fi[P.t[u]] = fv[u] + alf * pv[u];
+      const double r = rv[u] - alf * zv[u];
+      res[P.t[u]] = r;
+      v[0] += fabs(r);
+    }
+  }
   block_reduce_store<1>(v, pout);
 }
 
