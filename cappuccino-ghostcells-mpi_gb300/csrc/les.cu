@@ -4,7 +4,10 @@
 // step drivers after the pressure-velocity coupling when lcal(ivis) and lles
 // are set (main.f90:205).  Each element keeps the reference's operation
 // order; exp, log and pow are CUDA's, so results agree with the oracle's
-// libm to a few ulps rather than bit for bit.
+// libm to a few ulps rather than bit for bit.  With the FP32 coefficient
+// assembly of precision modes 1-2 the strain rate and the Smagorinsky
+// viscosity are evaluated in FP32 arithmetic (FP64 storage), like the
+// coefficients they feed.
 #include <math.h>
 
 #include "common.cuh"
@@ -15,7 +18,16 @@ namespace cap {
 namespace {
 
 // |S| = sqrt(2 s_ij s_ij) over k = 2..nkm, i = 3..nimm, j = 3..njmm
-// (find_strain_rate.f90:33-76; the vorticity invariant of :77 is not kept)
+// (find_strain_rate.f90:33-76; the vorticity invariant of :77 is not kept);
+// R = float in precision modes 1-2 with the FP32 coefficient assembly
+__device__ __forceinline__ double sqrt_l(double x) { return sqrt(x); }
+__device__ __forceinline__ float sqrt_l(float x) { return sqrtf(x); }
+__device__ __forceinline__ double pow_l(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float pow_l(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double exp_l(double x) { return exp(x); }
+__device__ __forceinline__ float exp_l(float x) { return expf(x); }
+
+template <typename R>
 __global__ void k_strain(Dims d, Box b, const double* __restrict__ gux, const double* __restrict__ guy,
                          const double* __restrict__ guz, const double* __restrict__ gvx,
                          const double* __restrict__ gvy, const double* __restrict__ gvz,
@@ -26,41 +38,44 @@ __global__ void k_strain(Dims d, Box b, const double* __restrict__ gux, const do
     int i, j, k;
     b.at(t, i, j, k);
     const int inp = ixk(d, i, j, k);
-    const double s11 = gux[inp];
-    const double s12 = 0.5 * (guy[inp] + gvx[inp]);
-    const double s13 = 0.5 * (guz[inp] + gwx[inp]);
-    const double s22 = gvy[inp];
-    const double s23 = 0.5 * (gvz[inp] + gwy[inp]);
-    const double s33 = gwz[inp];
-    strain[inp] = sqrt(2 * (s11 * s11 + s22 * s22 + s33 * s33 + 2 * (s12 * s12 + s13 * s13 + s23 * s23)));
+    const R s11 = R(gux[inp]);
+    const R s12 = R(0.5) * (R(guy[inp]) + R(gvx[inp]));
+    const R s13 = R(0.5) * (R(guz[inp]) + R(gwx[inp]));
+    const R s22 = R(gvy[inp]);
+    const R s23 = R(0.5) * (R(gvz[inp]) + R(gwy[inp]));
+    const R s33 = R(gwz[inp]);
+    strain[inp] = sqrt_l(R(2) * (s11 * s11 + s22 * s22 + s33 * s33 + R(2) * (s12 * s12 + s13 * s13 + s23 * s23)));
   }
 }
 
 // Smagorinsky viscosity, Van Driest damping and Schumann's length limit
 // (calc_vis_les.f90:42-73): the coefficient is the 0.17 assigned last (:66),
 // C_delta the default-real 0.158, the exponent the default-real 1./3.
+template <typename R>
 __global__ void k_vis_les(Dims d, Box b, const double* __restrict__ u, const double* __restrict__ v,
                           const double* __restrict__ w, const double* __restrict__ wd,
                           const double* __restrict__ vol, const double* __restrict__ strain,
-                          const double* __restrict__ den, double* __restrict__ vis, double viscos, double cappa,
-                          double urf) {
-  const double c_delta = (double)0.158f, c_les = (double)0.17f, third = (double)(1.f / 3.f);
+                          const double* __restrict__ den, double* __restrict__ vis, double viscos_d, double cappa_d,
+                          double urf_d) {
+  const R c_delta = R(0.158f), c_les = R(0.17f), third = R(1.f / 3.f);
+  const R viscos = R(viscos_d), cappa = R(cappa_d), urf = R(urf_d);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < b.count();
        t += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
     b.at(t, i, j, k);
     const int inp = ixk(d, i, j, k);
-    const double visold = vis[inp];
-    const double wldist = wd[inp];
-    const double uref = sqrt(u[inp] * u[inp] + v[inp] * v[inp] + w[inp] * w[inp]);
-    const double utau = sqrt(viscos * uref / wldist);
-    const double zplus = wldist * utau / viscos;
-    const double lm = c_les * pow(vol[inp], third);
-    const double ls = cappa / c_delta * wldist;
-    const double l = (lm < ls ? lm : ls) * (1. - exp(-zplus / 26.0));
-    const double vis_smag = l * l * strain[inp] * den[inp];
-    const double vnew = vis_smag + viscos;
-    vis[inp] = urf * vnew + (1. - urf) * visold;
+    const R visold = R(vis[inp]);
+    const R wldist = R(wd[inp]);
+    const R uu = R(u[inp]), vv = R(v[inp]), ww = R(w[inp]);
+    const R uref = sqrt_l(uu * uu + vv * vv + ww * ww);
+    const R utau = sqrt_l(viscos * uref / wldist);
+    const R zplus = wldist * utau / viscos;
+    const R lm = c_les * pow_l(R(vol[inp]), third);
+    const R ls = cappa / c_delta * wldist;
+    const R l = (lm < ls ? lm : ls) * (R(1) - exp_l(-zplus / R(26.0)));
+    const R vis_smag = l * l * R(strain[inp]) * R(den[inp]);
+    const R vnew = vis_smag + viscos;
+    vis[inp] = urf * vnew + (R(1) - urf) * visold;
   }
 }
 
@@ -126,7 +141,9 @@ int find_strain_rate() {
   if ((rc = grad_gauss(CAP_V, CAP_GRADV_X, CAP_GRADV_Y, CAP_GRADV_Z))) return rc;
   if ((rc = grad_gauss(CAP_W, CAP_GRADW_X, CAP_GRADW_Y, CAP_GRADW_Z))) return rc;
   Box b{3, d.nimm, 3, d.njmm, 2, d.nkm};
-  launch(k_strain, grid_for(b.count()), kThreads, c.st, d, b, (const double*)F[CAP_GRADU_X],
+  // precision modes 1-2 with the FP32 coefficient assembly: FP32 arithmetic
+  launch(c.fp32(4) ? k_strain<float> : k_strain<double>, grid_for(b.count()), kThreads, c.st, d, b,
+         (const double*)F[CAP_GRADU_X],
          (const double*)F[CAP_GRADU_Y], (const double*)F[CAP_GRADU_Z], (const double*)F[CAP_GRADV_X],
          (const double*)F[CAP_GRADV_Y], (const double*)F[CAP_GRADV_Z], (const double*)F[CAP_GRADW_X],
          (const double*)F[CAP_GRADW_Y], (const double*)F[CAP_GRADW_Z], F[CAP_STRAIN]);
@@ -140,7 +157,8 @@ int calc_vis_les() {
   double** F = c.f;
   const cappgpu_params& P = c.prm;
   Box b{3, d.nimm, 3, d.njmm, 2, d.nkm};
-  launch(k_vis_les, grid_for(b.count()), kThreads, c.st, d, b, (const double*)F[CAP_U], (const double*)F[CAP_V],
+  launch(c.fp32(4) ? k_vis_les<float> : k_vis_les<double>, grid_for(b.count()), kThreads, c.st, d, b,
+         (const double*)F[CAP_U], (const double*)F[CAP_V],
          (const double*)F[CAP_W], (const double*)F[CAP_WALLDIST], (const double*)F[CAP_VOL],
          (const double*)F[CAP_STRAIN], (const double*)F[CAP_DEN], F[CAP_VIS], P.viscos, P.cappa,
          P.urf[CAP_IVIS - 1]);
