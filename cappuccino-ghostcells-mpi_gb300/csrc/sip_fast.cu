@@ -487,24 +487,6 @@ __device__ __forceinline__ void pass_cells(const DG& g, int q0, int lane, CellPa
   }
 }
 
-// The same over rows: one warp takes a row (s, c), its lanes the row's cells
-// a = max(0, s-c-(Nj-1)) .. min(Ni-1, s-c).  Idle lanes at row ends, but all
-// of a warp's loads fall in one row of every array; the FP32 kernels with
-// many neighbour loads per cell (k_pk_spmv_fx) or little work per cell
-// (k_dot_fx) measured faster this way than with the compact walk.
-template <class F>
-__device__ __forceinline__ void for_rows(const DG& g, F&& f) {
-  const int lane = threadIdx.x & 31;
-  const int nrow = g.S * g.Nk;
-  const int step = (int)((gridDim.x * blockDim.x) >> 5);
-  for (int row = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); row < nrow; row += step) {
-    const int s = row / g.Nk, c = row - s * g.Nk;
-    const int hi = min(g.Ni - 1, s - c);
-    const long long base = (long long)row * g.P;
-    for (int a = max(0, s - c - (g.Nj - 1)) + lane; a <= hi; a += 32) f(base + a, a, s - a - c, c);
-  }
-}
-
 // ---------------------------------------------- batched CG iterations
 // The scalars of a CG iteration are formed by the kernel that needs them,
 // from the previous kernel's block partials, summed in a fixed order that is
