@@ -21,7 +21,8 @@
 // shared-memory ring, puts the sentinel back for the next launch and
 // publishes how many steps are staged.  The compute warp reads only shared
 // memory: its per-step inputs arrive by TMA, kLG hyperplanes per copy,
-// kLSlots copies in flight, and it checks the staged count once per copy.
+// kLSlots copies in flight, and it checks the staged count before a step
+// only when its last reading does not cover that step.
 //
 // The per-cell expressions are those of SipFwdF / SipBwdF (wave.cuh) with
 // the same operand order, so both engines give the same bits.  Backward
