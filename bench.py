@@ -13,14 +13,20 @@ fluxuvw x3, wall terms, three sipsol solves), PISO_multiple_correction
                step copies u,v,w,p,f1,f2,f3 from pinned host memory, runs
                cappgpu_piso_steps(1), and copies them back
   roofline     the SIP forward substitution (the hottest unit of the p
-               solve) against the measured HBM copy bandwidth
+               solve) against the measured HBM copy bandwidth, with the
+               FP64 issue rate measured in the same run beside it
   cpu_baseline the C oracle (the reference's algorithm restated,
-               single-threaded as the reference's recurrences are) on one
-               step of the same case on this machine's host
+               single-threaded as the reference's recurrences are) on the
+               first steps of the timed window, continued from the GPU's
+               post-warm-up state, on this machine's host
+  fp32_refined / fp32_learned  precision modes 1 and 2 over the same steps
+               from the same state; forms_summary repeats their headline
+               figures at the end of the line
 
 --impl reference times the oracle (the reference's CPU algorithm) on the
-same config; the reference itself is Fortran and no Fortran compiler exists
-in the build image.
+same config and the same window (--warmup steps untimed, then --steps
+timed); the reference itself is Fortran and no Fortran compiler exists in
+the build image.
 
 Multi-GPU: the step has no data-parallel split (the SIP recurrences are
 global), so N GPUs run N independent replicas (weak scaling), launched
@@ -148,6 +154,8 @@ def measured_bf16_peak():
     return 1900.0, "fallback"
 
 
+FP32_PARTS_DEFAULT = 11   # the library's default FP32 parts in precision modes 1-2
+CPU_SAMPLE = 2            # oracle steps of the cpu_baseline leg
 LEARN_STEPS = 20     # PISO steps whose pressure solves are recorded as training pairs
 LEARN_EPOCHS = 20
 LEARN_BLOCK = 64     # training window (cells per axis)
@@ -232,15 +240,32 @@ def time_oracle_steps(n, steps, warmup):
     return time.perf_counter() - t0
 
 
+def oracle_from_snapshot(lib, case, snap):
+    """An oracle state holding the library's state `snap` (every field, the
+    BC codes of the case and the parameters): the oracle continues the run
+    from where the device left it."""
+    import ctypes
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    fields, params = snap
+    st = oracle.State(case.ni, case.nj, case.nk)
+    for name, a in fields.items():
+        st.set_field(name, a)
+    for face, codes in case.bc.items():
+        st.bc(face)[:] = codes
+    ctypes.memmove(ctypes.addressof(st.params), ctypes.addressof(params), ctypes.sizeof(params))
+    return st
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
+    # the GPU arm's window: the same warm-up steps, then the same timed steps,
+    # each one PISO step of the same 128^3 case (about 5 s per step on one
+    # host core)
     steps = max(1, args.steps)
     warm = max(0, args.warmup)
-    # each timed step is one PISO step of the same 128^3 case; warm-up steps
-    # are capped at 1 to keep the arm within a few minutes
-    warm = min(warm, 1)
-    steps = min(steps, 3)
     t = time_oracle_steps(args.n, steps, warm)
     v = steps / t
     out = {
@@ -250,7 +275,8 @@ def run_reference(args, ws, rank):
         "config": {"workload": f"channel {args.n}^3 PISO (2 correctors, PCG-SIP p to 1e-6)",
                    "cells": args.n ** 3},
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                         "sample": f"{steps} PISO step(s) of the {args.n}^3 channel after {warm} warm-up"},
+                         "sample": f"steps {warm + 1}-{warm + steps} of the {args.n}^3 channel "
+                                   f"(the GPU arm's timed window), C oracle, 1 thread"},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference is Fortran (no compiler in the image); its algorithm restated in C "
                 "(oracle/) and run single-threaded, as its sequential SIP recurrences run",
@@ -268,6 +294,9 @@ def run_gpu(args, ws, rank, local):
     for _ in range(args.warmup):
         lib.piso_steps(1)
     snap = snapshot(lib)
+    # FP64 issue rate of this GPU (the ceiling of the FP64-bound kernels)
+    ms_rate, ops_rate = lib.profile_kernel(11, reps=3)
+    fp64_peak = ops_rate / (ms_rate / 1e3)
     clocks = ClockSampler(local)
     launches0 = lib.stats().launches
     group.barrier()
@@ -397,12 +426,29 @@ def run_gpu(args, ws, rank, local):
         lib.piso_steps(args.steps)
         tight[mode] = result_state(lib)
     lib.precision(0)
+    # every part in FP32, the coefficient assembly included (not the default:
+    # FP32 coefficients change the FP64 system the refinement solves)
+    restore(lib, snap)
+    converged_solves()
+    lib.set_option("fp32_parts", 31)
+    lib.precision(1)
+    lib.piso_steps(args.steps)
+    tight_all32 = result_state(lib)
+    lib.precision(0)
+    lib.set_option("fp32_parts", FP32_PARTS_DEFAULT)
     # FP64 with the pressure solves 100x tighter: how far the 1e-6 tolerance
     # itself lets a solution lie from the converged one
     restore(lib, snap)
     converged_solves(1e-2)
     lib.piso_steps(args.steps)
     tight_fine = result_state(lib)
+    # mode 1 at the same tighter tolerance: the arithmetic's own error
+    restore(lib, snap)
+    converged_solves(1e-2)
+    lib.precision(1)
+    lib.piso_steps(args.steps)
+    tight_fine32 = result_state(lib)
+    lib.precision(0)
     lib.set_option("tight_correctors", 0)
     restore(lib, snap)
     precision_check = {
@@ -412,6 +458,10 @@ def run_gpu(args, ws, rank, local):
         "fp32_refined_vs_fp64": state_errors(tight[1], tight[0]),
         "fp32_learned_vs_fp64": state_errors(tight[2], tight[0]),
         "fp32_refined_vs_fp64_solved_100x_tighter": state_errors(tight[1], tight_fine),
+        "fp32_refined_vs_fp64_both_solved_100x_tighter": state_errors(tight_fine32, tight_fine),
+        "fp32_all_parts_vs_fp64": state_errors(tight_all32, tight[0]),
+        "fp32_parts": {"default": FP32_PARTS_DEFAULT, "meaning": "1 pressure solve, 2 momentum solves, "
+                       "8 velocity gradients in FP32; 4 momentum assembly, 16 pressure assembly FP64"},
         "note": "every pressure corrector solved to the last one's tolerance and the momentum solves to 1e-9 "
                 "in all runs",
     }
@@ -425,6 +475,14 @@ def run_gpu(args, ws, rank, local):
                     (7, "sip_forward_fp32"), (8, "sip_backward_fp32")):
         m, b = lib.profile_kernel(w, reps=3)
         units[name] = {"ms": m, "GBps": b / (m / 1e3) / 1e9}
+    # FP64 instructions per interior cell, counted from the kernels' source:
+    # the SIP forward substitution 7 (3 multiplies, 3 subtractions, 1
+    # multiply), the 7-point product with its dot 15 (7 multiplies, 6
+    # subtractions, 1 multiply and 1 add)
+    fp64 = {"peak_lane_ops_per_s": fp64_peak, "peak_source": "measured in this run (profile unit 11)"}
+    for name, ms_u, per_cell in (("sip_forward", ms_fwd, 7), ("spmv_dot", units["spmv_dot"]["ms"], 15)):
+        rate = per_cell * cells / (ms_u / 1e3)
+        fp64[name] = {"fp64_ops_per_cell": per_cell, "lane_ops_per_s": rate, "frac": rate / fp64_peak}
 
     out = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
@@ -438,10 +496,10 @@ def run_gpu(args, ws, rank, local):
         "p_rel_residual": st.p_report.resl / st.p_report.res0 if st.p_report.res0 else None,
         "e2e": {"value": ws * e2e_steps / (e2e_ms / 1e3), "unit": "steps/s",
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
-        "roofline": {"bound": "hbm", "kernel": "SIP forward substitution (pcg-sip.f90:204-212)",
+        "roofline": {"bound": "hbm", "kernel": "SIP forward substitution (pcg-sip.f90:98-106)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": profiled_traffic(args.n),
-                     "algorithmic_bytes": bytes_fwd, "ms_per_launch": ms_fwd},
+                     "algorithmic_bytes": bytes_fwd, "ms_per_launch": ms_fwd, "fp64_issue": fp64},
         "units": units,
         "fp32_refined": fp32,
         "fp32_learned": learned,
@@ -450,9 +508,33 @@ def run_gpu(args, ws, rank, local):
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        t = time_oracle_steps(args.n, 1, 0)
-        out["cpu_baseline"] = {"value": 1.0 / t, "unit": "steps/s", "cores": 1, "kind": "port",
-                               "sample": f"1 PISO step of the {args.n}^3 channel (C oracle, 1 thread)"}
+        # the oracle continues from the GPU's post-warm-up state: the first
+        # CPU_SAMPLE steps of the timed window (about 10 s of one core)
+        st_cpu = oracle_from_snapshot(lib, case, snap)
+        t0 = time.perf_counter()
+        for _ in range(CPU_SAMPLE):
+            st_cpu.piso_steps(1)
+        t = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": CPU_SAMPLE / t, "unit": "steps/s", "cores": 1, "kind": "port",
+                               "sample": f"steps {args.warmup + 1}-{args.warmup + CPU_SAMPLE} of the {args.n}^3 "
+                                         f"channel from the GPU's post-warm-up state (C oracle, 1 thread)"}
+    # the forms' headline figures once more at the end of the line
+    out["forms_summary"] = {
+        "fp64_ms_per_step": ms / args.steps, "fp64_p_solve_ms": st.p_solve_ms,
+        "fp32_refined_steps_per_s": fp32["value"], "fp32_refined_ms_per_step": fp32["ms_per_step"],
+        "fp32_refined_p_solve_ms": fp32["p_solve_ms"],
+        "fp32_learned_steps_per_s": learned["value"], "fp32_learned_ms_per_step": learned["ms_per_step"],
+        "fp32_learned_p_solve_ms": learned["p_solve_ms"],
+        "speedup_fp32_refined": (ms / args.steps) / fp32["ms_per_step"],
+        "speedup_fp32_learned": (ms / args.steps) / learned["ms_per_step"],
+        "fp32_refined_errors": {k: v for k, v in precision_check["fp32_refined_vs_fp64"].items()
+                                if k.endswith("rel_l2")},
+        "fp64_tolerance_spread": {k: v for k, v in precision_check["fp64_vs_fp64_solved_100x_tighter"].items()
+                                  if k.endswith("rel_l2")},
+        "fp32_refined_errors_at_equal_tighter_tolerance": {
+            k: v for k, v in precision_check["fp32_refined_vs_fp64_both_solved_100x_tighter"].items()
+            if k.endswith("rel_l2")},
+    }
     group.close()
     lib.finalize()
     if rank == 0:

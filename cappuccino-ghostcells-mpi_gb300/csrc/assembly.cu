@@ -681,7 +681,7 @@ int piso_assemble(int idew, int idns, int idtb, int arvx, int arvy, int arvz, in
   Box b{2, d.nimm, 2, d.njmm, 2, d.nkmm};
   FaceGeoPtrs G{};
   bool geo = false;
-  if (c.fp32(4)) {
+  if (c.fp32(16)) {
     launch(k_piso_peq_faces<float, false>, grid_for(b.count()), kThreads, c.st, d, b, A, G);
   } else {
     int rc = face_geo(idew, idns, idtb, arvx, arvy, arvz, fif, &G, &geo);
@@ -892,7 +892,7 @@ __global__ void k_vel_corr(Dims d, Box b, int simple, double* u, double* v, doub
   }
 }
 
-// continuityErrors.h:378-394 partial sums (global, sum |local|) and the
+// continuityErrors.h:59-81 partial sums (global, sum |local|) and the
 // last cell's local error
 __global__ void k_continuity(Dims d, Box b, const double* __restrict__ f1, const double* __restrict__ f2,
                              const double* __restrict__ f3, double* part, double* last) {
@@ -928,7 +928,7 @@ int continuity_errors() {
   return CAPPGPU_OK;
 }
 
-// CourantNo.h:262-282: su = sum |F| over the cell faces (su zeroed first),
+// CourantNo.h:29-52: su = sum |F| over the cell faces (su zeroed first),
 // max(su/vol), sum vol, sum su.
 __global__ void k_courant(Dims d, Box b, double* su, const double* __restrict__ f1, const double* __restrict__ f2,
                           const double* __restrict__ f3, const double* __restrict__ vol, double* part) {

@@ -54,10 +54,20 @@ constexpr int kThreads = 256;
 constexpr int kRedBlocks = 608;   // 152 SMs x 4
 constexpr int kMaxRed = 4;        // values reduced by one kernel
 
+// Polls of the exit wait for the block's own TMA copies in flight.  A copy
+// from valid memory always lands, so this bound is independent of the
+// spin limit on predecessors (which a caller may set very low): the block
+// never leaves while a copy into its shared memory is still running.
+constexpr long long kDrainPolls = 1LL << 27;
+
+constexpr int kStageSlots = 8;   // staging arrays for unregistered host-pointer arguments
+
 struct Ctx {
   bool init = false;
   Dims d{};
-  double* f[CAP_NFIELDS] = {};
+  // fields, then kStageSlots staging arrays of the host-pointer entry points
+  // (allocated on first use; ids CAP_NFIELDS + k)
+  double* f[CAP_NFIELDS + kStageSlots] = {};
   int* bc[CAP_NBC] = {};
   int* li = nullptr;   // device li[1..ni]
   int* lk = nullptr;   // device lk[1..nk]
@@ -70,6 +80,10 @@ struct Ctx {
   double* work[8] = {};         // solver work vectors (nijk each)
   int* wf_flags = nullptr;      // wavefront tile flags / counters
   double* host_reg[CAP_NFIELDS] = {};  // registered host arrays
+  double* host_vec3[CAP_NFIELDS] = {}; // registered interleaved (3, nijk) host arrays, by x-component field
+  double* vec3buf = nullptr;           // device staging of one interleaved array (3 nijk doubles)
+  cappgpu_solve_report last_rep{};     // the last linear solve: report, solver and ifi
+  int last_solver = 0, last_ifi = 0;
   // instrumentation (cappgpu_get_stats)
   unsigned long long launches = 0;     // kernels launched since init
   double p_solve_ms = 0.0;             // last PISO/SIMPLE pressure solve
@@ -81,8 +95,11 @@ struct Ctx {
   int tight_correctors = 0;            // 1: every PISO corrector solves p to reltol, not only the last
   int cg_batch = 4;                    // CG iterations launched between two host reads of the exit test
   int inner_drop = 4;                  // FP32 inner CG stops at 10^-inner_drop of the outer residual
-  int fp32_parts = 15;                 // parts in FP32 in precision modes 1-2: 1 p solve, 2 sipsol,
-                                       // 4 coefficient assembly, 8 velocity gradients
+  long long spin_limit = 1LL << 21;    // polls of a wavefront wait on a predecessor before CAPPGPU_E_SPIN
+  int device = 0;                      // CUDA device ordinal current at cappgpu_init
+  int fp32_parts = 11;                 // parts in FP32 in precision modes 1-2: 1 p solve, 2 sipsol,
+                                       // 4 momentum assembly (fluxuvw, LES viscosity), 8 velocity
+                                       // gradients, 16 pressure-equation assembly
   bool fp32(int part) const { return precision >= 1 && (fp32_parts & part) != 0; }
   int precision = 0;                   // pcgsip: 0 FP64 plain, 1 FP32 preconditioned CG in FP64 refinement
   unsigned long long geo_gen = 1;      // bumped whenever a grid-geometry field may have changed
@@ -94,6 +111,7 @@ void set_error(const char* fmt, ...);
 // centres, face areas, interpolation factors) invalidates the per-face
 // geometry derived from it
 void note_write(int q);
+bool spmv_output_ok(int q);
 int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 
 #define CAP_CUDA(call)                                                     \

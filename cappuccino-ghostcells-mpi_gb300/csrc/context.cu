@@ -72,6 +72,16 @@ static const char* kFieldNames[CAP_NFIELDS] = {
     "gradu_x", "gradu_y", "gradu_z", "gradv_x", "gradv_y", "gradv_z",
     "gradw_x", "gradw_y", "gradw_z", "gradp_x", "gradp_y", "gradp_z"};
 
+// Output field of the 7-point products (cappgpu_spmv, cappgpu_spmv_noalloc):
+// not one of the coefficients it reads (ae..ap, read through restrict
+// pointers) nor a grid-geometry field (a product written there would
+// leave the geometry caches stale).
+bool spmv_output_ok(int q) {
+  if (q >= CAP_AE && q <= CAP_AP) return false;
+  if (q >= CAP_X && q <= CAP_AR3Z) return false;   // nodes, centres, vol, fx..fz, face areas
+  return true;
+}
+
 void note_write(int q) {
   switch (q) {
     case CAP_X: case CAP_Y: case CAP_Z: case CAP_XC: case CAP_YC: case CAP_ZC:
@@ -102,6 +112,7 @@ static void free_all() {
   if (c.hred) cudaFreeHost(c.hred);
   if (c.dscal) cudaFree(c.dscal);
   if (c.wf_flags) cudaFree(c.wf_flags);
+  if (c.vec3buf) cudaFree(c.vec3buf);
   for (auto& e : c.ev) { if (e) cudaEventDestroy(e); e = nullptr; }
   if (c.st) cudaStreamDestroy(c.st);
   c = Ctx();
@@ -142,6 +153,7 @@ int cappgpu_init(int ni, int nj, int nk) {
   d.nimm = d.nim - 1; d.njmm = d.njm - 1; d.nkmm = d.nkm - 1;
   d.nij = ni * nj; d.nik = ni * nk; d.njk = nj * nk; d.nijk = d.nij * nk;
   size_t nb = sizeof(double) * (size_t)d.nijk;
+  CAP_CUDA(cudaGetDevice(&c.device));   // the context's stream and arrays live on this device
   CAP_CUDA(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
   for (int q = 0; q < CAP_NFIELDS; ++q) {
     if (cudaMalloc(&c.f[q], nb) != cudaSuccess) { free_all(); set_error("out of device memory"); return CAPPGPU_E_NOMEM; }
@@ -289,7 +301,7 @@ int cappgpu_set_option(const char* key, int value) {
     ctx().inner_drop = value;
     return CAPPGPU_OK;
   }
-  if (strcmp(key, "fp32_parts") == 0 && value >= 0 && value <= 15) {
+  if (strcmp(key, "fp32_parts") == 0 && value >= 0 && value <= 31) {
     ctx().fp32_parts = value;
     return CAPPGPU_OK;
   }
@@ -304,6 +316,10 @@ int cappgpu_set_option(const char* key, int value) {
       facegeo_free();
       volr_free();
     }
+    return CAPPGPU_OK;
+  }
+  if (strcmp(key, "spin_limit") == 0 && value >= 1) {
+    ctx().spin_limit = value;
     return CAPPGPU_OK;
   }
   if (strcmp(key, "tight_correctors") == 0 && (value == 0 || value == 1)) {

@@ -10,6 +10,45 @@ namespace cap {
 int profile_unit(int which, double* algo_bytes);
 }
 
+namespace cap {
+namespace {
+
+// FP64 issue-rate probe: eight independent multiply-add chains per thread
+// (compiled without fused multiply-add, so each line is one FP64 multiply
+// and one FP64 add), every SM filled with 2048 threads.  The result is the
+// rate at which this GPU retires FP64 lane-operations, the ceiling of the
+// FP64 kernels here whose work per byte is above about 0.08 operations.
+constexpr int kRateIters = 2048;
+constexpr int kRateChains = 8;
+
+__global__ void __launch_bounds__(256) k_fp64_rate(double* out, double a, double b) {
+  double x[kRateChains];
+#pragma unroll
+  for (int q = 0; q < kRateChains; ++q) x[q] = 1e-3 * (threadIdx.x + q);
+  for (int it = 0; it < kRateIters; ++it) {
+#pragma unroll
+    for (int q = 0; q < kRateChains; ++q) x[q] = x[q] * a + b;
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int q = 0; q < kRateChains; ++q) s += x[q];
+  if (s == -1.0) out[0] = s;   // never true; keeps the chains live
+}
+
+int fp64_rate_unit(double* lane_ops) {
+  Ctx& c = ctx();
+  int sms = 0;
+  CAP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
+  const int blocks = sms * 8;
+  launch(k_fp64_rate, blocks, 256, c.st, c.dscal + 15, 0.999999, 1e-6);
+  CAP_CHECK_LAUNCH();
+  *lane_ops = (double)blocks * 256 * kRateIters * kRateChains * 2;
+  return CAPPGPU_OK;
+}
+
+}  // namespace
+}  // namespace cap
+
 using namespace cap;
 
 extern "C" {
@@ -54,26 +93,29 @@ int cappgpu_host_free(void* p) {
 
 // Time `reps` back-to-back runs of one hot-path unit on the current device
 // state with CUDA events on the library stream.
-//   which 0: SIP forward substitution over the interior (pcg-sip.f90:204-212)
-//         1: SIP backward substitution (pcg-sip.f90:218-227)
-//         2: 7-point product with fused dot (pcg-sip.f90:248-259)
+//   which 0: SIP forward substitution over the interior (pcg-sip.f90:98-106)
+//         1: SIP backward substitution (pcg-sip.f90:112-121)
+//         2: 7-point product with fused dot (pcg-sip.f90:142-153)
 //         3: grad_gauss of u (GRAD_GAUSS.f90)
 //         4: fluxuvw, east faces (fluxuvw-overrelaxed-correction.f90)
 //         5: piso_assemble_pressure_eq, east faces, ipc=1
-//         6: SIP factorisation (pcg-sip.f90:174-193)
+//         6: SIP factorisation (pcg-sip.f90:68-87)
 //         7, 8: FP32 forward / backward substitution of the precision-1 form
+//         9, 10: the learned guess's net (inference; training pass)
+//         11: the FP64 issue-rate probe (algo_bytes = FP64 lane-operations)
 // Units 0,1,2,6,7,8 work on solver scratch vectors; 3-5 overwrite the module
 // arrays they write (gradu, su.., ae/aw, f1, be), as the routines do.
 int cappgpu_profile_kernel(int which, int reps, double* ms_per_unit, double* algo_bytes) {
   CAP_REQUIRE_INIT();
-  if (reps < 1 || which < 0 || which > 10) { set_error("profile_kernel: bad arguments"); return CAPPGPU_E_ARG; }
+  if (reps < 1 || which < 0 || which > 11) { set_error("profile_kernel: bad arguments"); return CAPPGPU_E_ARG; }
   Ctx& c = ctx();
   double bytes = 0.0;
-  int rc = profile_unit(which, &bytes);   // warm-up
+  auto unit = [&](double* b) { return which == 11 ? fp64_rate_unit(b) : profile_unit(which, b); };
+  int rc = unit(&bytes);   // warm-up
   if (rc) return rc;
   CAP_CUDA(cudaEventRecord(c.ev[2], c.st));
   for (int r = 0; r < reps; ++r)
-    if ((rc = profile_unit(which, &bytes))) return rc;
+    if ((rc = unit(&bytes))) return rc;
   CAP_CUDA(cudaEventRecord(c.ev[3], c.st));
   CAP_CUDA(cudaEventSynchronize(c.ev[3]));
   float f = 0.f;

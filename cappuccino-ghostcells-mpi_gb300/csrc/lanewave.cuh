@@ -132,7 +132,7 @@ struct LaneLayout {
   static constexpr size_t smem = 128 + kLSlots * slot_bytes + sizeof(LaneSmem);
 };
 
-// z = (r - bb zB - bw zW - bs zS) bp   (pcg-sip.f90:208-209; SipFwdF)
+// z = (r - bb zB - bw zW - bs zS) bp   (pcg-sip.f90:102-103; SipFwdF)
 struct LaneFwdF {
   static constexpr int kMaps = 2;   // r, forward factors (bb, bw, bs, bp)
   __host__ __device__ static constexpr int nq(int m) { return m == 0 ? 1 : 4; }
@@ -144,7 +144,7 @@ struct LaneFwdF {
   }
 };
 
-// z = z - bn zN - be zE - bt zT   (pcg-sip.f90:222-223; SipBwdF), the
+// z = z - bn zN - be zE - bt zT   (pcg-sip.f90:116-117; SipBwdF), the
 // engine's S, W, B being the j+1, i+1, k+1 cells
 struct LaneBwdF {
   static constexpr int kMaps = 2;   // z, backward factors (bn, be, bt)
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(64, 1) k_lane_wave(const __grid_constant__ Op 
     for (int gq = waited; gq < issued; ++gq) {
       long long it = 0;
       while (!mbar_test(&sm.full[gq % kLSlots], (unsigned)((gq / kLSlots) & 1))) {
-        if (++it > 64LL * w.spin_limit) {
+        if (++it > kDrainPolls) {
           atomicExch(w.abort, 1);
           atomicCAS(w.err, 0, 1);
           break;

@@ -1,5 +1,5 @@
 // noalloc.cu -- cappgpu_spmv_noalloc: the product zk = A pk and the dot
-// pk.zk of cappgpu_spmv (pcg-sip.f90:253-261) with its reduction scratch in
+// pk.zk of cappgpu_spmv (pcg-sip.f90:143-155) with its reduction scratch in
 // a fixed device array instead of memory obtained from the allocator.
 //
 // Some callers cannot allocate device memory at the point where they need
@@ -20,8 +20,13 @@
 //
 // The first call on a device looks up the array's device address with
 // cudaGetSymbolAddress and keeps it; that first call should come before any
-// stream capture is started.
+// stream capture is started.  Calls must be made with the context's device
+// (the one current at cappgpu_init) current: the kernels run on the
+// context's stream, so another device's address of the array would be
+// wrong for them, and such calls are refused.
 #include <math.h>
+
+#include <atomic>
 
 #include "common.cuh"
 #include "kernels.cuh"
@@ -38,23 +43,31 @@ constexpr int kNaMaxDevices = 64;
 
 __device__ __align__(256) double g_na_scratch[kNaMaxParts + 1];   // partials, then the result
 
-double* g_na_ptr[kNaMaxDevices] = {};   // device address of g_na_scratch, per device ordinal
+// device address of g_na_scratch per device ordinal; atomic because two host
+// threads may make their first call at once (both look up the same address)
+std::atomic<double*> g_na_ptr[kNaMaxDevices] = {};
 
-int na_scratch(double** out) {
+int na_scratch(int ctx_dev, double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice", __FILE__, __LINE__);
+  if (dev != ctx_dev) {
+    set_error("spmv_noalloc: device %d is current, the context lives on device %d", dev, ctx_dev);
+    return CAPPGPU_E_ARG;
+  }
   if (dev < 0 || dev >= kNaMaxDevices) {
     set_error("spmv_noalloc: device ordinal %d beyond %d", dev, kNaMaxDevices);
     return CAPPGPU_E_ARG;
   }
-  if (!g_na_ptr[dev]) {   // set-up, once per device, with that device current
+  double* ptr = g_na_ptr[dev].load(std::memory_order_acquire);
+  if (!ptr) {   // set-up, once per device, with that device current
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_na_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress", __FILE__, __LINE__);
-    g_na_ptr[dev] = static_cast<double*>(p);
+    ptr = static_cast<double*>(p);
+    g_na_ptr[dev].store(ptr, std::memory_order_release);
   }
-  *out = g_na_ptr[dev];
+  *out = ptr;
   return CAPPGPU_OK;
 }
 
@@ -115,8 +128,8 @@ extern "C" {
 
 int cappgpu_spmv_noalloc(int pk, int zk, double* dot) {
   CAP_REQUIRE_INIT();
-  if (pk < 0 || pk >= CAP_NFIELDS || zk < 0 || zk >= CAP_NFIELDS || pk == zk) {
-    set_error("spmv_noalloc: bad fields %d %d", pk, zk);
+  if (pk < 0 || pk >= CAP_NFIELDS || zk < 0 || zk >= CAP_NFIELDS || pk == zk || !spmv_output_ok(zk)) {
+    set_error("spmv_noalloc: bad fields %d %d (zk may not be a matrix coefficient or a geometry field)", pk, zk);
     return CAPPGPU_E_ARG;
   }
   Ctx& c = ctx();
@@ -130,7 +143,7 @@ int cappgpu_spmv_noalloc(int pk, int zk, double* dot) {
     return CAPPGPU_E_ARG;
   }
   double* scratch = nullptr;
-  int rc = na_scratch(&scratch);
+  int rc = na_scratch(c.device, &scratch);
   if (rc) return rc;
   if (nparts > 0) {
     double** F = c.f;

@@ -315,7 +315,7 @@ WaveCtl next_ctl() {
   w.partials = F.wpart;
   w.mailW = F.mail;
   w.mailB = F.mail + (size_t)F.nblk * BC * F.g.Nj * 3;
-  w.spin_limit = 1LL << 21;
+  w.spin_limit = ctx().spin_limit;
   w.skip = nullptr;
   return w;
 }
@@ -348,7 +348,7 @@ LaneCtl lane_ctl(const int* skip) {
   w.err = F.flags + 1;
   w.mailW = G.lmailW;
   w.mailB = G.lmailB;
-  w.spin_limit = 1LL << 21;
+  w.spin_limit = ctx().spin_limit;
   w.skip = skip;
   return w;
 }
@@ -537,7 +537,7 @@ __device__ double2 block_scalar2(const double* __restrict__ part, int n, Fn fn) 
 }
 
 // sk = res.z from the backward sweep's partials; bet = sk/s0
-// (pcg-sip.f90:229-233); pk = zk + bet pk (pcg-sip.f90:241).  Two-phase
+// (pcg-sip.f90:127); pk = zk + bet pk (pcg-sip.f90:135).  Two-phase
 // passes of U chunks (see CellPass).
 __global__ void k_pk_x(DG g, const double* __restrict__ zk, const double* __restrict__ pko, double* __restrict__ pkn,
                        const double* __restrict__ wpart, int nwp, double* scal, const int* ctl) {
@@ -562,8 +562,8 @@ __global__ void k_pk_x(DG g, const double* __restrict__ zk, const double* __rest
   }
 }
 
-// pkapk from the product's partials, alf = sk/pkapk (pcg-sip.f90:261-263);
-// fi += alf pk; res -= alf zz; partial sums |res| (pcg-sip.f90:268-281)
+// pkapk from the product's partials, alf = sk/pkapk (pcg-sip.f90:157);
+// fi += alf pk; res -= alf zz; partial sums |res| (pcg-sip.f90:161-175)
 __global__ void k_update_x(DG g, double* __restrict__ fi, double* __restrict__ res, const double* __restrict__ pk,
                            const double* __restrict__ zz, const double* __restrict__ pin, double* scal,
                            double* pout, const int* ctl) {
@@ -598,8 +598,8 @@ __global__ void k_update_x(DG g, double* __restrict__ fi, double* __restrict__ r
   block_reduce_store<1>(v, pout);
 }
 
-// resl = sum |res| (pcg-sip.f90:283-285), s0 = sk, exit test
-// resl/res0 < resmax (pcg-sip.f90:286-289); target > 0 replaces the test by
+// resl = sum |res| (pcg-sip.f90:161-177), s0 = sk, exit test
+// resl/res0 < resmax (pcg-sip.f90:185-188); target > 0 replaces the test by
 // resl <= target (inner loop of the refinement form)
 __global__ void k_cg_check(const double* __restrict__ part, double* scal, int* ctl, double res0, double resmax,
                            double target, int nsw) {
@@ -643,9 +643,9 @@ __global__ void k_spmv_x(DG g, const double* __restrict__ ae, const double* __re
 }
 
 // scalar steps of the CG iteration; one warp, fixed summation order
-// mode 0: sk = sum(wave partials); bet = sk/s0      (pcg-sip.f90:229-233)
-// mode 1: pkapk = sum(partials); alf = sk/pkapk       (pcg-sip.f90:261-263)
-// mode 2: resl = sum(partials); s0 = sk               (pcg-sip.f90:283-287)
+// mode 0: sk = sum(wave partials); bet = sk/s0      (pcg-sip.f90:127)
+// mode 1: pkapk = sum(partials); alf = sk/pkapk       (pcg-sip.f90:157)
+// mode 2: resl = sum(partials); s0 = sk               (pcg-sip.f90:177-186)
 // mode 3: res1 = sum(partials)                       (sipsol.f90:69)
 __global__ void k_cg_scalars(int mode, const double* part, int n, double* scal) {
   const int lane = threadIdx.x;
@@ -729,8 +729,8 @@ __global__ void k_dot_fx(DG g, const float* __restrict__ x, const float* __restr
   block_reduce_store<1>(v, part);
 }
 
-// pk = zk + beta pk (pcg-sip.f90:241) at the cell and its six neighbours,
-// zz = A pk (pcg-sip.f90:247-257), partial sums pk.zz
+// pk = zk + beta pk (pcg-sip.f90:135) at the cell and its six neighbours,
+// zz = A pk (pcg-sip.f90:142-153), partial sums pk.zz
 __global__ void __launch_bounds__(kThreads, 4) k_pk_spmv_fx(DG g, const float* __restrict__ ae, const float* __restrict__ aw,
                              const float* __restrict__ an, const float* __restrict__ as,
                              const float* __restrict__ at, const float* __restrict__ ab,
@@ -789,7 +789,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_pk_spmv_fx(DG g, const float* _
 }
 
 // alf from the partials; x += alf pk; r -= alf zz; partial sums |r|
-// (pcg-sip.f90:261-281)
+// (pcg-sip.f90:157-175)
 __global__ void k_update_fx(DG g, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ pk,
                             const float* __restrict__ zz, const double* __restrict__ pin, double* scal, double* pout,
                             const int* ctl) {
@@ -925,7 +925,7 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   if (rc) return rc;
   CAP_CUDA(cudaMemsetAsync(F.flags, 0, sizeof(int) * 2, c.st));
   const double resmax = P.sor[ifi - 1];
-  // res = 0 (pcg-sip.f90:150), then the initial residual and its L1 norm
+  // res = 0 (pcg-sip.f90:44), then the initial residual and its L1 norm
   CAP_CUDA(cudaMemsetAsync(c.f[CAP_RES], 0, sizeof(double) * d.nijk, c.st));
   double res0 = 0.0;
   if ((rc = resid_natural(fif, &res0))) return rc;
@@ -936,8 +936,8 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   if ((rc = to_d(CAP_RES, D_RES))) return rc;
   if ((rc = to_d(fif, D_FI))) return rc;
   const size_t nb = sizeof(double) * (size_t)F.g.size();
-  CAP_CUDA(cudaMemsetAsync(F.d[D_PK0], 0, nb, c.st));   // pk = 0 (pcg-sip.f90:148)
-  CAP_CUDA(cudaMemsetAsync(F.d[D_Z], 0, nb, c.st));     // zk = 0 (pcg-sip.f90:149)
+  CAP_CUDA(cudaMemsetAsync(F.d[D_PK0], 0, nb, c.st));   // pk = 0 (pcg-sip.f90:42)
+  CAP_CUDA(cudaMemsetAsync(F.d[D_Z], 0, nb, c.st));     // zk = 0 (pcg-sip.f90:43)
   if ((rc = factor_wave())) return rc;
   launch(k_set_scal, 1, 1, c.st, c.dscal, (double)1.e20f);   // s0 = 1.e20 (default real)
   const SipFwdD fwd = make_fwd(D_RES, D_Z, nullptr);
@@ -1122,7 +1122,7 @@ int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
 // pcgsip in the FP32 + FP64-refinement form (cappgpu_precision(1)).
 // Outer loop in FP64: r = su - A fi over the interior with the reference's
 // residual (pcg-sip.f90:150-165) and its exit test resl/res0 < sor(ifi)
-// (pcg-sip.f90:283-289).  Inner loop: conjugate gradients on A d = r in
+// (pcg-sip.f90:185-188).  Inner loop: conjugate gradients on A d = r in
 // FP32 with the FP32 SIP preconditioner (factorisation and substitutions as
 // wavefronts), stopped once the FP32 residual has dropped far enough for the
 // FP64 test or by 10^-inner_drop; then fi += d.  iters counts inner

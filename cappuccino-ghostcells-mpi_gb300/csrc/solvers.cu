@@ -27,7 +27,7 @@ static Coef coef() {
        t_ += (long long)gridDim.x * blockDim.x)
 
 // res = su + sum a_nb fi_nb - ap fi over box; partial sum |res|
-// (pcg-sip.f90:155-165)
+// (pcg-sip.f90:48-59)
 __global__ void k_resid(Dims d, Box b, Coef A, const double* __restrict__ fi, double* res, double* part) {
   double v[1] = {0.0};
   BOX_LOOP(b) {
@@ -43,7 +43,7 @@ __global__ void k_resid(Dims d, Box b, Coef A, const double* __restrict__ fi, do
   block_reduce_store<1>(v, part);
 }
 
-// z = A p (pcg-sip.f90:253-255); partial sum p.z
+// z = A p (pcg-sip.f90:147-149); partial sum p.z
 __global__ void k_spmv(Dims d, Box b, Coef A, const double* __restrict__ p, double* z, double* part) {
   double v[1] = {0.0};
   BOX_LOOP(b) {
@@ -72,7 +72,7 @@ __global__ void k_dot(Dims d, Box b, const double* __restrict__ a, const double*
   block_reduce_store<2>(v, part);
 }
 
-// pk = zk + bet pk (pcg-sip.f90:241)
+// pk = zk + bet pk (pcg-sip.f90:135)
 __global__ void k_pk(Dims d, Box b, const double* __restrict__ zk, double* pk, double bet) {
   BOX_LOOP(b) {
     int i, j, k;
@@ -82,7 +82,7 @@ __global__ void k_pk(Dims d, Box b, const double* __restrict__ zk, double* pk, d
   }
 }
 
-// fi += alf pk; res -= alf zk; partial sum |res| (pcg-sip.f90:273-277)
+// fi += alf pk; res -= alf zk; partial sum |res| (pcg-sip.f90:167-171)
 __global__ void k_update(Dims d, Box b, double* fi, double* res, const double* __restrict__ pk,
                          const double* __restrict__ zk, double alf, double* part) {
   double v[1] = {0.0};
@@ -485,7 +485,7 @@ int dpcg(int fif, int ifi, cappgpu_solve_report* rep) {
   return finish_status(resl, done, rep);
 }
 
-int solve(int solver, int fi, int ifi, cappgpu_solve_report* rep) {
+static int solve_dispatch(int solver, int fi, int ifi, cappgpu_solve_report* rep) {
   switch (solver) {
     case CAPPGPU_SOLVER_SIPSOL: return sipsol(fi, ifi, rep);
     case CAPPGPU_SOLVER_CGSTAB: return bicgstab(fi, ifi, false, rep);
@@ -495,6 +495,18 @@ int solve(int solver, int fi, int ifi, cappgpu_solve_report* rep) {
     case CAPPGPU_SOLVER_DPCG: return dpcg(fi, ifi, rep);
     default: set_error("unknown solver %d", solver); return CAPPGPU_E_ARG;
   }
+}
+
+// every solve through the selector records its report (cappgpu_last_report)
+int solve(int solver, int fi, int ifi, cappgpu_solve_report* rep) {
+  cappgpu_solve_report r{};
+  const int rc = solve_dispatch(solver, fi, ifi, &r);
+  Ctx& c = ctx();
+  c.last_rep = r;
+  c.last_solver = solver;
+  c.last_ifi = ifi;
+  if (rep) *rep = r;
+  return rc;
 }
 
 static int check_solver_args(int fi, int ifi) {
@@ -566,8 +578,8 @@ int cappgpu_dpcg(int fi, int ifi, cappgpu_solve_report* rep) {
 
 int cappgpu_spmv(int pk, int zk, double* dot) {
   CAP_REQUIRE_INIT();
-  if (pk < 0 || pk >= CAP_NFIELDS || zk < 0 || zk >= CAP_NFIELDS || pk == zk) {
-    set_error("spmv: bad fields %d %d", pk, zk);
+  if (pk < 0 || pk >= CAP_NFIELDS || zk < 0 || zk >= CAP_NFIELDS || pk == zk || !spmv_output_ok(zk)) {
+    set_error("spmv: bad fields %d %d (zk may not be a matrix coefficient or a geometry field)", pk, zk);
     return CAPPGPU_E_ARG;
   }
   Ctx& c = ctx();

@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
       for (int gq = max(0, issued - NSLOT); gq < issued; ++gq) {
         long long it = 0;
         while (!mbar_test(&sm.full[gq % NSLOT], (unsigned)((gq / NSLOT) & 1))) {
-          if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); break; }
+          if (++it > kDrainPolls) { wave_fail(w, bail, 1); break; }
         }
       }
     }
@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
 
 struct St3 { double bn, be, bt; };
 
-// SIP forward substitution z = (r - bb zB - bw zW - bs zS) bp (pcg-sip.f90:208-209)
+// SIP forward substitution z = (r - bb zB - bw zW - bs zS) bp (pcg-sip.f90:102-103)
 struct SipFwdD {
   using St = double;
   static constexpr int kMaps = 2;   // r, forward factors (bb, bw, bs, bp)
@@ -538,8 +538,8 @@ struct SipFwdD {
   }
 };
 
-// SIP backward substitution z = z - bn zN - be zE - bt zT (pcg-sip.f90:222-223)
-// with the fused dot sk = sum res.z (pcg-sip.f90:224); the engine's S, W, B
+// SIP backward substitution z = z - bn zN - be zE - bt zT (pcg-sip.f90:116-117)
+// with the fused dot sk = sum res.z (pcg-sip.f90:118); the engine's S, W, B
 // neighbours are the j+1, i+1, k+1 cells here.
 struct SipBwdD {
   using St = double;
@@ -587,7 +587,7 @@ struct SipBwdFiD {
   }
 };
 
-// SIP factorisation (pcg-sip.f90:178-190); state passed on = (bn, be, bt)
+// SIP factorisation (pcg-sip.f90:68-87); state passed on = (bn, be, bt)
 struct SipFactorD {
   using St = St3;
   static constexpr int kMaps = 7;   // ae, aw, an, as, at, ab, ap
@@ -631,7 +631,7 @@ struct SipFactorD {
 
 // ------------------------------------------------- single-precision ops
 // The preconditioner of the FP32 + FP64-refinement form of the pressure
-// solve: the same SIP recurrences (pcg-sip.f90:178-223) on FP32 copies of
+// solve: the same SIP recurrences (pcg-sip.f90:68-121) on FP32 copies of
 // the matrix, FP32 arithmetic, zero ghost states for the substitutions.
 // These do not reproduce the reference's FP64 results bit for bit and are
 // not meant to; the refinement loop around them restores the FP64 residual.

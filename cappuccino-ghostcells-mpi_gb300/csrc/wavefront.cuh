@@ -16,7 +16,7 @@
 
 namespace cap {
 
-// SIP factorisation, sipsol.f90:34-46 (pcg-sip.f90:178-190, cgstab_sip.f90:64-76)
+// SIP factorisation, sipsol.f90:34-46 (pcg-sip.f90:68-87, cgstab_sip.f90:64-76)
 struct SipFactorOp {
   const double *ae, *aw, *an, *as, *at, *ab, *ap;
   double *bb, *bw, *bs, *bp, *bn, *be, *bt;
@@ -39,7 +39,7 @@ struct SipFactorOp {
 };
 
 // SIP forward substitution z = (r - bb zB - bw zW - bs zS) bp
-// (pcg-sip.f90:208-209; sipsol.f90:70-71 with r = z = res)
+// (pcg-sip.f90:102-103; sipsol.f90:70-71 with r = z = res)
 struct SipFwdOp {
   const double *r, *bb, *bw, *bs, *bp;
   double* z;
@@ -49,7 +49,7 @@ struct SipFwdOp {
   }
 };
 
-// SIP backward substitution z = z - bn zN - be zE - bt zT (pcg-sip.f90:222-223);
+// SIP backward substitution z = z - bn zN - be zE - bt zT (pcg-sip.f90:116-117);
 // with fi != nullptr also fi += z (sipsol.f90:86-88).
 struct SipBwdOp {
   const double *bn, *be, *bt;

@@ -92,6 +92,19 @@ SIGNATURES = {
     "cappgpu_host_free": [ctypes.c_void_p],
     "cappgpu_profile_kernel": [_INT, _INT, _DP, _DP],
     "cappgpu_set_option": [ctypes.c_char_p, _INT],
+    # host-pointer drop-ins of the assembly routines (hostcall.cu)
+    "cappgpu_register_vec3": [_INT, _DP],
+    "cappgpu_update_values_at_ghostcells_h": [],
+    "cappgpu_bpres_h": [_DP],
+    "cappgpu_exchange_h": [_DP],
+    "cappgpu_fluxuvw_h": [_INT, _INT, _INT] + [_DP] * 7,
+    "cappgpu_piso_assemble_pressure_eq_h": [_INT, _INT, _INT] + [_DP] * 7 + [_INT, _DP],
+    "cappgpu_assemble_pressure_eq_h": [_INT, _INT, _INT] + [_DP] * 7,
+    "cappgpu_calcuvw_h": [_REP],
+    "cappgpu_piso_gethbya_h": [],
+    "cappgpu_piso_multiple_correction_h": [_REP],
+    "cappgpu_last_report": [ctypes.POINTER(_INT), ctypes.POINTER(_INT), _REP],
+    "cappgpu_solver_report_line": [_INT, _INT, _REP, _INT, _INT, ctypes.c_char_p, _INT],
 }
 RESTYPES = {"cappgpu_last_error": ctypes.c_char_p, "cappgpu_field_name": ctypes.c_char_p}
 

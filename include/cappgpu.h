@@ -132,7 +132,7 @@ typedef struct cappgpu_params {
 } cappgpu_params;
 
 /* Report of one linear solve (the reference writes these three numbers to
-   unit 66, e.g. pcg-sip.f90:301-303). */
+   unit 66, e.g. pcg-sip.f90:195-197). */
 typedef struct cappgpu_solve_report {
   double res0;      /* initial L1 residual                                 */
   double resl;      /* final L1 residual                                   */
@@ -200,9 +200,13 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    result to well above the arithmetic's precision, so two precision modes
    are compared with 1; it is not the reference's algorithm.
    "fp32_parts": bitmask of the parts that run in FP32 in precision modes
-   1-2 (default 15): 1 the pressure solve (pcgsip), 2 the momentum solves
-   (sipsol), 4 the coefficient assembly (fluxuvw, PISO pressure assembly),
-   8 the velocity gradients (grad_gauss of u, v, w).
+   1-2 (default 11 = 1|2|8): 1 the pressure solve (pcgsip), 2 the momentum
+   solves (sipsol), 4 the momentum assembly (fluxuvw, LES strain rate and
+   viscosity), 8 the velocity gradients (grad_gauss of u, v, w), 16 the
+   PISO pressure-equation assembly.  Parts 1, 2 and 8 keep every field
+   within 1e-5 (velocity components) of the FP64 form over 20 steps of the
+   128^3 channel; parts 4 and 16 change the FP64 system the refinement
+   solves and are off by default.
    "lane_wave": engine of the FP32 SIP substitutions of precision modes 1-2:
    0 = the persistent hyperplane wavefront, one thread per line (default);
    1 = one warp per tile of 32 x 8 lines, neighbours by shuffles and
@@ -222,7 +226,13 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    pcgsip stops once its residual has dropped by 10^-inner_drop (1..9,
    default 4) and restarts from the FP64 residual.
    "learn_conv": convolutions of the learned guess's net, 1 = tcgen05
-   (default), 0 = mma.sync (kept for cross-checks). */
+   (default), 0 = mma.sync (kept for cross-checks).
+   "spin_limit": polls a wavefront block makes on a predecessor's edge
+   states (and 64x as many on its own input copies) before it gives up,
+   raises the device-wide abort flag and the solve returns CAPPGPU_E_SPIN
+   (>= 1, default 2^21, about a second).  After CAPPGPU_E_SPIN the library
+   resets the block tickets and edge mailboxes, so the next solve runs
+   normally. */
 int cappgpu_set_option(const char* key, int value);
 
 /* Arithmetic of the step.  0 = FP64 plain, the reference's arithmetic
@@ -230,11 +240,11 @@ int cappgpu_set_option(const char* key, int value);
    - pcgsip: the SIP factors and both substitutions in FP32 inside conjugate
      gradients in FP32, wrapped in an FP64 refinement loop whose exit test
      is the reference's (L1 norm of the FP64 residual su - A fi over res0
-     below sor(ifi), pcg-sip.f90:283-289);
+     below sor(ifi), pcg-sip.f90:185-188);
    - sipsol: FP64 residual and exit test per sweep (sipsol.f90:60-69, 96),
      FP32 factors and substitutions, FP64 update of fi;
-   - coefficient assembly (fluxuvw, PISO pressure assembly) and the velocity
-     gradients in FP32 arithmetic with FP64 storage;
+   - the velocity gradients in FP32 arithmetic with FP64 storage (and, when
+     option fp32_parts asks for them, the coefficient assembly);
    residuals, norms, dot products, the flux and velocity corrections, the
    pressure gradient and the continuity error stay FP64.  The iterates are
    not the reference's.  2 = mode 1 with the learned initial guess of the
@@ -346,15 +356,19 @@ int cappgpu_iccg_h(double* fi, int ifi);
 int cappgpu_cgstab_h(double* fi, int ifi);
 int cappgpu_cgstab_sip_h(double* fi, int ifi);
 
-/* 7-point product z = A p (the pcgsip SpMV pass, pcg-sip.f90:143-155) with
-   the fused dot pk.z over the interior; exposed for tests and benches. */
+/* 7-point product z = A p (the pcgsip SpMV pass, pcg-sip.f90:142-153) with
+   the fused dot pk.z over the interior; exposed for tests and benches.
+   zk may not be pk, a matrix coefficient (ae..ap) or a geometry field
+   (CAPPGPU_E_ARG). */
 int cappgpu_spmv(int pk, int zk, double* dot);
 
 /* cappgpu_spmv without any device allocation; no counterpart in the
    reference.  For callers that cannot allocate device memory where they need
    the product (the device pool is held by another allocator, or cudaMalloc's
    implicit synchronisation is not acceptable inside the step loop).  zk is
-   the same as cappgpu_spmv's; the dot is summed in a different fixed order.
+   the same as cappgpu_spmv's (and obeys the same restrictions); the dot is
+   summed in a different fixed order.  The device current at the call must
+   be the one cappgpu_init ran on (CAPPGPU_E_ARG otherwise).
    The reduction scratch is a fixed 32 KB device array: grids with more than
    8,388,608 interior cells are rejected with CAPPGPU_E_ARG.  The first call
    on a device performs a one-time set-up (it looks up the array's device
@@ -410,6 +424,59 @@ int cappgpu_piso_steps(int nsteps, cappgpu_solve_report* last_p_report);
 /* nsteps SIMPLE outer iterations (ghost update, calcuvw, calcp). */
 int cappgpu_simple_iters(int niters, cappgpu_solve_report* last_p_report);
 
+/* ====================================== host-pointer drop-ins (assembly) */
+/* For a host program that keeps the reference's module arrays in host
+   memory and calls the routines one at a time with its own arrays (the
+   Fortran shim).  Each call copies the registered module arrays the
+   routine reads to the device, resolves every array argument by address
+   (a registered array is its field; any other array is copied into a
+   staging array, at most 8 per call), runs the routine, copies back the
+   registered arrays it writes and the written arguments, and synchronises.
+   Grid geometry is device-resident: uploaded once with cappgpu_set_field
+   (or cappgpu_build_geometry) and never copied by these calls; register
+   geometry arrays only so that they are recognised as arguments. */
+/* Interleaved (3, nijk) host array -- the reference's gradu(3,nxyza)
+   layout -- for the three component fields starting at field_x (one of
+   CAP_GRADU_X, CAP_GRADV_X, CAP_GRADW_X, CAP_GRADP_X); NULL unregisters. */
+int cappgpu_register_vec3(int field_x, double* host);
+/* update_values_at_ghostcells (update_values_at_ghostcells_nonperiodic.f90:3-642) */
+int cappgpu_update_values_at_ghostcells_h(void);
+/* bpres(p) (bpres.f90:3-81) */
+int cappgpu_bpres_h(double* p);
+/* exchange(phi) (exchange_mpi.f90:4-89): the identity on one rank */
+int cappgpu_exchange_h(double* phi);
+/* fluxuvw(idew,idns,idtb,arvx,arvy,arvz,fif,acfe,acfw,fcf)
+   (fluxuvw-overrelaxed-correction.f90:3) */
+int cappgpu_fluxuvw_h(int idew, int idns, int idtb, const double* arvx, const double* arvy, const double* arvz,
+                      const double* fif, double* acfe, double* acfw, const double* fcf);
+/* piso_assemble_pressure_eq(idew,idns,idtb,arvx,arvy,arvz,fif,acfe,acfw,fcf,ipc,bp)
+   (PISO_assemble_pressure_eq.f90:3) */
+int cappgpu_piso_assemble_pressure_eq_h(int idew, int idns, int idtb, const double* arvx, const double* arvy,
+                                        const double* arvz, const double* fif, double* acfe, double* acfw,
+                                        double* fcf, int ipc, double* bp);
+/* assemble_pressure_eq(idew,idns,idtb,arvx,arvy,arvz,fif,acfe,acfw,fcf)
+   (assemble_pressure_eq.f90:3) */
+int cappgpu_assemble_pressure_eq_h(int idew, int idns, int idtb, const double* arvx, const double* arvy,
+                                   const double* arvz, const double* fif, double* acfe, double* acfw, double* fcf);
+/* calcuvw (calcuvw.f90:3), PISO_getHbyA (PISO_getHbyA.f90:3) and
+   PISO_multiple_correction (PISO_multiple_correction.f90:3): every
+   registered non-geometry module array is copied in before and back
+   after.  rep as for the field-id entry points. */
+int cappgpu_calcuvw_h(cappgpu_solve_report* rep);
+int cappgpu_piso_gethbya_h(void);
+int cappgpu_piso_multiple_correction_h(cappgpu_solve_report* rep);
+/* The last linear solve run through the solver selector (the *_h and
+   field-id solver entry points, PISO and SIMPLE pressure solves): solver
+   code, ifi and report. */
+int cappgpu_last_report(int* solver, int* ifi, cappgpu_solve_report* rep);
+/* The reference's unit-66 line for a solve report (pcg-sip.f90:195-197,
+   sipsol.f90:101-103, iccg.f90:192-194, cgstab.f90:278-280,
+   cgstab_sip.f90:273-275 with icorr and ipcorr, pcg-jacobi.f90:150-152)
+   into buf (n bytes, NUL-terminated); the iteration number is the Fortran
+   loop index (iters + 1 when the solve did not converge). */
+int cappgpu_solver_report_line(int solver, int ifi, const cappgpu_solve_report* rep, int icorr, int ipcorr,
+                               char* buf, int n);
+
 /* ======================================================= instrumentation */
 typedef struct cappgpu_stats {
   long long launches;               /* kernels launched since cappgpu_init  */
@@ -429,8 +496,10 @@ int cappgpu_host_free(void* p);
    pressure assembly east, 6 SIP factorisation, 7 / 8 FP32 forward / backward
    sweep of the precision-1 form, 9 forward pass of the learned guess's net
    on this grid, 10 its forward and backward pass on a 64^3 window of the
-   first recorded pair) on the current state; returns device ms per unit and
-   its algorithmic bytes (units 9 and 10: algorithmic FLOPs). */
+   first recorded pair, 11 the FP64 issue-rate probe: independent FP64
+   multiplies and adds filling every SM) on the current state; returns
+   device ms per unit and its algorithmic bytes (units 9 and 10:
+   algorithmic FLOPs; unit 11: FP64 lane-operations). */
 int cappgpu_profile_kernel(int which, int reps, double* ms_per_unit, double* algo_bytes);
 
 #ifdef __cplusplus

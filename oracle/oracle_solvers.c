@@ -512,7 +512,7 @@ int cap_dpcg(cap_state* s, int fif, int ifi, cappgpu_solve_report* rep) {
   return done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
 }
 
-/* The pcgsip SpMV pass alone (pcg-sip.f90:248-259): z = A p, returns p.z */
+/* The pcgsip SpMV pass alone (pcg-sip.f90:142-153): z = A p, returns p.z */
 double cap_spmv(cap_state* s, int pkf, int zkf) {
   COEF_PTRS;
   const double* pk = s->f[pkf];

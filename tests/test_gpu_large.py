@@ -5,7 +5,7 @@ A seeded symmetric, diagonally dominant 7-diagonal system is solved with
 PCG-SIP in the FP64 plain form and in the FP32 + FP64-refinement form; the
 final residual is recomputed independently on the host with numpy in the
 reference's formula (res = su + sum a_nb phi_nb - ap phi over the interior,
-pcg-sip.f90:268-281, sipsol.f90:66-69).  At this size the hyperplane layout
+pcg-sip.f90:161-175, sipsol.f90:66-69).  At this size the hyperplane layout
 has 129 M slots, so the test covers the 32-bit index arithmetic of the
 layout, of the compact cell walk and of the wavefront at the top of the
 configured range."""

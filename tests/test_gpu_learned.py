@@ -114,3 +114,45 @@ def test_trained_guess_lowers_the_initial_residual(gpu_lib):
     assert r2.resl / r2.res0 < case.params["sor"][IP - 1]
     print(f"learned guess: loss {loss0:.3f} -> {loss:.3f}, last residual ratio {st['last_ratio']:.3f}, "
           f"last solve {r2.iters} iterations vs {r1.iters} without")
+
+
+def test_guess_that_raises_the_residual_is_discarded(gpu_lib, oracle_mod):
+    """A net whose output is the constant 1 (all weights zero, the last
+    bias 1): the fitted guess is a level shift fi + alpha, and with the
+    right-hand side a single spike the shift spreads residual over every
+    cell, so the guess's FP64 L1 residual is about twice res0.  The guess
+    must be discarded (one more fallback, no guess kept) and the solve must
+    then be the precision-1 solve from the original start, bit for bit."""
+    from helpers import diag_dominant_matrix, push
+    st = oracle_mod.State(24, 20, 28)
+    rng = np.random.default_rng(17)
+    diag_dominant_matrix(st, rng, symmetric=True)
+    ni, nj, nk = st.dims
+    su = np.zeros(st.nijk)
+    su[(12 - 1) * ni * nj + (9 - 1) * nj + (11 - 1)] = 1.0   # cell (i, j, k) = (9, 11, 12)
+    st.set_field("su", su)
+    st.set_field("p", np.zeros(st.nijk))
+    st.params.update(dict(alfa=0.92, sor=[1e-8] * 10, nsw=[2000] * 10, ipr=3, jpr=3, kpr=3))
+    push(gpu_lib, st)
+    gpu_lib.learn_reset(1, seed=3)
+    n = gpu_lib.learn_params().size
+    w = np.zeros(n, np.float32)
+    w[-1] = 1.0
+    gpu_lib.learn_params(w)
+    try:
+        gpu_lib.precision(1)
+        r1 = gpu_lib.pcgsip("p", IP)
+        p1 = gpu_lib.get_field("p")
+        gpu_lib.set_field("p", np.zeros(st.nijk))
+        s0 = gpu_lib.learn_stats()
+        gpu_lib.precision(2)
+        r2 = gpu_lib.pcgsip("p", IP)
+        p2 = gpu_lib.get_field("p")
+        s1 = gpu_lib.learn_stats()
+    finally:
+        gpu_lib.precision(0)
+    assert s1["fallbacks"] == s0["fallbacks"] + 1 and s1["guesses"] == s0["guesses"]
+    assert s1["last_ratio"] > 1.5, s1
+    assert r1.status == 0 and r2.status == 0
+    assert r2.res0 == r1.res0 and r2.iters == r1.iters and r2.resl == r1.resl
+    np.testing.assert_array_equal(p2, p1)
