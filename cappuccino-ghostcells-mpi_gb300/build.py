@@ -41,8 +41,11 @@ def _stale():
 
 
 def build(force=False, verbose=False, jobs=None):
-    """Compile every .cu under csrc/ and link libcappgpu.so; returns its path."""
-    if not force and not _stale():
+    """Compile every .cu under csrc/ and link libcappgpu.so; returns its path.
+    Extra nvcc flags (e.g. -D overrides of tuning constants) may be given in
+    the environment variable CAPPGPU_NVCC_FLAGS."""
+    extra = os.environ.get("CAPPGPU_NVCC_FLAGS", "").split()
+    if not force and not extra and not _stale():
         return LIB
     OUT.mkdir(exist_ok=True)
     exe = nvcc()
@@ -50,7 +53,7 @@ def build(force=False, verbose=False, jobs=None):
 
     def compile_one(src):
         obj = OUT / (src.stem + ".o")
-        cmd = [exe, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+        cmd = [exe, *ARCH, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stderr}")

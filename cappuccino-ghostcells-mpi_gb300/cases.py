@@ -22,7 +22,7 @@ import math
 
 import numpy as np
 
-from .params import IU, IV, IW, IP, IVIS, SOLVER, NPHI
+from .params import IU, IV, IW, IP, ITE, IED, IVIS, SOLVER, NPHI
 
 DEFAULT_SEED = 20261203
 
@@ -294,6 +294,78 @@ def channel(N=(128, 128, 128), beta=2.0, seed=DEFAULT_SEED, L=(2 * math.pi, math
     return case
 
 
+def rans_channel(N=(512, 256, 256), beta=2.5, L=(8 * math.pi, 2 * math.pi, 2.0), re_tau=590.0):
+    """Large RANS channel: N cells over 8pi (x, reference i) x 2pi (spanwise,
+    j) x 2 (wall-normal, k); periodic in i and j; tanh wall stretching
+    beta = 2.5; nu = 1/590 (u_tau = 1 at Re_tau = 590); Menter's k-omega SST
+    (sst, lcal of te, ed and vis; calcscm.f90, modvis.f90); initial fields:
+    the log-law mean velocity u+ = ln(y+)/0.41 + 5.2 (u+ = y+ below
+    y+ = 11), the log-law equilibrium k = u_tau^2/sqrt(0.09) (scaled by
+    (y+/10)^2 below y+ = 10) and wall-resolved omega = u_tau/(sqrt(0.09)
+    0.41 y), floored at k = 1e-3 and omega = 1, and the eddy viscosity of
+    init.f90:474; PISO with 2 correctors at CFL 0.5; constant mass flux at
+    the initial profile's bulk velocity; upwind convection for k and omega.
+    From uniform k = 1e-3 and omega = 1 the SST path as the reference
+    builds it drives k in the wall-adjacent cells below zero in the first
+    step (the explicit diffusion correction at the wall face), clips it to
+    small (calcscm.f90:595-599), and the omega source alphasst P / nu_t
+    (calcscm.f90:425-427) is 0/0 in the next; the equilibrium profiles keep
+    nu_t > 0.
+
+    Two settings follow from the reference rather than from the model:
+    cmu stays 0 (init.f90:177 assigns it for the k-epsilon models only, and
+    modvis.f90:217 divides by it, so F2 = 1), and the top wall plane is
+    lk(nkmm) (params.top_plane = 1): calcuvw.f90:254 writes lk(nimm), which
+    lies outside the arrays for ni > nk."""
+    N3 = tuple(N) if not np.isscalar(N) else (N, N, N)
+    ni, nj, nk, g = build_grid(*channel_nodes(N3, L, beta))
+    p = _base_params()
+    viscos = 1.0 / re_tau
+    p.update(viscos=viscos, ltransient=1, bdf=1, btime=0.0, periodic=1, ncorr=2, npcor=1,
+             conumfix=1, conumfixvalue=0.5, timestep=1e-3, alfa=0.5, lles=0, const_mflux=1,
+             sst=1, cmu=0.0, top_plane=1)
+    for q in (ITE, IED, IVIS):
+        p["lcal"][q - 1] = 1
+    for q in (IU, IV, IW, ITE, IED):
+        p["sor"][q - 1] = 1e-3
+        p["nsw"][q - 1] = 20
+    # upwind convection of k and omega (gds = 0: no deferred correction,
+    # fluxscm-overrelaxed-correction.f90:197); with central differences k
+    # undershoots, is clipped to small and omega's P / nu_t term turns 0/0
+    p["gds"][ITE - 1] = p["gds"][IED - 1] = 0.0
+    p["sor"][IP - 1] = 1e-6
+    p["nsw"][IP - 1] = 2000
+    p["ipr"], p["jpr"], p["kpr"] = 3, 3, 3 + N3[2] // 2
+    case = Case("rans_channel", ni, nj, nk, fields=dict(g), params=p)
+    case.bc = _bc_arrays(ni, nj, nk, {})
+    _common_fields(case, ni * nj * nk)
+    shape = (nk, ni, nj)
+    zc = case.fields["zc"].reshape(shape)
+    yw = np.clip(1.0 - np.abs(zc), 1e-12, None)   # distance to the nearer wall
+    ypl = yw * re_tau
+    uplus = np.where(ypl < 11.0, ypl, np.log(np.maximum(ypl, 1.0)) / 0.41 + 5.2)
+    mask = np.zeros(shape, bool)
+    mask[2:-2, 2:-2, 2:-2] = True
+    u = np.where(mask, uplus, 0.0)
+    case.fields["u"] = u.reshape(-1)
+    sqb = math.sqrt(0.09)
+    k0 = np.maximum(np.minimum(1.0, (ypl / 10.0) ** 2) / sqb, 1e-3)
+    w0 = np.maximum(1.0 / (sqb * 0.41 * yw), 1.0)
+    case.fields["te"] = np.where(mask, k0, 0.0).reshape(-1)
+    case.fields["ed"] = np.where(mask, w0, 0.0).reshape(-1)
+    den = case.fields["den"]
+    vis = case.fields["vis"].copy()
+    inner = mask.reshape(-1)
+    vis[inner] = viscos + den[inner] * case.fields["te"][inner] / (case.fields["ed"][inner] + 1e-30)   # init.f90:474
+    case.fields["vis"] = vis
+    # bulk velocity of the initial profile (volume-weighted), held by const_mflux
+    vol = case.fields["vol"].reshape(shape)[2:-2, 2:-2, 2:-2]
+    ub = float((u[2:-2, 2:-2, 2:-2] * vol).sum() / vol.sum())
+    case.params["uin"] = ub
+    case.meta.update(config="RANS channel, k-omega SST", N=N3, beta=beta, L=L, re_tau=re_tau)
+    return case
+
+
 def poisson(N=(256, 256, 256), amp=0.1, seed=DEFAULT_SEED):
     """Skewed-grid pressure-correction system: uniform unit-cube nodes
     displaced by seeded sinusoids of amplitude amp*h per axis.  The matrix
@@ -329,6 +401,6 @@ def poisson(N=(256, 256, 256), amp=0.1, seed=DEFAULT_SEED):
 def finalize_case(case):
     """Steps that need the library's geometry (face areas, interpolation
     factors): initial fluxes for the transient cases."""
-    if case.name == "channel":
+    if case.name in ("channel", "rans_channel"):
         case.fields.update(initial_face_fluxes(case))
     return case

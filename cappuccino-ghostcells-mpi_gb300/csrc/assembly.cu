@@ -421,6 +421,7 @@ __global__ void k_calcuvw_sources(Dims d, Box b, SrcArgs A) {
 }
 
 // calcuvw.f90:161-337 (first-order wall model), one wall per launch
+// top: 0 the bottom wall, else the k plane of the top wall's cells
 __global__ void k_calcuvw_wall(Dims d, int top, const double* __restrict__ xc, const double* __restrict__ yc,
                                const double* __restrict__ zc, const double* __restrict__ fz,
                                const double* __restrict__ a3x, const double* __restrict__ a3y,
@@ -441,7 +442,7 @@ __global__ void k_calcuvw_wall(Dims d, int top, const double* __restrict__ xc, c
       inbc = ixk(d, i, j, 3); ingc = inbc - d.nij; iface = ingc;
       fxp = fz[ingc]; fxe = 1.0 - fxp;
     } else {
-      inbc = ixk(d, i, j, d.nimm); ingc = inbc + d.nij; iface = inbc;  // lk(nimm), calcuvw.f90:254
+      inbc = ixk(d, i, j, top); ingc = inbc + d.nij; iface = inbc;  // lk(nimm) (calcuvw.f90:254) or lk(nkmm)
       fxp = 1.0 - fz[inbc]; fxe = 1.0 - fxp;
     }
     double gzx = xc[inbc] * fxp + xc[ingc] * fxe;
@@ -534,9 +535,11 @@ int calcuvw(cappgpu_solve_report* rep3) {
   const cappgpu_params& P = c.prm;
   int rc;
   // the top-wall loop addresses lk(nimm) (calcuvw.f90:254): inside the
-  // array only when nimm+1 <= nk
-  if (d.nimm + 1 > d.nk) {
-    set_error("top wall index lk(nimm) of calcuvw.f90:254 leaves the array (ni=%d > nk=%d)", d.ni, d.nk);
+  // array only when nimm+1 <= nk; params.top_plane = 1 takes lk(nkmm)
+  const int ktop = P.top_plane ? d.nkmm : d.nimm;
+  if (ktop + 1 > d.nk) {
+    set_error("top wall index lk(nimm) of calcuvw.f90:254 leaves the array (ni=%d > nk=%d); "
+              "params.top_plane = 1 takes lk(nkmm)", d.ni, d.nk);
     return CAPPGPU_E_ARG;
   }
   if ((rc = grad_gauss(CAP_U, CAP_GRADU_X, CAP_GRADU_Y, CAP_GRADU_Z))) return rc;
@@ -555,7 +558,7 @@ int calcuvw(cappgpu_solve_report* rep3) {
   if ((rc = fluxuvw(1, d.nij, d.nj, CAP_AR2X, CAP_AR2Y, CAP_AR2Z, CAP_FY, CAP_AN, CAP_AS, CAP_F2))) return rc;
   if ((rc = fluxuvw(d.nij, d.nj, 1, CAP_AR3X, CAP_AR3Y, CAP_AR3Z, CAP_FZ, CAP_AT, CAP_AB, CAP_F3))) return rc;
   int gw = grid_for((long long)(d.nimm - 2) * (d.njmm - 2));
-  for (int top = 0; top < 2; ++top)
+  for (int top : {0, ktop})
     launch(k_calcuvw_wall, gw, kThreads, c.st, d, top, F[CAP_XC], F[CAP_YC], F[CAP_ZC], F[CAP_FZ], F[CAP_AR3X],
                                               F[CAP_AR3Y], F[CAP_AR3Z], F[CAP_U], F[CAP_V], F[CAP_W], F[CAP_VIS],
                                               F[CAP_AP], F[CAP_SPV], F[CAP_SP], F[CAP_SU], F[CAP_SV], F[CAP_SW]);

@@ -70,7 +70,10 @@ static const char* kFieldNames[CAP_NFIELDS] = {
     "bb", "bs", "bw", "bp", "bn", "be", "bt",
     "he", "hw", "hn", "hs", "ht", "hb",
     "gradu_x", "gradu_y", "gradu_z", "gradv_x", "gradv_y", "gradv_z",
-    "gradw_x", "gradw_y", "gradw_z", "gradp_x", "gradp_y", "gradp_z"};
+    "gradw_x", "gradw_y", "gradw_z", "gradp_x", "gradp_y", "gradp_z",
+    "gradte_x", "gradte_y", "gradte_z", "graded_x", "graded_y", "graded_z",
+    "gen", "alphasst", "bettasst", "domega", "prtinv_te", "prtinv_ed",
+    "teo", "edo", "teoo", "edoo"};
 
 // Output field of the 7-point products (cappgpu_spmv, cappgpu_spmv_noalloc):
 // not one of the coefficients it reads (ae..ap, read through restrict
@@ -306,7 +309,7 @@ int cappgpu_set_option(const char* key, int value) {
     return CAPPGPU_OK;
   }
   if (strcmp(key, "learn_conv") == 0 && value >= 0 && value <= 2) return learned_set_conv(value);
-  if (strcmp(key, "lane_wave") == 0 && (value == 0 || value == 1)) {
+  if (strcmp(key, "lane_wave") == 0 && value >= 0 && value <= 2) {
     ctx().lane_wave = value;
     return CAPPGPU_OK;
   }

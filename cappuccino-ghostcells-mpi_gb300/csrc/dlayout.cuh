@@ -157,6 +157,18 @@ __device__ __forceinline__ void tma_load4(void* dst, const void* map, int x, int
       : "memory");
 }
 
+// L2 prefetch of a tiled box (no shared memory, no completion to wait for):
+// a later copy of the same box then reads from L2 instead of HBM
+__device__ __forceinline__ void tma_prefetch3(const void* map, int x, int y, int z) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(map), "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+__device__ __forceinline__ void tma_prefetch4(const void* map, int x, int q, int y, int z) {
+  asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global.tile [%0, {%1, %2, %3, %4}];" ::"l"(map), "r"(x), "r"(q),
+               "r"(y), "r"(z)
+               : "memory");
+}
+
 // ---------------------------------------------------- layout conversion
 // natural -> diagonal for the interior box (one thread per interior cell,
 // reads coalesced along j)

@@ -9,10 +9,11 @@
 namespace cap {
 
 // calcuvw.f90:254 and calc_vis_les.f90:174 address the top wall with
-// lk(nimm); that is inside the array only when nimm+1 <= nk.
+// lk(nimm); that is inside the array only when nimm+1 <= nk (params.top_plane
+// = 1 takes lk(nkmm) instead).
 static int check_top_wall_index() {
   const Dims& d = ctx().d;
-  if (d.nimm + 1 > d.nk) {
+  if (!ctx().prm.top_plane && d.nimm + 1 > d.nk) {
     set_error("top wall index lk(nimm) of calcuvw.f90:254 leaves the array (ni=%d > nk=%d)", d.ni, d.nk);
     return CAPPGPU_E_ARG;
   }
@@ -32,17 +33,31 @@ static int shift_time_levels() {
   CAP_CUDA(cudaMemcpyAsync(F[CAP_UO], F[CAP_U], nb, cudaMemcpyDeviceToDevice, c.st));
   CAP_CUDA(cudaMemcpyAsync(F[CAP_VO], F[CAP_V], nb, cudaMemcpyDeviceToDevice, c.st));
   CAP_CUDA(cudaMemcpyAsync(F[CAP_WO], F[CAP_W], nb, cudaMemcpyDeviceToDevice, c.st));
+  if (c.prm.lcal[CAP_ITE - 1] || c.prm.lcal[CAP_IED - 1]) {   // main.f90:144-145, 153-154
+    if (c.prm.bdf) {
+      CAP_CUDA(cudaMemcpyAsync(F[CAP_TEOO], F[CAP_TEO], nb, cudaMemcpyDeviceToDevice, c.st));
+      CAP_CUDA(cudaMemcpyAsync(F[CAP_EDOO], F[CAP_EDO], nb, cudaMemcpyDeviceToDevice, c.st));
+    }
+    CAP_CUDA(cudaMemcpyAsync(F[CAP_TEO], F[CAP_TE], nb, cudaMemcpyDeviceToDevice, c.st));
+    CAP_CUDA(cudaMemcpyAsync(F[CAP_EDO], F[CAP_ED], nb, cudaMemcpyDeviceToDevice, c.st));
+  }
   return CAPPGPU_OK;
 }
 
-// main.f90:205: the SGS viscosity of the LES model after the pressure-
-// velocity coupling; the strain is formed here (the reference forms it in
-// calcscm, which this path does not run)
-static int les_viscosity() {
+// main.f90:196-205 after the pressure-velocity coupling: the k and omega
+// equations (calcscm) when lcal(ite) / lcal(ied) with the SST model, then
+// the eddy viscosity (modvis) or, with lles, the sub-grid viscosity (its
+// strain is formed here: the reference forms it in calcscm, which does not
+// run on the LES path)
+static int turbulence() {
   const cappgpu_params& P = ctx().prm;
+  int rc;
+  cappgpu_solve_report rep;
+  if (P.sst && P.lcal[CAP_ITE - 1] && (rc = calcscm(CAP_ITE, &rep)) < 0) return rc;
+  if (P.sst && P.lcal[CAP_IED - 1] && (rc = calcscm(CAP_IED, &rep)) < 0) return rc;
+  if (P.lcal[CAP_IVIS - 1] && !P.lles && P.sst && (rc = modvis())) return rc;
   if (!P.lcal[CAP_IVIS - 1] || !P.lles) return CAPPGPU_OK;
-  int rc = find_strain_rate();
-  if (rc) return rc;
+  if ((rc = find_strain_rate())) return rc;
   return calc_vis_les();
 }
 
@@ -66,7 +81,7 @@ int piso_steps(int nsteps, cappgpu_solve_report* last) {
     if (rc < 0) return rc;
     agg |= rc;
     if (last) *last = reps[nrep - 1];
-    if ((rc = les_viscosity())) return rc;    // main.f90:205
+    if ((rc = turbulence())) return rc;       // main.f90:196-205
     if (c.prm.ltransient && c.prm.const_mflux && (rc = const_massflux_correction())) return rc;   // main.f90:252
   }
   return agg;
@@ -90,7 +105,7 @@ int simple_iters(int niters, cappgpu_solve_report* last) {
     if (rc < 0) return rc;
     agg |= rc;
     if (last) *last = reps[nrep - 1];
-    if ((rc = les_viscosity())) return rc;    // main.f90:205
+    if ((rc = turbulence())) return rc;       // main.f90:196-205
   }
   return agg;
 }

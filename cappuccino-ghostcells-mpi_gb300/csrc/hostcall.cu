@@ -54,7 +54,7 @@ bool is_geometry(int q) { return q >= CAP_X && q <= CAP_WALLDIST; }
 
 // the x-component field of the interleaved gradient array q belongs to, or -1
 int vec3_base(int q) {
-  for (int b : {CAP_GRADU_X, CAP_GRADV_X, CAP_GRADW_X, CAP_GRADP_X})
+  for (int b : {CAP_GRADU_X, CAP_GRADV_X, CAP_GRADW_X, CAP_GRADP_X, CAP_GRADTE_X, CAP_GRADED_X})
     if (q >= b && q < b + 3) return b;
   return -1;
 }
@@ -236,7 +236,7 @@ extern "C" {
 int cappgpu_register_vec3(int field_x, double* host) {
   CAP_REQUIRE_INIT();
   if (vec3_base(field_x) != field_x) {
-    set_error("register_vec3: %d is not the x component of a gradient (gradu, gradv, gradw, gradp)", field_x);
+    set_error("register_vec3: %d is not the x component of a gradient (gradu, gradv, gradw, gradp, gradte, graded)", field_x);
     return CAPPGPU_E_ARG;
   }
   ctx().host_vec3[field_x] = host;
@@ -344,6 +344,34 @@ int cappgpu_piso_multiple_correction_h(cappgpu_solve_report* rep) {
   int rc = fr.begin();
   if (rc) return fr.end(rc);
   return fr.end(piso_multiple_correction(rep));
+}
+
+// calcscm(fi,gradfi,ifi) (calcscm.f90:3-602): fi is the registered te or
+// ed, gradfi the interleaved array registered for gradte or graded
+int cappgpu_calcscm_h(double* fi, double* gradfi, int ifi) {
+  CAP_REQUIRE_INIT();
+  Ctx& c = ctx();
+  const int f = ifi == CAP_ITE ? CAP_TE : ifi == CAP_IED ? CAP_ED : -1;
+  const int g = ifi == CAP_ITE ? CAP_GRADTE_X : CAP_GRADED_X;
+  if (f < 0 || !fi || c.host_reg[f] != fi || !gradfi || c.host_vec3[g] != gradfi) {
+    set_error("calcscm_h: fi and gradfi must be the registered te/gradte (ifi = 5) or ed/graded (ifi = 6)");
+    return CAPPGPU_E_ARG;
+  }
+  Frame fr(all_state(), all_state());
+  int rc = fr.begin();
+  if (rc) return fr.end(rc);
+  cappgpu_solve_report rep;
+  return fr.end(calcscm(ifi, &rep));
+}
+
+// modvis (modvis.f90:195-236, SST)
+int cappgpu_modvis_h(void) {
+  CAP_REQUIRE_INIT();
+  const std::vector<int> in = {CAP_TE, CAP_ED, CAP_DEN, CAP_STRAIN, CAP_VIS};
+  Frame fr(in, {CAP_VIS});
+  int rc = fr.begin();
+  if (rc) return fr.end(rc);
+  return fr.end(modvis());
 }
 
 int cappgpu_last_report(int* solver, int* ifi, cappgpu_solve_report* rep) {

@@ -62,5 +62,8 @@ int find_strain_rate();
 int calc_vis_les();
 // constant mass-flux forcing (mflux.cu)
 int const_massflux_correction();
+// k-omega SST (turb.cu): calcscm for ifi = ite / ied, modvis
+int calcscm(int ifi, cappgpu_solve_report* rep);
+int modvis();
 
 }  // namespace cap

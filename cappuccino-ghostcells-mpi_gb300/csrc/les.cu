@@ -81,8 +81,9 @@ __global__ void k_vis_les(Dims d, Box b, const double* __restrict__ u, const dou
 
 // wall-function viscosity of the bottom (top = 0) or top ghost layer
 // (calc_vis_les.f90:80-246): dnw dotted with the integer extents nx,ny,nz
-// and the top wall at lk(nimm), as in calcuvw
-__global__ void k_vis_les_wall(Dims d, int top, const double* __restrict__ xc, const double* __restrict__ yc,
+// and the top wall at lk(nimm), as in calcuvw (ktop: nimm, or nkmm with
+// params.top_plane)
+__global__ void k_vis_les_wall(Dims d, int top, int ktop, const double* __restrict__ xc, const double* __restrict__ yc,
                                const double* __restrict__ zc, const double* __restrict__ fz,
                                const double* __restrict__ a3x, const double* __restrict__ a3y,
                                const double* __restrict__ a3z, const double* __restrict__ u,
@@ -102,7 +103,7 @@ __global__ void k_vis_les_wall(Dims d, int top, const double* __restrict__ xc, c
       fxp = fz[ingc];
       fxe = 1.0 - fxp;
     } else {
-      inbc = ixk(d, i, j, d.nimm);
+      inbc = ixk(d, i, j, ktop);
       ingc = inbc + d.nij;
       iface = inbc;
       fxp = 1.0 - fz[inbc];
@@ -164,6 +165,7 @@ int calc_vis_les() {
          P.urf[CAP_IVIS - 1]);
   for (int top = 0; top < 2; ++top)
     launch(k_vis_les_wall, grid_for((long long)(d.nimm - 2) * (d.njmm - 2)), kThreads, c.st, d, top,
+           c.prm.top_plane ? d.nkmm : d.nimm,
            (const double*)F[CAP_XC], (const double*)F[CAP_YC], (const double*)F[CAP_ZC], (const double*)F[CAP_FZ],
            (const double*)F[CAP_AR3X], (const double*)F[CAP_AR3Y], (const double*)F[CAP_AR3Z],
            (const double*)F[CAP_U], (const double*)F[CAP_V], (const double*)F[CAP_W], F[CAP_VIS], P.viscos,
@@ -188,7 +190,7 @@ int cappgpu_find_strain_rate(void) {
 int cappgpu_calc_vis_les(void) {
   CAP_REQUIRE_INIT();
   const Dims& d = ctx().d;
-  if (d.nimm + 1 > d.nk) {   // the top wall at lk(nimm), calc_vis_les.f90:174
+  if (!ctx().prm.top_plane && d.nimm + 1 > d.nk) {   // the top wall at lk(nimm), calc_vis_les.f90:174
     set_error("top wall index lk(nimm) of calc_vis_les.f90:174 leaves the array (ni=%d > nk=%d)", d.ni, d.nk);
     return CAPPGPU_E_ARG;
   }

@@ -18,6 +18,7 @@
 #include "dlayout.cuh"
 #include "kernels.cuh"
 #include "lanewave.cuh"
+#include "mwave.cuh"
 #include "wave.cuh"
 
 namespace cap {
@@ -70,6 +71,13 @@ struct Fast32 {
   float* lmailW = nullptr;
   float* lmailB = nullptr;
   size_t lmail_n = 0;   // floats in lmailW + lmailB
+  // multi-line wavefront (mwave.cuh)
+  CUtensorMap mmap_r, mmap_z, mmap_fq, mmap_bq;   // boxes of one block
+  int mnBA = 0, mnBC = 0, mnblk = 0;
+  int2* morder = nullptr;
+  unsigned* mticket = nullptr;
+  double* mmail = nullptr;   // W edges of every block, then B edges (one 8-byte word per state)
+  size_t mmail_n = 0;
 };
 
 Fast32 G;
@@ -81,6 +89,9 @@ void fast32_release() {
   if (G.lorder) cudaFree(G.lorder);
   if (G.lticket) cudaFree(G.lticket);
   if (G.lmailW) cudaFree(G.lmailW);   // lmailB lies in the same allocation
+  if (G.morder) cudaFree(G.morder);
+  if (G.mticket) cudaFree(G.mticket);
+  if (G.mmail) cudaFree(G.mmail);
   G = Fast32();
 }
 
@@ -113,10 +124,13 @@ __global__ void k_fill_u32(unsigned* p, size_t n, unsigned v) {
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) p[t] = v;
 }
 
-// the warp-tile engine's mailboxes hold the sentinel between launches
+// the warp-tile and multi-line engines' mailboxes hold the sentinel between launches
 void fill_lane_mail(cudaStream_t st) {
   if (G.lmailW)
     launch(k_fill_u32, grid_for((long long)G.lmail_n), kThreads, st, (unsigned*)G.lmailW, G.lmail_n, kSentinelF);
+  if (G.mmail)
+    launch(k_fill_u64, grid_for((long long)G.mmail_n), kThreads, st, (unsigned long long*)G.mmail, G.mmail_n,
+           kSentinel);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -296,6 +310,35 @@ int fast32_setup() {
     G.lmailB = G.lmailW + nW;
     CAP_CUDA(cudaMemcpy(G.lorder, ord.data(), sizeof(int2) * G.lntile, cudaMemcpyHostToDevice));
     CAP_CUDA(cudaMemset(G.lticket, 0, sizeof(unsigned)));
+  }
+  {
+    // the multi-line wavefront: block boxes, topological block order, mailboxes
+    const DG& g = F.g;
+    int r = make_map_box(&G.mmap_r, G.e[E_R], 1, 4, kMBA + 4, kMBC, kMG);
+    if (!r) r = make_map_box(&G.mmap_z, G.e[E_Z], 1, 4, kMBA + 4, kMBC, kMG);
+    if (!r) r = make_map_box(&G.mmap_fq, G.fq, 4, 4, kMBA + 4, kMBC, kMG);
+    if (!r) r = make_map_box(&G.mmap_bq, G.bq, 3, 4, kMBA + 4, kMBC, kMG);
+    if (r) { fast32_release(); return r; }
+    G.mnBA = (g.Ni + kMBA - 1) / kMBA;
+    G.mnBC = (g.Nk + kMBC - 1) / kMBC;
+    G.mnblk = G.mnBA * G.mnBC;
+    std::vector<int2> ord;
+    ord.reserve(G.mnblk);
+    for (int dsum = 0; dsum <= G.mnBA + G.mnBC - 2; ++dsum)
+      for (int cc = 0; cc < G.mnBC; ++cc) {
+        const int aa = dsum - cc;
+        if (aa >= 0 && aa < G.mnBA) ord.push_back(make_int2(aa, cc));
+      }
+    G.mmail_n = (size_t)G.mnblk * (kMBA + kMBC) * g.Nj;
+    if (cudaMalloc(&G.morder, sizeof(int2) * G.mnblk) != cudaSuccess ||
+        cudaMalloc(&G.mticket, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&G.mmail, sizeof(double) * G.mmail_n) != cudaSuccess) {
+      fast32_release();
+      set_error("out of device memory");
+      return CAPPGPU_E_NOMEM;
+    }
+    CAP_CUDA(cudaMemcpy(G.morder, ord.data(), sizeof(int2) * G.mnblk, cudaMemcpyHostToDevice));
+    CAP_CUDA(cudaMemset(G.mticket, 0, sizeof(unsigned)));
     fill_lane_mail(c.st);
     CAP_CUDA(cudaStreamSynchronize(c.st));
   }
@@ -367,11 +410,49 @@ int run_lane(const Op& op, const int* skip) {
   return CAPPGPU_OK;
 }
 
+WaveCtl mwave_ctl(const int* skip) {
+  WaveCtl w;
+  w.ticket = G.mticket;
+  w.order = G.morder;
+  w.nBA = G.mnBA;
+  w.nBC = G.mnBC;
+  w.nblk = G.mnblk;
+  w.abort = F.flags;
+  w.err = F.flags + 1;
+  w.partials = nullptr;
+  w.mailW = G.mmail;
+  w.mailB = G.mmail + (size_t)G.mnblk * kMBC * F.g.Nj;
+  w.spin_limit = ctx().spin_limit;
+  w.skip = skip;
+  return w;
+}
+
+template <class Op, bool BWD>
+int run_mwave(const Op& op, const int* skip) {
+  Ctx& c = ctx();
+  constexpr size_t smem = mwave_smem_bytes<Op>();
+  static bool attr_set = false;   // once per process (one device per context)
+  if (!attr_set) {
+    CAP_CUDA(cudaFuncSetAttribute(k_mwave<Op, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  launch_smem(k_mwave<Op, BWD>, G.mnblk, mwave_threads(), smem, c.st, op, F.g, mwave_ctl(skip));
+  CAP_CHECK_LAUNCH();
+  return CAPPGPU_OK;
+}
+
 // The FP32 substitutions z = M^-1 r of the refinement form: the wavefront of
-// wave.cuh (default) or the warp-tile engine of lanewave.cuh (option
-// lane_wave = 1; the same bits, faster only on the largest grids).
+// wave.cuh (option lane_wave = 0), the warp-tile engine of lanewave.cuh (1)
+// or the multi-line wavefront of mwave.cuh (2); all give the same bits.
 int fp32_forward(const int* skip) {
-  if (ctx().lane_wave) {
+  if (ctx().lane_wave == 2) {
+    MSipFwdF op;
+    op.map[0] = G.mmap_r;
+    op.map[1] = G.mmap_fq;
+    op.z = G.e[E_Z];
+    return run_mwave<MSipFwdF, false>(op, skip);
+  }
+  if (ctx().lane_wave == 1) {
     LaneFwdF op;
     op.map[0] = G.lmap_r;
     op.map[1] = G.lmap_fq;
@@ -386,7 +467,14 @@ int fp32_forward(const int* skip) {
 }
 
 int fp32_backward(const int* skip) {
-  if (ctx().lane_wave) {
+  if (ctx().lane_wave == 2) {
+    MSipBwdF op;
+    op.map[0] = G.mmap_z;
+    op.map[1] = G.mmap_bq;
+    op.z = G.e[E_Z];
+    return run_mwave<MSipBwdF, true>(op, skip);
+  }
+  if (ctx().lane_wave == 1) {
     LaneBwdF op;
     op.map[0] = G.lmap_z;
     op.map[1] = G.lmap_bq;
@@ -835,6 +923,7 @@ static int wave_error_reset(const int* h) {
     cudaMemset(F.flags, 0, sizeof(int) * 2);
     cudaMemset(F.ticket, 0, sizeof(unsigned));
     if (G.lticket) cudaMemset(G.lticket, 0, sizeof(unsigned));
+    if (G.mticket) cudaMemset(G.mticket, 0, sizeof(unsigned));
     fill_mail(ctx().st);
     fill_lane_mail(ctx().st);
     cudaStreamSynchronize(ctx().st);

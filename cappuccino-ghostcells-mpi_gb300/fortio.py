@@ -19,8 +19,8 @@ ar2y, ar2z, ar3x, ar3y, ar3z (nijk reals).  The reference opens
 Restart file records: itime, time | gradpcmf (only with const_mflux) | f1,
 f2, f3, u, v, w, p, te, ed, t, vis, uu, vv, ww, uv, uw, vw, uo, vo, wo, teo,
 edo (nijk reals each).  writefiles writes to 'restart_file', readfiles reads
-'<restart_file>-<rank+1>'.  The Reynolds stresses uu..vw and teo, edo have
-no device field here: they are written as zeros and skipped on reading.
+'<restart_file>-<rank+1>'.  The Reynolds stresses uu..vw have no device
+field here: they are written as zeros and skipped on reading.
 """
 import struct
 
@@ -30,7 +30,7 @@ GRID_FIELDS = ("x", "y", "z", "xc", "yc", "zc", "vol", "fx", "fy", "fz",
                "ar1x", "ar1y", "ar1z", "ar2x", "ar2y", "ar2z", "ar3x", "ar3y", "ar3z")
 RESTART_FIELDS = ("f1", "f2", "f3", "u", "v", "w", "p", "te", "ed", "t", "vis",
                   "uu", "vv", "ww", "uv", "uw", "vw", "uo", "vo", "wo", "teo", "edo")
-_NO_FIELD = {"uu", "vv", "ww", "uv", "uw", "vw", "teo", "edo"}
+_NO_FIELD = {"uu", "vv", "ww", "uv", "uw", "vw"}
 BC_FACES = ("lbw", "lbe", "lbs", "lbn", "lbb", "lbt")
 
 

@@ -8,7 +8,8 @@
 ! fluxuvw-overrelaxed-correction.f90, calcuvw.f90,
 ! PISO_assemble_pressure_eq.f90, assemble_pressure_eq.f90, PISO_getHbyA.f90,
 ! PISO_multiple_correction.f90, bpres.f90, update_values_at_ghostcells*.f90,
-! exchange_mpi.f90, global_sum_mpi.f90 and global_max_mpi.f90, and links
+! calcscm.f90, modvis.f90, exchange_mpi.f90, global_sum_mpi.f90 and
+! global_max_mpi.f90, and links
 ! this file instead.  Each replacement below keeps the reference's name and
 ! dummy arguments.
 !
@@ -43,7 +44,9 @@ module cappgpu
        CAP_SU=49, CAP_SV=50, CAP_SW=51, CAP_RES=52, CAP_APU=53, CAP_APV=54, CAP_APW=55, &
        CAP_BB=56, CAP_BS=57, CAP_BW=58, CAP_BP=59, CAP_BN=60, CAP_BE=61, CAP_BT=62, &
        CAP_HE=63, CAP_HW=64, CAP_HN=65, CAP_HS=66, CAP_HT=67, CAP_HB=68, &
-       CAP_GRADU_X=69, CAP_GRADV_X=72, CAP_GRADW_X=75, CAP_GRADP_X=78, CAP_NFIELDS=81
+       CAP_GRADU_X=69, CAP_GRADV_X=72, CAP_GRADW_X=75, CAP_GRADP_X=78, &
+       CAP_GRADTE_X=81, CAP_GRADED_X=84, CAP_GEN=87, CAP_ALPHASST=88, CAP_BETTASST=89, CAP_DOMEGA=90, &
+       CAP_PRTINV_TE=91, CAP_PRTINV_ED=92, CAP_TEO=93, CAP_EDO=94, CAP_TEOO=95, CAP_EDOO=96, CAP_NFIELDS=97
 
   integer(c_int), parameter :: CAPPGPU_NOT_CONVERGED=1
   integer(c_int), parameter :: SOLVER_SIPSOL=1, SOLVER_CGSTAB=2, SOLVER_ICCG=3, SOLVER_PCGSIP=4, &
@@ -73,7 +76,9 @@ module cappgpu
     integer(c_int) :: ipr, jpr, kpr, ncorr, npcor, icorr, ipcorr, bdf, cn
     integer(c_int) :: lcds, lluds, lquds, lsmart, lavl, lmuscl, lumist, lgamma, lcds4, flux_limiter
     integer(c_int) :: const_mflux, lbuoy, boussinesq, lout, ltransient, lles, periodic, conumfix
-    integer(c_int) :: isol_p, piso_solver, low, loe, los, lon, lob, lot, pad_
+    integer(c_int) :: isol_p, piso_solver, low, loe, los, lon, lob, lot, sst
+    real(c_double) :: cmu
+    integer(c_int) :: top_plane, pad_
   end type
 
   interface
@@ -236,6 +241,14 @@ module cappgpu
       import :: c_int, cappgpu_solve_report
       type(cappgpu_solve_report), intent(out) :: rep(3)
     end function
+    integer(c_int) function cappgpu_calcscm_h(fi, gradfi, ifi) bind(c, name="cappgpu_calcscm_h")
+      import :: c_int, c_double
+      real(c_double), intent(inout) :: fi(*), gradfi(*)
+      integer(c_int), value :: ifi
+    end function
+    integer(c_int) function cappgpu_modvis_h() bind(c, name="cappgpu_modvis_h")
+      import :: c_int
+    end function
     integer(c_int) function cappgpu_piso_gethbya_h() bind(c, name="cappgpu_piso_gethbya_h")
       import :: c_int
     end function
@@ -262,6 +275,7 @@ contains
     use variables
     use time_mod
     use gradients
+    use omega_turb_models
     use bc
     integer(c_int) :: rc
     integer(c_int64_t) :: n
@@ -304,6 +318,20 @@ contains
     rc = cappgpu_register_vec3(CAP_GRADV_X, c_loc(gradv(1,1))); call chk(rc, 'gradv')
     rc = cappgpu_register_vec3(CAP_GRADW_X, c_loc(gradw(1,1))); call chk(rc, 'gradw')
     rc = cappgpu_register_vec3(CAP_GRADP_X, c_loc(gradp(1,1))); call chk(rc, 'gradp')
+    ! two-equation turbulence models (arrays allocated only with lturb)
+    call reg(CAP_GEN, gen)
+    call reg(CAP_TEO, teo); call reg(CAP_EDO, edo)
+    if (allocated(teoo)) then
+      call reg(CAP_TEOO, teoo); call reg(CAP_EDOO, edoo)
+    endif
+    if (allocated(gradte)) then
+      rc = cappgpu_register_vec3(CAP_GRADTE_X, c_loc(gradte(1,1))); call chk(rc, 'gradte')
+      rc = cappgpu_register_vec3(CAP_GRADED_X, c_loc(graded(1,1))); call chk(rc, 'graded')
+    endif
+    if (allocated(alphasst)) then
+      call reg(CAP_ALPHASST, alphasst); call reg(CAP_BETTASST, bettasst); call reg(CAP_DOMEGA, domega)
+      call reg(CAP_PRTINV_TE, prtinv_te); call reg(CAP_PRTINV_ED, prtinv_ed)
+    endif
   contains
     subroutine put(f, a)
       integer(c_int), intent(in) :: f
@@ -362,6 +390,7 @@ contains
     q%isol_p = cap_isol_p; q%piso_solver = cap_piso_solver
     q%low = merge(1, 0, low); q%loe = merge(1, 0, loe); q%los = merge(1, 0, los)
     q%lon = merge(1, 0, lon); q%lob = merge(1, 0, lob); q%lot = merge(1, 0, lot)
+    q%sst = merge(1, 0, sst); q%cmu = cmu
     rc = cappgpu_set_params(q)
     call chk(rc, 'set_params')
   end subroutine
@@ -599,6 +628,27 @@ subroutine calcuvw
   do q = 1, 3
     call solver_line(SOLVER_SIPSOL, int(q, c_int), rep(q))
   end do
+end subroutine
+
+! calcscm.f90:3-602 (k-omega SST): fi is te or ed, gradfi gradte or graded
+subroutine calcscm(fi, gradfi, ifi)
+  use types
+  use parameters
+  use cappgpu
+  implicit none
+  integer, intent(in) :: ifi
+  real(prec), dimension(nxyza) :: fi
+  real(prec), dimension(3,nxyza) :: gradfi
+  call cappgpu_push_params()
+  call run_solver(cappgpu_calcscm_h(fi, gradfi, int(ifi, c_int)), 'calcscm')
+end subroutine
+
+! modvis.f90:3-345 (the SST branch, :195-236)
+subroutine modvis
+  use cappgpu
+  implicit none
+  call cappgpu_push_params()
+  call chk(cappgpu_modvis_h(), 'modvis')
 end subroutine
 
 ! PISO_getHbyA.f90:3-233

@@ -104,6 +104,10 @@ SIGNATURES = {
     "cappgpu_piso_gethbya_h": [],
     "cappgpu_piso_multiple_correction_h": [_REP],
     "cappgpu_last_report": [ctypes.POINTER(_INT), ctypes.POINTER(_INT), _REP],
+    "cappgpu_calcscm": [_INT, _REP],
+    "cappgpu_modvis": [],
+    "cappgpu_calcscm_h": [_DP, _DP, _INT],
+    "cappgpu_modvis_h": [],
     "cappgpu_solver_report_line": [_INT, _INT, _REP, _INT, _INT, ctypes.c_char_p, _INT],
 }
 RESTYPES = {"cappgpu_last_error": ctypes.c_char_p, "cappgpu_field_name": ctypes.c_char_p}
@@ -381,6 +385,15 @@ class Library:
 
     def calc_vis_les(self):
         self._check(self.lib.cappgpu_calc_vis_les(), "calc_vis_les")
+
+    def calcscm(self, ifi):
+        """calcscm(fi, gradfi, ifi) for ifi = ite (te) or ied (ed), SST"""
+        rep = SolveReport()
+        self._check(self.lib.cappgpu_calcscm(int(ifi), ctypes.byref(rep)), "calcscm")
+        return rep
+
+    def modvis(self):
+        self._check(self.lib.cappgpu_modvis(), "modvis")
 
     def const_massflux_correction(self):
         self._check(self.lib.cappgpu_const_massflux_correction(), "const_massflux_correction")

@@ -21,6 +21,9 @@ FIELD_NAMES = [
     "he", "hw", "hn", "hs", "ht", "hb",
     "gradu_x", "gradu_y", "gradu_z", "gradv_x", "gradv_y", "gradv_z",
     "gradw_x", "gradw_y", "gradw_z", "gradp_x", "gradp_y", "gradp_z",
+    "gradte_x", "gradte_y", "gradte_z", "graded_x", "graded_y", "graded_z",
+    "gen", "alphasst", "bettasst", "domega", "prtinv_te", "prtinv_ed",
+    "teo", "edo", "teoo", "edoo",
 ]
 FIELD = {n: i for i, n in enumerate(FIELD_NAMES)}
 NFIELDS = len(FIELD_NAMES)
@@ -73,6 +76,9 @@ class Params(ctypes.Structure):
         ("piso_solver", ctypes.c_int),
         ("low", ctypes.c_int), ("loe", ctypes.c_int), ("los", ctypes.c_int),
         ("lon", ctypes.c_int), ("lob", ctypes.c_int), ("lot", ctypes.c_int),
+        ("sst", ctypes.c_int),
+        ("cmu", ctypes.c_double),
+        ("top_plane", ctypes.c_int),
         ("pad_", ctypes.c_int),
     ]
 

@@ -87,6 +87,15 @@ enum cappgpu_field {
   CAP_GRADV_X, CAP_GRADV_Y, CAP_GRADV_Z,
   CAP_GRADW_X, CAP_GRADW_Y, CAP_GRADW_Z,
   CAP_GRADP_X, CAP_GRADP_Y, CAP_GRADP_Z,
+  /* two-equation turbulence models (calcscm.f90, calculate_stuff_for_sst.f90,
+     modules variables, time_mod, gradients and omega_turb_models): gradte
+     and graded as component arrays, the production gen, the SST blending
+     results alphasst, bettasst, domega, prtinv_te, prtinv_ed, and the old
+     time levels of te and ed */
+  CAP_GRADTE_X, CAP_GRADTE_Y, CAP_GRADTE_Z,
+  CAP_GRADED_X, CAP_GRADED_Y, CAP_GRADED_Z,
+  CAP_GEN, CAP_ALPHASST, CAP_BETTASST, CAP_DOMEGA, CAP_PRTINV_TE, CAP_PRTINV_ED,
+  CAP_TEO, CAP_EDO, CAP_TEOO, CAP_EDOO,
   CAP_NFIELDS
 };
 
@@ -128,6 +137,15 @@ typedef struct cappgpu_params {
   int    piso_solver;               /* PISO p solver, PISO_multiple_correction.f90:138-142 (4 = pcgsip) */
   int    low, loe, los, lon, lob, lot;   /* outlet faces present, read with the
                                        grid (read_grid.f90:140); outbc    */
+  int    sst;                       /* Menter k-omega SST for te (k) and ed
+                                       (omega) when lcal(ite), lcal(ied)  */
+  double cmu;                       /* module cmu: init.f90:177 sets 0.09 for
+                                       standard k-epsilon only; modvis reads
+                                       it in the SST branch as well       */
+  int    top_plane;                 /* top-wall plane of calcuvw.f90:254 and
+                                       calc_vis_les.f90:174: 0 = lk(nimm) as
+                                       the reference writes it (the top wall
+                                       only when ni = nk), 1 = lk(nkmm)    */
   int    pad_;
 } cappgpu_params;
 
@@ -309,6 +327,29 @@ int cappgpu_calc_vis_les(void);
    step when ltransient and const_mflux are set (main.f90:252). */
 int cappgpu_const_massflux_correction(void);
 
+/* ===================================================== k-omega SST (RANS) */
+/* calcscm(fi,gradfi,ifi) (calcscm.f90:3-602) for ifi = ite (k in te) or
+   ied (omega in ed) with the SST model (params.sst): the gradient of fi
+   into gradte / graded, the volume sources (k: production |vis - viscos|
+   S^2 limited to 0.9 rho k omega, destruction; omega:
+   calculate_stuff_for_sst.f90:27-70 -- blending, cross diffusion --, then
+   alphasst P / nu_t and bettasst rho omega), the implicit time term, the
+   face fluxes of fluxscm-overrelaxed-correction.f90:40-230 in three
+   directions, Crank-Nicolson terms, ap and under-relaxation, sipsol
+   (rep), and fi >= small on the whole array.  The step drivers run both
+   after the pressure-velocity coupling when lcal(ite) / lcal(ied) and sst
+   are set (main.f90:196-197). */
+int cappgpu_calcscm(int ifi, cappgpu_solve_report* rep);
+/* modvis (modvis.f90:195-236, SST branch): eddy viscosity
+   viscos + rho a1 k / max(a1, omega, S F2) (the reference's three-argument
+   MAX), under-relaxed by urf(ivis); run by the step drivers when
+   lcal(ivis), sst and not lles (main.f90:203). */
+int cappgpu_modvis(void);
+/* Host-pointer drop-ins: fi must be the registered te or ed and gradfi
+   the interleaved array registered for gradte or graded. */
+int cappgpu_calcscm_h(double* fi, double* gradfi, int ifi);
+int cappgpu_modvis_h(void);
+
 /* ======================================================= index maps (a1) */
 /* setind.f90:34-40: li(i)=(i-1)*nj for i=1..ni, lk(k)=(k-1)*nij.  Writes
    the device copies back (tests compare them element-wise). */
@@ -437,7 +478,8 @@ int cappgpu_simple_iters(int niters, cappgpu_solve_report* last_p_report);
    geometry arrays only so that they are recognised as arguments. */
 /* Interleaved (3, nijk) host array -- the reference's gradu(3,nxyza)
    layout -- for the three component fields starting at field_x (one of
-   CAP_GRADU_X, CAP_GRADV_X, CAP_GRADW_X, CAP_GRADP_X); NULL unregisters. */
+   CAP_GRADU_X, CAP_GRADV_X, CAP_GRADW_X, CAP_GRADP_X, CAP_GRADTE_X,
+   CAP_GRADED_X); NULL unregisters. */
 int cappgpu_register_vec3(int field_x, double* host);
 /* update_values_at_ghostcells (update_values_at_ghostcells_nonperiodic.f90:3-642) */
 int cappgpu_update_values_at_ghostcells_h(void);

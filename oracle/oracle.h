@@ -90,6 +90,13 @@ void cap_find_strain_rate(cap_state* s);
 void cap_calc_vis_les(cap_state* s);
 /* const_massflux_correction.f90:1-22 */
 void cap_const_massflux_correction(cap_state* s);
+/* k-omega SST (oracle_turb.c): calculate_stuff_for_sst.f90, fluxscm-
+   overrelaxed-correction.f90, calcscm.f90 for ifi = ite / ied, modvis.f90 */
+void cap_calculate_stuff_for_sst(cap_state* s);
+void cap_fluxscm(cap_state* s, int idew, int idns, int idtb, int fi, int gx, int ifi, int arvx, int arvy, int arvz,
+                 int fif, int acfe, int acfw, int fcf);
+int cap_calcscm(cap_state* s, int ifi, cappgpu_solve_report* rep);
+void cap_modvis(cap_state* s);
 int cap_piso_steps(cap_state* s, int nsteps, cappgpu_solve_report* last);
 int cap_simple_iters(cap_state* s, int niters, cappgpu_solve_report* last);
 

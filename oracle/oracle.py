@@ -61,6 +61,10 @@ _SIGS = {
     "cap_find_strain_rate": ([_VP], None),
     "cap_calc_vis_les": ([_VP], None),
     "cap_const_massflux_correction": ([_VP], None),
+    "cap_calculate_stuff_for_sst": ([_VP], None),
+    "cap_fluxscm": ([_VP] + [_INT] * 13, None),
+    "cap_calcscm": ([_VP, _INT, _REP], _INT),
+    "cap_modvis": ([_VP], None),
     "cap_piso_steps": ([_VP, _INT, _REP], _INT),
     "cap_simple_iters": ([_VP, _INT, _REP], _INT),
 }
@@ -248,6 +252,21 @@ class State:
 
     def const_massflux_correction(self):
         self.L.cap_const_massflux_correction(self.ptr)
+
+    def calculate_stuff_for_sst(self):
+        self.L.cap_calculate_stuff_for_sst(self.ptr)
+
+    def fluxscm(self, idew, idns, idtb, fi, gx, ifi, *names):
+        self.L.cap_fluxscm(self.ptr, idew, idns, idtb, fid(fi), fid(gx), ifi, *(fid(n) for n in names))
+
+    def calcscm(self, ifi):
+        rep = SolveReport()
+        rc = self.L.cap_calcscm(self.ptr, ifi, ctypes.byref(rep))
+        assert rc >= 0, rc
+        return rep
+
+    def modvis(self):
+        self.L.cap_modvis(self.ptr)
 
     def piso_steps(self, n):
         rep = SolveReport()

@@ -205,8 +205,9 @@ static void calcuvw_wall(cap_state* s, int top) {
         inbc = IXK(i, j, 3); ingc = inbc - s->nij; iface = ingc;
         fxp = fz[ingc]; fxe = 1.0 - fxp;
       } else {
-        /* the reference takes lk(nimm) for the top wall (calcuvw.f90:254) */
-        inbc = IXK(i, j, s->nimm); ingc = inbc + s->nij; iface = inbc;
+        /* the reference takes lk(nimm) for the top wall (calcuvw.f90:254);
+           params.top_plane = 1 takes lk(nkmm) */
+        inbc = IXK(i, j, s->prm.top_plane ? s->nkmm : s->nimm); ingc = inbc + s->nij; iface = inbc;
         fxp = 1.0 - fz[inbc]; fxe = 1.0 - fxp;
       }
       double gzx = xc[inbc] * fxp + xc[ingc] * fxe;
@@ -273,7 +274,7 @@ int cap_calcuvw(cap_state* s, cappgpu_solve_report* rep3) {
   const cappgpu_params* P = &s->prm;
   /* the top-wall loop addresses lk(nimm) (calcuvw.f90:254); outside the
      array when nimm+1 > nk */
-  if (s->nimm + 1 > s->nk) return CAPPGPU_E_ARG;
+  if ((s->prm.top_plane ? s->nkmm : s->nimm) + 1 > s->nk) return CAPPGPU_E_ARG;
   cap_grad_gauss(s, CAP_U, CAP_GRADU_X, CAP_GRADU_Y, CAP_GRADU_Z);
   cap_grad_gauss(s, CAP_V, CAP_GRADV_X, CAP_GRADV_Y, CAP_GRADV_Z);
   cap_grad_gauss(s, CAP_W, CAP_GRADW_X, CAP_GRADW_Y, CAP_GRADW_Z);
@@ -1010,7 +1011,7 @@ void cap_calc_vis_les(cap_state* s) {
           inbc = IXK(i, j, 3); ingc = inbc - s->nij; iface = ingc;
           fxp = fz[ingc]; fxe = 1.0 - fxp;
         } else {
-          inbc = IXK(i, j, s->nimm); ingc = inbc + s->nij; iface = inbc;
+          inbc = IXK(i, j, s->prm.top_plane ? s->nkmm : s->nimm); ingc = inbc + s->nij; iface = inbc;
           fxp = 1.0 - fz[inbc]; fxe = 1.0 - fxp;
         }
         const double gzx = xc[inbc] * fxp + xc[ingc] * fxe;
@@ -1035,6 +1036,25 @@ void cap_calc_vis_les(cap_state* s) {
       }
 }
 
+/* main.f90:196-205 after the pressure-velocity coupling: the k and omega
+   equations (calcscm) when lcal(ite) / lcal(ied), then the eddy viscosity
+   (modvis) or, with lles, the sub-grid viscosity (calc_vis_les; its strain
+   is formed here, as calcscm -- which forms it in the reference -- does not
+   run on the LES path). */
+static int turbulence(cap_state* s) {
+  const cappgpu_params* P = &s->prm;
+  int rc = 0;
+  cappgpu_solve_report rep;
+  if (P->sst && P->lcal[CAP_ITE - 1] && (rc = cap_calcscm(s, CAP_ITE, &rep)) < 0) return rc;
+  if (P->sst && P->lcal[CAP_IED - 1] && (rc = cap_calcscm(s, CAP_IED, &rep)) < 0) return rc;
+  if (P->lcal[CAP_IVIS - 1] && !P->lles && P->sst) cap_modvis(s);
+  if (P->lcal[CAP_IVIS - 1] && P->lles) {
+    cap_find_strain_rate(s);
+    cap_calc_vis_les(s);
+  }
+  return 0;
+}
+
 /* main.f90:140-207 with maxit = 1 iteration per time step (transient PISO).
    The reference's residual-normalised convergence test (main.f90:218-237)
    uses snorin, which only bcin sets for inlet cases; the drivers here run
@@ -1043,15 +1063,24 @@ int cap_piso_steps(cap_state* s, int nsteps, cappgpu_solve_report* last) {
   cappgpu_params* P = &s->prm;
   const size_t nb = sizeof(double) * s->nijk;
   int rc = 0;
+  const int turb = P->lcal[CAP_ITE - 1] || P->lcal[CAP_IED - 1];
   for (int st = 0; st < nsteps; ++st) {
     if (P->bdf) {
       memcpy(s->f[CAP_UOO], s->f[CAP_UO], nb);
       memcpy(s->f[CAP_VOO], s->f[CAP_VO], nb);
       memcpy(s->f[CAP_WOO], s->f[CAP_WO], nb);
+      if (turb) {   /* main.f90:144-145 */
+        memcpy(s->f[CAP_TEOO], s->f[CAP_TEO], nb);
+        memcpy(s->f[CAP_EDOO], s->f[CAP_EDO], nb);
+      }
     }
     memcpy(s->f[CAP_UO], s->f[CAP_U], nb);
     memcpy(s->f[CAP_VO], s->f[CAP_V], nb);
     memcpy(s->f[CAP_WO], s->f[CAP_W], nb);
+    if (turb) {   /* main.f90:153-154 */
+      memcpy(s->f[CAP_TEO], s->f[CAP_TE], nb);
+      memcpy(s->f[CAP_EDO], s->f[CAP_ED], nb);
+    }
     cap_courant(s);
     cap_update_values_at_ghostcells(s);
     cappgpu_solve_report r3[3];
@@ -1063,12 +1092,7 @@ int cap_piso_steps(cap_state* s, int nsteps, cappgpu_solve_report* last) {
     if (r < 0) return r;
     rc |= r;
     if (last) *last = reps[P->ncorr * P->npcor - 1];
-    /* main.f90:205; the strain is formed here (the reference forms it in
-       calcscm, which this path does not run) */
-    if (P->lcal[CAP_IVIS - 1] && P->lles) {
-      cap_find_strain_rate(s);
-      cap_calc_vis_les(s);
-    }
+    if ((r = turbulence(s)) < 0) return r;
     if (P->ltransient && P->const_mflux) cap_const_massflux_correction(s);   /* main.f90:252 */
   }
   return rc;
@@ -1089,10 +1113,7 @@ int cap_simple_iters(cap_state* s, int niters, cappgpu_solve_report* last) {
     if (r < 0) return r;
     rc |= r;
     if (last) *last = reps[P->ncorr * P->npcor - 1];
-    if (P->lcal[CAP_IVIS - 1] && P->lles) {   /* main.f90:205 */
-      cap_find_strain_rate(s);
-      cap_calc_vis_les(s);
-    }
+    if ((r = turbulence(s)) < 0) return r;
   }
   return rc;
 }

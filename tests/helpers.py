@@ -15,7 +15,7 @@ def with_fluxes(case, st):
     them from its own, bit-identical, geometry)."""
     for n in ("ar1x", "ar1y", "ar1z", "ar2x", "ar2y", "ar2z", "ar3x", "ar3y", "ar3z", "fx", "fy", "fz"):
         case.fields[n] = st.field(n).copy()
-    if case.name == "channel":
+    if case.name in ("channel", "rans_channel"):
         fl = cappgpu.cases.initial_face_fluxes(case)
         for n, a in fl.items():
             case.fields[n] = a

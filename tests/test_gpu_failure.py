@@ -62,12 +62,15 @@ def test_spin_limit_reports_and_next_solve_recovers(gpu_lib, oracle_mod, solver)
     compare(gpu_lib, st, exact=exact, rtol=1e-10, names=["p", "bb", "bs", "bw", "bp", "bn", "be", "bt"])
 
 
-def test_spin_limit_in_the_refinement_form(gpu_lib, oracle_mod):
-    """The FP32 wavefronts of precision mode 1 report the same way, and the
-    next mode-1 solve reaches the same result as one on a fresh start."""
+@pytest.mark.parametrize("engine", [0, 2])
+def test_spin_limit_in_the_refinement_form(gpu_lib, oracle_mod, engine):
+    """The FP32 wavefronts of precision mode 1 (one line per thread, or the
+    multi-line engine) report the same way, and the next mode-1 solve
+    reaches the same result as one on a fresh start."""
     st = system(oracle_mod, "pcgsip", seed=6)
     push(gpu_lib, st)
     gpu_lib.precision(1)
+    gpu_lib.set_option("lane_wave", engine)
     try:
         good = gpu_lib.solve("pcgsip", "p", IP)
         p_good = gpu_lib.get_field("p")
@@ -85,3 +88,4 @@ def test_spin_limit_in_the_refinement_form(gpu_lib, oracle_mod):
         assert again.iters == good.iters
     finally:
         gpu_lib.precision(0)
+        gpu_lib.set_option("lane_wave", 0)

@@ -197,18 +197,19 @@ def test_mixed_sipsol_meets_fp64_exit_test(gpu_lib, oracle_mod, dims, sor):
 
 
 @pytest.mark.parametrize("solver", ["pcgsip", "sipsol"])
-@pytest.mark.parametrize("dims", [(14, 13, 12), (40, 37, 35), (70, 9, 45)])
+@pytest.mark.parametrize("dims", [(14, 13, 12), (40, 37, 35), (70, 9, 45), (104, 23, 71)])
 def test_fp32_substitution_engines_agree_bit_for_bit(gpu_lib, oracle_mod, solver, dims):
     """The FP32 substitutions of the refinement form run on the wavefront of
-    wave.cuh (option lane_wave 0, default) or on the warp-tile engine
-    (lane_wave 1).  Both evaluate each cell's expression on the same
-    operands in the same order, so the whole solve -- iterations, residuals,
-    solution -- is the same to the bit.  The shapes cover one tile, several
-    tiles along a and c, and extents that are not multiples of the tile."""
+    wave.cuh (option lane_wave 0), on the warp-tile engine (lane_wave 1) or
+    on the multi-line wavefront (lane_wave 2).  All evaluate each cell's
+    expression on the same operands in the same order, so the whole solve
+    -- iterations, residuals, solution -- is the same to the bit.  The
+    shapes cover one tile or block, several along a and c, and extents that
+    are not multiples of either."""
     st = _state(oracle_mod, dims, 5, 1e-6)
     st.set_field("res", np.zeros_like(st.field("res")))
     out = {}
-    for lw in (0, 1):
+    for lw in (0, 1, 2):
         push(gpu_lib, st)
         gpu_lib.set_option("lane_wave", lw)
         gpu_lib.precision(1)
@@ -218,22 +219,27 @@ def test_fp32_substitution_engines_agree_bit_for_bit(gpu_lib, oracle_mod, solver
             gpu_lib.precision(0)
             gpu_lib.set_option("lane_wave", 0)
         out[lw] = (r, gpu_lib.get_field("p"), gpu_lib.get_field("res"))
-    (r0, p0, q0), (r1, p1, q1) = out[0], out[1]
-    assert r0.status == 0 and r1.status == 0
-    assert r1.iters == r0.iters
-    assert r1.resl == r0.resl and r1.res0 == r0.res0
-    np.testing.assert_array_equal(p1, p0)
-    np.testing.assert_array_equal(q1, q0)
+    r0, p0, q0 = out[0]
+    assert r0.status == 0
+    for lw in (1, 2):
+        r1, p1, q1 = out[lw]
+        assert r1.status == 0
+        assert r1.iters == r0.iters, lw
+        assert r1.resl == r0.resl and r1.res0 == r0.res0, lw
+        np.testing.assert_array_equal(p1, p0)
+        np.testing.assert_array_equal(q1, q0)
 
 
-def test_fp32_substitution_engine_repeated_calls(gpu_lib, oracle_mod):
-    """Mailboxes and the tile ticket are left clean by every launch: the
-    same solve repeated on the warp-tile engine gives the same bits."""
-    st = _state(oracle_mod, (40, 37, 35), 6, 1e-6)
+@pytest.mark.parametrize("engine", [1, 2])
+def test_fp32_substitution_engine_repeated_calls(gpu_lib, oracle_mod, engine):
+    """Mailboxes and the block ticket are left clean by every launch: the
+    same solve repeated on the warp-tile or multi-line engine gives the
+    same bits."""
+    st = _state(oracle_mod, (70, 37, 45), 6, 1e-6)
     res = []
     for _ in range(3):
         push(gpu_lib, st)
-        gpu_lib.set_option("lane_wave", 1)
+        gpu_lib.set_option("lane_wave", engine)
         gpu_lib.precision(1)
         try:
             r = gpu_lib.pcgsip("p", IP)
