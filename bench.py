@@ -569,6 +569,76 @@ def run_profile(args):
     print(json.dumps(out), flush=True)
 
 
+def run_learned_config(args):
+    """The learned-guess configuration as specified: 2000 (RHS, p') pairs,
+    random 64^3 windows of the pressure solves of 200 steps of the 128^3
+    channel in precision 1 (two solves a step, five windows a solve),
+    normalised by the RMS of the solve's initial residual; the 16/32/64
+    U-Net trained with Adam at lr 1e-3 for 20 epochs on the residual-norm
+    loss; then inference on a 192^3 channel: per step and per solve the
+    PCG iterations and the p'-solve time to the same tolerance with the
+    guess (precision 2) and without it (precision 1) from the same state,
+    and the fallback rate (guesses discarded because they did not lower
+    the FP64 residual).  Prints one JSON line (no bench line)."""
+    import cappgpu
+    steps_rec, per_solve, block, epochs, pairs = 200, 5, 64, 20, 2000
+    out = {"learned_config": True, "seed": 20261203}
+    lib = cappgpu.Library()
+    lib.load_case(make_case(128))
+    lib.learn_reset(pairs, seed=20261203)
+    lib.learn_windows(block, per_solve)
+    lib.precision(1)
+    lib.learn_collect(True)
+    t0 = time.perf_counter()
+    lib.piso_steps(steps_rec)
+    lib.learn_collect(False)
+    t1 = time.perf_counter()
+    loss = lib.learn_train(epochs, block=block, lr=1e-3)
+    t2 = time.perf_counter()
+    out["train"] = {"grid": [128, 128, 128], "steps": steps_rec, "pairs": lib.learn_stats()["samples"],
+                    "window": block, "epochs": epochs, "lr": 1e-3, "loss_last_epoch": loss,
+                    "collect_s": t1 - t0, "train_s": t2 - t1}
+    params = lib.learn_params()
+    lib.finalize()
+
+    n = args.learned_size
+    lib = cappgpu.Library()
+    lib.load_case(make_case(n))
+    lib.learn_reset(0, seed=20261203)
+    lib.learn_params(params)
+    lib.precision(0)
+    lib.piso_steps(args.warmup)
+    snap = snapshot(lib)
+    forms = {}
+    for mode in (1, 2):
+        restore(lib, snap)
+        lib.precision(mode)
+        lib.piso_steps(1)   # warm-up of the buffers of the form
+        restore(lib, snap)
+        s0 = lib.learn_stats()
+        per_step = []
+        for _ in range(args.steps):
+            lib.timer_start()
+            lib.piso_steps(1)
+            ms = lib.timer_stop()
+            st = lib.stats()
+            per_step.append({"ms": ms, "p_solve_ms": st.p_solve_ms, "p_iters": st.p_report.iters,
+                             "p_rel_residual": st.p_report.resl / st.p_report.res0 if st.p_report.res0 else None})
+        s1 = lib.learn_stats()
+        kept, dropped = s1["guesses"] - s0["guesses"], s1["fallbacks"] - s0["fallbacks"]
+        forms["fp32_learned" if mode == 2 else "fp32_refined"] = {
+            "ms_per_step": sum(q["ms"] for q in per_step) / len(per_step),
+            "last_p_solve_ms": sum(q["p_solve_ms"] for q in per_step) / len(per_step),
+            "last_p_iters": [q["p_iters"] for q in per_step],
+            "guesses_kept": kept if mode == 2 else None, "guesses_discarded": dropped if mode == 2 else None,
+            "fallback_rate": (dropped / (kept + dropped)) if mode == 2 and kept + dropped else None,
+            "per_step": per_step}
+    lib.precision(0)
+    lib.finalize()
+    out["inference"] = {"grid": [n, n, n], "warmup_fp64_steps": args.warmup, "steps": args.steps, **forms}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -579,7 +649,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", choices=["step64", "step32", "net"],
                     help="run a small fixed workload for an ncu capture instead of the bench")
+    ap.add_argument("--learned-config", action="store_true",
+                    help="train the learned guess as its configuration specifies and compare it at --learned-size")
+    ap.add_argument("--learned-size", type=int, default=192)
     args = ap.parse_args()
+    if args.learned_config:
+        run_learned_config(args)
+        return
     if args.profile:
         run_profile(args)
         return

@@ -94,9 +94,13 @@ struct Net {
   size_t part_n = 0;
   double* dsum = nullptr;        // device scalars: loss
   int* err = nullptr;            // set by a tensor-core convolution whose wait ran out
-  // recorded pairs: [sample][8][sV]: r^, then A^ as xp, xm, yp, ym, zp, zm, diag
+  // recorded pairs: [sample][8][sV]: r^, then A^ as xp, xm, yp, ym, zp, zm, diag;
+  // a sample is the whole interior, or (window mode, wper > 0) a random
+  // sD^3 window of it, wper windows per recorded solve
   int max_samples = 0, nsamples = 0, next = 0;
   int sD = 0, sH = 0, sW = 0;
+  int wper = 0;
+  unsigned long long wrng = 0;   // window origins (xorshift64*)
   float* store = nullptr;
   // statistics of the guesses
   int guesses = 0, fallbacks = 0;
@@ -545,17 +549,20 @@ __global__ void k_scales(Dims d, const double* __restrict__ r, const double* __r
   block_reduce_store<2>(a, part);
 }
 
-// a recorded pair: r^ = r0/rms(r0), A^ = A/mean(ap) in window axes
-// (x = j: an, as; y = i: ae, aw; z = k: at, ab)
+// a recorded pair: r^ = r0/rms(r0), A^ = A/mean(ap) (both scales over the
+// whole interior) in window axes (x = j: an, as; y = i: ae, aw; z = k: at,
+// ab), on the window of wz x wy x wx cells at (z0, y0, x0) of the interior
 __global__ void k_record(Dims d, const double* __restrict__ r, const double* __restrict__ ae,
                          const double* __restrict__ aw, const double* __restrict__ an, const double* __restrict__ as,
                          const double* __restrict__ at, const double* __restrict__ ab, const double* __restrict__ ap,
-                         const double* __restrict__ sums, int Ni, int Nj, int Nk, float* __restrict__ smp) {
-  const int V = Ni * Nj * Nk;
-  const double rinv = sums[0] > 0.0 ? 1.0 / sqrt(sums[0] / V) : 0.0;
-  const double ainv = sums[1] != 0.0 ? (double)V / sums[1] : 0.0;
+                         const double* __restrict__ sums, int Ni, int Nj, int Nk, int z0, int y0, int x0, int wz, int wy,
+                         int wx, float* __restrict__ smp) {
+  const long long Vi = (long long)Ni * Nj * Nk;
+  const int V = wz * wy * wx;
+  const double rinv = sums[0] > 0.0 ? 1.0 / sqrt(sums[0] / Vi) : 0.0;
+  const double ainv = sums[1] != 0.0 ? (double)Vi / sums[1] : 0.0;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-    const int x = v % Nj, y = (v / Nj) % Ni, z = v / (Nj * Ni);
+    const int x = x0 + v % wx, y = y0 + (v / wx) % wy, z = z0 + v / (wx * wy);
     const int n = nat_of(d, x, y, z);
     smp[v] = (float)(r[n] * rinv);
     smp[1LL * V + v] = (float)(an[n] * ainv);
@@ -1030,7 +1037,8 @@ int learned_solve_start(int fif, double res0) {
   const int Ni = d.nimm - 2, Nj = d.njmm - 2, Nk = d.nkmm - 2;
   const long long Vi = (long long)Ni * Nj * Nk;
   if (!(res0 > 0.0) || !isfinite(res0)) return CAPPGPU_OK;
-  const bool rec = N.collect && N.max_samples > 0 && N.sD == Nk && N.sH == Ni && N.sW == Nj;
+  const bool rec = N.collect && N.max_samples > 0 &&
+                   (N.wper > 0 ? N.sD <= Nk && N.sD <= Ni && N.sD <= Nj : N.sD == Nk && N.sH == Ni && N.sW == Nj);
   const bool guess = c.precision == 2 && N.trained;
   if (!rec && !guess) return CAPPGPU_OK;
   launch(k_scales, kRedBlocks, kThreads, c.st, d, (const double*)c.f[CAP_RES], (const double*)c.f[CAP_AP], Ni, Nj, Nk,
@@ -1039,14 +1047,28 @@ int learned_solve_start(int fif, double res0) {
   int rc = finish_reduce(2);
   if (rc) return rc;
   if (rec) {
-    float* smp = N.store + (size_t)N.next * 8 * Vi;
-    launch(k_record, grid_for(Vi), kThreads, c.st, d, (const double*)c.f[CAP_RES], (const double*)c.f[CAP_AE],
-           (const double*)c.f[CAP_AW], (const double*)c.f[CAP_AN], (const double*)c.f[CAP_AS],
-           (const double*)c.f[CAP_AT], (const double*)c.f[CAP_AB], (const double*)c.f[CAP_AP],
-           (const double*)c.redout, Ni, Nj, Nk, smp);
-    CAP_CHECK_LAUNCH();
-    N.next = (N.next + 1) % N.max_samples;
-    if (N.nsamples < N.max_samples) ++N.nsamples;
+    const long long sV = (long long)N.sD * N.sH * N.sW;
+    auto rnd = [&](unsigned m) {   // xorshift64*
+      unsigned long long& q = N.wrng;
+      q ^= q >> 12; q ^= q << 25; q ^= q >> 27;
+      return (unsigned)((q * 0x2545f4914f6cdd1dULL) >> 33) % m;
+    };
+    for (int k = 0; k < (N.wper > 0 ? N.wper : 1); ++k) {
+      int z0 = 0, y0 = 0, x0 = 0;
+      if (N.wper > 0) {
+        z0 = (int)rnd((unsigned)(Nk - N.sD + 1));
+        y0 = (int)rnd((unsigned)(Ni - N.sH + 1));
+        x0 = (int)rnd((unsigned)(Nj - N.sW + 1));
+      }
+      float* smp = N.store + (size_t)N.next * 8 * sV;
+      launch(k_record, grid_for(sV), kThreads, c.st, d, (const double*)c.f[CAP_RES], (const double*)c.f[CAP_AE],
+             (const double*)c.f[CAP_AW], (const double*)c.f[CAP_AN], (const double*)c.f[CAP_AS],
+             (const double*)c.f[CAP_AT], (const double*)c.f[CAP_AB], (const double*)c.f[CAP_AP],
+             (const double*)c.redout, Ni, Nj, Nk, z0, y0, x0, N.sD, N.sH, N.sW, smp);
+      CAP_CHECK_LAUNCH();
+      N.next = (N.next + 1) % N.max_samples;
+      if (N.nsamples < N.max_samples) ++N.nsamples;
+    }
   }
   if (!guess) return CAPPGPU_OK;
   // the guess: fi + alpha * net(r0 / rms(r0)), kept only if it lowers the
@@ -1155,6 +1177,31 @@ int cappgpu_learn_reset(int max_samples, unsigned long long seed) {
   if (rc) return rc;
   N.ready = true;
   CAP_CUDA(cudaStreamSynchronize(ctx().st));
+  return CAPPGPU_OK;
+}
+
+int cappgpu_learn_windows(int block, int per_solve) {
+  CAP_REQUIRE_INIT();
+  if (!N.ready) { set_error("learn_windows: call cappgpu_learn_reset first"); return CAPPGPU_E_NOINIT; }
+  const Dims& d = ctx().d;
+  const int Ni = d.nimm - 2, Nj = d.njmm - 2, Nk = d.nkmm - 2;
+  if (per_solve < 1 || block < 4 || block % 4 != 0 || block > Ni || block > Nj || block > Nk) {
+    set_error("learn_windows: block %d (a multiple of 4 within the interior %d x %d x %d), %d windows per solve",
+              block, Ni, Nj, Nk, per_solve);
+    return CAPPGPU_E_ARG;
+  }
+  cudaFree(N.store);
+  N.store = nullptr;
+  const long long V = (long long)block * block * block;
+  if (N.max_samples > 0 && cudaMalloc(&N.store, sizeof(float) * 8 * (size_t)N.max_samples * V) != cudaSuccess) {
+    N.max_samples = 0;
+    set_error("learn_windows: out of device memory for the windows");
+    return CAPPGPU_E_NOMEM;
+  }
+  N.sD = N.sH = N.sW = block;
+  N.wper = per_solve;
+  N.wrng = N.seed * 0x9e3779b97f4a7c15ULL + 777;
+  N.nsamples = N.next = 0;
   return CAPPGPU_OK;
 }
 

@@ -11,13 +11,17 @@
 // On GB300 a double-precision instruction occupies its SM sub-partition
 // for 64 cycles whatever the number of active lanes, so a step costs at
 // least the op's FP64 instruction count x 64 cycles.  The compute warps do
-// nothing but that arithmetic and one barrier per hyperplane; three other
-// roles run beside them:
+// nothing but that arithmetic and one barrier per hyperplane: a cell's
+// inputs and its products with the own j-predecessor are formed before the
+// step's barrier (Op::pre), only the W and B neighbours after it (Op::post).
+// Two other roles run beside them:
 //  * the pacing warp streams the block's inputs with tensor-memory-access
 //    (TMA) copies, kG hyperplanes per copy, into kSlots shared-memory slots,
-//    checks ahead of each step that the copy has landed (mbarrier) and that
-//    the edge states are staged, and releases the step through named
-//    barrier 1 (bar.red.or, which also carries the stop flag);
+//    checks that a copy has landed (mbarrier) one step before the compute
+//    warps read it and that the edge states are staged, and releases the
+//    step through a named barrier: bar.red.or on barrier 1 at a copy
+//    group's first step (it also carries the stop flag), bar.sync on
+//    barrier 3 at the others;
 //  * the communication warp moves edge states across blocks through global
 //    mailboxes in which the data is its own flag: every entry holds a
 //    signalling-NaN sentinel that no arithmetic result can equal, the
@@ -58,6 +62,11 @@ struct WaveCtl {
 constexpr int kG = 4;        // hyperplanes per TMA copy
 constexpr int kMaxSlots = 8; // copies in flight (per op: Op::kSlots)
 constexpr int kRing = 32;    // planes of staged edge states (a power of two)
+#ifndef CAP_WAVE_COMM_WARPS
+#define CAP_WAVE_COMM_WARPS 1
+#endif
+constexpr int kComm = CAP_WAVE_COMM_WARPS;   // communication warps: 1 stages both edges, 2 one edge each
+static_assert(kComm == 1 || kComm == 2, "communication warps");
 constexpr unsigned long long kSentinel = 0x7FF0DEAD5EA1F00DULL;   // signalling NaN
 // a slot is refilled at the start of the next group, so two slots at least;
 // the ring holds the planes between two updates of the consumed-plane count
@@ -88,21 +97,26 @@ struct WaveLayout {
 };
 
 // The compute thread's view of its inputs in one slot: element q of map m
-// at the current plane and line.
+// at box plane zb of its line.  off[m] is the byte offset of the line's
+// element (q = 0, zb = 0) in a slot; with zb and q known at compile time the
+// rest of the address is an immediate.
 template <class Op, int BA, int BC>
 struct InView {
   using L = WaveLayout<Op, BA, BC>;
   const unsigned char* slot;
-  int zb, yb, xb8, xb4;   // plane and row in the box; column for 8- and 4-byte maps
+  int zb;                  // plane in the box
+  int off[Op::kMaps];
+  // xb8 / xb4: the line's column for 8- and 4-byte maps, yb its row
+  __device__ __forceinline__ void init(int xb8, int xb4, int yb) {
+#pragma unroll
+    for (int m = 0; m < Op::kMaps; ++m)
+      off[m] = (int)L::map_off(m) + (yb * Op::nq(m) * L::bw(m) + (Op::esize(m) == 8 ? xb8 : xb4)) * Op::esize(m);
+  }
   __device__ __forceinline__ int at(int m, int q) const {
-    return ((zb * BC + yb) * Op::nq(m) + q) * L::bw(m) + (Op::esize(m) == 8 ? xb8 : xb4);
+    return off[m] + (zb * BC * Op::nq(m) + q) * L::bw(m) * Op::esize(m);
   }
-  __device__ __forceinline__ double d(int m, int q) const {
-    return reinterpret_cast<const double*>(slot + L::map_off(m))[at(m, q)];
-  }
-  __device__ __forceinline__ float f(int m, int q) const {
-    return reinterpret_cast<const float*>(slot + L::map_off(m))[at(m, q)];
-  }
+  __device__ __forceinline__ double d(int m, int q) const { return *reinterpret_cast<const double*>(slot + at(m, q)); }
+  __device__ __forceinline__ float f(int m, int q) const { return *reinterpret_cast<const float*>(slot + at(m, q)); }
 };
 
 // The cell a compute thread works on at the current step.
@@ -127,9 +141,9 @@ struct WaveSmem {
   int bail;                                // any warp gave up
 };
 
-// compute warps (one thread per line) + communication warp + pacing warp(s)
+// compute warps (one thread per line) + communication warp(s) + pacing warp(s)
 template <class Op, int BA, int BC>
-constexpr int wave_threads() { return BA * BC + 32 + 32 * Op::kPacers; }
+constexpr int wave_threads() { return BA * BC + 32 * kComm + 32 * Op::kPacers; }
 
 template <class Op, int BA, int BC>
 constexpr size_t wave_smem_bytes() {
@@ -291,10 +305,10 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   const int blk_id = bc * w.nBA + ba;
   const int ngroups = (s1 - s0 + kG) / kG;
 
-  if (tid >= NC + 32) {
+  if (tid >= NC + 32 * kComm) {
     // ------------------------------------------------------- pacing warps
     const int lane = (tid - NC) & 31;
-    const int pw = (tid - NC - 32) >> 5;   // this pacer's index
+    const int pw = (tid - NC - 32 * kComm) >> 5;   // this pacer's index
     auto issue = [&](int gq) {   // TMA copy of group gq (planes s0 + gq*kG ...) into its slot
       const int slot = gq % NSLOT, sg = s0 + gq * kG;
       const int alo = BWD ? g.Ni - (ba + 1) * BA : ba * BA;   // first column of the block's lines
@@ -309,38 +323,53 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
         else tma_load4(dst + L::map_off(m), &op.map[m], x0, 0, y0, z0, &sm.full[slot]);
       }
     };
+    // the copy of group gq has landed (bounded wait); false when the block gives up
+    auto landed = [&](int gq) {
+      long long it = 0;
+      while (!mbar_test(&sm.full[gq % NSLOT], (unsigned)((gq / NSLOT) & 1))) {
+        if (*bail) return false;
+        if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); return false; }
+      }
+      return true;
+    };
     // pacer 0 owns the copies (issue, refill, drain); group starts fall on
     // its steps because kG is a multiple of NP
     static_assert(kG % NP == 0, "group starts on pacer 0");
     int issued = min(NSLOT, ngroups);
     if (pw == 0 && lane == 0)
       for (int gq = 0; gq < issued; ++gq) issue(gq);
+    // prologue: the first group's inputs are in shared memory before the
+    // compute warps read them, ahead of their first step's barrier
+    int pend = (pw == 0 && lane == 0 && !landed(0)) ? 1 : 0;   // a failed check, carried by the next group barrier
+    bool stop = named_bar_red_or(1, NB, pend != 0);
     unsigned long long knownW = 0, knownB = 0;
     int gi = 0, ds = 0;
-    for (int s = s0; s <= s1; ++s) {
-      int st = 0;
-      if (lane == 0 && (s - s0) % NP == pw) {
-        if (ds == 0) {   // the copy of this group of planes has landed
-          long long it = 0;
-          while (!mbar_test(&sm.full[gi % NSLOT], (unsigned)((gi / NSLOT) & 1))) {
-            if (*bail) { st = 1; break; }
-            if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); st = 1; break; }
-          }
-        }
+    for (int s = s0; s <= s1 && !stop; ++s) {
+      if (lane == 0 && !pend && (s - s0) % NP == pw) {
         const unsigned long long needW = (unsigned long long)(unsigned)(min(s, s1W + 1) + 1);
         const unsigned long long needB = (unsigned long long)(unsigned)(min(s, s1B + 1) + 1);
-        if (!st && (knownW < needW || knownB < needB)) {   // the edge states of plane s-1 are staged
+        if (knownW < needW || knownB < needB) {   // the edge states of plane s-1 are staged
           long long it = 0;
           for (;;) {
             knownW = ld_acquire_cta_shared(&sm.stagedW);
             knownB = ld_acquire_cta_shared(&sm.stagedB);
             if (knownW >= needW && knownB >= needB) break;
-            if (*bail) { st = 1; break; }
-            if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); st = 1; break; }
+            if (*bail) { pend = 1; break; }
+            if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); pend = 1; break; }
           }
         }
+        // last step of a group: the compute warps read the next group's
+        // inputs between this step's barrier and the next one
+        if (!pend && ds == kG - 1 && gi + 1 < ngroups && !landed(gi + 1)) pend = 1;
       }
-      if (named_bar_red_or(1, NB, st != 0)) break;   // (only a pacer's lane 0 can set it) the compute warps start step s
+      // a group's first step: the barrier also carries the stop decision;
+      // the other steps take a plain barrier (a failed check lets the
+      // compute warps finish the group on inputs that are discarded)
+      if (ds == 0) {
+        if (named_bar_red_or(1, NB, pend != 0)) break;
+      } else {
+        named_bar_sync(3, NB);
+      }
       if (pw == 0 && lane == 0 && ds == 0 && gi > 0) {
         // step s-1 is complete: the edge rings up to plane s-2 and the slot
         // of the previous group are free
@@ -367,8 +396,9 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   }
 
   if (tid >= NC) {
-    // --------------------------------------------- communication warp
-    const int lane = tid - NC;
+    // --------------------------------------------- communication warp(s)
+    const int lane = (tid - NC) & 31;
+    const int cw = (tid - NC) >> 5;   // with two warps: 0 stages the W edge, 1 the B edge
     double* srcW = ba > 0 ? w.mailW + (size_t)(blk_id - 1) * BC * g.Nj * NS : nullptr;
     double* srcB = bc > 0 ? w.mailB + (size_t)(blk_id - w.nBA) * BA * g.Nj * NS : nullptr;
     auto lineW = [&](int e, int& av, int& cv, int& pa, int& pc) {
@@ -379,7 +409,8 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
     };
     EdgeProbe<St, kPW * BC / 32> PW;
     EdgeProbe<St, kPW * BA / 32> PB;
-    int loadedW = s0 - 2, loadedB = s0 - 2;   // last staged plane
+    int loadedW = kComm == 2 && cw == 1 ? s1W : s0 - 2;   // last staged plane (an edge the warp
+    int loadedB = kComm == 2 && cw == 0 ? s1B : s0 - 2;   // does not stage starts complete)
     long long idle = 0;
     while (loadedW < s1W || loadedB < s1B) {
       // warp-uniform decisions: the staging uses warp-wide ballots
@@ -415,6 +446,12 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   }
 
   // ------------------------------------------------------ compute warps
+  // Per step: the cell's inputs are read and the products with the own
+  // j-predecessor formed (Op::pre) before the step's barrier, the W and B
+  // neighbours after it (Op::post).  The steps of a copy group are unrolled,
+  // so box offsets and buffer parities are constants and the running
+  // indices advance by one addition per step.
+  static_assert(BA % 2 == 0 && BC % 2 == 0 && kG % 2 == 0, "even group starts: a step's plane parity is static");
   const int al = tid % BA, cl = tid / BA;
   const int av = ba * BA + al, cv = bc * BC + cl;     // virtual (mirrored when BWD) line
   const bool line_ok = av < g.Ni && cv < g.Nk;
@@ -423,22 +460,15 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   const int sfirst = av + cv;                         // step of this line's first cell
   InView<Op, BA, BC> in;                              // this line's column and row in an input box
   if (!BWD) {
-    in.xb8 = al;
-    in.xb4 = al;
-    in.yb = cl;
+    in.init(al, al, cl);
   } else {
     const int alo = g.Ni - (ba + 1) * BA;
-    in.xb8 = (alo - (alo & ~1)) + BA - 1 - al;
-    in.xb4 = (alo - (alo & ~3)) + BA - 1 - al;
-    in.yb = BC - 1 - cl;
+    in.init((alo - (alo & ~1)) + BA - 1 - al, (alo - (alo & ~3)) + BA - 1 - al, BC - 1 - cl);
   }
   const bool edgeE = al == BA - 1 && ba + 1 < w.nBA;   // feeds the next block along a
   const bool edgeT = cl == BC - 1 && bc + 1 < w.nBC;   // feeds the next block along c
   double* mW = w.mailW + ((size_t)blk_id * BC + cl) * g.Nj * NS;
   double* mB = w.mailB + ((size_t)blk_id * BA + al) * g.Nj * NS;
-  const St sg = line_ok ? op.ghost(g.nat(a, BWD ? g.Nj : -1, c)) : St{};   // j-predecessor of the first cell
-  // per-thread addresses: W, B of the previous plane and this cell's slot,
-  // for both buffer parities
   // W and B come from the previous plane's buffer inside the block and from
   // the staged edge rings on its first column / row
   const St* const rdW0 = al > 0 ? &sm.sbuf[0][cl + 1][al] : nullptr;
@@ -447,50 +477,62 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   const St* const rdB1 = cl > 0 ? &sm.sbuf[1][cl][al + 1] : nullptr;
   St* const wr0 = &sm.sbuf[0][cl + 1][al + 1];
   St* const wr1 = &sm.sbuf[1][cl + 1][al + 1];
-  const long long cpa = (long long)c * g.P + a;
+  // S: the j-predecessor, the ghost cell until the line's first cell
+  St prevS = line_ok ? op.ghost(g.nat(a, BWD ? g.Nj : -1, c)) : St{};
   const int nat_first = g.nat(a, BWD ? g.Nj - 1 : 0, c);
-  Cell x;
+  int bv = s0 - sfirst;                               // the line's j offset at the current step
+  Cell x;                                             // running indices of the current step's cell
   x.a = a;
   x.c = c;
-  St prevS{};
+  x.sr = BWD ? g.S - 1 - s0 : s0;
+  x.di = (long long)x.sr * g.plane + (long long)c * g.P + a;
+  x.nat = BWD ? nat_first - bv : nat_first + bv;
+  const long long dstep = BWD ? -g.plane : g.plane;
   double part = 0.0;
-  int ds = 0;
+  bool stop = named_bar_red_or(1, NB, false);        // prologue: the first group has landed
   const unsigned char* slot = inbuf;
   const unsigned char* const slot_end = inbuf + NSLOT * L::slot_bytes;
-  for (int s = s0; s <= s1; ++s) {
-    if (named_bar_red_or(1, NB, false)) break;   // plane s-1 computed; inputs and edge states of plane s ready
-    const int bv = s - sfirst;
-    if (line_ok && (unsigned)bv < (unsigned)g.Nj) {
-      const bool odd = (s & 1) != 0;   // the previous plane is in buffer 0 when s is odd
-      const int rs = ring_slot(s - 1);
-      const St W = *(al > 0 ? (odd ? rdW0 : rdW1) : &sm.ringW[rs][cl]);
-      const St B = *(cl > 0 ? (odd ? rdB0 : rdB1) : &sm.ringB[rs][al]);
-      const St S = bv > 0 ? prevS : sg;
-      x.sr = BWD ? g.S - 1 - s : s;
-      x.di = (long long)x.sr * g.plane + cpa;
-      x.nat = BWD ? nat_first - bv : nat_first + bv;
-      in.slot = slot;
+  for (int sg = s0; sg <= s1 && !stop; sg += kG) {
+    in.slot = slot;
+#pragma unroll
+    for (int ds = 0; ds < kG; ++ds) {
+      if (sg + ds > s1) break;
+      const bool act = line_ok && (unsigned)bv < (unsigned)g.Nj;
       in.zb = BWD ? kG - 1 - ds : ds;
-      const St out = op.compute(in, g, x, W, S, B, part);
-      *(odd ? wr1 : wr0) = out;
-      prevS = out;
-      if (edgeE || edgeT) {
-        unsigned long long u[NS];
+      typename Op::Pre pv{};
+      if (act) pv = op.pre(in, prevS);
+      if (ds == 0) {
+        if (named_bar_red_or(1, NB, false)) { stop = true; break; }   // plane s-1 computed; edge states staged
+      } else {
+        named_bar_sync(3, NB);
+      }
+      if (act) {
+        const bool odd = (ds & 1) != 0;   // the plane's parity (group starts are even); previous plane in buffer !odd
+        const int rs = ring_slot(sg + ds - 1);
+        const St W = *(al > 0 ? (odd ? rdW0 : rdW1) : &sm.ringW[rs][cl]);
+        const St B = *(cl > 0 ? (odd ? rdB0 : rdB1) : &sm.ringB[rs][al]);
+        const St out = op.post(in, pv, g, x, W, B, part);
+        *(odd ? wr1 : wr0) = out;
+        prevS = out;
+        if (edgeE || edgeT) {
+          unsigned long long u[NS];
 #pragma unroll
-        for (int k = 0; k < NS; ++k) u[k] = 0;
-        memcpy(u, &out, sizeof(St));
+          for (int k = 0; k < NS; ++k) u[k] = 0;
+          memcpy(u, &out, sizeof(St));
 #pragma unroll
-        for (int k = 0; k < NS; ++k) {
-          if (edgeE) st_relaxed_b64(mW + (size_t)bv * NS + k, u[k]);
-          if (edgeT) st_relaxed_b64(mB + (size_t)bv * NS + k, u[k]);
+          for (int k = 0; k < NS; ++k) {
+            if (edgeE) st_relaxed_b64(mW + (size_t)bv * NS + k, u[k]);
+            if (edgeT) st_relaxed_b64(mB + (size_t)bv * NS + k, u[k]);
+          }
         }
       }
+      ++bv;
+      x.di += dstep;
+      x.sr += BWD ? -1 : 1;
+      x.nat += BWD ? -1 : 1;
     }
-    if (++ds == kG) {
-      ds = 0;
-      slot += L::slot_bytes;
-      if (slot == slot_end) slot = inbuf;
-    }
+    slot += L::slot_bytes;
+    if (slot == slot_end) slot = inbuf;
   }
   if (Op::kReduce) {
     const int lane = tid & 31, wid = tid >> 5;
@@ -530,9 +572,14 @@ struct SipFwdD {
   double* z;                  // hyperplane layout (output; may alias r)
   const double* ghost_src;    // natural array of ghost values, or null (zero)
   __device__ St ghost(int nat) const { return ghost_src ? ghost_src[nat] : 0.0; }
+  struct Pre { double r, bb, bw, bp, tS; };   // tS = bs zS
   template <class In>
-  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
-    const double v = (in.d(0, 0) - in.d(1, 0) * B - in.d(1, 1) * W - in.d(1, 2) * S) * in.d(1, 3);
+  __device__ Pre pre(const In& in, St S) const {
+    return Pre{in.d(0, 0), in.d(1, 0), in.d(1, 1), in.d(1, 3), in.d(1, 2) * S};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& p, const DG&, const Cell& x, St W, St B, double&) const {
+    const double v = (p.r - p.bb * B - p.bw * W - p.tS) * p.bp;
     z[x.di] = v;
     return v;
   }
@@ -554,11 +601,16 @@ struct SipBwdD {
   double* z;
   const double* ghost_src;
   __device__ St ghost(int nat) const { return ghost_src ? ghost_src[nat] : 0.0; }
+  struct Pre { double t, be, bt, res; };   // t = z - bn zS
   template <class In>
-  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double& part) const {
-    const double v = in.d(0, 0) - in.d(1, 0) * S - in.d(1, 1) * W - in.d(1, 2) * B;
+  __device__ Pre pre(const In& in, St S) const {
+    return Pre{in.d(0, 0) - in.d(1, 0) * S, in.d(1, 1), in.d(1, 2), in.d(2, 0)};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& p, const DG&, const Cell& x, St W, St B, double& part) const {
+    const double v = p.t - p.be * W - p.bt * B;
     z[x.di] = v;
-    part += in.d(2, 0) * v;
+    part += p.res * v;
     return v;
   }
 };
@@ -578,11 +630,16 @@ struct SipBwdFiD {
   double* fi;                 // hyperplane layout
   const double* ghost_src;    // module res (stale ghost values, as the reference reads them)
   __device__ St ghost(int nat) const { return ghost_src[nat]; }
+  struct Pre { double t, be, bt, fi; };   // t = z - bn zS
   template <class In>
-  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
-    const double v = in.d(0, 0) - in.d(1, 0) * S - in.d(1, 1) * W - in.d(1, 2) * B;
+  __device__ Pre pre(const In& in, St S) const {
+    return Pre{in.d(0, 0) - in.d(1, 0) * S, in.d(1, 1), in.d(1, 2), in.d(2, 0)};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& p, const DG&, const Cell& x, St W, St B, double&) const {
+    const double v = p.t - p.be * W - p.bt * B;
     z[x.di] = v;
-    fi[x.di] = in.d(2, 0) + v;
+    fi[x.di] = p.fi + v;
     return v;
   }
 };
@@ -603,18 +660,26 @@ struct SipFactorD {
   double* bq;                                       // backward factors, 3 components
   double alfa;
   __device__ St ghost(int nat) const { return St3{bnn[nat], ben[nat], btn[nat]}; }
+  // pre: the terms of the j-predecessor S (bs and its products)
+  struct Pre { double ab, aw, ap, an, ae, at, bsv, sbe, sbt, sbn; };
   template <class In>
-  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
-    const double bbv = -in.d(5, 0) / (1.0 + alfa * (B.bn + B.be));
-    const double bwv = -in.d(1, 0) / (1.0 + alfa * (W.bn + W.bt));
+  __device__ Pre pre(const In& in, St S) const {
     const double bsv = -in.d(3, 0) / (1.0 + alfa * (S.be + S.bt));
+    return Pre{in.d(5, 0), in.d(1, 0), in.d(6, 0), in.d(2, 0), in.d(0, 0), in.d(4, 0),
+               bsv, bsv * S.be, bsv * S.bt, bsv * S.bn};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& q, const DG& g, const Cell& x, St W, St B, double&) const {
+    const double bbv = -q.ab / (1.0 + alfa * (B.bn + B.be));
+    const double bwv = -q.aw / (1.0 + alfa * (W.bn + W.bt));
+    const double bsv = q.bsv;
     const double p1 = alfa * (bbv * B.bn + bwv * W.bn);
-    const double p2 = alfa * (bbv * B.be + bsv * S.be);
-    const double p3 = alfa * (bwv * W.bt + bsv * S.bt);
-    const double bpv = 1.0 / (in.d(6, 0) + p1 + p2 + p3 - bbv * B.bt - bwv * W.be - bsv * S.bn + CAP_SMALL);
-    const double bnv = (-in.d(2, 0) - p1) * bpv;
-    const double bev = (-in.d(0, 0) - p2) * bpv;
-    const double btv = (-in.d(4, 0) - p3) * bpv;
+    const double p2 = alfa * (bbv * B.be + q.sbe);
+    const double p3 = alfa * (bwv * W.bt + q.sbt);
+    const double bpv = 1.0 / (q.ap + p1 + p2 + p3 - bbv * B.bt - bwv * W.be - q.sbn + CAP_SMALL);
+    const double bnv = (-q.an - p1) * bpv;
+    const double bev = (-q.ae - p2) * bpv;
+    const double btv = (-q.at - p3) * bpv;
     const int nat = x.nat;
     bbn[nat] = bbv; bwn[nat] = bwv; bsn[nat] = bsv; bpn[nat] = bpv;
     bnn[nat] = bnv; ben[nat] = bev; btn[nat] = btv;
@@ -650,9 +715,14 @@ struct SipFwdF {
   CUtensorMap map[kMaps];
   float* z;
   __device__ St ghost(int) const { return 0.0f; }
+  struct Pre { float r, bb, bw, bp, tS; };
   template <class In>
-  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
-    const float v = (in.f(0, 0) - in.f(1, 0) * B - in.f(1, 1) * W - in.f(1, 2) * S) * in.f(1, 3);
+  __device__ Pre pre(const In& in, St S) const {
+    return Pre{in.f(0, 0), in.f(1, 0), in.f(1, 1), in.f(1, 3), in.f(1, 2) * S};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& p, const DG&, const Cell& x, St W, St B, double&) const {
+    const float v = (p.r - p.bb * B - p.bw * W - p.tS) * p.bp;
     z[x.di] = v;
     return v;
   }
@@ -670,9 +740,14 @@ struct SipBwdF {
   CUtensorMap map[kMaps];
   float* z;
   __device__ St ghost(int) const { return 0.0f; }
+  struct Pre { float t, be, bt; };
   template <class In>
-  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
-    const float v = in.f(0, 0) - in.f(1, 0) * S - in.f(1, 1) * W - in.f(1, 2) * B;
+  __device__ Pre pre(const In& in, St S) const {
+    return Pre{in.f(0, 0) - in.f(1, 0) * S, in.f(1, 1), in.f(1, 2)};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& p, const DG&, const Cell& x, St W, St B, double&) const {
+    const float v = p.t - p.be * W - p.bt * B;
     z[x.di] = v;
     return v;
   }
@@ -693,18 +768,25 @@ struct SipFactorF {
   float* bq;                       // backward factors, 3 components
   float alfa;
   __device__ St ghost(int nat) const { return St3f{(float)bnn[nat], (float)ben[nat], (float)btn[nat]}; }
+  struct Pre { float ab, aw, ap, an, ae, at, bsv, sbe, sbt, sbn; };
   template <class In>
-  __device__ St compute(const In& in, const DG& g, const Cell& x, St W, St S, St B, double&) const {
-    const float bbv = -in.f(5, 0) / (1.0f + alfa * (B.bn + B.be));
-    const float bwv = -in.f(1, 0) / (1.0f + alfa * (W.bn + W.bt));
+  __device__ Pre pre(const In& in, St S) const {
     const float bsv = -in.f(3, 0) / (1.0f + alfa * (S.be + S.bt));
+    return Pre{in.f(5, 0), in.f(1, 0), in.f(6, 0), in.f(2, 0), in.f(0, 0), in.f(4, 0),
+               bsv, bsv * S.be, bsv * S.bt, bsv * S.bn};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& q, const DG& g, const Cell& x, St W, St B, double&) const {
+    const float bbv = -q.ab / (1.0f + alfa * (B.bn + B.be));
+    const float bwv = -q.aw / (1.0f + alfa * (W.bn + W.bt));
+    const float bsv = q.bsv;
     const float p1 = alfa * (bbv * B.bn + bwv * W.bn);
-    const float p2 = alfa * (bbv * B.be + bsv * S.be);
-    const float p3 = alfa * (bwv * W.bt + bsv * S.bt);
-    const float bpv = 1.0f / (in.f(6, 0) + p1 + p2 + p3 - bbv * B.bt - bwv * W.be - bsv * S.bn + 1e-30f);
-    const float bnv = (-in.f(2, 0) - p1) * bpv;
-    const float bev = (-in.f(0, 0) - p2) * bpv;
-    const float btv = (-in.f(4, 0) - p3) * bpv;
+    const float p2 = alfa * (bbv * B.be + q.sbe);
+    const float p3 = alfa * (bwv * W.bt + q.sbt);
+    const float bpv = 1.0f / (q.ap + p1 + p2 + p3 - bbv * B.bt - bwv * W.be - q.sbn + 1e-30f);
+    const float bnv = (-q.an - p1) * bpv;
+    const float bev = (-q.ae - p2) * bpv;
+    const float btv = (-q.at - p3) * bpv;
     fq[g.dqs(x.sr, x.c, x.a, 0, 4)] = bbv;
     fq[g.dqs(x.sr, x.c, x.a, 1, 4)] = bwv;
     fq[g.dqs(x.sr, x.c, x.a, 2, 4)] = bsv;

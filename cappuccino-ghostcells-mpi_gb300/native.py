@@ -61,6 +61,7 @@ SIGNATURES = {
     "cappgpu_precision": [_INT],
     "cappgpu_learn_reset": [_INT, ctypes.c_ulonglong],
     "cappgpu_learn_collect": [_INT],
+    "cappgpu_learn_windows": [_INT, _INT],
     "cappgpu_learn_train": [_INT, _INT, ctypes.c_double, _DP],
     "cappgpu_learn_params": [ctypes.POINTER(ctypes.c_float), _INT, _INT],
     "cappgpu_learn_stats": [ctypes.POINTER(_INT), ctypes.POINTER(_INT), ctypes.POINTER(_INT), _DP],
@@ -283,6 +284,11 @@ class Library:
     # ------------------------------------------------ learned initial guess
     def learn_reset(self, max_samples, seed=0):
         self._check(self.lib.cappgpu_learn_reset(int(max_samples), int(seed)), "learn_reset")
+
+    def learn_windows(self, block, per_solve):
+        """Record random block^3 windows of each solve (per_solve of them)
+        instead of the whole interior; clears the recorded pairs."""
+        self._check(self.lib.cappgpu_learn_windows(int(block), int(per_solve)), "learn_windows")
 
     def learn_collect(self, on=True):
         self._check(self.lib.cappgpu_learn_collect(1 if on else 0), "learn_collect")

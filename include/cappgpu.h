@@ -284,6 +284,11 @@ int cappgpu_precision(int mode);
    judge and fallback.
    cappgpu_learn_reset     (re)creates the net with seeded weights and room
                            for max_samples recorded pairs of this grid
+   cappgpu_learn_windows   records random block^3 windows of the solves
+                           instead of the whole interior, per_solve windows
+                           per solve, into the room of max_samples windows
+                           (block a multiple of 4 within the interior);
+                           clears the recorded pairs
    cappgpu_learn_collect   records (initial residual, operator) of the
                            pressure solves that follow (precision 1 or 2)
    cappgpu_learn_train     Adam on random block^3 windows of the pairs
@@ -299,6 +304,7 @@ int cappgpu_precision(int mode);
                            multiples of 4) from the host, for tests: output,
                            parameter gradients and loss */
 int cappgpu_learn_reset(int max_samples, unsigned long long seed);
+int cappgpu_learn_windows(int block, int per_solve);
 int cappgpu_learn_collect(int on);
 int cappgpu_learn_train(int epochs, int block, double lr, double* loss);
 int cappgpu_learn_params(float* host, int n, int direction);

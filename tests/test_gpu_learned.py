@@ -116,6 +116,33 @@ def test_trained_guess_lowers_the_initial_residual(gpu_lib):
           f"last solve {r2.iters} iterations vs {r1.iters} without")
 
 
+def test_window_recording_and_training(gpu_lib):
+    """The training set as the learned-guess configuration builds it: random
+    block^3 windows of each recorded solve (per_solve of them), the store
+    cycling at its room; training on the windows lowers the loss; window
+    sizes that are not a multiple of 4 or exceed the interior are refused."""
+    case = cappgpu.cases.channel(N=(16, 16, 24))
+    gpu_lib.load_case(case)
+    gpu_lib.precision(1)
+    try:
+        gpu_lib.learn_reset(20, seed=4)
+        gpu_lib.learn_windows(8, 3)
+        gpu_lib.learn_collect(True)
+        gpu_lib.piso_steps(2)                      # 4 solves x 3 windows
+        assert gpu_lib.learn_stats()["samples"] == 12
+        gpu_lib.piso_steps(2)
+        assert gpu_lib.learn_stats()["samples"] == 20
+        gpu_lib.learn_collect(False)
+        loss0 = gpu_lib.learn_train(1, block=8, lr=1e-3)
+        loss = gpu_lib.learn_train(30, block=8, lr=1e-3)
+        assert np.isfinite(loss) and loss < loss0
+        for bad in (6, 20):
+            with pytest.raises(cappgpu.CappError):
+                gpu_lib.learn_windows(bad, 1)
+    finally:
+        gpu_lib.precision(0)
+
+
 def test_guess_that_raises_the_residual_is_discarded(gpu_lib, oracle_mod):
     """A net whose output is the constant 1 (all weights zero, the last
     bias 1): the fitted guess is a level shift fi + alpha, and with the
