@@ -68,18 +68,30 @@ def test_rans_channel_piso_steps_match_the_oracle(gpu_lib, oracle_mod):
 def test_rans_channel_512x256x256_both_precision_forms(gpu_lib):
     """The large RANS channel (516 x 260 x 260 storage, 33.5 M cells) on one
     GPU: two time steps in the FP64 form and two in precision mode 1 from
-    the same state, every field finite, k and omega positive, and the two
-    forms close."""
+    the same state, every field finite, k and omega positive.  As the
+    reference runs them, the first corrector's p solve stops at 0.1 and the
+    other solves at 1e-3, so the two forms stop at different points inside
+    those bands; with every p corrector solved to 1e-6 and the momentum and
+    turbulence solves to 1e-9 the forms are compared field by field."""
     case = cappgpu.cases.rans_channel(N=(512, 256, 256))
     gpu_lib.load_case(case)
     names = cappgpu.FIELD_NAMES
     snap = {n: gpu_lib.get_field(n) for n in names}
     params = gpu_lib.get_params()
-    out = {}
-    for mode in (0, 1):
+    fields = ("u", "v", "w", "p", "te", "ed", "vis")
+
+    def run(mode, tight):
         for n, a in snap.items():
             gpu_lib.set_field(n, a)
-        gpu_lib.set_params(params)
+        pr = cappgpu.Params()
+        import ctypes
+        ctypes.memmove(ctypes.addressof(pr), ctypes.addressof(params), ctypes.sizeof(pr))
+        if tight:
+            for q in (0, 1, 2, 4, 5):   # u, v, w, te, ed
+                pr.sor[q] = 1e-9
+                pr.nsw[q] = 400
+        gpu_lib.set_params(pr)
+        gpu_lib.set_option("tight_correctors", 1 if tight else 0)
         gpu_lib.precision(mode)
         try:
             gpu_lib.timer_start()
@@ -87,17 +99,25 @@ def test_rans_channel_512x256x256_both_precision_forms(gpu_lib):
             ms = gpu_lib.timer_stop()
         finally:
             gpu_lib.precision(0)
+            gpu_lib.set_option("tight_correctors", 0)
         assert rep.status >= 0
-        f = {n: gpu_lib.get_field(n) for n in ("u", "v", "w", "p", "te", "ed", "vis")}
+        f = {n: gpu_lib.get_field(n) for n in fields}
         for n, a in f.items():
             assert np.all(np.isfinite(a)), (mode, n)
         assert f["te"].min() > 0 and f["ed"].min() > 0
-        pr = gpu_lib.get_params()
-        out[mode] = (f, ms / 2, rep, pr.sumlocalconterr)
-    f64, f32 = out[0][0], out[1][0]
-    rel = {n: float(np.linalg.norm(f32[n] - f64[n]) / np.linalg.norm(f64[n])) for n in f64}
-    print(f"RANS channel 512x256x256: FP64 {out[0][1]:.0f} ms/step (p solve {out[0][2].iters} it), "
-          f"mode 1 {out[1][1]:.0f} ms/step ({out[1][2].iters} it); mode 1 vs FP64 "
-          + ", ".join(f"{n} {v:.1e}" for n, v in rel.items()))
+        return f, ms / 2, rep
+
+    def rel(a, b):
+        return {n: float(np.linalg.norm(a[n] - b[n]) / np.linalg.norm(b[n])) for n in b}
+
+    out = {(m, t): run(m, t) for t in (False, True) for m in (0, 1)}
+    loose = rel(out[(1, False)][0], out[(0, False)][0])
+    tight = rel(out[(1, True)][0], out[(0, True)][0])
+    fmt = lambda d: ", ".join(f"{n} {v:.1e}" for n, v in d.items())
+    print(f"RANS channel 512x256x256: FP64 {out[(0, False)][1]:.0f} ms/step (p solve {out[(0, False)][2].iters} it), "
+          f"mode 1 {out[(1, False)][1]:.0f} ms/step ({out[(1, False)][2].iters} it); mode 1 vs FP64 as the "
+          f"reference runs them: {fmt(loose)}; with every solve converged: {fmt(tight)}")
     for n in ("u", "te", "ed", "vis"):
-        assert rel[n] < 1e-3, (n, rel[n])
+        assert loose[n] < 1e-3, (n, loose[n])
+    for n in fields:
+        assert tight[n] < 1e-3, (n, tight[n])
