@@ -30,6 +30,8 @@ struct DG {
   int Ni, Nj, Nk, S;   // interior extents and hyperplane count
   int P;               // row pitch (Ni rounded up to a multiple of 4)
   int nj, nij;         // natural strides
+  int kb;              // natural k-plane index (0-based) of c = 0: 2 (k = 3) for the interior box,
+                       // 1 (k = 2) for the box that also holds the k ghost layers
   long long plane;     // Nk*P
   long long ncell;     // Ni*Nj*Nk
   int nchunk;          // ceil(ncell / 32)
@@ -45,16 +47,19 @@ struct DG {
   __host__ __device__ long long dqs(int s, int c, int a, int q, int NQ) const {
     return ((long long)s * Nk * NQ + (long long)c * NQ + q) * P + a;
   }
-  // 0-based natural index of interior-local (a,b,c); valid for a,b,c >= -1
-  __host__ __device__ int nat(int a, int b, int c) const { return (c + 2) * nij + (a + 2) * nj + (b + 2); }
+  // 0-based natural index of box-local (a,b,c); valid for a,b,c >= -1
+  __host__ __device__ int nat(int a, int b, int c) const { return (c + kb) * nij + (a + 2) * nj + (b + 2); }
   __host__ __device__ long long size() const { return (long long)S * plane; }
 };
 
-inline DG make_dg(const Dims& d) {
+// the box i = 3..nimm, j = 3..njmm and k = 3..nkmm (the interior), or with
+// ghost_k k = 2..nkm (the loops of iccg.f90 and cgstab*.f90)
+inline DG make_dg(const Dims& d, bool ghost_k = false) {
   DG g;
   g.Ni = d.nimm - 2;
   g.Nj = d.njmm - 2;
-  g.Nk = d.nkmm - 2;
+  g.Nk = d.nkmm - 2 + (ghost_k ? 2 : 0);
+  g.kb = ghost_k ? 1 : 2;
   g.S = g.Ni + g.Nj + g.Nk - 2;
   g.P = (g.Ni + 3) & ~3;
   g.nj = d.nj;

@@ -20,6 +20,9 @@ int dpcg(int fi, int ifi, cappgpu_solve_report* rep);
 int pcgsip_fast(int fi, int ifi, cappgpu_solve_report* rep);
 int pcgsip_mixed(int fi, int ifi, cappgpu_solve_report* rep);
 int sipsol_fast(int fi, int ifi, cappgpu_solve_report* rep);
+int cgstab_sip_fast(int fi, int ifi, cappgpu_solve_report* rep);
+int iccg_fast(int fi, int ifi, cappgpu_solve_report* rep);
+int resid_natural_k(int fif, int k0, int k1, double* res0);
 int sipsol_mixed(int fi, int ifi, cappgpu_solve_report* rep);
 int fast_profile_unit(int which, double* bytes);
 void fast_free();

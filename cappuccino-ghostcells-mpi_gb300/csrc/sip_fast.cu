@@ -51,7 +51,16 @@ struct Fast {
   int* hstat = nullptr;       // pinned host copies: [0..3] ctl, [4..5] flags
 };
 
-Fast F;
+// one instance per box: [0] the interior (pcgsip, sipsol), [1] the box with
+// the k ghost layers (cgstab_sip); F names the instance of the current box
+Fast g_fast[2];
+int g_box = 0;
+#define F (g_fast[g_box])
+struct BoxScope {
+  int prev;
+  explicit BoxScope(int b) : prev(g_box) { g_box = b; }
+  ~BoxScope() { g_box = prev; }
+};
 
 // FP32 copies for the FP32 + FP64-refinement form of pcgsip
 enum EBuf { E_AE, E_AW, E_AN, E_AS, E_AT, E_AB, E_AP, E_R, E_Z, E_P0, E_P1, E_ZZ, E_X, E_NBUF };
@@ -96,7 +105,7 @@ void fast32_release() {
 }
 
 void fast_release() {
-  fast32_release();
+  if (g_box == 0) fast32_release();
   for (auto& p : F.d) { if (p) cudaFree(p); p = nullptr; }
   if (F.fq) cudaFree(F.fq);
   if (F.bq) cudaFree(F.bq);
@@ -190,7 +199,7 @@ int fast_setup() {
   if (F.ready && memcmp(&F.dims, &d, sizeof(Dims)) == 0) return CAPPGPU_OK;
   fast_release();
   F.dims = d;
-  F.g = make_dg(d);
+  F.g = make_dg(d, g_box == 1);
   size_t n = (size_t)F.g.size();
   for (int q = 0; q < D_NBUF; ++q) {
     if (cudaMalloc(&F.d[q], n * sizeof(double)) != cudaSuccess) { fast_release(); set_error("out of device memory"); return CAPPGPU_E_NOMEM; }
@@ -516,8 +525,8 @@ __device__ __forceinline__ void walk_cells(const DG& g, int& s, int& c, int& a, 
   }
 }
 
-template <int U = 2, class F>
-__device__ __forceinline__ void for_cells(const DG& g, F&& f) {
+template <int U = 2, class Fn>
+__device__ __forceinline__ void for_cells(const DG& g, Fn&& f) {
   const int lane = threadIdx.x & 31;
   const int nw = (int)((gridDim.x * blockDim.x) >> 5);
   for (int q0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * U; q0 < g.nchunk; q0 += nw * U) {
@@ -914,9 +923,115 @@ __global__ void k_update_fx(DG g, float* __restrict__ x, float* __restrict__ r, 
   block_reduce_store<1>(v, pout);
 }
 
+
+// ------------------------------------------------ BiCGStab, SIP-preconditioned
+// cgstab_sip.f90:3-279 on the box with the k ghost layers; the scalars of
+// the iteration stay on the device (c.dscal[8..15])
+enum { BS_ALF = 8, BS_BETO, BS_GAM, BS_BET, BS_OM, BS_UKR, BS_VRES, BS_VV };
+
+__global__ void k_bicg_init_scal(double* s) {   // alf = beto = gam = 1 (cgstab_sip.f90:95-97)
+  s[BS_ALF] = 1.0;
+  s[BS_BETO] = 1.0;
+  s[BS_GAM] = 1.0;
+}
+
+// partial sums of a.b (cgstab_sip.f90:106-114)
+__global__ void k_dot_x(DG g, const double* __restrict__ a, const double* __restrict__ b, double* part, const int* ctl) {
+  if (*(volatile const int*)ctl) return;
+  double v[1] = {0.0};
+  for_cells(g, [&](long long t_, int, int, int) { v[0] += a[t_] * b[t_]; });
+  block_reduce_store<1>(v, part);
+}
+
+// scalar steps, one block, fixed summation order
+// mode 0: bet = res.reso; om = bet gam/(alf beto + small); beto = bet (cgstab_sip.f90:106-116)
+// mode 1: ukreso = uk.reso; gam = bet/ukreso                          (cgstab_sip.f90:170-179)
+// mode 2: vres = vk.res, vv = vk.vk; alf = vres/(vv + small)          (cgstab_sip.f90:233-245)
+__global__ void k_bicg_scal(int mode, const double* __restrict__ part, double* s, const int* ctl) {
+  if (*(volatile const int*)ctl) return;
+  const double x0 = block_sum_fixed(part, kRedBlocks);
+  const double x1 = mode == 2 ? block_sum_fixed(part + kRedBlocks, kRedBlocks) : 0.0;
+  if (threadIdx.x == 0) {
+    if (mode == 0) {
+      s[BS_BET] = x0;
+      s[BS_OM] = x0 * s[BS_GAM] / (s[BS_ALF] * s[BS_BETO] + CAP_SMALL);
+      s[BS_BETO] = x0;
+    } else if (mode == 1) {
+      s[BS_UKR] = x0;
+      s[BS_GAM] = s[BS_BET] / x0;
+    } else {
+      s[BS_VRES] = x0;
+      s[BS_VV] = x1;
+      s[BS_ALF] = x0 / (x1 + CAP_SMALL);
+    }
+  }
+}
+
+// pk = res + om (pk - alf uk) (cgstab_sip.f90:120-127)
+__global__ void k_bicg_pk_x(DG g, const double* __restrict__ res, double* __restrict__ pk,
+                            const double* __restrict__ uk, const double* __restrict__ s, const int* ctl) {
+  if (*(volatile const int*)ctl) return;
+  const double om = s[BS_OM], alf = s[BS_ALF];
+  for_cells(g, [&](long long t_, int, int, int) { pk[t_] = res[t_] + om * (pk[t_] - alf * uk[t_]); });
+}
+
+// y = A p (cgstab_sip.f90:156-166, 219-229) with the partial sums of y.w, and with
+// two_dots also of y.y
+__global__ void k_spmv_dot_x(DG g, const double* __restrict__ ae, const double* __restrict__ aw,
+                             const double* __restrict__ an, const double* __restrict__ as,
+                             const double* __restrict__ at, const double* __restrict__ ab,
+                             const double* __restrict__ ap, const double* __restrict__ pk, double* __restrict__ y,
+                             const double* __restrict__ w, int two_dots, double* part, const int* ctl) {
+  if (*(volatile const int*)ctl) return;
+  double v[2] = {0.0, 0.0};
+  for_cells(g, [&](long long t_, int a, int b, int c) {
+    const long long P = t_;
+    const double pP = pk[P];
+    const double pE = a + 1 < g.Ni ? pk[P + g.plane + 1] : 0.0;
+    const double pW = a > 0 ? pk[P - g.plane - 1] : 0.0;
+    const double pN = b + 1 < g.Nj ? pk[P + g.plane] : 0.0;
+    const double pS = b > 0 ? pk[P - g.plane] : 0.0;
+    const double pT = c + 1 < g.Nk ? pk[P + g.plane + g.P] : 0.0;
+    const double pB = c > 0 ? pk[P - g.plane - g.P] : 0.0;
+    const double r = ap[P] * pP - ae[P] * pE - aw[P] * pW - an[P] * pN - as[P] * pS - at[P] * pT - ab[P] * pB;
+    y[P] = r;
+    v[0] += r * w[P];
+    if (two_dots) v[1] += r * r;
+  });
+  block_reduce_store<2>(v, part);
+}
+
+// fi += s zk; res -= s y; with part the partial sums |res|
+// (cgstab_sip.f90:183-191, 249-259)
+__global__ void k_bicg_upd_x(DG g, double* __restrict__ fi, double* __restrict__ res, const double* __restrict__ zk,
+                             const double* __restrict__ y, const double* __restrict__ s, int si, double* part,
+                             const int* ctl) {
+  if (*(volatile const int*)ctl) return;
+  const double sc = s[si];
+  double v[1] = {0.0};
+  for_cells(g, [&](long long t_, int, int, int) {
+    fi[t_] = fi[t_] + sc * zk[t_];
+    const double r = res[t_] - sc * y[t_];
+    res[t_] = r;
+    v[0] += fabs(r);
+  });
+  if (part) block_reduce_store<1>(v, part);
+}
+
+// zk = zk/(d + small) (iccg.f90:102-108)
+__global__ void k_divd_x(DG g, double* __restrict__ zk, const double* __restrict__ dg, const int* ctl) {
+  if (*(volatile const int*)ctl) return;
+  for_cells(g, [&](long long t_, int, int, int) { zk[t_] = zk[t_] / (dg[t_] + CAP_SMALL); });
+}
+
 }  // namespace
 
-void fast_free() { fast_release(); }
+void fast_free() {
+  for (int b = 1; b >= 0; --b) {
+    BoxScope box(b);
+    fast_release();
+  }
+}
 
 static int wave_error_reset(const int* h) {
   if (h[1] != 0) {
@@ -1073,6 +1188,203 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
     rep->res0 = res0;
     rep->resl = resl;
     rep->iters = l;
+    rep->status = done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+  }
+  if (hctl[2] || !isfinite(resl)) {
+    set_error("linear solver residual is not finite");
+    if (rep) rep->status = CAPPGPU_E_NONFINITE;
+    return CAPPGPU_E_NONFINITE;
+  }
+  return done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+}
+
+// cgstab_sip (cgstab_sip.f90:3-279) on the box i = 3..nimm, j = 3..njmm,
+// k = 2..nkm (the routine's loops take the k ghost layers in): SIP
+// factorisation and both substitutions of each preconditioner solve as
+// persistent wavefronts, every vector in the hyperplane layout, the
+// scalars on the device; the host reads the exit test once per batch of
+// iterations.
+int cgstab_sip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  cappgpu_params& P = c.prm;
+  BoxScope box(1);
+  int rc = fast_setup();
+  if (rc) return rc;
+  CAP_CUDA(cudaMemsetAsync(F.flags, 0, sizeof(int) * 2, c.st));
+  const double resmax = P.sor[ifi - 1];
+  // res over the box and res0 (cgstab_sip.f90:45-57)
+  double res0 = 0.0;
+  if ((rc = resid_natural_k(fif, 2, d.nkm, &res0))) return rc;
+  const int cf[7] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP};
+  for (int q = 0; q < 7; ++q)
+    if ((rc = to_d(cf[q], D_AE + q))) return rc;
+  if ((rc = to_d(CAP_RES, D_RES))) return rc;
+  if ((rc = to_d(fif, D_FI))) return rc;
+  // reso = res; pk = uk = zk = vk = 0 (cgstab_sip.f90:83-94); reso in D_SU,
+  // pk in D_PK0, uk in D_ZZ, vk in D_PK1
+  const size_t nb = sizeof(double) * (size_t)F.g.size();
+  CAP_CUDA(cudaMemcpyAsync(F.d[D_SU], F.d[D_RES], nb, cudaMemcpyDeviceToDevice, c.st));
+  for (int q : {D_PK0, D_ZZ, D_Z, D_PK1}) CAP_CUDA(cudaMemsetAsync(F.d[q], 0, nb, c.st));
+  if ((rc = factor_wave())) return rc;   // cgstab_sip.f90:59-79
+  launch(k_bicg_init_scal, 1, 1, c.st, c.dscal);
+  const SipFwdD fwd_p = make_fwd(D_PK0, D_Z, nullptr);
+  const SipFwdD fwd_r = make_fwd(D_RES, D_Z, nullptr);
+  const SipBwdD bwd = make_bwd(D_Z, D_RES);   // its dot is not used here
+  const int ns = P.nsw[ifi - 1];
+  P.resor[ifi - 1] = res0;   // cgstab_sip.f90:263 (l = 1)
+  CAP_CUDA(cudaMemsetAsync(F.ctl, 0, sizeof(int) * 4, c.st));
+  double* const part0 = c.partials;
+  double* const part1 = c.partials + 2 * kRedBlocks;
+  const DG& g = F.g;
+  const double* A[7];
+  for (int q = 0; q < 7; ++q) A[q] = F.d[D_AE + q];
+  int hctl[4] = {0, 0, 0, 0};
+  for (int launched = 0; launched < ns;) {
+    const int batch = ns - launched < c.cg_batch ? ns - launched : c.cg_batch;
+    for (int q = 0; q < batch; ++q) {
+      launch(k_dot_x, kRedBlocks, kThreads, c.st, g, (const double*)F.d[D_RES], (const double*)F.d[D_SU], part0,
+             (const int*)F.ctl);
+      launch(k_bicg_scal, 1, kThreads, c.st, 0, (const double*)part0, c.dscal, (const int*)F.ctl);
+      launch(k_bicg_pk_x, kRedBlocks, kThreads, c.st, g, (const double*)F.d[D_RES], F.d[D_PK0],
+             (const double*)F.d[D_ZZ], (const double*)c.dscal, (const int*)F.ctl);
+      CAP_CHECK_LAUNCH();
+      if ((rc = run_wave<SipFwdD, false>(fwd_p, F.ctl))) return rc;   // m zk = pk
+      if ((rc = run_wave<SipBwdD, true>(bwd, F.ctl))) return rc;
+      launch(k_spmv_dot_x, kRedBlocks, kThreads, c.st, g, A[0], A[1], A[2], A[3], A[4], A[5], A[6],
+             (const double*)F.d[D_Z], F.d[D_ZZ], (const double*)F.d[D_SU], 0, part0, (const int*)F.ctl);
+      launch(k_bicg_scal, 1, kThreads, c.st, 1, (const double*)part0, c.dscal, (const int*)F.ctl);
+      launch(k_bicg_upd_x, kRedBlocks, kThreads, c.st, g, F.d[D_FI], F.d[D_RES], (const double*)F.d[D_Z],
+             (const double*)F.d[D_ZZ], (const double*)c.dscal, (int)BS_GAM, (double*)nullptr, (const int*)F.ctl);
+      CAP_CHECK_LAUNCH();
+      if ((rc = run_wave<SipFwdD, false>(fwd_r, F.ctl))) return rc;   // m zk = res
+      if ((rc = run_wave<SipBwdD, true>(bwd, F.ctl))) return rc;
+      launch(k_spmv_dot_x, kRedBlocks, kThreads, c.st, g, A[0], A[1], A[2], A[3], A[4], A[5], A[6],
+             (const double*)F.d[D_Z], F.d[D_PK1], (const double*)F.d[D_RES], 1, part0, (const int*)F.ctl);
+      launch(k_bicg_scal, 1, kThreads, c.st, 2, (const double*)part0, c.dscal, (const int*)F.ctl);
+      launch(k_bicg_upd_x, kRedBlocks, kThreads, c.st, g, F.d[D_FI], F.d[D_RES], (const double*)F.d[D_Z],
+             (const double*)F.d[D_PK1], (const double*)c.dscal, (int)BS_ALF, part1, (const int*)F.ctl);
+      launch(k_cg_check, 1, kThreads, c.st, (const double*)part1, c.dscal, F.ctl, res0, resmax, 0.0, ns);
+      CAP_CHECK_LAUNCH();
+    }
+    launched += batch;
+    CAP_CUDA(cudaMemcpyAsync(F.hstat, F.ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.st));
+    if ((rc = sync_status())) return rc;
+    for (int q = 0; q < 4; ++q) hctl[q] = F.hstat[q];
+    if (hctl[0]) break;
+  }
+  CAP_CUDA(cudaMemcpy(F.hres, c.dscal + 5, sizeof(double), cudaMemcpyDeviceToHost));
+  const int l = hctl[1];
+  const double resl = l > 0 ? F.hres[0] : res0;
+  const bool done = hctl[3] != 0;
+  if ((rc = from_d(D_FI, fif))) return rc;
+  if ((rc = from_d(D_RES, CAP_RES))) return rc;
+  if (rep) {
+    rep->res0 = res0;
+    rep->resl = resl;
+    rep->iters = done ? l : ns;
+    rep->status = done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+  }
+  if (hctl[2] || !isfinite(resl)) {
+    set_error("linear solver residual is not finite");
+    if (rep) rep->status = CAPPGPU_E_NONFINITE;
+    return CAPPGPU_E_NONFINITE;
+  }
+  return done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
+}
+
+// iccg (iccg.f90:3-197) on the box i = 3..nimm, j = 3..njmm, k = 2..nkm:
+// the IC(0) diagonal and both substitutions as persistent wavefronts, the
+// CG vector passes and the exit test of pcgsip_fast.
+int iccg_fast(int fif, int ifi, cappgpu_solve_report* rep) {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  cappgpu_params& P = c.prm;
+  BoxScope box(1);
+  int rc = fast_setup();
+  if (rc) return rc;
+  CAP_CUDA(cudaMemsetAsync(F.flags, 0, sizeof(int) * 2, c.st));
+  const double resmax = P.sor[ifi - 1];
+  // res = 0, then res and res0 over the box (iccg.f90:45-62)
+  CAP_CUDA(cudaMemsetAsync(c.f[CAP_RES], 0, sizeof(double) * d.nijk, c.st));
+  double res0 = 0.0;
+  if ((rc = resid_natural_k(fif, 2, d.nkm, &res0))) return rc;
+  const int cf[7] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP};
+  for (int q = 0; q < 7; ++q)
+    if ((rc = to_d(cf[q], D_AE + q))) return rc;
+  if ((rc = to_d(CAP_RES, D_RES))) return rc;
+  if ((rc = to_d(fif, D_FI))) return rc;
+  // pk = zk = d = 0; d in D_SU
+  const size_t nb = sizeof(double) * (size_t)F.g.size();
+  for (int q : {D_PK0, D_Z, D_SU}) CAP_CUDA(cudaMemsetAsync(F.d[q], 0, nb, c.st));
+  {
+    IcDiagD op;
+    op.map[0] = F.map[D_AP];
+    op.map[1] = F.map[D_AW];
+    op.map[2] = F.map[D_AS];
+    op.map[3] = F.map[D_AB];
+    op.dg = F.d[D_SU];
+    if ((rc = run_wave<IcDiagD, false>(op))) return rc;
+  }
+  launch(k_set_scal, 1, 1, c.st, c.dscal, (double)1.e20f);   // s0 = 1.e20 (default real)
+  IcFwdD fwd;
+  fwd.map[0] = F.map[D_RES];
+  fwd.map[1] = F.map[D_AW];
+  fwd.map[2] = F.map[D_AS];
+  fwd.map[3] = F.map[D_AB];
+  fwd.map[4] = F.map[D_SU];
+  fwd.z = F.d[D_Z];
+  IcBwdD bwd;
+  bwd.map[0] = F.map[D_Z];
+  bwd.map[1] = F.map[D_AE];
+  bwd.map[2] = F.map[D_AN];
+  bwd.map[3] = F.map[D_AT];
+  bwd.map[4] = F.map[D_SU];
+  bwd.map[5] = F.map[D_RES];
+  bwd.z = F.d[D_Z];
+  const int ns = P.nsw[ifi - 1];
+  P.resor[ifi - 1] = res0;   // iccg.f90:182 (l = 1)
+  CAP_CUDA(cudaMemsetAsync(F.ctl, 0, sizeof(int) * 4, c.st));
+  double* const part0 = c.partials;
+  double* const part1 = c.partials + kRedBlocks;
+  int cur = 0;
+  int hctl[4] = {0, 0, 0, 0};
+  for (int launched = 0; launched < ns;) {
+    const int batch = ns - launched < c.cg_batch ? ns - launched : c.cg_batch;
+    for (int q = 0; q < batch; ++q) {
+      if ((rc = run_wave<IcFwdD, false>(fwd, F.ctl))) return rc;
+      launch(k_divd_x, kRedBlocks, kThreads, c.st, F.g, F.d[D_Z], (const double*)F.d[D_SU], (const int*)F.ctl);
+      CAP_CHECK_LAUNCH();
+      if ((rc = run_wave<IcBwdD, true>(bwd, F.ctl))) return rc;
+      double* pko = F.d[cur ? D_PK1 : D_PK0];
+      double* pkn = F.d[cur ? D_PK0 : D_PK1];
+      launch(k_pk_x, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_Z], (const double*)pko, pkn,
+             (const double*)F.wpart, F.nblk, c.dscal, (const int*)F.ctl);
+      launch(k_spmv_x, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
+             (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
+             (const double*)F.d[D_AP], (const double*)pkn, F.d[D_ZZ], part0, (const int*)F.ctl);
+      launch(k_update_x, kRedBlocks, kThreads, c.st, F.g, F.d[D_FI], F.d[D_RES], (const double*)pkn,
+             (const double*)F.d[D_ZZ], (const double*)part0, c.dscal, part1, (const int*)F.ctl);
+      launch(k_cg_check, 1, kThreads, c.st, (const double*)part1, c.dscal, F.ctl, res0, resmax, 0.0, ns);
+      CAP_CHECK_LAUNCH();
+      cur ^= 1;
+    }
+    launched += batch;
+    CAP_CUDA(cudaMemcpyAsync(F.hstat, F.ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.st));
+    if ((rc = sync_status())) return rc;
+    for (int q = 0; q < 4; ++q) hctl[q] = F.hstat[q];
+    if (hctl[0]) break;
+  }
+  CAP_CUDA(cudaMemcpy(F.hres, c.dscal + 5, sizeof(double), cudaMemcpyDeviceToHost));
+  const int l = hctl[1];
+  const double resl = l > 0 ? F.hres[0] : res0;
+  const bool done = hctl[3] != 0;
+  if ((rc = from_d(D_FI, fif))) return rc;
+  if ((rc = from_d(D_RES, CAP_RES))) return rc;
+  if (rep) {
+    rep->res0 = res0;
+    rep->resl = resl;
+    rep->iters = done ? l : ns;
     rep->status = done ? CAPPGPU_OK : CAPPGPU_NOT_CONVERGED;
   }
   if (hctl[2] || !isfinite(resl)) {

@@ -222,6 +222,16 @@ int resid_natural(int fif, double* res0) {
   return reduce_fetch(1, res0);
 }
 
+// the same over i = 3..nimm, j = 3..njmm and k = k0..k1 (cgstab_sip.f90:45-57 takes k = 2..nkm)
+int resid_natural_k(int fif, int k0, int k1, double* res0) {
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  Box b{3, d.nimm, 3, d.njmm, k0, k1};
+  launch(k_resid, kRedBlocks, kThreads, c.st, d, b, coef(), (const double*)c.f[fif], c.f[CAP_RES], c.partials);
+  CAP_CHECK_LAUNCH();
+  return reduce_fetch(1, res0);
+}
+
 int spmv_dot2_natural(const double* p, double* z, const double* r, double* out2) {
   Ctx& c = ctx();
   const Dims& d = c.d;
@@ -304,6 +314,7 @@ int pcgsip(int fif, int ifi, cappgpu_solve_report* rep) {
 // iccg.f90:3-197
 int iccg(int fif, int ifi, cappgpu_solve_report* rep) {
   Ctx& c = ctx();
+  if (c.wave_impl == 1 && c.d.nimm >= 4 && c.d.njmm >= 4 && c.d.nkmm >= 4) return iccg_fast(fif, ifi, rep);
   const Dims& d = c.d;
   double** F = c.f;
   cappgpu_params& P = c.prm;
@@ -360,6 +371,8 @@ int iccg(int fif, int ifi, cappgpu_solve_report* rep) {
 // here they are zero there (work vectors are cleared first).
 int bicgstab(int fif, int ifi, bool sip, cappgpu_solve_report* rep) {
   Ctx& c = ctx();
+  if (sip && c.wave_impl == 1 && c.d.nimm >= 4 && c.d.njmm >= 4 && c.d.nkmm >= 4)
+    return cgstab_sip_fast(fif, ifi, rep);
   const Dims& d = c.d;
   double** F = c.f;
   cappgpu_params& P = c.prm;

@@ -694,6 +694,90 @@ struct SipFactorD {
   }
 };
 
+// ICCG (iccg.f90:3-197).  IC(0) diagonal d = 1/(ap - aw^2 dW - as^2 dS -
+// ab^2 dB) (iccg.f90:73-80; its 1. is exactly 1); state passed on = d; written to the
+// hyperplane layout only (the reference's d is a local work array).
+struct IcDiagD {
+  using St = double;
+  static constexpr int kMaps = 4;   // ap, aw, as, ab
+  static constexpr bool kReduce = false;
+  static constexpr int kSlots = 3;
+  static constexpr int kPacers = 1;
+  static constexpr int kPW = 4;
+  __host__ __device__ static constexpr int nq(int) { return 1; }
+  __host__ __device__ static constexpr int esize(int) { return 8; }
+  CUtensorMap map[kMaps];
+  double* dg;
+  __device__ St ghost(int) const { return 0.0; }   // the work array is zero outside the loop box
+  struct Pre { double ap, aww, abb, sS; };          // sS = as^2 dS
+  template <class In>
+  __device__ Pre pre(const In& in, St S) const {
+    const double as = in.d(2, 0);
+    return Pre{in.d(0, 0), in.d(1, 0) * in.d(1, 0), in.d(3, 0) * in.d(3, 0), as * as * S};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& p, const DG&, const Cell& x, St W, St B, double&) const {
+    const double v = 1.0 / (p.ap - p.aww * W - p.sS - p.abb * B);
+    dg[x.di] = v;
+    return v;
+  }
+};
+
+// ICCG forward substitution z = (r + aw zW + as zS + ab zB) d (iccg.f90:92-99)
+struct IcFwdD {
+  using St = double;
+  static constexpr int kMaps = 5;   // r, aw, as, ab, d
+  static constexpr bool kReduce = false;
+  static constexpr int kSlots = 3;
+  static constexpr int kPacers = 1;
+  static constexpr int kPW = 4;
+  __host__ __device__ static constexpr int nq(int) { return 1; }
+  __host__ __device__ static constexpr int esize(int) { return 8; }
+  CUtensorMap map[kMaps];
+  double* z;
+  __device__ St ghost(int) const { return 0.0; }
+  struct Pre { double r, aw, ab, dg, sS; };   // sS = as zS
+  template <class In>
+  __device__ Pre pre(const In& in, St S) const {
+    return Pre{in.d(0, 0), in.d(1, 0), in.d(3, 0), in.d(4, 0), in.d(2, 0) * S};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& p, const DG&, const Cell& x, St W, St B, double&) const {
+    const double v = (p.r + p.aw * W + p.sS + p.ab * B) * p.dg;
+    z[x.di] = v;
+    return v;
+  }
+};
+
+// ICCG backward substitution z = (z + ae zE + an zN + at zT) d with the
+// dot sk = sum res z in the same loop (iccg.f90:112-124); the
+// engine's S, W, B neighbours are the j+1, i+1, k+1 cells here.
+struct IcBwdD {
+  using St = double;
+  static constexpr int kMaps = 6;   // z (after the division by d), ae, an, at, d, res
+  static constexpr bool kReduce = true;
+  static constexpr int kSlots = 3;
+  static constexpr int kPacers = 1;
+  static constexpr int kPW = 4;
+  __host__ __device__ static constexpr int nq(int) { return 1; }
+  __host__ __device__ static constexpr int esize(int) { return 8; }
+  CUtensorMap map[kMaps];
+  double* z;
+  __device__ St ghost(int) const { return 0.0; }
+  struct Pre { double z, ae, at, dg, res, sS; };   // sS = an zN
+  template <class In>
+  __device__ Pre pre(const In& in, St S) const {
+    return Pre{in.d(0, 0), in.d(1, 0), in.d(3, 0), in.d(4, 0), in.d(5, 0), in.d(2, 0) * S};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& p, const DG&, const Cell& x, St W, St B, double& part) const {
+    const double v = (p.z + p.ae * W + p.sS + p.at * B) * p.dg;
+    z[x.di] = v;
+    part += p.res * v;
+    return v;
+  }
+};
+
 // ------------------------------------------------- single-precision ops
 // The preconditioner of the FP32 + FP64-refinement form of the pressure
 // solve: the same SIP recurrences (pcg-sip.f90:68-121) on FP32 copies of

@@ -509,14 +509,16 @@ def test_top_wall_index_guard(gpu_lib, oracle_mod):
 
 @pytest.mark.parametrize("shape", [(40, 12, 30), (37, 21, 19), (5, 3, 70)])
 @pytest.mark.parametrize("wave", [1, 0])
-@pytest.mark.parametrize("solver", ["pcgsip", "sipsol"])
+@pytest.mark.parametrize("solver", ["pcgsip", "sipsol", "cgstab_sip", "iccg"])
 def test_sip_wavefront_multiblock(gpu_lib, oracle_mod, shape, wave, solver):
-    """pcgsip and sipsol with the persistent wavefront over many line blocks
-    (and with one launch per hyperplane) against the oracle: SIP factors
-    bit-exact (sipsol: the solution too), same iteration count."""
+    """pcgsip, sipsol, cgstab_sip and iccg with the persistent wavefront over
+    many line blocks (and with one launch per hyperplane) against the
+    oracle: SIP factors bit-exact (sipsol: the solution too), same iteration
+    count.  The loops of cgstab_sip and iccg take the k ghost layers in
+    (k = 2..nkm): their wavefronts run on that box."""
     st = oracle_mod.State(*[n + 4 for n in shape])
     rng = np.random.default_rng(sum(shape))
-    diag_dominant_matrix(st, rng, symmetric=solver == "pcgsip")
+    diag_dominant_matrix(st, rng, symmetric=solver in ("pcgsip", "iccg"))
     randomize(st, rng, ["bb", "bs", "bw", "bp", "bn", "be", "bt"], -0.3, 0.3)
     randomize(st, rng, ["p", "res"])
     st.params.update(dict(alfa=0.92, sor=[1e-9] * 10, nsw=[400] * 10, ipr=3, jpr=3, kpr=3))
