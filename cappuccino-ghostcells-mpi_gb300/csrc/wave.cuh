@@ -67,6 +67,12 @@ constexpr int kRing = 32;    // planes of staged edge states (a power of two)
 #endif
 constexpr int kComm = CAP_WAVE_COMM_WARPS;   // communication warps: 1 stages both edges, 2 one edge each
 static_assert(kComm == 1 || kComm == 2, "communication warps");
+// steps per barrier of the pacing warp in the FP32 substitutions and
+// factorisation (a copy group: its edge-plane checks cover the whole group)
+#ifndef CAP_FP32_SYNC_STEPS
+#define CAP_FP32_SYNC_STEPS 4
+#endif
+constexpr int kFp32SyncSteps = CAP_FP32_SYNC_STEPS;
 constexpr unsigned long long kSentinel = 0x7FF0DEAD5EA1F00DULL;   // signalling NaN
 // a slot is refilled at the start of the next group, so two slots at least;
 // the ring holds the planes between two updates of the consumed-plane count
@@ -264,6 +270,13 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   constexpr int NSLOT = Op::kSlots;
   constexpr int NP = Op::kPacers;        // pacing warps; pacer p checks the steps with (s - s0) % NP == p
   constexpr int NB = NC + 32 * NP;       // threads in named barrier 1
+  // The pacing warp takes part in the barrier of every Op::kSyncSteps-th
+  // step of a copy group (every step when 1); before it, it checks the edge
+  // planes of the steps up to the next such barrier and, at the group's
+  // last one, the next group's copy.  The compute warps take the other
+  // steps' barriers among themselves (named barrier 4).
+  constexpr int E = Op::kSyncSteps;
+  static_assert(E >= 1 && kG % E == 0 && (E == 1 || NP == 1), "pacing steps");
   static_assert(NC % 32 == 0, "block shape");
   constexpr int kPW = Op::kPW;           // edge planes examined per communication pass
   static_assert(32 % BC == 0 && (kPW * BC) % 32 == 0 && (kPW * BA) % 32 == 0, "edge staging shape");
@@ -345,9 +358,14 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
     unsigned long long knownW = 0, knownB = 0;
     int gi = 0, ds = 0;
     for (int s = s0; s <= s1 && !stop; ++s) {
+      if (ds % E != 0) {   // not part of this step's barrier
+        if (++ds == kG) { ds = 0; ++gi; }
+        continue;
+      }
       if (lane == 0 && !pend && (s - s0) % NP == pw) {
-        const unsigned long long needW = (unsigned long long)(unsigned)(min(s, s1W + 1) + 1);
-        const unsigned long long needB = (unsigned long long)(unsigned)(min(s, s1B + 1) + 1);
+        const int sl = min(s + E - 1, s1);   // the last step whose edge planes are checked now
+        const unsigned long long needW = (unsigned long long)(unsigned)(min(sl, s1W + 1) + 1);
+        const unsigned long long needB = (unsigned long long)(unsigned)(min(sl, s1B + 1) + 1);
         if (knownW < needW || knownB < needB) {   // the edge states of plane s-1 are staged
           long long it = 0;
           for (;;) {
@@ -358,9 +376,10 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
             if (++it > 64LL * w.spin_limit) { wave_fail(w, bail, 1); pend = 1; break; }
           }
         }
-        // last step of a group: the compute warps read the next group's
-        // inputs between this step's barrier and the next one
-        if (!pend && ds == kG - 1 && gi + 1 < ngroups && !landed(gi + 1)) pend = 1;
+        // the compute warps read the next group's inputs after the barrier
+        // of this group's last step: checked before the pacing warp's last
+        // barrier of the group
+        if (!pend && ds == kG - E && gi + 1 < ngroups && !landed(gi + 1)) pend = 1;
       }
       // a group's first step: the barrier also carries the stop decision;
       // the other steps take a plain barrier (a failed check lets the
@@ -503,8 +522,10 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
       if (act) pv = op.pre(in, prevS);
       if (ds == 0) {
         if (named_bar_red_or(1, NB, false)) { stop = true; break; }   // plane s-1 computed; edge states staged
-      } else {
+      } else if (ds % E == 0) {
         named_bar_sync(3, NB);
+      } else {
+        named_bar_sync(4, NC);
       }
       if (act) {
         const bool odd = (ds & 1) != 0;   // the plane's parity (group starts are even); previous plane in buffer !odd
@@ -565,6 +586,7 @@ struct SipFwdD {
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 3;
   static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = 1;
   static constexpr int kPW = 4;   // edge planes polled per communication pass
   __host__ __device__ static constexpr int nq(int m) { return m == 0 ? 1 : 4; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
@@ -594,6 +616,7 @@ struct SipBwdD {
   static constexpr bool kReduce = true;
   static constexpr int kSlots = 3;
   static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = 1;
   static constexpr int kPW = 4;   // edge planes polled per communication pass
   __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
@@ -622,6 +645,7 @@ struct SipBwdFiD {
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 3;
   static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = 1;
   static constexpr int kPW = 4;   // edge planes polled per communication pass
   __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
@@ -651,6 +675,7 @@ struct SipFactorD {
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 3;
   static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = 1;
   static constexpr int kPW = 4;   // edge planes polled per communication pass
   __host__ __device__ static constexpr int nq(int) { return 1; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
@@ -703,6 +728,7 @@ struct IcDiagD {
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 3;
   static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = 1;
   static constexpr int kPW = 4;
   __host__ __device__ static constexpr int nq(int) { return 1; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
@@ -730,6 +756,7 @@ struct IcFwdD {
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 3;
   static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = 1;
   static constexpr int kPW = 4;
   __host__ __device__ static constexpr int nq(int) { return 1; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
@@ -758,6 +785,7 @@ struct IcBwdD {
   static constexpr bool kReduce = true;
   static constexpr int kSlots = 3;
   static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = 1;
   static constexpr int kPW = 4;
   __host__ __device__ static constexpr int nq(int) { return 1; }
   __host__ __device__ static constexpr int esize(int) { return 8; }
@@ -792,7 +820,8 @@ struct SipFwdF {
   static constexpr int kMaps = 2;   // r, forward factors (bb, bw, bs, bp)
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 6;
-  static constexpr int kPacers = 2;
+  static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = kFp32SyncSteps;
   static constexpr int kPW = 8;
   __host__ __device__ static constexpr int nq(int m) { return m == 0 ? 1 : 4; }
   __host__ __device__ static constexpr int esize(int) { return 4; }
@@ -817,7 +846,8 @@ struct SipBwdF {
   static constexpr int kMaps = 2;   // z, backward factors (bn, be, bt)
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 6;
-  static constexpr int kPacers = 2;
+  static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = kFp32SyncSteps;
   static constexpr int kPW = 8;
   __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
   __host__ __device__ static constexpr int esize(int) { return 4; }
@@ -843,6 +873,7 @@ struct SipFactorF {
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 4;
   static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = kFp32SyncSteps;
   static constexpr int kPW = 8;
   __host__ __device__ static constexpr int nq(int) { return 1; }
   __host__ __device__ static constexpr int esize(int) { return 4; }
