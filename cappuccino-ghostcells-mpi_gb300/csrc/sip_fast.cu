@@ -25,7 +25,13 @@ namespace cap {
 
 namespace {
 
-constexpr int BA = 16, BC = 8;   // lines per wavefront block (a x c)
+#ifndef CAP_WAVE_BA
+#define CAP_WAVE_BA 16
+#endif
+#ifndef CAP_WAVE_BC
+#define CAP_WAVE_BC 8
+#endif
+constexpr int BA = CAP_WAVE_BA, BC = CAP_WAVE_BC;   // lines per wavefront block (a x c)
 
 enum DBuf { D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_SU, D_RES, D_FI, D_Z, D_ZZ, D_PK0, D_PK1, D_NBUF };
 
