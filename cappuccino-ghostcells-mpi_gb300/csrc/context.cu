@@ -325,6 +325,14 @@ int cappgpu_set_option(const char* key, int value) {
     ctx().spin_limit = value;
     return CAPPGPU_OK;
   }
+  if (strcmp(key, "sip_slabs") == 0 && value >= 1 && value <= 64) {
+    ctx().sip_slabs = value;
+    return CAPPGPU_OK;
+  }
+  if (strcmp(key, "sip_slab_axis") == 0 && (value == 0 || value == 1)) {
+    ctx().sip_slab_axis = value;
+    return CAPPGPU_OK;
+  }
   if (strcmp(key, "tight_correctors") == 0 && (value == 0 || value == 1)) {
     ctx().tight_correctors = value;
     return CAPPGPU_OK;

@@ -375,11 +375,29 @@ WaveCtl next_ctl() {
   w.mailB = F.mail + (size_t)F.nblk * BC * F.g.Nj * 3;
   w.spin_limit = ctx().spin_limit;
   w.skip = nullptr;
+  w.slabBA = w.slabBC = 0;
   return w;
 }
 
+// blocks per slab of the block-local SIP of the refinement form (option
+// sip_slabs along the axis sip_slab_axis: 0 = i, 1 = k; wavefront engine 0),
+// as {along a, along c}; {0, 0} when the recurrence spans the whole box.
+// The slabs must end on block boundaries from both ends of the box (forward
+// and mirrored backward blocks): the count is the largest n <= sip_slabs,
+// n >= 2, for which the extent along the axis is a multiple of n block
+// widths.
+int2 slab_blocks() {
+  const Ctx& c = ctx();
+  if (c.sip_slabs <= 1 || c.lane_wave != 0) return make_int2(0, 0);
+  const bool alongA = c.sip_slab_axis == 0;
+  const int ext = alongA ? F.g.Ni : F.g.Nk, width = alongA ? BA : BC, nb = alongA ? F.nBA : F.nBC;
+  for (int n = c.sip_slabs; n >= 2; --n)
+    if (ext % (width * n) == 0) return alongA ? make_int2(nb / n, 0) : make_int2(0, nb / n);
+  return make_int2(0, 0);
+}
+
 template <class Op, bool BWD>
-int run_wave(const Op& op, const int* skip = nullptr) {
+int run_wave(const Op& op, const int* skip = nullptr, int2 slab = make_int2(0, 0)) {
   Ctx& c = ctx();
   constexpr size_t smem = wave_smem_bytes<Op, BA, BC>();
   static bool attr_set = false;   // once per process (one device per context)
@@ -389,6 +407,8 @@ int run_wave(const Op& op, const int* skip = nullptr) {
   }
   WaveCtl w = next_ctl();
   w.skip = skip;
+  w.slabBA = slab.x;
+  w.slabBC = slab.y;
   launch_smem(k_wave<Op, BA, BC, BWD>, F.nblk, wave_threads<Op, BA, BC>(), smem, c.st, op, F.g, w);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
@@ -439,6 +459,7 @@ WaveCtl mwave_ctl(const int* skip) {
   w.mailB = G.mmail + (size_t)G.mnblk * kMBC * F.g.Nj;
   w.spin_limit = ctx().spin_limit;
   w.skip = skip;
+  w.slabBA = w.slabBC = 0;
   return w;
 }
 
@@ -478,7 +499,7 @@ int fp32_forward(const int* skip) {
   fwd.map[0] = G.map[E_R];
   fwd.map[1] = G.map_fq;
   fwd.z = G.e[E_Z];
-  return run_wave<SipFwdF, false>(fwd, skip);
+  return run_wave<SipFwdF, false>(fwd, skip, slab_blocks());
 }
 
 int fp32_backward(const int* skip) {
@@ -500,7 +521,7 @@ int fp32_backward(const int* skip) {
   bwd.map[0] = G.map[E_Z];
   bwd.map[1] = G.map_bq;
   bwd.z = G.e[E_Z];
-  return run_wave<SipBwdF, true>(bwd, skip);
+  return run_wave<SipBwdF, true>(bwd, skip, slab_blocks());
 }
 
 // ------------------------------------------------------ vector kernels (D)
@@ -1484,7 +1505,7 @@ int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     op.fq = G.fq;
     op.bq = G.bq;
     op.alfa = (float)P.alfa;
-    if ((rc = run_wave<SipFactorF, false>(op))) return rc;
+    if ((rc = run_wave<SipFactorF, false>(op, nullptr, slab_blocks()))) return rc;
   }
   const int ns = P.nsw[ifi - 1];
   double res1 = 0.0, rsm = 0.0;
@@ -1569,7 +1590,7 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
     op.fq = G.fq;
     op.bq = G.bq;
     op.alfa = (float)P.alfa;
-    if ((rc = run_wave<SipFactorF, false>(op))) return rc;
+    if ((rc = run_wave<SipFactorF, false>(op, nullptr, slab_blocks()))) return rc;
   }
   const size_t nf = sizeof(float) * (size_t)g.size();
   int total = 0;

@@ -57,6 +57,9 @@ struct WaveCtl {
   double* mailB;                  // per block: BA x Nj states of its last c-row
   long long spin_limit;
   const int* skip;                // when non-null and *skip != 0 at launch, every block exits at once
+  int slabBA, slabBC;             // > 0: the recurrence restarts every slabBA blocks along a / slabBC blocks
+                                  // along c (block-local SIP per slab); a slab's first line / row sees zero
+                                  // states before it
 };
 
 constexpr int kG = 4;        // hyperplanes per TMA copy
@@ -180,7 +183,8 @@ struct EdgeProbe {
 
 template <class Op, int E, bool BWD, class LineFn>
 __device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, Op::kPW * E / 32>& P, const Op& op, const DG& g,
-                                           int lane, int loaded, int hi, const double* mail, LineFn line) {
+                                           int lane, int loaded, int hi, const double* mail, LineFn line,
+                                           bool zero_ghost = false) {
   using St = typename Op::St;
   constexpr int NS = state_words<St>();
 #pragma unroll
@@ -200,7 +204,7 @@ __device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, Op::kPW * 
         const int a = BWD ? g.Ni - 1 - pa : pa;
         const int b = BWD ? g.Nj - 1 - bv : bv;
         const int c = BWD ? g.Nk - 1 - pc : pc;
-        const St v = op.ghost(g.nat(a, b, c));
+        const St v = zero_ghost ? St{} : op.ghost(g.nat(a, b, c));
 #pragma unroll
         for (int k = 0; k < NS; ++k) P.u[r][k] = 0;
         memcpy(P.u[r], &v, sizeof(St));
@@ -418,8 +422,10 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
     // --------------------------------------------- communication warp(s)
     const int lane = (tid - NC) & 31;
     const int cw = (tid - NC) >> 5;   // with two warps: 0 stages the W edge, 1 the B edge
-    double* srcW = ba > 0 ? w.mailW + (size_t)(blk_id - 1) * BC * g.Nj * NS : nullptr;
-    double* srcB = bc > 0 ? w.mailB + (size_t)(blk_id - w.nBA) * BA * g.Nj * NS : nullptr;
+    const bool slabW = ba > 0 && w.slabBA > 0 && ba % w.slabBA == 0;   // first block column of an i-slab
+    double* srcW = ba > 0 && !slabW ? w.mailW + (size_t)(blk_id - 1) * BC * g.Nj * NS : nullptr;
+    const bool slab0 = bc > 0 && w.slabBC > 0 && bc % w.slabBC == 0;   // first block row of a k-slab
+    double* srcB = bc > 0 && !slab0 ? w.mailB + (size_t)(blk_id - w.nBA) * BA * g.Nj * NS : nullptr;
     auto lineW = [&](int e, int& av, int& cv, int& pa, int& pc) {
       av = ba * BA; cv = bc * BC + e; pa = av - 1; pc = cv;
     };
@@ -437,8 +443,8 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
       const int cur = __shfl_sync(0xffffffffu, *(volatile int*)&sm.done, 0);
       const int limit = max(cur, s0) + kRing - 2;   // ring capacity
       const int hiW = min(s1W, limit), hiB = min(s1B, limit);
-      probe_edge<Op, BC, BWD>(PW, op, g, lane, loadedW, hiW, srcW, lineW);
-      probe_edge<Op, BA, BWD>(PB, op, g, lane, loadedB, hiB, srcB, lineB);
+      probe_edge<Op, BC, BWD>(PW, op, g, lane, loadedW, hiW, srcW, lineW, slabW);
+      probe_edge<Op, BA, BWD>(PB, op, g, lane, loadedB, hiB, srcB, lineB, slab0);
       const int nW = commit_edge<St, BC, kPW>(PW, g, lane, loadedW, srcW, sm.ringW, lineW);
       const int nB = commit_edge<St, BA, kPW>(PB, g, lane, loadedB, srcB, sm.ringB, lineB);
       if (nW + nB > 0) {
@@ -484,8 +490,10 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
     const int alo = g.Ni - (ba + 1) * BA;
     in.init((alo - (alo & ~1)) + BA - 1 - al, (alo - (alo & ~3)) + BA - 1 - al, BC - 1 - cl);
   }
-  const bool edgeE = al == BA - 1 && ba + 1 < w.nBA;   // feeds the next block along a
-  const bool edgeT = cl == BC - 1 && bc + 1 < w.nBC;   // feeds the next block along c
+  const bool edgeE = al == BA - 1 && ba + 1 < w.nBA &&   // feeds the next block along a
+                     !(w.slabBA > 0 && (ba + 1) % w.slabBA == 0);   // (not across an i-slab boundary)
+  const bool edgeT = cl == BC - 1 && bc + 1 < w.nBC &&   // feeds the next block along c
+                     !(w.slabBC > 0 && (bc + 1) % w.slabBC == 0);   // (not across a k-slab boundary)
   double* mW = w.mailW + ((size_t)blk_id * BC + cl) * g.Nj * NS;
   double* mB = w.mailB + ((size_t)blk_id * BA + al) * g.Nj * NS;
   // W and B come from the previous plane's buffer inside the block and from

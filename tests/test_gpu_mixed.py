@@ -170,6 +170,46 @@ def test_mixed_channel128_twenty_steps_per_field_errors(gpu_lib):
         assert err_fine[k] <= 1e-5, (k, err_fine[k])
 
 
+@pytest.mark.parametrize("axis,slabs", [(0, 2), (1, 2), (1, 4)])
+@pytest.mark.parametrize("solver", ["pcgsip", "sipsol"])
+def test_block_local_sip_per_slab(gpu_lib, oracle_mod, axis, slabs, solver):
+    """The FP32 SIP of the refinement form restarted at every i-slab (axis 0)
+    or k-slab (axis 1) (options sip_slabs, sip_slab_axis; interior
+    32 x 33 x 32: 2 block columns of 16 lines, 4 block rows of 8): both
+    solvers still meet the reference's exit test on the FP64 residual, within
+    the tolerance's reach of the FP64 solution, with the SIP over the whole
+    box and with the slabs."""
+    dims, sor = (36, 37, 36), 1e-6
+    st = _state(oracle_mod, dims, 11, sor)
+    st.set_field("res", np.zeros_like(st.field("res")))
+    push(gpu_lib, st)
+    gpu_lib.precision(0)
+    r64 = getattr(gpu_lib, solver)("p", IP)
+    p64 = gpu_lib.get_field("p")
+    out, sol = {}, {}
+    for n in (1, slabs):
+        push(gpu_lib, st)
+        gpu_lib.set_option("sip_slabs", n)
+        gpu_lib.set_option("sip_slab_axis", axis)
+        gpu_lib.precision(1)
+        try:
+            out[n] = getattr(gpu_lib, solver)("p", IP)
+        finally:
+            gpu_lib.precision(0)
+            gpu_lib.set_option("sip_slabs", 8)
+            gpu_lib.set_option("sip_slab_axis", 0)
+        sol[n] = gpu_lib.get_field("p")
+        r = out[n]
+        assert r.status == 0 and r64.status == 0
+        assert r.res0 == pytest.approx(r64.res0, rel=1e-12)
+        assert r.resl / r.res0 < sor
+        assert np.linalg.norm(sol[n] - p64) <= 1e3 * sor * np.linalg.norm(p64)
+    # the slabs change the preconditioner: a different iteration path
+    assert out[slabs].iters != out[1].iters or not np.array_equal(sol[slabs], sol[1])
+    print(f"{solver}: whole box {out[1].iters} it, {slabs} {'ik'[axis]}-slabs {out[slabs].iters} it, "
+          f"FP64 {r64.iters} it")
+
+
 @pytest.mark.parametrize("dims,sor", [((14, 13, 12), 1e-6), ((40, 37, 35), 1e-4)])
 def test_mixed_sipsol_meets_fp64_exit_test(gpu_lib, oracle_mod, dims, sor):
     """sipsol in precision mode 1: FP64 residual and exit test, FP32 SIP
@@ -212,12 +252,14 @@ def test_fp32_substitution_engines_agree_bit_for_bit(gpu_lib, oracle_mod, solver
     for lw in (0, 1, 2):
         push(gpu_lib, st)
         gpu_lib.set_option("lane_wave", lw)
+        gpu_lib.set_option("sip_slabs", 1)   # the other engines run the SIP over the whole box
         gpu_lib.precision(1)
         try:
             r = getattr(gpu_lib, solver)("p", IP)
         finally:
             gpu_lib.precision(0)
             gpu_lib.set_option("lane_wave", 0)
+            gpu_lib.set_option("sip_slabs", 8)
         out[lw] = (r, gpu_lib.get_field("p"), gpu_lib.get_field("res"))
     r0, p0, q0 = out[0]
     assert r0.status == 0
