@@ -580,13 +580,18 @@ def run_learned_config(args):
     PCG iterations and the p'-solve time to the same tolerance with the
     guess (precision 2) and without it (precision 1) from the same state,
     and the fallback rate (guesses discarded because they did not lower
-    the FP64 residual).  Prints one JSON line (no bench line)."""
+    the FP64 residual).  --learn-loss supervised / energy trains on the
+    recorded converged corrections instead (all: the three losses from the
+    same start and pairs).  Prints one JSON line (no bench line)."""
     import cappgpu
     steps_rec, per_solve, block, epochs, pairs = 200, 5, 64, 20, 2000
+    kinds = {"residual": 0, "supervised": 1, "energy": 2}
+    chosen = list(kinds) if args.learn_loss == "all" else [args.learn_loss]
     out = {"learned_config": True, "seed": 20261203}
     lib = cappgpu.Library()
     lib.load_case(make_case(128))
     lib.learn_reset(pairs, seed=20261203)
+    p0 = lib.learn_params()
     lib.learn_windows(block, per_solve)
     lib.precision(1)
     lib.learn_collect(True)
@@ -594,24 +599,30 @@ def run_learned_config(args):
     lib.piso_steps(steps_rec)
     lib.learn_collect(False)
     t1 = time.perf_counter()
-    loss = lib.learn_train(epochs, block=block, lr=1e-3)
-    t2 = time.perf_counter()
     out["train"] = {"grid": [128, 128, 128], "steps": steps_rec, "pairs": lib.learn_stats()["samples"],
-                    "window": block, "epochs": epochs, "lr": 1e-3, "loss_last_epoch": loss,
-                    "collect_s": t1 - t0, "train_s": t2 - t1}
-    params = lib.learn_params()
+                    "window": block, "epochs": epochs, "lr": 1e-3, "collect_s": t1 - t0}
+    params = {}
+    for name in chosen:
+        lib.learn_params(p0)
+        lib.set_option("learn_loss", kinds[name])
+        t2 = time.perf_counter()
+        loss = lib.learn_train(epochs, block=block, lr=1e-3)
+        out["train"][name] = {"loss_last_epoch": loss, "train_s": time.perf_counter() - t2}
+        params[name] = lib.learn_params()
+    lib.set_option("learn_loss", 0)
     lib.finalize()
 
     n = args.learned_size
     lib = cappgpu.Library()
     lib.load_case(make_case(n))
     lib.learn_reset(0, seed=20261203)
-    lib.learn_params(params)
     lib.precision(0)
     lib.piso_steps(args.warmup)
     snap = snapshot(lib)
     forms = {}
-    for mode in (1, 2):
+    for mode, name in [(1, None)] + [(2, q) for q in chosen]:
+        if name:
+            lib.learn_params(params[name])
         restore(lib, snap)
         lib.precision(mode)
         lib.piso_steps(1)   # warm-up of the buffers of the form
@@ -627,12 +638,12 @@ def run_learned_config(args):
                              "p_rel_residual": st.p_report.resl / st.p_report.res0 if st.p_report.res0 else None})
         s1 = lib.learn_stats()
         kept, dropped = s1["guesses"] - s0["guesses"], s1["fallbacks"] - s0["fallbacks"]
-        forms["fp32_learned" if mode == 2 else "fp32_refined"] = {
+        forms[f"fp32_learned_{name}" if name else "fp32_refined"] = {
             "ms_per_step": sum(q["ms"] for q in per_step) / len(per_step),
             "last_p_solve_ms": sum(q["p_solve_ms"] for q in per_step) / len(per_step),
             "last_p_iters": [q["p_iters"] for q in per_step],
-            "guesses_kept": kept if mode == 2 else None, "guesses_discarded": dropped if mode == 2 else None,
-            "fallback_rate": (dropped / (kept + dropped)) if mode == 2 and kept + dropped else None,
+            "guesses_kept": kept if name else None, "guesses_discarded": dropped if name else None,
+            "fallback_rate": (dropped / (kept + dropped)) if name and kept + dropped else None,
             "per_step": per_step}
     lib.precision(0)
     lib.finalize()
@@ -653,6 +664,8 @@ def main():
     ap.add_argument("--learned-config", action="store_true",
                     help="train the learned guess as its configuration specifies and compare it at --learned-size")
     ap.add_argument("--learned-size", type=int, default=192)
+    ap.add_argument("--learn-loss", default="residual", choices=["residual", "supervised", "energy", "all"],
+                    help="training loss of --learned-config (residual: the configuration's)")
     args = ap.parse_args()
     if args.learned_config:
         run_learned_config(args)

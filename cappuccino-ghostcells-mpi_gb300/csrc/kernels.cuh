@@ -38,6 +38,7 @@ int learned_solve_start(int fif, double res0);
 int learned_solve_end(int fif);
 int learned_profile_unit(int which, double* flops);
 int learned_set_conv(int impl);
+int learned_set_loss(int kind);
 // natural-layout residual r = su - A fi over the interior of an arbitrary
 // field array, written to res, with its L1 norm (solvers.cu)
 int resid_into(const double* fi, double* res, double* l1);

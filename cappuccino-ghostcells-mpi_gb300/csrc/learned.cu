@@ -66,6 +66,7 @@ constexpr int kOffLastW = offB(kNL - 1) + kCO[kNL - 1];
 constexpr int kOffLastB = kOffLastW + kC1;
 constexpr int kParams = kOffLastB + 1;
 constexpr int kChunk = 8192;   // voxels per weight-gradient partial
+constexpr int kPlanes = 9;     // planes of a recorded pair: r^, A^ (7), the converged correction t^
 
 __constant__ int cCI[kNL] = {16, 16, 16, 32, 32, 64, 96, 32, 48, 16};
 __constant__ int cCO[kNL] = {16, 16, 32, 32, 64, 64, 32, 32, 16, 16};
@@ -79,7 +80,7 @@ struct Acts {
   long long V1 = 0;
   bf16 *a0, *a1, *cat1, *p1, *a3, *cat2, *p2, *a5, *b3, *a7, *x2, *a9, *x1;
   bf16 *gx1, *ga9, *gcat1, *gx2, *ga7, *gcat2, *gb3, *ga5, *gp2, *ga3, *gp1, *ga1;
-  float *out, *gout, *rhs, *coef, *res;
+  float *out, *gout, *rhs, *coef, *res, *tgt;
   void* base = nullptr;
 };
 
@@ -94,14 +95,26 @@ struct Net {
   size_t part_n = 0;
   double* dsum = nullptr;        // device scalars: loss
   int* err = nullptr;            // set by a tensor-core convolution whose wait ran out
-  // recorded pairs: [sample][8][sV]: r^, then A^ as xp, xm, yp, ym, zp, zm, diag;
-  // a sample is the whole interior, or (window mode, wper > 0) a random
-  // sD^3 window of it, wper windows per recorded solve
+  // recorded pairs: [sample][kPlanes][sV]: r^, then A^ as xp, xm, yp, ym, zp,
+  // zm, diag, then the solve's converged correction t^ on the same scale
+  // (A^ t^ = r^ to the solve's tolerance); a sample is the whole interior,
+  // or (window mode, wper > 0) a random sD^3 window of it, wper windows per
+  // recorded solve
   int max_samples = 0, nsamples = 0, next = 0;
   int sD = 0, sH = 0, sW = 0;
   int wper = 0;
   unsigned long long wrng = 0;   // window origins (xorshift64*)
   float* store = nullptr;
+  // the solve being recorded: fi at its start, the start's scale sums
+  // (|r0|^2, sum ap) and the samples whose t^ its end fills (slot, z0, y0, x0)
+  double* fi0 = nullptr;
+  long long fi0_n = 0;
+  double* tsum = nullptr;
+  std::vector<int4> pend;
+  // training loss: 0 residual norm |A^ d - r^|^2/|r^|^2 (the learned-guess
+  // configuration's), 1 supervised |d - t^|^2/|t^|^2, 2 energy norm
+  // (d - t^)'A^(d - t^) / t^'A^t^
+  int loss = 0;
   // statistics of the guesses
   int guesses = 0, fallbacks = 0;
   double last_ratio = 0.0, last_alpha = 0.0, last_beta = 0.0;
@@ -121,6 +134,7 @@ void net_free() {
   acts_free();
   cudaFree(N.part); cudaFree(N.dsum); cudaFree(N.err);
   cudaFree(N.store);
+  cudaFree(N.fi0); cudaFree(N.tsum);
   N = Net();
 }
 
@@ -486,6 +500,79 @@ __global__ void k_resloss_grad(const float* __restrict__ res, const float* __res
   }
 }
 
+// supervised loss: partials of |out - tgt|^2 and |tgt|^2
+__global__ void k_suploss(const float* __restrict__ out, const float* __restrict__ tgt, int V, double* part) {
+  double a[2] = {0.0, 0.0};
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const float e = out[v] - tgt[v];
+    a[0] += (double)e * e;
+    a[1] += (double)tgt[v] * tgt[v];
+  }
+  block_reduce_store<2>(a, part);
+}
+
+// gout = 2 (out - tgt) / |tgt|^2; loss[0] = ratio
+__global__ void k_suploss_grad(const float* __restrict__ out, const float* __restrict__ tgt,
+                               const double* __restrict__ sums, float* __restrict__ gout, double* loss, int V) {
+  const float sc = sums[1] > 0.0 ? (float)(2.0 / sums[1]) : 0.f;
+  if (blockIdx.x == 0 && threadIdx.x == 0) loss[0] = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    gout[v] = sc * (out[v] - tgt[v]);
+}
+
+// (A^ q)_v of the window operator for q = a - b (b may be null)
+__device__ __forceinline__ float apply_w(const float* __restrict__ cf, const float* __restrict__ a,
+                                         const float* __restrict__ b, int v, const Vox& P, int D, int H, int W, int V) {
+  auto q = [&](int u) { return b ? a[u] - b[u] : a[u]; };
+  float s = cf[6 * (long long)V + v] * q(v);
+  if (P.x + 1 < W) s -= cf[v] * q(v + 1);
+  if (P.x > 0) s -= cf[(long long)V + v] * q(v - 1);
+  if (P.y + 1 < H) s -= cf[2 * (long long)V + v] * q(v + W);
+  if (P.y > 0) s -= cf[3 * (long long)V + v] * q(v - W);
+  if (P.z + 1 < D) s -= cf[4 * (long long)V + v] * q(v + H * W);
+  if (P.z > 0) s -= cf[5 * (long long)V + v] * q(v - H * W);
+  return s;
+}
+
+// energy-norm loss: res = A^ e with e = out - tgt; partials of e'A^e and
+// tgt'A^tgt
+__global__ void k_enloss(const float* __restrict__ out, const float* __restrict__ tgt, const float* __restrict__ cf,
+                         float* __restrict__ res, int D, int H, int W, double* part) {
+  const int V = D * H * W;
+  double a[2] = {0.0, 0.0};
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const Vox P(v, H, W);
+    const float r = apply_w(cf, out, tgt, v, P, D, H, W, V);
+    res[v] = r;
+    a[0] += (double)(out[v] - tgt[v]) * r;
+    a[1] += (double)tgt[v] * apply_w(cf, tgt, nullptr, v, P, D, H, W, V);
+  }
+  block_reduce_store<2>(a, part);
+}
+
+// gout = (A^ e + A^' e) / tgt'A^tgt (the gradient of e'A^e for an A^ that
+// need not be exactly symmetric in FP32); loss[0] = ratio
+__global__ void k_enloss_grad(const float* __restrict__ out, const float* __restrict__ tgt,
+                              const float* __restrict__ res, const float* __restrict__ cf,
+                              const double* __restrict__ sums, float* __restrict__ gout, double* loss, int D, int H,
+                              int W) {
+  const int V = D * H * W;
+  const float sc = sums[1] > 0.0 ? (float)(1.0 / sums[1]) : 0.f;
+  if (blockIdx.x == 0 && threadIdx.x == 0) loss[0] = sums[1] > 0.0 ? sums[0] / sums[1] : 0.0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const Vox P(v, H, W);
+    auto e = [&](int u) { return out[u] - tgt[u]; };
+    float s = cf[6 * (long long)V + v] * e(v);
+    if (P.x + 1 < W) s -= cf[(long long)V + v + 1] * e(v + 1);
+    if (P.x > 0) s -= cf[v - 1] * e(v - 1);
+    if (P.y + 1 < H) s -= cf[3 * (long long)V + v + W] * e(v + W);
+    if (P.y > 0) s -= cf[2 * (long long)V + v - W] * e(v - W);
+    if (P.z + 1 < D) s -= cf[5 * (long long)V + v + H * W] * e(v + H * W);
+    if (P.z > 0) s -= cf[4 * (long long)V + v - H * W] * e(v - H * W);
+    gout[v] = sc * (res[v] + s);
+  }
+}
+
 // Adam (lr, 0.9, 0.999, 1e-8) on the FP32 parameters
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ gp, float* __restrict__ m, float* __restrict__ v,
                        int n, float lr, float c1, float c2) {
@@ -513,9 +600,10 @@ __global__ void k_cast_w(const float* __restrict__ p, bf16* __restrict__ wb, bf1
   wt[cWoff[l] + (ci * 27 + (26 - tap)) * CO + co] = w;
 }
 
-// training window from a recorded pair: input (channel 0 = r^), r^, A^
+// training window from a recorded pair: input (channel 0 = r^), r^, A^, t^
 __global__ void k_window(const float* __restrict__ smp, int sD, int sH, int sW, int z0, int y0, int x0, int B,
-                         bf16* __restrict__ in, float* __restrict__ rhs, float* __restrict__ cf) {
+                         bf16* __restrict__ in, float* __restrict__ rhs, float* __restrict__ cf,
+                         float* __restrict__ tgt) {
   const int V = B * B * B;
   const long long sV = (long long)sD * sH * sW;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
@@ -528,6 +616,7 @@ __global__ void k_window(const float* __restrict__ smp, int sD, int sH, int sW, 
     rhs[v] = r;
 #pragma unroll
     for (int q = 0; q < 7; ++q) cf[(long long)q * V + v] = smp[(1 + q) * sV + s];
+    tgt[v] = smp[8 * sV + s];
   }
 }
 
@@ -572,6 +661,23 @@ __global__ void k_record(Dims d, const double* __restrict__ r, const double* __r
     smp[5LL * V + v] = (float)(at[n] * ainv);
     smp[6LL * V + v] = (float)(ab[n] * ainv);
     smp[7LL * V + v] = (float)(ap[n] * ainv);
+    smp[8LL * V + v] = 0.f;   // t^, filled at the end of the solve
+  }
+}
+
+// t^ of a recorded window at the end of its solve: (fi - fi0) scaled as the
+// pair, t^ = (fi - fi0) mean(ap) / rms(r0), so that A^ t^ = r^ when the solve
+// has converged (sums = the start's |r0|^2 and sum of ap)
+__global__ void k_record_target(Dims d, const double* __restrict__ fi, const double* __restrict__ fi0,
+                                const double* __restrict__ sums, int Ni, int Nj, int Nk, int z0, int y0, int x0,
+                                int wz, int wy, int wx, float* __restrict__ tgt) {
+  const long long Vi = (long long)Ni * Nj * Nk;
+  const int V = wz * wy * wx;
+  const double sc = sums[0] > 0.0 ? (sums[1] / (double)Vi) / sqrt(sums[0] / Vi) : 0.0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const int x = x0 + v % wx, y = y0 + (v / wx) % wy, z = z0 + v / (wx * wy);
+    const int n = nat_of(d, x, y, z);
+    tgt[v] = (float)((fi[n] - fi0[n]) * sc);
   }
 }
 
@@ -641,6 +747,7 @@ int ensure_acts(long long V1) {
       {(void**)&A.gp2, V3 * 32 * b},   {(void**)&A.ga3, V2 * 32 * b},  {(void**)&A.gp1, V2 * 16 * b},
       {(void**)&A.ga1, V1 * 16 * b},   {(void**)&A.out, V1 * 4},       {(void**)&A.gout, V1 * 4},
       {(void**)&A.rhs, V1 * 4},        {(void**)&A.coef, 7 * V1 * 4},  {(void**)&A.res, V1 * 4},
+      {(void**)&A.tgt, V1 * 4},
   };
   long long total = 0;
   for (auto& it : items) total += (it.bytes + 255) & ~255LL;
@@ -901,21 +1008,33 @@ int forward(int D, int H, int W) {
   return CAPPGPU_OK;
 }
 
-// residual-norm loss of A.out against A.rhs / A.coef (loss in N.dsum[0]),
-// then the backward pass into N.gp
+// the training loss of A.out (N.loss: residual norm against A.rhs / A.coef,
+// supervised or energy norm against A.tgt; loss in N.dsum[0]), then the
+// backward pass into N.gp
 int backward(int D, int H, int W) {
   Ctx& c = ctx();
   Acts& A = N.A;
   const int V = D * H * W;
   const int D2 = D / 2, H2 = H / 2, W2 = W / 2, D3 = D / 4, H3 = H / 4, W3 = W / 4;
   const long long V2 = V / 8, V3 = V / 64;
-  launch(k_resloss, kRedBlocks, kThreads, c.st, (const float*)A.out, (const float*)A.rhs, (const float*)A.coef, A.res, D,
-         H, W, c.partials);
+  const float *out = A.out, *tgt = A.tgt, *cf = A.coef;
+  if (N.loss == 1)
+    launch(k_suploss, kRedBlocks, kThreads, c.st, out, tgt, V, c.partials);
+  else if (N.loss == 2)
+    launch(k_enloss, kRedBlocks, kThreads, c.st, out, tgt, cf, A.res, D, H, W, c.partials);
+  else
+    launch(k_resloss, kRedBlocks, kThreads, c.st, out, (const float*)A.rhs, cf, A.res, D, H, W, c.partials);
   CAP_CHECK_LAUNCH();
   int rc = finish_reduce(2);
   if (rc) return rc;
-  launch(k_resloss_grad, grid_for(V), kThreads, c.st, (const float*)A.res, (const float*)A.coef,
-         (const double*)c.redout, A.gout, N.dsum, D, H, W);
+  const double* sums = c.redout;
+  if (N.loss == 1)
+    launch(k_suploss_grad, grid_for(V), kThreads, c.st, out, tgt, sums, A.gout, N.dsum, V);
+  else if (N.loss == 2)
+    launch(k_enloss_grad, grid_for(V), kThreads, c.st, out, tgt, (const float*)A.res, cf, sums, A.gout, N.dsum, D, H,
+           W);
+  else
+    launch(k_resloss_grad, grid_for(V), kThreads, c.st, (const float*)A.res, cf, sums, A.gout, N.dsum, D, H, W);
   const int lb = 512;
   launch(k_last_bwd, lb, 256, c.st, (const bf16*)A.x1, (const float*)A.gout, (const float*)N.p, A.gx1, V, N.part);
   launch(k_sum_cols, 1, 32, c.st, (const float*)N.part, lb, kC1 + 1, N.gp + kOffLastW);
@@ -1021,7 +1140,7 @@ int learned_profile_unit(int which, double* flops) {
   const int V = B * B * B;
   if ((rc = ensure_acts(V))) return rc;
   launch(k_window, grid_for(V), kThreads, c.st, (const float*)N.store, N.sD, N.sH, N.sW, 0, 0, 0, B, N.A.a0, N.A.rhs,
-         N.A.coef);
+         N.A.coef, N.A.tgt);
   CAP_CHECK_LAUNCH();
   *flops = (fwd_flops_per_voxel() + bwd_flops_per_voxel()) * (double)V;
   if ((rc = forward(B, B, B))) return rc;
@@ -1032,6 +1151,7 @@ int learned_profile_unit(int which, double* flops) {
 // start of a solve: r0 (module res) and res0 are known.
 int learned_solve_start(int fif, double res0) {
   if (!N.ready) return CAPPGPU_OK;
+  N.pend.clear();
   Ctx& c = ctx();
   const Dims& d = c.d;
   const int Ni = d.nimm - 2, Nj = d.njmm - 2, Nk = d.nkmm - 2;
@@ -1047,6 +1167,20 @@ int learned_solve_start(int fif, double res0) {
   int rc = finish_reduce(2);
   if (rc) return rc;
   if (rec) {
+    // fi and the scale sums at the start: the end of the solve forms t^ from them
+    if (N.fi0_n < d.nijk) {
+      cudaFree(N.fi0);
+      N.fi0 = nullptr;
+      N.fi0_n = 0;
+      if (cudaMalloc(&N.fi0, sizeof(double) * d.nijk) != cudaSuccess) {
+        set_error("learned guess: out of device memory for the recorded solve's start");
+        return CAPPGPU_E_NOMEM;
+      }
+      N.fi0_n = d.nijk;
+    }
+    if (!N.tsum) CAP_CUDA(cudaMalloc(&N.tsum, sizeof(double) * 2));
+    CAP_CUDA(cudaMemcpyAsync(N.fi0, c.f[fif], sizeof(double) * d.nijk, cudaMemcpyDeviceToDevice, c.st));
+    CAP_CUDA(cudaMemcpyAsync(N.tsum, c.redout, sizeof(double) * 2, cudaMemcpyDeviceToDevice, c.st));
     const long long sV = (long long)N.sD * N.sH * N.sW;
     auto rnd = [&](unsigned m) {   // xorshift64*
       unsigned long long& q = N.wrng;
@@ -1060,12 +1194,13 @@ int learned_solve_start(int fif, double res0) {
         y0 = (int)rnd((unsigned)(Ni - N.sH + 1));
         x0 = (int)rnd((unsigned)(Nj - N.sW + 1));
       }
-      float* smp = N.store + (size_t)N.next * 8 * sV;
+      float* smp = N.store + (size_t)N.next * kPlanes * sV;
       launch(k_record, grid_for(sV), kThreads, c.st, d, (const double*)c.f[CAP_RES], (const double*)c.f[CAP_AE],
              (const double*)c.f[CAP_AW], (const double*)c.f[CAP_AN], (const double*)c.f[CAP_AS],
              (const double*)c.f[CAP_AT], (const double*)c.f[CAP_AB], (const double*)c.f[CAP_AP],
              (const double*)c.redout, Ni, Nj, Nk, z0, y0, x0, N.sD, N.sH, N.sW, smp);
       CAP_CHECK_LAUNCH();
+      N.pend.push_back(make_int4(N.next, z0, y0, x0));
       N.next = (N.next + 1) % N.max_samples;
       if (N.nsamples < N.max_samples) ++N.nsamples;
     }
@@ -1136,9 +1271,29 @@ int learned_solve_start(int fif, double res0) {
   return CAPPGPU_OK;
 }
 
-// At the end of a solve: nothing to record (the residual-norm loss needs
-// only the solve's initial residual and operator).
-int learned_solve_end(int) { return CAPPGPU_OK; }
+// At the end of a solve: the converged correction t^ of the windows its
+// start recorded.
+int learned_solve_end(int fif) {
+  if (N.pend.empty()) return CAPPGPU_OK;
+  Ctx& c = ctx();
+  const Dims& d = c.d;
+  const int Ni = d.nimm - 2, Nj = d.njmm - 2, Nk = d.nkmm - 2;
+  const long long sV = (long long)N.sD * N.sH * N.sW;
+  for (const int4& q : N.pend) {
+    launch(k_record_target, grid_for(sV), kThreads, c.st, d, (const double*)c.f[fif], (const double*)N.fi0,
+           (const double*)N.tsum, Ni, Nj, Nk, q.y, q.z, q.w, N.sD, N.sH, N.sW,
+           N.store + ((size_t)q.x * kPlanes + 8) * sV);
+    CAP_CHECK_LAUNCH();
+  }
+  N.pend.clear();
+  return CAPPGPU_OK;
+}
+
+int learned_set_loss(int kind) {
+  if (kind < 0 || kind > 2) return CAPPGPU_E_ARG;
+  N.loss = kind;
+  return CAPPGPU_OK;
+}
 
 }  // namespace cap
 
@@ -1166,7 +1321,7 @@ int cappgpu_learn_reset(int max_samples, unsigned long long seed) {
   CAP_CUDA(cudaMemset(N.err, 0, sizeof(int)));
   CAP_CUDA(cudaMemset(N.gp, 0, sizeof(float) * kParams));
   CAP_CUDA(cudaMemset(N.dsum, 0, sizeof(double) * 4));
-  if (max_samples > 0 && cudaMalloc(&N.store, sizeof(float) * 8 * (size_t)max_samples * V) != cudaSuccess) {
+  if (max_samples > 0 && cudaMalloc(&N.store, sizeof(float) * kPlanes * (size_t)max_samples * V) != cudaSuccess) {
     net_free();
     set_error("learn_reset: out of device memory for %d samples", max_samples);
     return CAPPGPU_E_NOMEM;
@@ -1193,7 +1348,7 @@ int cappgpu_learn_windows(int block, int per_solve) {
   cudaFree(N.store);
   N.store = nullptr;
   const long long V = (long long)block * block * block;
-  if (N.max_samples > 0 && cudaMalloc(&N.store, sizeof(float) * 8 * (size_t)N.max_samples * V) != cudaSuccess) {
+  if (N.max_samples > 0 && cudaMalloc(&N.store, sizeof(float) * kPlanes * (size_t)N.max_samples * V) != cudaSuccess) {
     N.max_samples = 0;
     set_error("learn_windows: out of device memory for the windows");
     return CAPPGPU_E_NOMEM;
@@ -1235,8 +1390,8 @@ int cappgpu_learn_train(int epochs, int block, double lr, double* loss) {
       const int sidx = (int)rnd((unsigned)N.nsamples);
       const int z0 = (int)rnd((unsigned)(N.sD - B + 1)), y0 = (int)rnd((unsigned)(N.sH - B + 1)),
                 x0 = (int)rnd((unsigned)(N.sW - B + 1));
-      launch(k_window, grid_for(V), kThreads, c.st, (const float*)(N.store + (size_t)sidx * 8 * sV), N.sD, N.sH, N.sW,
-             z0, y0, x0, B, N.A.a0, N.A.rhs, N.A.coef);
+      launch(k_window, grid_for(V), kThreads, c.st, (const float*)(N.store + (size_t)sidx * kPlanes * sV), N.sD, N.sH,
+             N.sW, z0, y0, x0, B, N.A.a0, N.A.rhs, N.A.coef, N.A.tgt);
       CAP_CHECK_LAUNCH();
       if ((rc = forward(B, B, B))) return rc;
       if ((rc = backward(B, B, B))) return rc;
@@ -1262,6 +1417,10 @@ int cappgpu_learn_params(float* host, int n, int direction) {
     CAP_CUDA(cudaMemcpy(host, N.p, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
   } else {
     CAP_CUDA(cudaMemcpy(N.p, host, sizeof(float) * kParams, cudaMemcpyHostToDevice));
+    // new parameters: Adam starts afresh
+    CAP_CUDA(cudaMemsetAsync(N.m, 0, sizeof(float) * kParams, ctx().st));
+    CAP_CUDA(cudaMemsetAsync(N.v, 0, sizeof(float) * kParams, ctx().st));
+    N.adam_t = 0;
     int rc = cast_weights();
     if (rc) return rc;
     N.trained = true;
@@ -1286,12 +1445,16 @@ int cappgpu_learn_fit(double* alpha, double* beta) {
   return CAPPGPU_OK;
 }
 
-int cappgpu_learn_check(const float* rhs, const float* coef, int D, int H, int W, float* output, float* grad,
-                        double* loss) {
+int cappgpu_learn_check_loss(int kind, const float* rhs, const float* coef, const float* target, int D, int H, int W,
+                             float* output, float* grad, double* loss) {
   CAP_REQUIRE_INIT();
   if (!N.ready) { set_error("learn_check: call cappgpu_learn_reset first"); return CAPPGPU_E_NOINIT; }
   if (!rhs || !coef || D < 4 || H < 4 || W < 4 || ((D | H | W) & 3)) {
     set_error("learn_check: extents must be multiples of 4");
+    return CAPPGPU_E_ARG;
+  }
+  if (kind < 0 || kind > 2 || (kind > 0 && !target)) {
+    set_error("learn_check: loss kind %d (0 residual, 1 supervised, 2 energy; 1-2 need the target)", kind);
     return CAPPGPU_E_ARG;
   }
   Ctx& c = ctx();
@@ -1303,12 +1466,38 @@ int cappgpu_learn_check(const float* rhs, const float* coef, int D, int H, int W
   CAP_CUDA(cudaMemcpy(N.A.a0, in.data(), sizeof(bf16) * in.size(), cudaMemcpyHostToDevice));
   CAP_CUDA(cudaMemcpy(N.A.rhs, rhs, sizeof(float) * V, cudaMemcpyHostToDevice));
   CAP_CUDA(cudaMemcpy(N.A.coef, coef, sizeof(float) * 7 * V, cudaMemcpyHostToDevice));
-  if ((rc = forward(D, H, W))) return rc;
-  if ((rc = backward(D, H, W))) return rc;
+  if (target) CAP_CUDA(cudaMemcpy(N.A.tgt, target, sizeof(float) * V, cudaMemcpyHostToDevice));
+  const int keep = N.loss;
+  N.loss = kind;
+  if (!(rc = forward(D, H, W))) rc = backward(D, H, W);
+  N.loss = keep;
+  if (rc) return rc;
   if ((rc = check_err())) return rc;
   if (output) CAP_CUDA(cudaMemcpy(output, N.A.out, sizeof(float) * V, cudaMemcpyDeviceToHost));
   if (grad) CAP_CUDA(cudaMemcpy(grad, N.gp, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
   if (loss) CAP_CUDA(cudaMemcpy(loss, N.dsum, sizeof(double), cudaMemcpyDeviceToHost));
+  return CAPPGPU_OK;
+}
+
+int cappgpu_learn_check(const float* rhs, const float* coef, int D, int H, int W, float* output, float* grad,
+                        double* loss) {
+  return cappgpu_learn_check_loss(0, rhs, coef, nullptr, D, H, W, output, grad, loss);
+}
+
+int cappgpu_learn_sample(int index, float* host, long long n) {
+  CAP_REQUIRE_INIT();
+  if (!N.ready) { set_error("learn_sample: call cappgpu_learn_reset first"); return CAPPGPU_E_NOINIT; }
+  const long long sV = (long long)N.sD * N.sH * N.sW, need = kPlanes * sV;
+  if (index < 0 || index >= N.nsamples) {
+    set_error("learn_sample: pair %d of %d recorded", index, N.nsamples);
+    return CAPPGPU_E_ARG;
+  }
+  if (!host || n != need) {
+    set_error("learn_sample: %lld values for %d planes of %d x %d x %d", need, kPlanes, N.sD, N.sH, N.sW);
+    return CAPPGPU_E_ARG;
+  }
+  CAP_CUDA(cudaStreamSynchronize(ctx().st));
+  CAP_CUDA(cudaMemcpy(host, N.store + (size_t)index * need, sizeof(float) * need, cudaMemcpyDeviceToHost));
   return CAPPGPU_OK;
 }
 

@@ -12,6 +12,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "common.cuh"
@@ -32,6 +33,15 @@ namespace {
 #define CAP_WAVE_BC 8
 #endif
 constexpr int BA = CAP_WAVE_BA, BC = CAP_WAVE_BC;   // lines per wavefront block (a x c)
+// the FP32 factorisation and substitutions of the refinement form have a
+// block shape of their own (their slabs set the critical path, not the box)
+#ifndef CAP_WAVE32_BA
+#define CAP_WAVE32_BA CAP_WAVE_BA
+#endif
+#ifndef CAP_WAVE32_BC
+#define CAP_WAVE32_BC CAP_WAVE_BC
+#endif
+constexpr int BA32 = CAP_WAVE32_BA, BC32 = CAP_WAVE32_BC;
 
 enum DBuf { D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_SU, D_RES, D_FI, D_Z, D_ZZ, D_PK0, D_PK1, D_NBUF };
 
@@ -46,6 +56,8 @@ struct Fast {
   CUtensorMap map_fq, map_bq;
   int nBA = 0, nBC = 0, nblk = 0;
   int2* order = nullptr;
+  int nBA32 = 0, nBC32 = 0, nblk32 = 0;   // the same for the FP32 block shape
+  int2* order32 = nullptr;
   int4* chunk = nullptr;      // compact-order chunk starts (DG::chunk)
   unsigned* ticket = nullptr;
   int* flags = nullptr;       // [0] abort, [1] err
@@ -116,6 +128,7 @@ void fast_release() {
   if (F.fq) cudaFree(F.fq);
   if (F.bq) cudaFree(F.bq);
   if (F.order) cudaFree(F.order);
+  if (F.order32) cudaFree(F.order32);
   if (F.chunk) cudaFree(F.chunk);
   if (F.mail) cudaFree(F.mail);
   if (F.ticket) cudaFree(F.ticket);
@@ -199,6 +212,21 @@ int make_map(CUtensorMap* m, void* ptr, int nq, int esize) {
   return make_map_box(m, ptr, nq, esize, BA + 16 / esize, BC, kG);
 }
 
+// the same for an array the FP32 block shape copies from
+int make_map32(CUtensorMap* m, void* ptr, int nq) { return make_map_box(m, ptr, nq, 4, BA32 + 4, BC32, kG); }
+
+// blocks of na x nc lines in topological order (by diagonal ba + bc)
+std::vector<int2> block_order(int na, int nc) {
+  std::vector<int2> ord;
+  ord.reserve((size_t)na * nc);
+  for (int dsum = 0; dsum <= na + nc - 2; ++dsum)
+    for (int bc = 0; bc < nc; ++bc) {
+      const int ba = dsum - bc;
+      if (ba >= 0 && ba < na) ord.push_back(make_int2(ba, bc));
+    }
+  return ord;
+}
+
 int fast_setup() {
   Ctx& c = ctx();
   const Dims& d = c.d;
@@ -227,16 +255,16 @@ int fast_setup() {
   F.nBA = (F.g.Ni + BA - 1) / BA;
   F.nBC = (F.g.Nk + BC - 1) / BC;
   F.nblk = F.nBA * F.nBC;
-  // topological order: by diagonal ba+bc
-  std::vector<int2> ord;
-  ord.reserve(F.nblk);
-  for (int dsum = 0; dsum <= F.nBA + F.nBC - 2; ++dsum)
-    for (int bc = 0; bc < F.nBC; ++bc) {
-      int ba = dsum - bc;
-      if (ba >= 0 && ba < F.nBA) ord.push_back(make_int2(ba, bc));
-    }
-  CAP_CUDA(cudaMalloc(&F.order, sizeof(int2) * F.nblk));
-  CAP_CUDA(cudaMemcpy(F.order, ord.data(), sizeof(int2) * F.nblk, cudaMemcpyHostToDevice));
+  F.nBA32 = (F.g.Ni + BA32 - 1) / BA32;
+  F.nBC32 = (F.g.Nk + BC32 - 1) / BC32;
+  F.nblk32 = F.nBA32 * F.nBC32;
+  {
+    const std::vector<int2> ord = block_order(F.nBA, F.nBC), ord32 = block_order(F.nBA32, F.nBC32);
+    CAP_CUDA(cudaMalloc(&F.order, sizeof(int2) * F.nblk));
+    CAP_CUDA(cudaMemcpy(F.order, ord.data(), sizeof(int2) * F.nblk, cudaMemcpyHostToDevice));
+    CAP_CUDA(cudaMalloc(&F.order32, sizeof(int2) * F.nblk32));
+    CAP_CUDA(cudaMemcpy(F.order32, ord32.data(), sizeof(int2) * F.nblk32, cudaMemcpyHostToDevice));
+  }
   {
     // start (s, c, a) of every 32-cell chunk of the compact cell order
     const DG& g = F.g;
@@ -257,7 +285,7 @@ int fast_setup() {
     CAP_CUDA(cudaMemcpy(F.chunk, ch.data(), sizeof(int4) * ch.size(), cudaMemcpyHostToDevice));
     F.g.chunk = F.chunk;
   }
-  F.mail_n = (size_t)F.nblk * (BA + BC) * F.g.Nj * 3;   // up to 3 doubles per state
+  F.mail_n = std::max((size_t)F.nblk * (BA + BC), (size_t)F.nblk32 * (BA32 + BC32)) * F.g.Nj * 3;   // up to 3 doubles per state
   CAP_CUDA(cudaMalloc(&F.mail, F.mail_n * sizeof(double)));
   fill_mail(c.st);
   CAP_CUDA(cudaMalloc(&F.ticket, sizeof(unsigned)));
@@ -290,9 +318,9 @@ int fast32_setup() {
   CAP_CUDA(cudaMemsetAsync(G.fq, 0, 4 * n * sizeof(float), c.st));
   CAP_CUDA(cudaMemsetAsync(G.bq, 0, 3 * n * sizeof(float), c.st));
   int rc = CAPPGPU_OK;
-  for (int q = 0; q < E_NBUF && !rc; ++q) rc = make_map(&G.map[q], G.e[q], 1, 4);
-  if (!rc) rc = make_map(&G.map_fq, G.fq, 4, 4);
-  if (!rc) rc = make_map(&G.map_bq, G.bq, 3, 4);
+  for (int q = 0; q < E_NBUF && !rc; ++q) rc = make_map32(&G.map[q], G.e[q], 1);
+  if (!rc) rc = make_map32(&G.map_fq, G.fq, 4);
+  if (!rc) rc = make_map32(&G.map_bq, G.bq, 3);
   // the warp-tile engine: tile boxes, topological tile order, mailboxes
   const int lbw = kLW + 4;
   if (!rc) rc = make_map_box(&G.lmap_r, G.e[E_R], 1, 4, lbw, kCW, kLG);
@@ -361,18 +389,37 @@ int fast32_setup() {
   return CAPPGPU_OK;
 }
 
-WaveCtl next_ctl() {
+// the block shape of a wavefront operator: the FP32 ones of the refinement
+// form have their own
+template <class Op>
+struct WaveShape {
+  static constexpr int a = BA, c = BC;
+  static constexpr bool fp32 = false;
+};
+template <class Op>
+struct WaveShape32 {
+  static constexpr int a = BA32, c = BC32;
+  static constexpr bool fp32 = true;
+};
+template <>
+struct WaveShape<SipFwdF> : WaveShape32<SipFwdF> {};
+template <>
+struct WaveShape<SipBwdF> : WaveShape32<SipBwdF> {};
+template <>
+struct WaveShape<SipFactorF> : WaveShape32<SipFactorF> {};
+
+WaveCtl next_ctl(bool fp32 = false) {
   WaveCtl w;
   w.ticket = F.ticket;
-  w.order = F.order;
-  w.nBA = F.nBA;
-  w.nBC = F.nBC;
-  w.nblk = F.nblk;
+  w.order = fp32 ? F.order32 : F.order;
+  w.nBA = fp32 ? F.nBA32 : F.nBA;
+  w.nBC = fp32 ? F.nBC32 : F.nBC;
+  w.nblk = fp32 ? F.nblk32 : F.nblk;
   w.abort = F.flags;
   w.err = F.flags + 1;
-  w.partials = F.wpart;
+  w.partials = fp32 ? nullptr : F.wpart;   // (no FP32 operator reduces)
   w.mailW = F.mail;
-  w.mailB = F.mail + (size_t)F.nblk * BC * F.g.Nj * 3;
+  w.mailB = F.mail + (size_t)w.nblk * (fp32 ? BC32 : BC) * F.g.Nj * 3;
   w.spin_limit = ctx().spin_limit;
   w.skip = nullptr;
   w.slabBA = w.slabBC = 0;
@@ -390,7 +437,7 @@ int2 slab_blocks() {
   const Ctx& c = ctx();
   if (c.sip_slabs <= 1 || c.lane_wave != 0) return make_int2(0, 0);
   const bool alongA = c.sip_slab_axis == 0;
-  const int ext = alongA ? F.g.Ni : F.g.Nk, width = alongA ? BA : BC, nb = alongA ? F.nBA : F.nBC;
+  const int ext = alongA ? F.g.Ni : F.g.Nk, width = alongA ? BA32 : BC32, nb = alongA ? F.nBA32 : F.nBC32;
   for (int n = c.sip_slabs; n >= 2; --n)
     if (ext % (width * n) == 0) return alongA ? make_int2(nb / n, 0) : make_int2(0, nb / n);
   return make_int2(0, 0);
@@ -399,17 +446,18 @@ int2 slab_blocks() {
 template <class Op, bool BWD>
 int run_wave(const Op& op, const int* skip = nullptr, int2 slab = make_int2(0, 0)) {
   Ctx& c = ctx();
-  constexpr size_t smem = wave_smem_bytes<Op, BA, BC>();
+  using S = WaveShape<Op>;
+  constexpr size_t smem = wave_smem_bytes<Op, S::a, S::c>();
   static bool attr_set = false;   // once per process (one device per context)
   if (!attr_set) {
-    CAP_CUDA(cudaFuncSetAttribute(k_wave<Op, BA, BC, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CAP_CUDA(cudaFuncSetAttribute(k_wave<Op, S::a, S::c, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set = true;
   }
-  WaveCtl w = next_ctl();
+  WaveCtl w = next_ctl(S::fp32);
   w.skip = skip;
   w.slabBA = slab.x;
   w.slabBC = slab.y;
-  launch_smem(k_wave<Op, BA, BC, BWD>, F.nblk, wave_threads<Op, BA, BC>(), smem, c.st, op, F.g, w);
+  launch_smem(k_wave<Op, S::a, S::c, BWD>, w.nblk, wave_threads<Op, S::a, S::c>(), smem, c.st, op, F.g, w);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
 }

@@ -71,6 +71,10 @@ SIGNATURES = {
     "cappgpu_const_massflux_correction": [],
     "cappgpu_learn_check": [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _INT, _INT, _INT,
                             ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _DP],
+    "cappgpu_learn_check_loss": [_INT, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                 ctypes.POINTER(ctypes.c_float), _INT, _INT, _INT, ctypes.POINTER(ctypes.c_float),
+                                 ctypes.POINTER(ctypes.c_float), _DP],
+    "cappgpu_learn_sample": [_INT, ctypes.POINTER(ctypes.c_float), ctypes.c_longlong],
     "cappgpu_fluxuvw": [_INT] * 10,
     "cappgpu_calcuvw": [_REP],
     "cappgpu_piso_assemble_pressure_eq": [_INT] * 12,
@@ -318,24 +322,42 @@ class Library:
         return {"samples": s.value, "guesses": g.value, "fallbacks": f.value, "last_ratio": r.value,
                 "last_alpha": a.value, "last_beta": b.value}
 
-    def learn_check(self, rhs, coef):
-        """One forward + backward pass of the residual-norm loss on a (D, H, W)
-        normalised residual and its (7, D, H, W) window operator (planes xp, xm,
-        yp, ym, zp, zm, diag): output, parameter gradients, loss."""
+    def learn_check(self, rhs, coef, target=None, kind=0):
+        """One forward + backward pass of a training loss on a (D, H, W)
+        normalised residual and its (7, D, H, W) window operator (planes xp,
+        xm, yp, ym, zp, zm, diag): kind 0 the residual norm, 1 supervised and
+        2 energy norm against `target` (D, H, W).  Returns output, parameter
+        gradients, loss."""
         fp = ctypes.POINTER(ctypes.c_float)
         rhs = np.ascontiguousarray(rhs, np.float32)
         coef = np.ascontiguousarray(coef, np.float32)
         D, H, W = rhs.shape
         if coef.shape != (7, D, H, W):
             raise ValueError("coef must have shape (7, D, H, W)")
+        tp = ctypes.cast(None, fp)
+        if target is not None:
+            target = np.ascontiguousarray(target, np.float32)
+            if target.shape != rhs.shape:
+                raise ValueError("target must have the shape of rhs")
+            tp = target.ctypes.data_as(fp)
         out = np.empty_like(rhs)
         n = self.lib.cappgpu_learn_params(ctypes.cast(None, fp), 0, 0)
         grad = np.empty(n, np.float32)
         loss = ctypes.c_double()
-        self._check(self.lib.cappgpu_learn_check(rhs.ctypes.data_as(fp), coef.ctypes.data_as(fp), D, H, W,
-                                                 out.ctypes.data_as(fp), grad.ctypes.data_as(fp), ctypes.byref(loss)),
+        self._check(self.lib.cappgpu_learn_check_loss(int(kind), rhs.ctypes.data_as(fp), coef.ctypes.data_as(fp), tp,
+                                                      D, H, W, out.ctypes.data_as(fp), grad.ctypes.data_as(fp),
+                                                      ctypes.byref(loss)),
                     "learn_check")
         return out, grad, loss.value
+
+    def learn_sample(self, index, shape):
+        """Recorded pair `index` as (9, *shape) float32 planes: r^, A^ (xp, xm,
+        yp, ym, zp, zm, diag), the converged correction t^; `shape` is the
+        sample's (D, H, W) = (k, i, j) extent."""
+        a = np.empty((9,) + tuple(shape), np.float32)
+        self._check(self.lib.cappgpu_learn_sample(int(index), a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                  a.size), "learn_sample")
+        return a
 
     def spmv(self, pk, zk):
         dot = ctypes.c_double()

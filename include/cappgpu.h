@@ -254,6 +254,10 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    default 4) and restarts from the FP64 residual.
    "learn_conv": convolutions of the learned guess's net, 1 = tcgen05
    (default), 0 = mma.sync (kept for cross-checks).
+   "learn_loss": the training loss of cappgpu_learn_train, 0 = residual
+   norm |A^ d - r^|^2/|r^|^2 on the window (default; the learned-guess
+   configuration's), 1 = supervised |d - t^|^2/|t^|^2 against the recorded
+   converged correction, 2 = its energy norm (d - t^)'A^(d - t^)/t^'A^t^.
    "spin_limit": polls a wavefront block makes on a predecessor's edge
    states (and 64x as many on its own input copies) before it gives up,
    raises the device-wide abort flag and the solve returns CAPPGPU_E_SPIN
@@ -303,15 +307,27 @@ int cappgpu_precision(int mode);
    cappgpu_learn_train     Adam on random block^3 windows of the pairs
                            (block rounded down to a multiple of 4);
                            *loss = mean loss of the last epoch
-   cappgpu_learn_params    FP32 parameters out (direction 0) or in (1); with
-                           host == NULL returns the parameter count
+   cappgpu_learn_params    FP32 parameters out (direction 0) or in (1, Adam's
+                           moments reset); with host == NULL returns the
+                           parameter count
    cappgpu_learn_stats     pairs recorded, guesses kept, guesses discarded,
                            residual ratio of the last guess
    cappgpu_learn_check     one forward and backward pass on a D x H x W
                            normalised residual and its window operator
                            (7 planes xp, xm, yp, ym, zp, zm, diag; extents
                            multiples of 4) from the host, for tests: output,
-                           parameter gradients and loss */
+                           parameter gradients and loss
+   cappgpu_learn_check_loss the same with the loss kind of option
+                           "learn_loss" (0 residual norm |A d - r|^2/|r|^2,
+                           1 supervised |d - t|^2/|t|^2, 2 energy norm
+                           (d - t)'A(d - t)/t'At) and, for kinds 1-2, the
+                           target t
+   cappgpu_learn_sample    copies recorded pair `index` out: 9 planes of
+                           the sample's extent (r^ = r0/rms(r0); A^ = A /
+                           mean(ap) as xp, xm, yp, ym, zp, zm, diag; the
+                           solve's converged correction t^ = (fi_end -
+                           fi_start) mean(ap)/rms(r0), so A^ t^ = r^ to the
+                           solve's tolerance); n must be that count */
 int cappgpu_learn_reset(int max_samples, unsigned long long seed);
 int cappgpu_learn_windows(int block, int per_solve);
 int cappgpu_learn_collect(int on);
@@ -323,6 +339,9 @@ int cappgpu_learn_stats(int* samples, int* guesses, int* fallbacks, double* last
 int cappgpu_learn_fit(double* alpha, double* beta);
 int cappgpu_learn_check(const float* rhs, const float* coef, int D, int H, int W, float* output, float* grad,
                         double* loss);
+int cappgpu_learn_check_loss(int kind, const float* rhs, const float* coef, const float* target, int D, int H, int W,
+                             float* output, float* grad, double* loss);
+int cappgpu_learn_sample(int index, float* host, long long n);
 
 /* ================================================= LES sub-grid viscosity */
 /* find_strain_rate.f90:20-79 (gauss branch): Green-Gauss gradients of u, v,

@@ -6,7 +6,8 @@ U-Net of 3x3x3 convolutions (zero padding, ReLU) with 16/32/64 channels,
 (up-sampled first, then the encoder's output of the level), and a 1x1x1
 convolution to one channel; trained on the residual-norm loss
 |A d - r|^2 / |r|^2 with A the 7-point window operator (neighbours outside the
-window are zero).  The library stores weights and activations in BF16 and
+window are zero), or against a recorded converged correction t on the
+supervised loss |d - t|^2 / |t|^2 or the energy norm (d - t)'A(d - t) / t'At.  The library stores weights and activations in BF16 and
 accumulates in FP32; the oracle rounds the same quantities to BF16 and
 computes everything else in FP32, so outputs and gradients agree to the BF16
 rounding of the intermediate tensors.
@@ -97,12 +98,22 @@ def apply_a(coef, d):
             - c[3] * q[1:-1, :-2, 1:-1] - c[4] * q[2:, 1:-1, 1:-1] - c[5] * q[:-2, 1:-1, 1:-1])
 
 
-def loss_and_grad(p, rhs, coef):
-    """Residual-norm loss and its gradient with respect to the parameter vector."""
+def loss_and_grad(p, rhs, coef, target=None, kind=0):
+    """A training loss and its gradient with respect to the parameter vector:
+    kind 0 the residual norm |A d - r|^2/|r|^2, 1 supervised |d - t|^2/|t|^2,
+    2 energy norm (d - t)'A(d - t)/t'At against the target t."""
     import torch
     out, leaves = forward(p, rhs, requires_grad=True)
     r = torch.as_tensor(np.asarray(rhs, np.float32))
-    loss = ((apply_a(coef, out) - r) ** 2).sum() / (r ** 2).sum()
+    if kind == 0:
+        loss = ((apply_a(coef, out) - r) ** 2).sum() / (r ** 2).sum()
+    else:
+        t = torch.as_tensor(np.asarray(target, np.float32))
+        e = out - t
+        if kind == 1:
+            loss = (e ** 2).sum() / (t ** 2).sum()
+        else:
+            loss = (e * apply_a(coef, e)).sum() / (t * apply_a(coef, t)).sum()
     loss.backward()
     g = []
     for l, (ci, co) in enumerate(zip(CI, CO)):

@@ -73,6 +73,76 @@ def test_forward_and_gradients_match_cpu_oracle(gpu_lib, dims, impl):
         assert _rel(grad[sl], grad_o[sl]) < 1e-1, name
 
 
+@pytest.mark.parametrize("kind", [1, 2])
+@pytest.mark.parametrize("dims", [(8, 12, 16), (16, 16, 20)])
+def test_target_losses_match_cpu_oracle(gpu_lib, dims, kind):
+    """The supervised (1) and energy-norm (2) losses against a converged
+    correction: loss, output and every layer's gradients against the CPU
+    oracle (halo-tile tensor-core convolutions)."""
+    pytest.importorskip("torch")
+    import learned_oracle as lo
+    gpu_lib.init(12, 12, 12)
+    gpu_lib.learn_reset(0, seed=13)
+    p = gpu_lib.learn_params()
+    rng = np.random.default_rng(6)
+    rhs = rng.standard_normal(dims).astype(np.float32)
+    coef = _window_operator(rng, dims)
+    target = rng.standard_normal(dims).astype(np.float32)
+    gpu_lib.set_option("learn_conv", 1)
+    out, grad, loss = gpu_lib.learn_check(rhs, coef, target=target, kind=kind)
+    loss_o, out_o, grad_o = lo.loss_and_grad(p, rhs, coef, target=target, kind=kind)
+    assert _rel(out, out_o) < 2e-2
+    assert abs(loss - loss_o) <= 2e-2 * loss_o
+    assert _rel(grad, grad_o) < 5e-2
+    for name, sl in lo.param_slices():
+        assert _rel(grad[sl], grad_o[sl]) < 1e-1, name
+    with pytest.raises(cappgpu.CappError):   # a target loss without a target
+        gpu_lib.learn_check(rhs, coef, kind=kind)
+
+
+def test_recorded_target_is_the_converged_correction(gpu_lib):
+    """Each recorded pair carries the solve's converged correction on the
+    pair's scale: A^ t^ - r^ is the solve's final residual over its initial
+    one (relative L1), and training on the supervised and energy-norm losses
+    against it lowers them."""
+    torch = pytest.importorskip("torch")
+    import learned_oracle as lo
+    case = cappgpu.cases.channel(N=(16, 16, 24))
+    gpu_lib.load_case(case)
+    ni, nj, nk = case.interior
+    gpu_lib.precision(1)
+    try:
+        gpu_lib.learn_reset(8, seed=5)
+        gpu_lib.learn_collect(True)
+        rep = gpu_lib.piso_steps(2)                 # 4 pressure solves recorded
+        gpu_lib.learn_collect(False)
+        assert gpu_lib.learn_stats()["samples"] == 4
+        smp = gpu_lib.learn_sample(3, (nk, ni, nj))   # the last solve
+        r, coef, t = smp[0], smp[1:8], smp[8]
+        p0 = gpu_lib.learn_params()
+        losses = {}
+        for kind in (1, 2):
+            # from the same start each time; the loss on the whole last pair
+            # before and after training
+            gpu_lib.learn_params(p0)
+            gpu_lib.set_option("learn_loss", kind)
+            l0 = gpu_lib.learn_check(r, coef, target=t, kind=kind)[2]
+            gpu_lib.learn_train(30, block=16, lr=1e-3)
+            l1 = gpu_lib.learn_check(r, coef, target=t, kind=kind)[2]
+            losses[kind] = (l0, l1)
+    finally:
+        gpu_lib.precision(0)
+        gpu_lib.set_option("learn_loss", 0)
+    at = lo.apply_a(coef, torch.as_tensor(t)).numpy()
+    ratio = float(np.abs(at - r).sum() / np.abs(r).sum())
+    assert rep.status == 0 and np.abs(t).max() > 0
+    assert abs(ratio - rep.resl / rep.res0) <= 1e-3 + 0.05 * rep.resl / rep.res0, (ratio, rep.resl / rep.res0)
+    for kind, (l0, l1) in losses.items():
+        assert np.isfinite(l1) and l1 < l0, (kind, l0, l1)
+    print(f"recorded target: |A^t^ - r^|/|r^| {ratio:.2e} (solve {rep.resl / rep.res0:.2e}); "
+          f"supervised loss {losses[1][0]:.3f} -> {losses[1][1]:.3f}, energy {losses[2][0]:.3f} -> {losses[2][1]:.3f}")
+
+
 def test_learn_check_rejects_extents_not_multiple_of_4(gpu_lib):
     gpu_lib.init(12, 12, 12)
     gpu_lib.learn_reset(0, seed=1)
