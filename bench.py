@@ -349,7 +349,7 @@ def run_gpu(args, ws, rank, local):
             "p_solve_ms": st32.p_solve_ms, "p_iters": st32.p_report.iters,
             "p_rel_residual": st32.p_report.resl / st32.p_report.res0 if st32.p_report.res0 else None,
             "form": "FP32 SIP-preconditioned CG inside FP64 iterative refinement (exit test on the FP64 residual); "
-                    "the FP32 SIP block-local per i-slab (up to 8 slabs of whole 16-line block columns)",
+                    "the FP32 SIP block-local per i-slab (every 8-line block column along i a slab)",
             "errors_vs_fp64": errs}
 
     # precision mode 2: the refinement form starting from the learned guess.

@@ -91,7 +91,7 @@ struct Ctx {
   cudaEvent_t ev[4] = {};
   int wave_impl = 1;                   // 1 persistent wavefront, 0 one launch per hyperplane
   int lane_wave = 0;                   // FP32 substitutions: 0 the wavefront of wave.cuh, 1 the warp-tile engine
-  int sip_slabs = 8;                   // FP32 SIP of the refinement form (wavefront 0): block-local per slab
+  int sip_slabs = 4096;                // FP32 SIP of the refinement form (wavefront 0): block-local per slab
                                        // (as the reference's SIP per MPI rank), at most this many slabs
   int sip_slab_axis = 0;               // the slabs' axis: 0 = i, 1 = k
   int face_geo = 1;                    // 1: FP64 face kernels read the per-face geometry cache

@@ -326,7 +326,7 @@ int cappgpu_set_option(const char* key, int value) {
     ctx().spin_limit = value;
     return CAPPGPU_OK;
   }
-  if (strcmp(key, "sip_slabs") == 0 && value >= 1 && value <= 64) {
+  if (strcmp(key, "sip_slabs") == 0 && value >= 1 && value <= 4096) {
     ctx().sip_slabs = value;
     return CAPPGPU_OK;
   }

@@ -34,12 +34,14 @@ namespace {
 #endif
 constexpr int BA = CAP_WAVE_BA, BC = CAP_WAVE_BC;   // lines per wavefront block (a x c)
 // the FP32 factorisation and substitutions of the refinement form have a
-// block shape of their own (their slabs set the critical path, not the box)
+// block shape of their own: narrow along a, where each block column is a
+// slab of its own, and deep along c, where the blocks hand over (8 x 32
+// lines: 3 hand-overs at 128^3 instead of 15)
 #ifndef CAP_WAVE32_BA
-#define CAP_WAVE32_BA CAP_WAVE_BA
+#define CAP_WAVE32_BA 8
 #endif
 #ifndef CAP_WAVE32_BC
-#define CAP_WAVE32_BC CAP_WAVE_BC
+#define CAP_WAVE32_BC 32
 #endif
 constexpr int BA32 = CAP_WAVE32_BA, BC32 = CAP_WAVE32_BC;
 

@@ -170,16 +170,16 @@ def test_mixed_channel128_twenty_steps_per_field_errors(gpu_lib):
         assert err_fine[k] <= 1e-5, (k, err_fine[k])
 
 
-@pytest.mark.parametrize("axis,slabs", [(0, 2), (1, 2), (1, 4)])
+@pytest.mark.parametrize("axis,slabs", [(0, 2), (0, 4), (1, 2)])
 @pytest.mark.parametrize("solver", ["pcgsip", "sipsol"])
 def test_block_local_sip_per_slab(gpu_lib, oracle_mod, axis, slabs, solver):
     """The FP32 SIP of the refinement form restarted at every i-slab (axis 0)
     or k-slab (axis 1) (options sip_slabs, sip_slab_axis; interior
-    32 x 33 x 32: 2 block columns of 16 lines, 4 block rows of 8): both
+    32 x 33 x 64: 4 FP32 block columns of 8 lines, 2 block rows of 32): both
     solvers still meet the reference's exit test on the FP64 residual, within
     the tolerance's reach of the FP64 solution, with the SIP over the whole
     box and with the slabs."""
-    dims, sor = (36, 37, 36), 1e-6
+    dims, sor = (36, 37, 68), 1e-6
     st = _state(oracle_mod, dims, 11, sor)
     st.set_field("res", np.zeros_like(st.field("res")))
     push(gpu_lib, st)
@@ -196,7 +196,7 @@ def test_block_local_sip_per_slab(gpu_lib, oracle_mod, axis, slabs, solver):
             out[n] = getattr(gpu_lib, solver)("p", IP)
         finally:
             gpu_lib.precision(0)
-            gpu_lib.set_option("sip_slabs", 8)
+            gpu_lib.set_option("sip_slabs", 4096)
             gpu_lib.set_option("sip_slab_axis", 0)
         sol[n] = gpu_lib.get_field("p")
         r = out[n]
@@ -259,7 +259,7 @@ def test_fp32_substitution_engines_agree_bit_for_bit(gpu_lib, oracle_mod, solver
         finally:
             gpu_lib.precision(0)
             gpu_lib.set_option("lane_wave", 0)
-            gpu_lib.set_option("sip_slabs", 8)
+            gpu_lib.set_option("sip_slabs", 4096)
         out[lw] = (r, gpu_lib.get_field("p"), gpu_lib.get_field("res"))
     r0, p0, q0 = out[0]
     assert r0.status == 0
