@@ -64,6 +64,7 @@ struct Fast {
   unsigned* ticket = nullptr;
   int* flags = nullptr;       // [0] abort, [1] err
   int* ctl = nullptr;         // iteration control: [0] stop at iteration, [1] iterations, [2] non-finite, [3] converged
+  unsigned* cgcount = nullptr;   // blocks done with the update pass (cg_check_last; 0 between passes)
   double* wpart = nullptr;    // per-block partials of the wavefront
   double* mail = nullptr;     // edge mailboxes (sentinel when empty)
   size_t mail_n = 0;
@@ -135,6 +136,7 @@ void fast_release() {
   if (F.mail) cudaFree(F.mail);
   if (F.ticket) cudaFree(F.ticket);
   if (F.ctl) cudaFree(F.ctl);
+  if (F.cgcount) cudaFree(F.cgcount);
   if (F.flags) cudaFree(F.flags);
   if (F.wpart) cudaFree(F.wpart);
   if (F.hres) cudaFreeHost(F.hres);
@@ -299,6 +301,8 @@ int fast_setup() {
   CAP_CUDA(cudaMallocHost(&F.hstat, sizeof(int) * 8));
   CAP_CUDA(cudaMalloc(&F.ctl, sizeof(int) * 4));
   CAP_CUDA(cudaMemset(F.ctl, 0, sizeof(int) * 4));
+  CAP_CUDA(cudaMalloc(&F.cgcount, sizeof(unsigned)));
+  CAP_CUDA(cudaMemset(F.cgcount, 0, sizeof(unsigned)));
   CAP_CUDA(cudaStreamSynchronize(c.st));
   F.ready = true;
   return CAPPGPU_OK;
@@ -664,15 +668,18 @@ __device__ __forceinline__ void pass_cells(const DG& g, int q0, int lane, CellPa
 // ---------------------------------------------- batched CG iterations
 // The scalars of a CG iteration are formed by the kernel that needs them,
 // from the previous kernel's block partials, summed in a fixed order that is
-// the same in every block (deterministic).  A one-block check kernel ends
-// the iteration: it records the residual norm and, once the exit test
-// holds (or nsw iterations ran, or the norm is not finite), sets ctl[0];
-// every later kernel of the batch then returns at once.  The host reads
-// ctl once per batch.
+// the same in every block (deterministic).  The last block to finish the
+// update pass (or a one-block check kernel) ends the iteration: it records
+// the residual norm and, once the exit test holds (or nsw iterations ran,
+// or the norm is not finite), sets ctl[0]; every later kernel of the batch
+// then returns at once.  The host reads ctl once per batch.
+//
+// The partials are read through L2 (ld.global.cg): in the last-block form
+// they were written by other blocks of the same launch.
 __device__ double block_sum_fixed(const double* __restrict__ part, int n) {
   __shared__ double sh[kThreads];
   double v = 0.0;
-  for (int q = threadIdx.x; q < n; q += kThreads) v += part[q];
+  for (int q = threadIdx.x; q < n; q += kThreads) v += __ldcg(part + q);
   sh[threadIdx.x] = v;
   __syncthreads();
   for (int st = kThreads / 2; st > 0; st >>= 1) {
@@ -684,28 +691,82 @@ __device__ double block_sum_fixed(const double* __restrict__ part, int n) {
   return r;
 }
 
+// resl = sum |res| (pcg-sip.f90:161-177), s0 = sk, exit test
+// resl/res0 < resmax (pcg-sip.f90:185-188); target > 0 replaces the test by
+// resl <= target (inner loop of the refinement form)
+__device__ void cg_check_body(const double* __restrict__ part, double* scal, int* ctl, double res0, double resmax,
+                              double target, int nsw) {
+  const double resl = block_sum_fixed(part, kRedBlocks);
+  if (threadIdx.x == 0) {
+    scal[5] = resl;
+    scal[0] = scal[1];
+    const int it = ctl[1] + 1;
+    ctl[1] = it;
+    const bool bad = !isfinite(resl);
+    const bool conv = target > 0.0 ? resl <= target : resl / (res0 + CAP_SMALL) < resmax;
+    if (bad) ctl[2] = 1;
+    if (conv && !bad) ctl[3] = 1;
+    if (bad || conv || it >= nsw) ctl[0] = it;
+  }
+}
+
+__global__ void k_cg_check(const double* __restrict__ part, double* scal, int* ctl, double res0, double resmax,
+                           double target, int nsw) {
+  if (*(volatile const int*)ctl) return;
+  cg_check_body(part, scal, ctl, res0, resmax, target, nsw);
+}
+
+// The exit test in the last block of an update pass, in place of a
+// one-block k_cg_check launch: every block's thread 0 publishes its partial
+// (block_reduce_store) and counts itself in; the block that counts last
+// sums all partials in the fixed order and runs the test, then re-arms the
+// count for the next pass.
+struct CgCheck {
+  double res0, resmax, target;
+  int nsw;
+  unsigned* count;
+};
+
+__device__ void cg_check_last(const double* part, double* scal, int* ctl, const CgCheck& k) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();   // this block's partial before its count
+    last = atomicAdd(k.count, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();     // every block's partial after the count
+  cg_check_body(part, scal, ctl, k.res0, k.resmax, k.target, k.nsw);
+  if (threadIdx.x == 0) *k.count = 0u;
+}
+
 // a sum of block partials and a scalar formed from it by one thread, for
-// the many-block vector kernels: one warp sums (lane-strided, then a shuffle
-// tree), so the block issues few FP64 instructions -- on GB300 each holds its
+// the many-block vector kernels: every thread loads its few partials (one
+// round trip to L2 for the block, not one per partial of a lane), one warp
+// sums the threads' values (lane-strided, then a shuffle tree), so the
+// block issues few FP64 instructions -- on GB300 each holds its
 // sub-partition for 64 cycles whatever the active lanes, and an FP64
 // division per thread of every block cost more than the vector pass itself.
-// The one-block check kernel keeps the 256-thread tree above, which is
-// faster there.
 template <class Fn>
 __device__ double2 block_scalar2(const double* __restrict__ part, int n, Fn fn) {
-  __shared__ double sh[2];
+  __shared__ double sh[kThreads + 2];
+  double t = 0.0;
+  for (int q = threadIdx.x; q < n; q += kThreads) t += part[q];
+  sh[threadIdx.x] = t;
+  __syncthreads();
   if (threadIdx.x < 32) {
     double v = 0.0;
-    for (int q = threadIdx.x; q < n; q += 32) v += part[q];
+#pragma unroll
+    for (int q = 0; q < kThreads / 32; ++q) v += sh[threadIdx.x + 32 * q];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (threadIdx.x == 0) {
-      sh[0] = v;
-      sh[1] = fn(v);
+      sh[kThreads] = v;
+      sh[kThreads + 1] = fn(v);
     }
   }
   __syncthreads();
-  const double2 r = make_double2(sh[0], sh[1]);
+  const double2 r = make_double2(sh[kThreads], sh[kThreads + 1]);
   __syncthreads();
   return r;
 }
@@ -740,7 +801,7 @@ __global__ void k_pk_x(DG g, const double* __restrict__ zk, const double* __rest
 // fi += alf pk; res -= alf zz; partial sums |res| (pcg-sip.f90:161-175)
 __global__ void k_update_x(DG g, double* __restrict__ fi, double* __restrict__ res, const double* __restrict__ pk,
                            const double* __restrict__ zz, const double* __restrict__ pin, double* scal,
-                           double* pout, const int* ctl) {
+                           double* pout, int* ctl, const CgCheck chk) {
   if (*(volatile const int*)ctl) return;
   const double2 sa = block_scalar2(pin, kRedBlocks, [&](double v) { return scal[1] / v; });
   const double pkapk = sa.x, alf = sa.y;
@@ -770,27 +831,9 @@ __global__ void k_update_x(DG g, double* __restrict__ fi, double* __restrict__ r
     }
   }
   block_reduce_store<1>(v, pout);
+  cg_check_last(pout, scal, ctl, chk);
 }
 
-// resl = sum |res| (pcg-sip.f90:161-177), s0 = sk, exit test
-// resl/res0 < resmax (pcg-sip.f90:185-188); target > 0 replaces the test by
-// resl <= target (inner loop of the refinement form)
-__global__ void k_cg_check(const double* __restrict__ part, double* scal, int* ctl, double res0, double resmax,
-                           double target, int nsw) {
-  if (*(volatile const int*)ctl) return;
-  const double resl = block_sum_fixed(part, kRedBlocks);
-  if (threadIdx.x == 0) {
-    scal[5] = resl;
-    scal[0] = scal[1];
-    const int it = ctl[1] + 1;
-    ctl[1] = it;
-    const bool bad = !isfinite(resl);
-    const bool conv = target > 0.0 ? resl <= target : resl / (res0 + CAP_SMALL) < resmax;
-    if (bad) ctl[2] = 1;
-    if (conv && !bad) ctl[3] = 1;
-    if (bad || conv || it >= nsw) ctl[0] = it;
-  }
-}
 
 // zz = A pk with the partial sums of pk.zz (k_spmv_d), skipped once stopped
 __global__ void k_spmv_x(DG g, const double* __restrict__ ae, const double* __restrict__ aw,
@@ -966,7 +1009,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_pk_spmv_fx(DG g, const float* _
 // (pcg-sip.f90:157-175)
 __global__ void k_update_fx(DG g, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ pk,
                             const float* __restrict__ zz, const double* __restrict__ pin, double* scal, double* pout,
-                            const int* ctl) {
+                            int* ctl, const CgCheck chk) {
   if (*(volatile const int*)ctl) return;
   const double2 sa = block_scalar2(pin, kRedBlocks, [&](double v) { return scal[1] / v; });
   const double pkapk = sa.x, alfd = sa.y;
@@ -998,6 +1041,7 @@ __global__ void k_update_fx(DG g, float* __restrict__ x, float* __restrict__ r, 
   }
   double v[1] = {(double)acc};
   block_reduce_store<1>(v, pout);
+  cg_check_last(pout, scal, ctl, chk);
 }
 
 
@@ -1244,8 +1288,8 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
              (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
              (const double*)F.d[D_AP], (const double*)pkn, F.d[D_ZZ], part0, (const int*)F.ctl);
       launch(k_update_x, kRedBlocks, kThreads, c.st, F.g, F.d[D_FI], F.d[D_RES], (const double*)pkn,
-             (const double*)F.d[D_ZZ], (const double*)part0, c.dscal, part1, (const int*)F.ctl);
-      launch(k_cg_check, 1, kThreads, c.st, (const double*)part1, c.dscal, F.ctl, res0, resmax, 0.0, ns);
+             (const double*)F.d[D_ZZ], (const double*)part0, c.dscal, part1, F.ctl,
+             CgCheck{res0, resmax, 0.0, ns, F.cgcount});
       CAP_CHECK_LAUNCH();
       cur ^= 1;
     }
@@ -1441,8 +1485,8 @@ int iccg_fast(int fif, int ifi, cappgpu_solve_report* rep) {
              (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
              (const double*)F.d[D_AP], (const double*)pkn, F.d[D_ZZ], part0, (const int*)F.ctl);
       launch(k_update_x, kRedBlocks, kThreads, c.st, F.g, F.d[D_FI], F.d[D_RES], (const double*)pkn,
-             (const double*)F.d[D_ZZ], (const double*)part0, c.dscal, part1, (const int*)F.ctl);
-      launch(k_cg_check, 1, kThreads, c.st, (const double*)part1, c.dscal, F.ctl, res0, resmax, 0.0, ns);
+             (const double*)F.d[D_ZZ], (const double*)part0, c.dscal, part1, F.ctl,
+             CgCheck{res0, resmax, 0.0, ns, F.cgcount});
       CAP_CHECK_LAUNCH();
       cur ^= 1;
     }
@@ -1692,8 +1736,8 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
                (const float*)G.e[E_AP], (const float*)G.e[E_Z], (const float*)pko, pkn, G.e[E_ZZ],
                (const double*)part0, c.dscal, part1, (const int*)F.ctl);
         launch(k_update_fx, kRedBlocks, kThreads, c.st, g, G.e[E_X], G.e[E_R], (const float*)pkn,
-               (const float*)G.e[E_ZZ], (const double*)part1, c.dscal, part2, (const int*)F.ctl);
-        launch(k_cg_check, 1, kThreads, c.st, (const double*)part2, c.dscal, F.ctl, res0, resmax, target, budget);
+               (const float*)G.e[E_ZZ], (const double*)part1, c.dscal, part2, F.ctl,
+               CgCheck{res0, resmax, target, budget, F.cgcount});
         CAP_CHECK_LAUNCH();
         cur ^= 1;
       }
