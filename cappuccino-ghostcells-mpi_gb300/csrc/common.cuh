@@ -90,6 +90,7 @@ struct Ctx {
   cappgpu_solve_report p_rep{};        // its report
   cudaEvent_t ev[4] = {};
   int wave_impl = 1;                   // 1 persistent wavefront, 0 one launch per hyperplane
+  int fused_dot = 1;                   // FP32 CG (wavefront 0): sk = r.z in the backward substitution
   int lane_wave = 0;                   // FP32 substitutions: 0 the wavefront of wave.cuh, 1 the warp-tile engine
   int sip_slabs = 4096;                // FP32 SIP of the refinement form (wavefront 0): block-local per slab
                                        // (as the reference's SIP per MPI rank), at most this many slabs

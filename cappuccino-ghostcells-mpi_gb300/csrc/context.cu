@@ -310,6 +310,10 @@ int cappgpu_set_option(const char* key, int value) {
   }
   if (strcmp(key, "learn_conv") == 0 && value >= 0 && value <= 2) return learned_set_conv(value);
   if (strcmp(key, "learn_loss") == 0 && value >= 0 && value <= 2) return learned_set_loss(value);
+  if (strcmp(key, "fused_dot") == 0 && (value == 0 || value == 1)) {
+    ctx().fused_dot = value;
+    return CAPPGPU_OK;
+  }
   if (strcmp(key, "lane_wave") == 0 && value >= 0 && value <= 2) {
     ctx().lane_wave = value;
     return CAPPGPU_OK;

@@ -296,7 +296,7 @@ int fast_setup() {
   CAP_CUDA(cudaMemset(F.ticket, 0, sizeof(unsigned)));
   CAP_CUDA(cudaMalloc(&F.flags, sizeof(int) * 2));
   CAP_CUDA(cudaMemset(F.flags, 0, sizeof(int) * 2));
-  CAP_CUDA(cudaMalloc(&F.wpart, sizeof(double) * F.nblk));
+  CAP_CUDA(cudaMalloc(&F.wpart, sizeof(double) * std::max(F.nblk, F.nblk32)));
   CAP_CUDA(cudaMallocHost(&F.hres, sizeof(double) * 4));
   CAP_CUDA(cudaMallocHost(&F.hstat, sizeof(int) * 8));
   CAP_CUDA(cudaMalloc(&F.ctl, sizeof(int) * 4));
@@ -413,6 +413,8 @@ template <>
 struct WaveShape<SipBwdF> : WaveShape32<SipBwdF> {};
 template <>
 struct WaveShape<SipFactorF> : WaveShape32<SipFactorF> {};
+template <>
+struct WaveShape<SipBwdDotF> : WaveShape32<SipBwdDotF> {};
 
 WaveCtl next_ctl(bool fp32 = false) {
   WaveCtl w;
@@ -423,7 +425,7 @@ WaveCtl next_ctl(bool fp32 = false) {
   w.nblk = fp32 ? F.nblk32 : F.nblk;
   w.abort = F.flags;
   w.err = F.flags + 1;
-  w.partials = fp32 ? nullptr : F.wpart;   // (no FP32 operator reduces)
+  w.partials = F.wpart;
   w.mailW = F.mail;
   w.mailB = F.mail + (size_t)w.nblk * (fp32 ? BC32 : BC) * F.g.Nj * 3;
   w.spin_limit = ctx().spin_limit;
@@ -554,6 +556,23 @@ int fp32_forward(const int* skip) {
   fwd.map[1] = G.map_fq;
   fwd.z = G.e[E_Z];
   return run_wave<SipFwdF, false>(fwd, skip, slab_blocks());
+}
+
+int fp32_backward(const int* skip);
+
+// the backward substitution with sk = r.z fused (wavefront engine 0): the
+// partials of its blocks in F.wpart, their count returned in *nparts; the
+// other engines leave the dot to a vector pass (*nparts = 0)
+int fp32_backward_dot(const int* skip, int* nparts) {
+  *nparts = 0;
+  if (ctx().lane_wave != 0 || !ctx().fused_dot) return fp32_backward(skip);
+  SipBwdDotF bwd;
+  bwd.map[0] = G.map[E_Z];
+  bwd.map[1] = G.map_bq;
+  bwd.map[2] = G.map[E_R];
+  bwd.z = G.e[E_Z];
+  *nparts = F.nblk32;
+  return run_wave<SipBwdDotF, true>(bwd, skip, slab_blocks());
 }
 
 int fp32_backward(const int* skip) {
@@ -953,9 +972,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_pk_spmv_fx(DG g, const float* _
                              const float* __restrict__ at, const float* __restrict__ ab,
                              const float* __restrict__ ap, const float* __restrict__ zk,
                              const float* __restrict__ pko, float* __restrict__ pkn, float* __restrict__ zz,
-                             const double* __restrict__ pin, double* scal, double* pout, const int* ctl) {
+                             const double* __restrict__ pin, int npin, double* scal, double* pout, const int* ctl) {
   if (*(volatile const int*)ctl) return;
-  const double2 sb = block_scalar2(pin, kRedBlocks, [&](double v) { return v / scal[0]; });
+  const double2 sb = block_scalar2(pin, npin, [&](double v) { return v / scal[0]; });
   const double sk = sb.x, betd = sb.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) { scal[1] = sk; scal[4] = betd; }
   const float bet = (float)betd;
@@ -1726,15 +1745,21 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
       const int batch = budget - launched < c.cg_batch ? budget - launched : c.cg_batch;
       for (int q = 0; q < batch; ++q) {
         if ((rc = fp32_forward(F.ctl))) return rc;
-        if ((rc = fp32_backward(F.ctl))) return rc;
+        int nwp = 0;   // sk = r.z: partials of the backward sweep's blocks, or of a vector pass
+        if ((rc = fp32_backward_dot(F.ctl, &nwp))) return rc;
         float* pko = G.e[cur ? E_P1 : E_P0];
         float* pkn = G.e[cur ? E_P0 : E_P1];
-        launch(k_dot_fx, kRedBlocks, kThreads, c.st, g, (const float*)G.e[E_R], (const float*)G.e[E_Z], part0,
-               (const int*)F.ctl);
+        const double* psk = F.wpart;
+        if (nwp == 0) {
+          launch(k_dot_fx, kRedBlocks, kThreads, c.st, g, (const float*)G.e[E_R], (const float*)G.e[E_Z], part0,
+                 (const int*)F.ctl);
+          psk = part0;
+          nwp = kRedBlocks;
+        }
         launch(k_pk_spmv_fx, kRedBlocks, kThreads, c.st, g, (const float*)G.e[E_AE], (const float*)G.e[E_AW],
                (const float*)G.e[E_AN], (const float*)G.e[E_AS], (const float*)G.e[E_AT], (const float*)G.e[E_AB],
-               (const float*)G.e[E_AP], (const float*)G.e[E_Z], (const float*)pko, pkn, G.e[E_ZZ],
-               (const double*)part0, c.dscal, part1, (const int*)F.ctl);
+               (const float*)G.e[E_AP], (const float*)G.e[E_Z], (const float*)pko, pkn, G.e[E_ZZ], psk, nwp,
+               c.dscal, part1, (const int*)F.ctl);
         launch(k_update_fx, kRedBlocks, kThreads, c.st, g, G.e[E_X], G.e[E_R], (const float*)pkn,
                (const float*)G.e[E_ZZ], (const double*)part1, c.dscal, part2, F.ctl,
                CgCheck{res0, resmax, target, budget, F.cgcount});

@@ -41,6 +41,8 @@
 #pragma once
 #include <cuda.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "dlayout.cuh"
 
@@ -264,6 +266,19 @@ __device__ __forceinline__ void free_edge(const EdgeProbe<St, kPW * E / 32>& P, 
     }
   }
 }
+
+// the type a thread accumulates the op's reduction in: Op::Part where the op
+// names one (FP32 ops: one FP64 conversion per thread, not per cell -- on
+// GB300 each FP64 instruction, conversions included, holds its
+// sub-partition for 64 cycles), double otherwise
+template <class Op, class = void>
+struct PartOf {
+  using type = double;
+};
+template <class Op>
+struct PartOf<Op, std::void_t<typename Op::Part>> {
+  using type = typename Op::Part;
+};
 
 template <class Op, int BA, int BC, bool BWD>
 __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __grid_constant__ Op op, const DG g, const WaveCtl w) {
@@ -515,7 +530,7 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   x.di = (long long)x.sr * g.plane + (long long)c * g.P + a;
   x.nat = BWD ? nat_first - bv : nat_first + bv;
   const long long dstep = BWD ? -g.plane : g.plane;
-  double part = 0.0;
+  typename PartOf<Op>::type part = 0;                // this thread's share of the op's reduction
   bool stop = named_bar_red_or(1, NB, false);        // prologue: the first group has landed
   const unsigned char* slot = inbuf;
   const unsigned char* const slot_end = inbuf + NSLOT * L::slot_bytes;
@@ -565,7 +580,7 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   }
   if (Op::kReduce) {
     const int lane = tid & 31, wid = tid >> 5;
-    double x = part;
+    double x = (double)part;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (lane == 0) sm.red[wid] = x;
@@ -871,6 +886,36 @@ struct SipBwdF {
   __device__ St post(const In&, const Pre& p, const DG&, const Cell& x, St W, St B, double&) const {
     const float v = p.t - p.be * W - p.bt * B;
     z[x.di] = v;
+    return v;
+  }
+};
+
+// the same with the dot sk = sum r.z fused (the FP32 CG of the refinement
+// form; pcg-sip.f90:118), partials per block
+struct SipBwdDotF {
+  using St = float;
+  using Part = float;   // per-thread FP32 sum, as the vector pass forms it
+  static constexpr int kMaps = 3;   // z, backward factors (bn, be, bt), r
+  static constexpr bool kReduce = true;
+  static constexpr int kSlots = 6;
+  static constexpr int kPacers = 1;
+  static constexpr int kSyncSteps = kFp32SyncSteps;
+  static constexpr int kPW = 8;
+  __host__ __device__ static constexpr int nq(int m) { return m == 1 ? 3 : 1; }
+  __host__ __device__ static constexpr int esize(int) { return 4; }
+  CUtensorMap map[kMaps];
+  float* z;
+  __device__ St ghost(int) const { return 0.0f; }
+  struct Pre { float t, be, bt, r; };
+  template <class In>
+  __device__ Pre pre(const In& in, St S) const {
+    return Pre{in.f(0, 0) - in.f(1, 0) * S, in.f(1, 1), in.f(1, 2), in.f(2, 0)};
+  }
+  template <class In>
+  __device__ St post(const In&, const Pre& p, const DG&, const Cell& x, St W, St B, float& part) const {
+    const float v = p.t - p.be * W - p.bt * B;
+    z[x.di] = v;
+    part += p.r * v;
     return v;
   }
 };

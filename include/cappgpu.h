@@ -225,6 +225,9 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    within 1e-5 (velocity components) of the FP64 form over 20 steps of the
    128^3 channel; parts 4 and 16 change the FP64 system the refinement
    solves and are off by default.
+   "fused_dot": 1 = the FP32 CG of precision modes 1-2 forms sk = r.z in the
+   backward substitution (wavefront engine 0, default); 0 = in a vector
+   pass after it, as the other engines do (the same sum in another order).
    "lane_wave": engine of the FP32 SIP substitutions of precision modes 1-2:
    0 = the persistent hyperplane wavefront, one thread per line (default);
    1 = one warp per tile of 32 x 8 lines, neighbours by shuffles and

@@ -253,6 +253,7 @@ def test_fp32_substitution_engines_agree_bit_for_bit(gpu_lib, oracle_mod, solver
         push(gpu_lib, st)
         gpu_lib.set_option("lane_wave", lw)
         gpu_lib.set_option("sip_slabs", 1)   # the other engines run the SIP over the whole box
+        gpu_lib.set_option("fused_dot", 0)   # and form r.z in a vector pass
         gpu_lib.precision(1)
         try:
             r = getattr(gpu_lib, solver)("p", IP)
@@ -260,6 +261,7 @@ def test_fp32_substitution_engines_agree_bit_for_bit(gpu_lib, oracle_mod, solver
             gpu_lib.precision(0)
             gpu_lib.set_option("lane_wave", 0)
             gpu_lib.set_option("sip_slabs", 4096)
+            gpu_lib.set_option("fused_dot", 1)
         out[lw] = (r, gpu_lib.get_field("p"), gpu_lib.get_field("res"))
     r0, p0, q0 = out[0]
     assert r0.status == 0
@@ -270,6 +272,37 @@ def test_fp32_substitution_engines_agree_bit_for_bit(gpu_lib, oracle_mod, solver
         assert r1.resl == r0.resl and r1.res0 == r0.res0, lw
         np.testing.assert_array_equal(p1, p0)
         np.testing.assert_array_equal(q1, q0)
+
+
+@pytest.mark.parametrize("dims", [(14, 13, 12), (40, 37, 68), (104, 23, 71)])
+def test_fused_dot_in_the_backward_substitution(gpu_lib, oracle_mod, dims):
+    """sk = r.z formed in the FP32 backward substitution (option fused_dot,
+    the default) or in a vector pass after it: the same sum in another
+    order, so both solves meet the FP64 exit test within an iteration or two
+    of each other and agree to the tolerance's reach; the fused form gives
+    the same bits when repeated."""
+    sor = 1e-6
+    st = _state(oracle_mod, dims, 7, sor)
+    st.set_field("res", np.zeros_like(st.field("res")))
+    out = {}
+    for fused in (1, 0, 1):
+        push(gpu_lib, st)
+        gpu_lib.set_option("fused_dot", fused)
+        gpu_lib.precision(1)
+        try:
+            r = gpu_lib.pcgsip("p", IP)
+        finally:
+            gpu_lib.precision(0)
+            gpu_lib.set_option("fused_dot", 1)
+        assert r.status == 0 and r.resl / r.res0 < sor
+        p = gpu_lib.get_field("p")
+        if fused in out:
+            assert r.iters == out[fused][0].iters and r.resl == out[fused][0].resl
+            np.testing.assert_array_equal(p, out[fused][1])
+        out[fused] = (r, p)
+    (r1, p1), (r0, p0) = out[1], out[0]
+    assert abs(r1.iters - r0.iters) <= 2
+    assert np.linalg.norm(p1 - p0) <= 1e3 * sor * np.linalg.norm(p0)
 
 
 @pytest.mark.parametrize("engine", [1, 2])
