@@ -469,7 +469,7 @@ def run_gpu(args, ws, rank, local):
 
     # roofline of the SIP forward substitution on the current state
     peak, peak_kind = measured_peaks()
-    ms_fwd, bytes_fwd = lib.profile_kernel(0, reps=3)
+    ms_fwd, bytes_fwd = lib.profile_kernel(0, reps=10)
     achieved = bytes_fwd / (ms_fwd / 1e3) / 1e9
     units = {}
     for w, name in ((1, "sip_backward"), (2, "spmv_dot"), (6, "sip_factor"), (3, "grad_gauss"),
