@@ -241,16 +241,103 @@ __global__ void k_grad_gauss(Dims d, const double* __restrict__ u, const double*
   }
 }
 
+// The same gradient in FP32 arithmetic from FP32 copies of the geometry
+// (fx, fy, fz, ar1x..ar3z and 1/vol, each rounded once per grid) and of the
+// field (rounded once per call): the FP32 terms of k_grad_gauss<float> in
+// the same order, so the same bits, without its ≈30 FP64 -> FP32
+// conversions per cell (GB300 runs them on the FP64 pipe, 64 cycles per
+// warp instruction) and with half the bytes read.  G holds the 13 geometry
+// planes of n floats each in the order fx, fy, fz, a1x, a1y, a1z, a2x, a2y,
+// a2z, a3x, a3y, a3z, 1/vol.
+__global__ void k_grad_gauss32(Dims d, const float* __restrict__ u, const float* __restrict__ G, long long n,
+                               double* __restrict__ dx, double* __restrict__ dy, double* __restrict__ dz) {
+  const float *fx = G, *fy = G + n, *fz = G + 2 * n;
+  const float *a1x = G + 3 * n, *a1y = G + 4 * n, *a1z = G + 5 * n;
+  const float *a2x = G + 6 * n, *a2y = G + 7 * n, *a2z = G + 8 * n;
+  const float *a3x = G + 9 * n, *a3y = G + 10 * n, *a3z = G + 11 * n, *volr = G + 12 * n;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < d.nijk; t += (long long)gridDim.x * blockDim.x) {
+    int p = (int)t;
+    int k = p / d.nij + 1;
+    int r = p - (k - 1) * d.nij;
+    int i = r / d.nj + 1;
+    int j = r - (i - 1) * d.nj + 1;
+    auto inF = [&](int ii, int jj, int kk) {
+      return kk >= 2 && kk <= d.nkm && ii >= 2 && ii <= d.nimm && jj >= 2 && jj <= d.njmm;
+    };
+    float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+    if (inF(i, j, k - 1)) {  // bottom face
+      int q = p - d.nij;
+      float ut = u[p] * fz[q] + u[q] * (1.0f - fz[q]);
+      gx = gx - (ut * a3x[q]);
+      gy = gy - (ut * a3y[q]);
+      gz = gz - (ut * a3z[q]);
+    }
+    if (inF(i - 1, j, k)) {  // west face
+      int q = p - d.nj;
+      float ue = u[p] * fx[q] + u[q] * (1.0f - fx[q]);
+      gx = gx - (ue * a1x[q]);
+      gy = gy - (ue * a1y[q]);
+      gz = gz - (ue * a1z[q]);
+    }
+    if (inF(i, j - 1, k)) {  // south face
+      int q = p - 1;
+      float un = u[p] * fy[q] + u[q] * (1.0f - fy[q]);
+      gx = gx - (un * a2x[q]);
+      gy = gy - (un * a2y[q]);
+      gz = gz - (un * a2z[q]);
+    }
+    if (inF(i, j, k)) {  // own east, north, top faces
+      float ue = u[p + d.nj] * fx[p] + u[p] * (1.0f - fx[p]);
+      float un = u[p + 1] * fy[p] + u[p] * (1.0f - fy[p]);
+      float ut = u[p + d.nij] * fz[p] + u[p] * (1.0f - fz[p]);
+      gx = gx + (ue * a1x[p] + un * a2x[p] + ut * a3x[p]);
+      gy = gy + (ue * a1y[p] + un * a2y[p] + ut * a3y[p]);
+      gz = gz + (ue * a1z[p] + un * a2z[p] + ut * a3z[p]);
+    }
+    if (k >= 2 && k <= d.nkm && i >= 3 && i <= d.nimm && j >= 3 && j <= d.njmm) {
+      const float vr = volr[p];
+      gx = gx * vr;
+      gy = gy * vr;
+      gz = gz * vr;
+    }
+    dx[p] = gx;
+    dy[p] = gy;
+    dz[p] = gz;
+  }
+}
+
 // 1/vol of every cell for the FP64 gradient (an FP64 division per cell and
-// call otherwise), rebuilt after a write into a geometry field or vol
+// call otherwise), and the FP32 geometry of k_grad_gauss32, rebuilt after a
+// write into a geometry field or vol
 namespace {
 double* g_volr = nullptr;
 unsigned long long g_volr_gen = 0;
 int g_volr_n = 0;
+float* g_geo32 = nullptr;   // 13 geometry planes, then the field's FP32 copy
+unsigned long long g_geo32_gen = 0;
+int g_geo32_n = 0;
 
 __global__ void k_recip(long long n, const double* __restrict__ v, double* __restrict__ r) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
     r[t] = 1.0 / v[t];
+}
+
+struct Geo13 {
+  const double* g[12];   // fx, fy, fz, a1x .. a3z
+  const double* vol;
+};
+
+__global__ void k_geo32(long long n, Geo13 src, float* __restrict__ G) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < 12; ++q) G[q * n + t] = (float)src.g[q][t];
+    G[12 * n + t] = 1.0f / (float)src.vol[t];
+  }
+}
+
+__global__ void k_to_f32(long long n, const double* __restrict__ x, float* __restrict__ y) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    y[t] = (float)x[t];
 }
 }  // namespace
 
@@ -259,6 +346,39 @@ void volr_free() {
   g_volr = nullptr;
   g_volr_gen = 0;
   g_volr_n = 0;
+  if (g_geo32) cudaFree(g_geo32);
+  g_geo32 = nullptr;
+  g_geo32_gen = 0;
+  g_geo32_n = 0;
+}
+
+// the FP32 geometry planes followed by room for the field (14 x nijk
+// floats), or null (no room, or option face_geo 0: convert per call)
+static float* geo32_cache() {
+  Ctx& c = ctx();
+  if (!c.face_geo) return nullptr;
+  const long long n = c.d.nijk;
+  if (g_geo32_n != c.d.nijk) {
+    if (g_geo32) cudaFree(g_geo32);
+    g_geo32 = nullptr;
+    g_geo32_n = 0;
+    if (cudaMalloc(&g_geo32, sizeof(float) * 14 * (size_t)n) != cudaSuccess) {
+      cudaGetLastError();
+      g_geo32 = nullptr;
+      return nullptr;
+    }
+    g_geo32_n = c.d.nijk;
+    g_geo32_gen = 0;
+  }
+  if (g_geo32_gen != c.geo_gen) {
+    double** F = c.f;
+    Geo13 src{{F[CAP_FX], F[CAP_FY], F[CAP_FZ], F[CAP_AR1X], F[CAP_AR1Y], F[CAP_AR1Z], F[CAP_AR2X], F[CAP_AR2Y],
+               F[CAP_AR2Z], F[CAP_AR3X], F[CAP_AR3Y], F[CAP_AR3Z]},
+              F[CAP_VOL]};
+    launch(k_geo32, grid_for(n), kThreads, c.st, n, src, g_geo32);
+    g_geo32_gen = c.geo_gen;
+  }
+  return g_geo32;
 }
 
 static const double* volr_cache() {
@@ -287,6 +407,18 @@ int grad_gauss(int uf, int dxf, int dyf, int dzf) {
   // assembly) in FP32 arithmetic; the pressure gradient of the velocity
   // correction stays FP64
   const bool f32 = c.fp32(8) && uf != CAP_P;
+  if (f32) {
+    float* G = geo32_cache();
+    if (G) {
+      const long long n = c.d.nijk;
+      float* u32 = G + 13 * n;
+      launch(k_to_f32, grid_for(n), kThreads, c.st, n, (const double*)F[uf], u32);
+      launch(k_grad_gauss32, grid_for(n), kThreads, c.st, c.d, (const float*)u32, (const float*)G, n, F[dxf], F[dyf],
+             F[dzf]);
+      CAP_CHECK_LAUNCH();
+      return CAPPGPU_OK;
+    }
+  }
   const double* vr = f32 ? nullptr : volr_cache();
   auto k = f32 ? k_grad_gauss<float, false> : vr ? k_grad_gauss<double, true> : k_grad_gauss<double, false>;
   launch(k, grid_for(c.d.nijk), kThreads, c.st,

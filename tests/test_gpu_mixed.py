@@ -274,6 +274,46 @@ def test_fp32_substitution_engines_agree_bit_for_bit(gpu_lib, oracle_mod, solver
         np.testing.assert_array_equal(q1, q0)
 
 
+@pytest.mark.parametrize("make", ["channel", "poisson"])
+def test_fp32_gradient_from_cached_fp32_geometry(gpu_lib, make):
+    """The FP32 velocity gradient of precision modes 1-2 from the FP32 copy of
+    the geometry (option face_geo 1, the default) gives the bits of the
+    per-call conversion (face_geo 0), ghost and padding cells included, and
+    lies within FP32 rounding of the FP64 gradient; a geometry write
+    rebuilds the copy."""
+    case = getattr(cappgpu.cases, make)(N=(20, 12, 16))
+    gpu_lib.load_case(case)
+    names = ("gradu_x", "gradu_y", "gradu_z")
+    u = gpu_lib.get_field("u")
+    rng = np.random.default_rng(3)
+    gpu_lib.set_field("u", u + 0.1 * rng.standard_normal(u.shape))
+
+    def grad(mode, face_geo):
+        gpu_lib.set_option("face_geo", face_geo)
+        gpu_lib.precision(mode)
+        try:
+            gpu_lib.grad_gauss("u", *names)
+        finally:
+            gpu_lib.precision(0)
+            gpu_lib.set_option("face_geo", 1)
+        return [gpu_lib.get_field(n) for n in names]
+
+    g64 = grad(0, 1)
+    g32c = grad(1, 1)
+    g32 = grad(1, 0)
+    for a, b, c in zip(g32c, g32, g64):
+        np.testing.assert_array_equal(a, b)
+        assert np.linalg.norm(a - c) <= 1e-5 * np.linalg.norm(c)
+    # a geometry write (vol) invalidates the FP32 copy
+    vol = gpu_lib.get_field("vol")
+    gpu_lib.set_field("vol", 2.0 * vol)
+    h32c, h32 = grad(1, 1), grad(1, 0)
+    for a, b, c in zip(h32c, h32, g32):
+        np.testing.assert_array_equal(a, b)
+        assert not np.array_equal(a, c)
+    gpu_lib.set_field("vol", vol)
+
+
 @pytest.mark.parametrize("dims", [(14, 13, 12), (40, 37, 68), (104, 23, 71)])
 def test_fused_dot_in_the_backward_substitution(gpu_lib, oracle_mod, dims):
     """sk = r.z formed in the FP32 backward substitution (option fused_dot,
