@@ -180,8 +180,8 @@ __global__ void __launch_bounds__(mwave_threads(), 1) k_mwave(const __grid_const
       const int cur = __shfl_sync(0xffffffffu, *(volatile int*)&sm.done, 0);
       const int limit = max(cur, s0) + kRing - 2;   // ring capacity
       const int hiW = min(s1W, limit), hiB = min(s1B, limit);
-      probe_edge<Op, BC, BWD>(PW, op, g, lane, loadedW, hiW, srcW, lineW);
-      probe_edge<Op, BA, BWD>(PB, op, g, lane, loadedB, hiB, srcB, lineB);
+      probe_edge<Op, BC, BWD>(PW, op, g, lane, loadedW, hiW, srcW, lineW, make_int2(0, g.Ni), g.Ni);
+      probe_edge<Op, BA, BWD>(PB, op, g, lane, loadedB, hiB, srcB, lineB, make_int2(0, g.Ni), g.Ni);
       const int nW = commit_edge<float, BC, Op::kPW>(PW, g, lane, loadedW, srcW, sm.ringW, lineW);
       const int nB = commit_edge<float, BA, Op::kPW>(PB, g, lane, loadedB, srcB, sm.ringB, lineB);
       if (nW + nB > 0) {

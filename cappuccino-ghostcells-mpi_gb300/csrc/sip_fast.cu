@@ -431,6 +431,7 @@ WaveCtl next_ctl(bool fp32 = false) {
   w.spin_limit = ctx().spin_limit;
   w.skip = nullptr;
   w.slabBA = w.slabBC = 0;
+  w.mirrorA = 0;
   return w;
 }
 
@@ -438,16 +439,21 @@ WaveCtl next_ctl(bool fp32 = false) {
 // sip_slabs along the axis sip_slab_axis: 0 = i, 1 = k; wavefront engine 0),
 // as {along a, along c}; {0, 0} when the recurrence spans the whole box.
 // The slabs must end on block boundaries from both ends of the box (forward
-// and mirrored backward blocks): the count is the largest n <= sip_slabs,
-// n >= 2, for which the extent along the axis is a multiple of n block
-// widths.
+// and mirrored backward blocks).  Along a the backward blocks are mirrored
+// about the extent of whole blocks (WaveCtl::mirrorA), so they cover the
+// forward blocks' a ranges and any count n that divides the block columns
+// works; along c the extent must be a multiple of n block heights.  The
+// count is the largest such n <= sip_slabs, n >= 2.
 int2 slab_blocks() {
   const Ctx& c = ctx();
   if (c.sip_slabs <= 1 || c.lane_wave != 0) return make_int2(0, 0);
-  const bool alongA = c.sip_slab_axis == 0;
-  const int ext = alongA ? F.g.Ni : F.g.Nk, width = alongA ? BA32 : BC32, nb = alongA ? F.nBA32 : F.nBC32;
+  if (c.sip_slab_axis == 0) {
+    for (int n = std::min(c.sip_slabs, F.nBA32); n >= 2; --n)
+      if (F.nBA32 % n == 0) return make_int2(F.nBA32 / n, 0);
+    return make_int2(0, 0);
+  }
   for (int n = c.sip_slabs; n >= 2; --n)
-    if (ext % (width * n) == 0) return alongA ? make_int2(nb / n, 0) : make_int2(0, nb / n);
+    if (F.g.Nk % (BC32 * n) == 0) return make_int2(0, F.nBC32 / n);
   return make_int2(0, 0);
 }
 
@@ -465,6 +471,9 @@ int run_wave(const Op& op, const int* skip = nullptr, int2 slab = make_int2(0, 0
   w.skip = skip;
   w.slabBA = slab.x;
   w.slabBC = slab.y;
+  // slabs along a: the mirrored blocks end where the forward ones do (the
+  // FP32 ops' ghost states are zero, as the mirror offset requires)
+  if (S::fp32 && slab.x > 0) w.mirrorA = F.nBA32 * BA32;
   launch_smem(k_wave<Op, S::a, S::c, BWD>, w.nblk, wave_threads<Op, S::a, S::c>(), smem, c.st, op, F.g, w);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
@@ -516,6 +525,7 @@ WaveCtl mwave_ctl(const int* skip) {
   w.spin_limit = ctx().spin_limit;
   w.skip = skip;
   w.slabBA = w.slabBC = 0;
+  w.mirrorA = 0;
   return w;
 }
 

@@ -62,6 +62,10 @@ struct WaveCtl {
   int slabBA, slabBC;             // > 0: the recurrence restarts every slabBA blocks along a / slabBC blocks
                                   // along c (block-local SIP per slab); a slab's first line / row sees zero
                                   // states before it
+  int mirrorA;                    // > 0 (mirrored blocks of an op with zero ghost states only): mirror a
+                                  // about this extent, nBA x BA, instead of Ni, so that the blocks cover the
+                                  // same a ranges as the forward ones; the first mirrored block then starts
+                                  // with mirrorA - Ni lines outside the box
 };
 
 constexpr int kG = 4;        // hyperplanes per TMA copy
@@ -186,7 +190,7 @@ struct EdgeProbe {
 template <class Op, int E, bool BWD, class LineFn>
 __device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, Op::kPW * E / 32>& P, const Op& op, const DG& g,
                                            int lane, int loaded, int hi, const double* mail, LineFn line,
-                                           bool zero_ghost = false) {
+                                           int2 avr, int Mi, bool zero_ghost = false) {
   using St = typename Op::St;
   constexpr int NS = state_words<St>();
 #pragma unroll
@@ -196,14 +200,14 @@ __device__ __forceinline__ void probe_edge(EdgeProbe<typename Op::St, Op::kPW * 
     line(e, av, cv, pa, pc);
     const int bv = q - pa - pc;   // the predecessor cell lies on plane q; the consumer has the same b
     P.inwin[r] = q <= hi;
-    P.need[r] = q <= hi && av < g.Ni && cv < g.Nk && bv >= 0 && bv < g.Nj;
+    P.need[r] = q <= hi && av >= avr.x && av < avr.y && cv < g.Nk && bv >= 0 && bv < g.Nj;
     if (P.need[r]) {
       if (mail) {
         const double* m = mail + ((size_t)e * g.Nj + bv) * NS;
 #pragma unroll
         for (int k = 0; k < NS; ++k) P.u[r][k] = ld_relaxed_b64(m + k);
       } else {
-        const int a = BWD ? g.Ni - 1 - pa : pa;
+        const int a = BWD ? Mi - 1 - pa : pa;
         const int b = BWD ? g.Nj - 1 - bv : bv;
         const int c = BWD ? g.Nk - 1 - pc : pc;
         const St v = zero_ghost ? St{} : op.ghost(g.nat(a, b, c));
@@ -329,11 +333,16 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   __syncthreads();
   if (!sm.start_ok) return;
   const int ba = sm.blk[0], bc = sm.blk[1];
+  // the extent a is mirrored about, the steps of the (virtual) box and the
+  // range of virtual a inside the box
+  const int Mi = BWD && w.mirrorA > 0 ? w.mirrorA : g.Ni;
+  const int SV = Mi + g.Nj + g.Nk - 2;
+  const int2 avr = make_int2(BWD ? Mi - g.Ni : 0, BWD ? Mi : g.Ni);
   const int s0 = ba * BA + bc * BC;
-  const int s1 = min(g.S - 1, s0 + (BA - 1) + (BC - 1) + (g.Nj - 1));
+  const int s1 = min(SV - 1, s0 + (BA - 1) + (BC - 1) + (g.Nj - 1));
   // last plane of the W / B predecessor lines
-  const int s1W = min(g.S - 1, s0 - 1 + (BC - 1) + (g.Nj - 1));
-  const int s1B = min(g.S - 1, s0 - 1 + (BA - 1) + (g.Nj - 1));
+  const int s1W = min(SV - 1, s0 - 1 + (BC - 1) + (g.Nj - 1));
+  const int s1B = min(SV - 1, s0 - 1 + (BA - 1) + (g.Nj - 1));
   const int blk_id = bc * w.nBA + ba;
   const int ngroups = (s1 - s0 + kG) / kG;
 
@@ -343,9 +352,9 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
     const int pw = (tid - NC - 32 * kComm) >> 5;   // this pacer's index
     auto issue = [&](int gq) {   // TMA copy of group gq (planes s0 + gq*kG ...) into its slot
       const int slot = gq % NSLOT, sg = s0 + gq * kG;
-      const int alo = BWD ? g.Ni - (ba + 1) * BA : ba * BA;   // first column of the block's lines
+      const int alo = BWD ? Mi - (ba + 1) * BA : ba * BA;   // first column of the block's lines
       const int y0 = BWD ? g.Nk - (bc + 1) * BC : bc * BC;
-      const int z0 = BWD ? g.S - sg - kG : sg;
+      const int z0 = BWD ? SV - sg - kG : sg;
       unsigned char* dst = inbuf + slot * L::slot_bytes;
       mbar_arrive_tx(&sm.full[slot], (unsigned)L::tx_bytes);
 #pragma unroll
@@ -458,8 +467,8 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
       const int cur = __shfl_sync(0xffffffffu, *(volatile int*)&sm.done, 0);
       const int limit = max(cur, s0) + kRing - 2;   // ring capacity
       const int hiW = min(s1W, limit), hiB = min(s1B, limit);
-      probe_edge<Op, BC, BWD>(PW, op, g, lane, loadedW, hiW, srcW, lineW, slabW);
-      probe_edge<Op, BA, BWD>(PB, op, g, lane, loadedB, hiB, srcB, lineB, slab0);
+      probe_edge<Op, BC, BWD>(PW, op, g, lane, loadedW, hiW, srcW, lineW, avr, Mi, slabW);
+      probe_edge<Op, BA, BWD>(PB, op, g, lane, loadedB, hiB, srcB, lineB, avr, Mi, slab0);
       const int nW = commit_edge<St, BC, kPW>(PW, g, lane, loadedW, srcW, sm.ringW, lineW);
       const int nB = commit_edge<St, BA, kPW>(PB, g, lane, loadedB, srcB, sm.ringB, lineB);
       if (nW + nB > 0) {
@@ -494,15 +503,15 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   static_assert(BA % 2 == 0 && BC % 2 == 0 && kG % 2 == 0, "even group starts: a step's plane parity is static");
   const int al = tid % BA, cl = tid / BA;
   const int av = ba * BA + al, cv = bc * BC + cl;     // virtual (mirrored when BWD) line
-  const bool line_ok = av < g.Ni && cv < g.Nk;
-  const int a = BWD ? g.Ni - 1 - av : av;
+  const bool line_ok = av >= avr.x && av < avr.y && cv < g.Nk;
+  const int a = BWD ? Mi - 1 - av : av;
   const int c = BWD ? g.Nk - 1 - cv : cv;
   const int sfirst = av + cv;                         // step of this line's first cell
   InView<Op, BA, BC> in;                              // this line's column and row in an input box
   if (!BWD) {
     in.init(al, al, cl);
   } else {
-    const int alo = g.Ni - (ba + 1) * BA;
+    const int alo = Mi - (ba + 1) * BA;
     in.init((alo - (alo & ~1)) + BA - 1 - al, (alo - (alo & ~3)) + BA - 1 - al, BC - 1 - cl);
   }
   const bool edgeE = al == BA - 1 && ba + 1 < w.nBA &&   // feeds the next block along a
@@ -526,7 +535,7 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   Cell x;                                             // running indices of the current step's cell
   x.a = a;
   x.c = c;
-  x.sr = BWD ? g.S - 1 - s0 : s0;
+  x.sr = BWD ? SV - 1 - s0 : s0;
   x.di = (long long)x.sr * g.plane + (long long)c * g.P + a;
   x.nat = BWD ? nat_first - bv : nat_first + bv;
   const long long dstep = BWD ? -g.plane : g.plane;
@@ -553,7 +562,9 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
       if (act) {
         const bool odd = (ds & 1) != 0;   // the plane's parity (group starts are even); previous plane in buffer !odd
         const int rs = ring_slot(sg + ds - 1);
-        const St W = *(al > 0 ? (odd ? rdW0 : rdW1) : &sm.ringW[rs][cl]);
+        // (the first line inside a mirrored box that starts inside the block
+        // has no neighbour line before it: the op's zero ghost state)
+        const St W = av == avr.x && al > 0 ? St{} : *(al > 0 ? (odd ? rdW0 : rdW1) : &sm.ringW[rs][cl]);
         const St B = *(cl > 0 ? (odd ? rdB0 : rdB1) : &sm.ringB[rs][al]);
         const St out = op.post(in, pv, g, x, W, B, part);
         *(odd ? wr1 : wr0) = out;

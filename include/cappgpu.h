@@ -244,12 +244,13 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    factorisation and substitutions restart at every slab of the interior
    (1..4096, default 4096; 1 = over the whole box): block-local SIP per
    slab, as the reference's SIP runs per MPI rank, so the slabs'
-   recurrences run side by side.  The count used is the largest n <=
-   sip_slabs, n >= 2, for which the interior extent along the slab axis is
-   a multiple of n FP32 block widths (8 lines along i, 32 along k); with
-   none, the whole box.  The default makes every 8-line block column along
-   i a slab of its own.  It changes the preconditioner of the refinement,
-   not its FP64 exit test.
+   recurrences run side by side.  The FP32 blocks are 8 lines along i and
+   32 along k; the count used is the largest n <= sip_slabs, n >= 2, that
+   divides the number of block columns along i (ceil(Ni/8)), or along k for
+   which the interior extent is a multiple of n x 32; with none, the whole
+   box.  The default makes every 8-line block column along i a slab of its
+   own.  It changes the preconditioner of the refinement, not its FP64 exit
+   test.
    "sip_slab_axis": the axis of those slabs, 0 = i (default), 1 = k.
    "cg_batch": conjugate-gradient iterations of pcgsip launched between two
    host reads of the device-side exit test (1..64, default 4; surplus

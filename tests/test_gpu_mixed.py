@@ -172,14 +172,16 @@ def test_mixed_channel128_twenty_steps_per_field_errors(gpu_lib):
 
 @pytest.mark.parametrize("axis,slabs", [(0, 2), (0, 4), (1, 2)])
 @pytest.mark.parametrize("solver", ["pcgsip", "sipsol"])
-def test_block_local_sip_per_slab(gpu_lib, oracle_mod, axis, slabs, solver):
+@pytest.mark.parametrize("dims", [(36, 37, 68), (34, 37, 68)])
+def test_block_local_sip_per_slab(gpu_lib, oracle_mod, axis, slabs, solver, dims):
     """The FP32 SIP of the refinement form restarted at every i-slab (axis 0)
-    or k-slab (axis 1) (options sip_slabs, sip_slab_axis; interior
-    32 x 33 x 64: 4 FP32 block columns of 8 lines, 2 block rows of 32): both
-    solvers still meet the reference's exit test on the FP64 residual, within
-    the tolerance's reach of the FP64 solution, with the SIP over the whole
-    box and with the slabs."""
-    dims, sor = (36, 37, 68), 1e-6
+    or k-slab (axis 1) (options sip_slabs, sip_slab_axis; interior 32 or 30
+    x 33 x 64: 4 FP32 block columns of 8 lines, the last one partial in the
+    second case, whose mirrored backward blocks then start 2 lines outside
+    the box; 2 block rows of 32): both solvers still meet the reference's
+    exit test on the FP64 residual, within the tolerance's reach of the FP64
+    solution, with the SIP over the whole box and with the slabs."""
+    sor = 1e-6
     st = _state(oracle_mod, dims, 11, sor)
     st.set_field("res", np.zeros_like(st.field("res")))
     push(gpu_lib, st)
