@@ -91,8 +91,10 @@ struct Fast32 {
   float* e[E_NBUF] = {};
   float* fq = nullptr;   // forward factors, 4 components
   float* bq = nullptr;   // backward factors, 3 components
-  CUtensorMap map[E_NBUF];
+  CUtensorMap map[E_NBUF];       // boxes of the FP32 block shape (slabs)
   CUtensorMap map_fq, map_bq;
+  CUtensorMap wmap[E_NBUF];      // boxes of the FP64 block shape (SIP over the whole box)
+  CUtensorMap wmap_fq, wmap_bq;
   // warp-tile substitution engine (lanewave.cuh)
   CUtensorMap lmap_r, lmap_z, lmap_fq, lmap_bq;   // boxes of one tile
   int lnA = 0, lnC = 0, lntile = 0, lnt = 0;
@@ -327,6 +329,9 @@ int fast32_setup() {
   for (int q = 0; q < E_NBUF && !rc; ++q) rc = make_map32(&G.map[q], G.e[q], 1);
   if (!rc) rc = make_map32(&G.map_fq, G.fq, 4);
   if (!rc) rc = make_map32(&G.map_bq, G.bq, 3);
+  for (int q = 0; q < E_NBUF && !rc; ++q) rc = make_map(&G.wmap[q], G.e[q], 1, 4);
+  if (!rc) rc = make_map(&G.wmap_fq, G.fq, 4, 4);
+  if (!rc) rc = make_map(&G.wmap_bq, G.bq, 3, 4);
   // the warp-tile engine: tile boxes, topological tile order, mailboxes
   const int lbw = kLW + 4;
   if (!rc) rc = make_map_box(&G.lmap_r, G.e[E_R], 1, 4, lbw, kCW, kLG);
@@ -395,27 +400,6 @@ int fast32_setup() {
   return CAPPGPU_OK;
 }
 
-// the block shape of a wavefront operator: the FP32 ones of the refinement
-// form have their own
-template <class Op>
-struct WaveShape {
-  static constexpr int a = BA, c = BC;
-  static constexpr bool fp32 = false;
-};
-template <class Op>
-struct WaveShape32 {
-  static constexpr int a = BA32, c = BC32;
-  static constexpr bool fp32 = true;
-};
-template <>
-struct WaveShape<SipFwdF> : WaveShape32<SipFwdF> {};
-template <>
-struct WaveShape<SipBwdF> : WaveShape32<SipBwdF> {};
-template <>
-struct WaveShape<SipFactorF> : WaveShape32<SipFactorF> {};
-template <>
-struct WaveShape<SipBwdDotF> : WaveShape32<SipBwdDotF> {};
-
 WaveCtl next_ctl(bool fp32 = false) {
   WaveCtl w;
   w.ticket = F.ticket;
@@ -457,26 +441,44 @@ int2 slab_blocks() {
   return make_int2(0, 0);
 }
 
-template <class Op, bool BWD>
-int run_wave(const Op& op, const int* skip = nullptr, int2 slab = make_int2(0, 0)) {
+// a wavefront launch on the FP64 block shape (SH 0) or the FP32 one (SH 1)
+template <class Op, bool BWD, int SH>
+int run_wave_sh(const Op& op, const int* skip, int2 slab) {
   Ctx& c = ctx();
-  using S = WaveShape<Op>;
-  constexpr size_t smem = wave_smem_bytes<Op, S::a, S::c>();
+  constexpr int A = SH ? BA32 : BA, C = SH ? BC32 : BC;
+  constexpr size_t smem = wave_smem_bytes<Op, A, C>();
   static bool attr_set = false;   // once per process (one device per context)
   if (!attr_set) {
-    CAP_CUDA(cudaFuncSetAttribute(k_wave<Op, S::a, S::c, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CAP_CUDA(cudaFuncSetAttribute(k_wave<Op, A, C, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set = true;
   }
-  WaveCtl w = next_ctl(S::fp32);
+  WaveCtl w = next_ctl(SH == 1);
   w.skip = skip;
   w.slabBA = slab.x;
   w.slabBC = slab.y;
   // slabs along a: the mirrored blocks end where the forward ones do (the
   // FP32 ops' ghost states are zero, as the mirror offset requires)
-  if (S::fp32 && slab.x > 0) w.mirrorA = F.nBA32 * BA32;
-  launch_smem(k_wave<Op, S::a, S::c, BWD>, w.nblk, wave_threads<Op, S::a, S::c>(), smem, c.st, op, F.g, w);
+  if (SH == 1 && slab.x > 0) w.mirrorA = F.nBA32 * BA32;
+  launch_smem(k_wave<Op, A, C, BWD>, w.nblk, wave_threads<Op, A, C>(), smem, c.st, op, F.g, w);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
+}
+
+template <class Op, bool BWD>
+int run_wave(const Op& op, const int* skip = nullptr) {
+  return run_wave_sh<Op, BWD, 0>(op, skip, make_int2(0, 0));
+}
+
+// The FP32 ops of the refinement form: with slabs on the FP32 block shape
+// (narrow along a, deep along c), over the whole box on the FP64 one (the
+// deep blocks lose there: 82 against 44 ms for the last pressure solve of
+// a 124^3 channel step); maps[0] and maps[1] are the op's tensor maps for
+// the two shapes.
+template <class Op, bool BWD>
+int run_wave32(Op op, const CUtensorMap* const maps[2], const int* skip, int2 slab) {
+  const bool sh32 = slab.x > 0 || slab.y > 0;
+  for (int m = 0; m < Op::kMaps; ++m) op.map[m] = maps[sh32 ? 1 : 0][m];
+  return sh32 ? run_wave_sh<Op, BWD, 1>(op, skip, slab) : run_wave_sh<Op, BWD, 0>(op, skip, slab);
 }
 
 LaneCtl lane_ctl(const int* skip) {
@@ -562,13 +564,24 @@ int fp32_forward(const int* skip) {
     return run_lane<LaneFwdF, false>(op, skip);
   }
   SipFwdF fwd;
-  fwd.map[0] = G.map[E_R];
-  fwd.map[1] = G.map_fq;
   fwd.z = G.e[E_Z];
-  return run_wave<SipFwdF, false>(fwd, skip, slab_blocks());
+  const CUtensorMap w64[2] = {G.wmap[E_R], G.wmap_fq}, w32[2] = {G.map[E_R], G.map_fq};
+  const CUtensorMap* const maps[2] = {w64, w32};
+  return run_wave32<SipFwdF, false>(fwd, maps, skip, slab_blocks());
 }
 
 int fp32_backward(const int* skip);
+
+// the FP32 SIP factorisation (maps: the FP32 copies of ae .. ap)
+int fp32_factor(const SipFactorF& op) {
+  CUtensorMap w64[7], w32[7];
+  for (int q = 0; q < 7; ++q) {
+    w64[q] = G.wmap[E_AE + q];
+    w32[q] = G.map[E_AE + q];
+  }
+  const CUtensorMap* const maps[2] = {w64, w32};
+  return run_wave32<SipFactorF, false>(op, maps, nullptr, slab_blocks());
+}
 
 // the backward substitution with sk = r.z fused (wavefront engine 0): the
 // partials of its blocks in F.wpart, their count returned in *nparts; the
@@ -577,12 +590,12 @@ int fp32_backward_dot(const int* skip, int* nparts) {
   *nparts = 0;
   if (ctx().lane_wave != 0 || !ctx().fused_dot) return fp32_backward(skip);
   SipBwdDotF bwd;
-  bwd.map[0] = G.map[E_Z];
-  bwd.map[1] = G.map_bq;
-  bwd.map[2] = G.map[E_R];
   bwd.z = G.e[E_Z];
-  *nparts = F.nblk32;
-  return run_wave<SipBwdDotF, true>(bwd, skip, slab_blocks());
+  const int2 slab = slab_blocks();
+  const CUtensorMap w64[3] = {G.wmap[E_Z], G.wmap_bq, G.wmap[E_R]}, w32[3] = {G.map[E_Z], G.map_bq, G.map[E_R]};
+  const CUtensorMap* const maps[2] = {w64, w32};
+  *nparts = slab.x > 0 || slab.y > 0 ? F.nblk32 : F.nblk;
+  return run_wave32<SipBwdDotF, true>(bwd, maps, skip, slab);
 }
 
 int fp32_backward(const int* skip) {
@@ -601,10 +614,10 @@ int fp32_backward(const int* skip) {
     return run_lane<LaneBwdF, true>(op, skip);
   }
   SipBwdF bwd;
-  bwd.map[0] = G.map[E_Z];
-  bwd.map[1] = G.map_bq;
   bwd.z = G.e[E_Z];
-  return run_wave<SipBwdF, true>(bwd, skip, slab_blocks());
+  const CUtensorMap w64[2] = {G.wmap[E_Z], G.wmap_bq}, w32[2] = {G.map[E_Z], G.map_bq};
+  const CUtensorMap* const maps[2] = {w64, w32};
+  return run_wave32<SipBwdF, true>(bwd, maps, skip, slab_blocks());
 }
 
 // ------------------------------------------------------ vector kernels (D)
@@ -1621,14 +1634,13 @@ int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
   CAP_CHECK_LAUNCH();
   {   // FP32 SIP factorisation
     SipFactorF op;
-    for (int q = 0; q < 7; ++q) op.map[q] = G.map[E_AE + q];
     op.bnn = c.f[CAP_BN];
     op.ben = c.f[CAP_BE];
     op.btn = c.f[CAP_BT];
     op.fq = G.fq;
     op.bq = G.bq;
     op.alfa = (float)P.alfa;
-    if ((rc = run_wave<SipFactorF, false>(op, nullptr, slab_blocks()))) return rc;
+    if ((rc = fp32_factor(op))) return rc;
   }
   const int ns = P.nsw[ifi - 1];
   double res1 = 0.0, rsm = 0.0;
@@ -1706,14 +1718,13 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
   CAP_CHECK_LAUNCH();
   {   // FP32 SIP factorisation
     SipFactorF op;
-    for (int q = 0; q < 7; ++q) op.map[q] = G.map[E_AE + q];
     op.bnn = c.f[CAP_BN];
     op.ben = c.f[CAP_BE];
     op.btn = c.f[CAP_BT];
     op.fq = G.fq;
     op.bq = G.bq;
     op.alfa = (float)P.alfa;
-    if ((rc = run_wave<SipFactorF, false>(op, nullptr, slab_blocks()))) return rc;
+    if ((rc = fp32_factor(op))) return rc;
   }
   const size_t nf = sizeof(float) * (size_t)g.size();
   int total = 0;
