@@ -275,6 +275,14 @@ __device__ __forceinline__ void free_edge(const EdgeProbe<St, kPW * E / 32>& P, 
 // names one (FP32 ops: one FP64 conversion per thread, not per cell -- on
 // GB300 each FP64 instruction, conversions included, holds its
 // sub-partition for 64 cycles), double otherwise
+// ops whose ghost (boundary) state is zero declare kZeroGhost; only their
+// mirrored launches may take a mirror extent (WaveCtl::mirrorA), and the
+// others compile without its checks
+template <class Op, class = void>
+struct ZeroGhost : std::false_type {};
+template <class Op>
+struct ZeroGhost<Op, std::void_t<decltype(Op::kZeroGhost)>> : std::bool_constant<Op::kZeroGhost> {};
+
 template <class Op, class = void>
 struct PartOf {
   using type = double;
@@ -335,7 +343,8 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
   const int ba = sm.blk[0], bc = sm.blk[1];
   // the extent a is mirrored about, the steps of the (virtual) box and the
   // range of virtual a inside the box
-  const int Mi = BWD && w.mirrorA > 0 ? w.mirrorA : g.Ni;
+  constexpr bool kMirror = BWD && ZeroGhost<Op>::value;
+  const int Mi = kMirror && w.mirrorA > 0 ? w.mirrorA : g.Ni;
   const int SV = Mi + g.Nj + g.Nk - 2;
   const int2 avr = make_int2(BWD ? Mi - g.Ni : 0, BWD ? Mi : g.Ni);
   const int s0 = ba * BA + bc * BC;
@@ -564,7 +573,7 @@ __global__ void __launch_bounds__(wave_threads<Op, BA, BC>(), 1) k_wave(const __
         const int rs = ring_slot(sg + ds - 1);
         // (the first line inside a mirrored box that starts inside the block
         // has no neighbour line before it: the op's zero ghost state)
-        const St W = av == avr.x && al > 0 ? St{} : *(al > 0 ? (odd ? rdW0 : rdW1) : &sm.ringW[rs][cl]);
+        const St W = kMirror && av == avr.x && al > 0 ? St{} : *(al > 0 ? (odd ? rdW0 : rdW1) : &sm.ringW[rs][cl]);
         const St B = *(cl > 0 ? (odd ? rdB0 : rdB1) : &sm.ringB[rs][al]);
         const St out = op.post(in, pv, g, x, W, B, part);
         *(odd ? wr1 : wr0) = out;
@@ -851,6 +860,7 @@ struct St3f { float bn, be, bt; };
 
 struct SipFwdF {
   using St = float;
+  static constexpr bool kZeroGhost = true;   // ghost() is zero: mirror extents allowed
   static constexpr int kMaps = 2;   // r, forward factors (bb, bw, bs, bp)
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 6;
@@ -877,6 +887,7 @@ struct SipFwdF {
 
 struct SipBwdF {
   using St = float;
+  static constexpr bool kZeroGhost = true;   // ghost() is zero: mirror extents allowed
   static constexpr int kMaps = 2;   // z, backward factors (bn, be, bt)
   static constexpr bool kReduce = false;
   static constexpr int kSlots = 6;
@@ -905,6 +916,7 @@ struct SipBwdF {
 // form; pcg-sip.f90:118), partials per block
 struct SipBwdDotF {
   using St = float;
+  static constexpr bool kZeroGhost = true;   // ghost() is zero: mirror extents allowed
   using Part = float;   // per-thread FP32 sum, as the vector pass forms it
   static constexpr int kMaps = 3;   // z, backward factors (bn, be, bt), r
   static constexpr bool kReduce = true;
