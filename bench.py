@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark: PISO time steps of the 128^3 channel on one GB300.
 
-Metric (the benchmark spec): PISO steps/s and the p'-solve time to a 1e-6
+Metric: PISO steps/s and the p'-solve time to a 1e-6
 relative residual.  A "step" is one PISO time step of main.f90:134-207:
 time-level shift, CourantNo.h, ghost-cell update, calcuvw (gradients,
 fluxuvw x3, wall terms, three sipsol solves), PISO_multiple_correction
