@@ -299,6 +299,10 @@ def run_gpu(args, ws, rank, local):
     fp64_peak = ops_rate / (ms_rate / 1e3)
     clocks = ClockSampler(local)
     launches0 = lib.stats().launches
+    # CUDA events around every SIP forward substitution of the timed steps
+    # (the roofline's kernel, timed inside the timed region)
+    lib.set_option("sweep_timing", 1)
+    lib.sweep_stats(reset=True)
     group.barrier()
     clocks.start()
     lib.timer_start()
@@ -306,6 +310,8 @@ def run_gpu(args, ws, rank, local):
     ms = lib.timer_stop()
     clk = clocks.stop()
     group.barrier()
+    sweep_ms, sweep_n = lib.sweep_stats(reset=True)
+    lib.set_option("sweep_timing", 0)
     launches = lib.stats().launches - launches0
     st = lib.stats()
     ref_state = result_state(lib)   # FP64 plain result of the timed steps
@@ -469,7 +475,8 @@ def run_gpu(args, ws, rank, local):
 
     # roofline of the SIP forward substitution on the current state
     peak, peak_kind = measured_peaks()
-    ms_fwd, bytes_fwd = lib.profile_kernel(0, reps=10)
+    ms_alone, bytes_fwd = lib.profile_kernel(0, reps=10)   # the same launch timed alone, for comparison
+    ms_fwd = sweep_ms / sweep_n if sweep_n else ms_alone
     achieved = bytes_fwd / (ms_fwd / 1e3) / 1e9
     units = {}
     for w, name in ((1, "sip_backward"), (2, "spmv_dot"), (6, "sip_factor"), (3, "grad_gauss"),
@@ -500,7 +507,10 @@ def run_gpu(args, ws, rank, local):
         "roofline": {"bound": "hbm", "kernel": "SIP forward substitution (pcg-sip.f90:98-106)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": profiled_traffic(args.n),
-                     "algorithmic_bytes": bytes_fwd, "ms_per_launch": ms_fwd, "fp64_issue": fp64},
+                     "algorithmic_bytes": bytes_fwd, "ms_per_launch": ms_fwd,
+                     "timed": (f"CUDA events around each of the {sweep_n} pcgsip forward substitutions of the "
+                               f"timed steps" if sweep_n else "the launch timed alone"),
+                     "ms_per_launch_alone": ms_alone, "fp64_issue": fp64},
         "units": units,
         "fp32_refined": fp32,
         "fp32_learned": learned,

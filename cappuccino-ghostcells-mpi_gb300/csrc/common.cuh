@@ -89,6 +89,13 @@ struct Ctx {
   double p_solve_ms = 0.0;             // last PISO/SIMPLE pressure solve
   cappgpu_solve_report p_rep{};        // its report
   cudaEvent_t ev[4] = {};
+  // option sweep_timing: CUDA events around the FP64 pcgsip forward sweeps
+  // (one pair per iteration of a batch), their durations summed at the
+  // batch's host read (cappgpu_sweep_stats)
+  int sweep_timing = 0;
+  cudaEvent_t sw_ev[2 * 64] = {};
+  double sw_ms = 0.0;
+  long long sw_n = 0;
   int wave_impl = 1;                   // 1 persistent wavefront, 0 one launch per hyperplane
   int fused_dot = 1;                   // FP32 CG (wavefront 0): sk = r.z in the backward substitution
   int lane_wave = 0;                   // FP32 substitutions: 0 the wavefront of wave.cuh, 1 the warp-tile engine

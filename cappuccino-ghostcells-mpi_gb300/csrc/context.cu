@@ -117,6 +117,7 @@ static void free_all() {
   if (c.wf_flags) cudaFree(c.wf_flags);
   if (c.vec3buf) cudaFree(c.vec3buf);
   for (auto& e : c.ev) { if (e) cudaEventDestroy(e); e = nullptr; }
+  for (auto& e : c.sw_ev) { if (e) cudaEventDestroy(e); e = nullptr; }
   if (c.st) cudaStreamDestroy(c.st);
   c = Ctx();
 }
@@ -310,6 +311,13 @@ int cappgpu_set_option(const char* key, int value) {
   }
   if (strcmp(key, "learn_conv") == 0 && value >= 0 && value <= 2) return learned_set_conv(value);
   if (strcmp(key, "learn_loss") == 0 && value >= 0 && value <= 2) return learned_set_loss(value);
+  if (strcmp(key, "sweep_timing") == 0 && (value == 0 || value == 1)) {
+    Ctx& c = ctx();
+    if (value && !c.sw_ev[0])
+      for (auto& e : c.sw_ev) CAP_CUDA(cudaEventCreate(&e));
+    c.sweep_timing = value;
+    return CAPPGPU_OK;
+  }
   if (strcmp(key, "fused_dot") == 0 && (value == 0 || value == 1)) {
     ctx().fused_dot = value;
     return CAPPGPU_OK;

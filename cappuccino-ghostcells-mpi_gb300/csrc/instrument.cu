@@ -70,6 +70,18 @@ int cappgpu_timer_stop(double* ms) {
   return CAPPGPU_OK;
 }
 
+int cappgpu_sweep_stats(double* ms_total, long long* launches, int reset) {
+  CAP_REQUIRE_INIT();
+  Ctx& c = ctx();
+  if (ms_total) *ms_total = c.sw_ms;
+  if (launches) *launches = c.sw_n;
+  if (reset) {
+    c.sw_ms = 0.0;
+    c.sw_n = 0;
+  }
+  return CAPPGPU_OK;
+}
+
 int cappgpu_get_stats(cappgpu_stats* s) {
   CAP_REQUIRE_INIT();
   if (!s) return CAPPGPU_E_ARG;

@@ -1319,8 +1319,11 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   for (int launched = 0; launched < ns;) {
     // a batch of iterations; those after the exit test return at once
     const int batch = ns - launched < c.cg_batch ? ns - launched : c.cg_batch;
+    const bool timed = c.sweep_timing && c.sw_ev[0];
     for (int q = 0; q < batch; ++q) {
+      if (timed) CAP_CUDA(cudaEventRecord(c.sw_ev[2 * q], c.st));
       if ((rc = run_wave<SipFwdD, false>(fwd, F.ctl))) return rc;
+      if (timed) CAP_CUDA(cudaEventRecord(c.sw_ev[2 * q + 1], c.st));
       if ((rc = run_wave<SipBwdD, true>(bwd, F.ctl))) return rc;
       double* pko = F.d[cur ? D_PK1 : D_PK0];
       double* pkn = F.d[cur ? D_PK0 : D_PK1];
@@ -1337,8 +1340,19 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
     }
     launched += batch;
     CAP_CUDA(cudaMemcpyAsync(F.hstat, F.ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, c.st));
+    const int it_before = hctl[1];
     if ((rc = sync_status())) return rc;
     for (int q = 0; q < 4; ++q) hctl[q] = F.hstat[q];
+    if (timed) {
+      // the sweeps of iterations up to the exit test ran; later ones returned at once
+      const int real = std::min(batch, hctl[1] - it_before);
+      for (int q = 0; q < real; ++q) {
+        float f = 0.f;
+        CAP_CUDA(cudaEventElapsedTime(&f, c.sw_ev[2 * q], c.sw_ev[2 * q + 1]));
+        c.sw_ms += f;
+        ++c.sw_n;
+      }
+    }
     if (hctl[0]) break;
   }
   CAP_CUDA(cudaMemcpy(F.hres, c.dscal + 5, sizeof(double), cudaMemcpyDeviceToHost));

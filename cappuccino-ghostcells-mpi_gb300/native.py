@@ -75,6 +75,7 @@ SIGNATURES = {
                                  ctypes.POINTER(ctypes.c_float), _INT, _INT, _INT, ctypes.POINTER(ctypes.c_float),
                                  ctypes.POINTER(ctypes.c_float), _DP],
     "cappgpu_learn_sample": [_INT, ctypes.POINTER(ctypes.c_float), ctypes.c_longlong],
+    "cappgpu_sweep_stats": [_DP, ctypes.POINTER(ctypes.c_longlong), _INT],
     "cappgpu_fluxuvw": [_INT] * 10,
     "cappgpu_calcuvw": [_REP],
     "cappgpu_piso_assemble_pressure_eq": [_INT] * 12,
@@ -349,6 +350,14 @@ class Library:
                                                       ctypes.byref(loss)),
                     "learn_check")
         return out, grad, loss.value
+
+    def sweep_stats(self, reset=True):
+        """(summed ms, count) of the FP64 pcgsip forward substitutions timed
+        with option sweep_timing since the last reset."""
+        ms, n = ctypes.c_double(), ctypes.c_longlong()
+        self._check(self.lib.cappgpu_sweep_stats(ctypes.byref(ms), ctypes.byref(n), 1 if reset else 0),
+                    "sweep_stats")
+        return ms.value, n.value
 
     def learn_sample(self, index, shape):
         """Recorded pair `index` as (9, *shape) float32 planes: r^, A^ (xp, xm,

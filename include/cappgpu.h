@@ -225,6 +225,8 @@ int cappgpu_find_intersection_point(const double* p, double* out);
    within 1e-5 (velocity components) of the FP64 form over 20 steps of the
    128^3 channel; parts 4 and 16 change the FP64 system the refinement
    solves and are off by default.
+   "sweep_timing": 1 = CUDA events around every FP64 pcgsip forward
+   substitution (read by cappgpu_sweep_stats; default 0).
    "fused_dot": 1 = the FP32 CG of precision modes 1-2 forms sk = r.z in the
    backward substitution (wavefront engine 0, default); 0 = in a vector
    pass after it, as the other engines do (the same sum in another order).
@@ -568,6 +570,12 @@ typedef struct cappgpu_stats {
 
 /* CUDA events on the library's stream around a region of calls. */
 int cappgpu_timer_start(void);
+/* With option "sweep_timing" 1: the summed duration (CUDA events on the
+   library's stream) and count of the FP64 pcgsip forward SIP substitutions
+   that ran since the last reset (those of iterations after the exit test,
+   which return at once, are not counted); reset != 0 zeroes both after
+   reading. */
+int cappgpu_sweep_stats(double* ms_total, long long* launches, int reset);
 int cappgpu_timer_stop(double* ms);
 int cappgpu_get_stats(cappgpu_stats* s);
 /* Page-locked host buffers (for host<->device copies at full speed). */

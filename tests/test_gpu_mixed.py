@@ -316,6 +316,33 @@ def test_fp32_gradient_from_cached_fp32_geometry(gpu_lib, make):
     gpu_lib.set_field("vol", vol)
 
 
+@pytest.mark.parametrize("batch", [1, 4, 7])
+def test_sweep_timing_counts_the_forward_substitutions(gpu_lib, oracle_mod, batch):
+    """Option sweep_timing: CUDA events around every FP64 pcgsip forward
+    substitution; one per iteration that ran (the launches after the exit
+    test, which return at once, are not counted), whatever the batch, and
+    the same solution as without the events."""
+    st = _state(oracle_mod, (40, 37, 35), 9, 1e-6)
+    st.set_field("res", np.zeros_like(st.field("res")))
+    push(gpu_lib, st)
+    r0 = gpu_lib.pcgsip("p", IP)
+    p0 = gpu_lib.get_field("p")
+    push(gpu_lib, st)
+    gpu_lib.set_option("cg_batch", batch)
+    gpu_lib.set_option("sweep_timing", 1)
+    try:
+        gpu_lib.sweep_stats(reset=True)
+        r1 = gpu_lib.pcgsip("p", IP)
+        ms, n = gpu_lib.sweep_stats(reset=True)
+    finally:
+        gpu_lib.set_option("sweep_timing", 0)
+        gpu_lib.set_option("cg_batch", 4)
+    assert r1.iters == r0.iters and r1.resl == r0.resl
+    np.testing.assert_array_equal(gpu_lib.get_field("p"), p0)
+    assert n == r1.iters and ms > 0.0
+    assert gpu_lib.sweep_stats() == (0.0, 0)
+
+
 @pytest.mark.parametrize("dims", [(14, 13, 12), (40, 37, 68), (104, 23, 71)])
 def test_fused_dot_in_the_backward_substitution(gpu_lib, oracle_mod, dims):
     """sk = r.z formed in the FP32 backward substitution (option fused_dot,
