@@ -5,9 +5,12 @@
 // maps built here once per grid.
 //
 // Arithmetic per cell is the reference's; the scalars alpha, beta and the
-// norms come from deterministic device reductions and stay on the device
-// (the host reads one residual norm per iteration for the convergence
-// test, as the reference evaluates rsm < resmax).
+// norms come from deterministic device reductions and stay on the device,
+// where the last block of each update pass applies the reference's exit
+// test; the host reads the test's flag once per batch of iterations
+// (option cg_batch).  The same file holds the FP32 refinement forms of
+// pcgsip and sipsol (precision modes 1-2: FP32 SIP, block-local per slab,
+// inside FP64 iterative refinement), cgstab_sip and iccg on the same engine.
 #include <cuda.h>
 #include <math.h>
 #include <string.h>

@@ -38,6 +38,16 @@
 //
 // Backward recurrences (successors i+1, j+1, k+1) run the same engine in
 // mirrored coordinates.
+//
+// Block-local recurrences (the FP32 preconditioner of the refinement form):
+// WaveCtl::slabBA / slabBC restart the recurrence every so many blocks
+// along a / c -- a slab's first line or row takes zero states, no block
+// waits on or writes the mailbox across the boundary, and the slabs'
+// wavefronts run side by side.  For slabs along a the mirrored blocks are
+// mirrored about whole blocks (WaveCtl::mirrorA) so that they end where the
+// forward blocks do; ops allow this only with zero ghost states
+// (Op::kZeroGhost).  Ops may also reduce a per-cell quantity (Op::kReduce,
+// accumulated per thread in Op::Part, one partial per block).
 #pragma once
 #include <cuda.h>
 
