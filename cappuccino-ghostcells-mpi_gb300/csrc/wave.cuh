@@ -281,10 +281,6 @@ __device__ __forceinline__ void free_edge(const EdgeProbe<St, kPW * E / 32>& P, 
   }
 }
 
-// the type a thread accumulates the op's reduction in: Op::Part where the op
-// names one (FP32 ops: one FP64 conversion per thread, not per cell -- on
-// GB300 each FP64 instruction, conversions included, holds its
-// sub-partition for 64 cycles), double otherwise
 // ops whose ghost (boundary) state is zero declare kZeroGhost; only their
 // mirrored launches may take a mirror extent (WaveCtl::mirrorA), and the
 // others compile without its checks
@@ -293,6 +289,10 @@ struct ZeroGhost : std::false_type {};
 template <class Op>
 struct ZeroGhost<Op, std::void_t<decltype(Op::kZeroGhost)>> : std::bool_constant<Op::kZeroGhost> {};
 
+// the type a thread accumulates the op's reduction in: Op::Part where the op
+// names one (FP32 ops: one FP64 conversion per thread, not per cell -- on
+// GB300 each FP64 instruction, conversions included, holds its
+// sub-partition for 64 cycles), double otherwise
 template <class Op, class = void>
 struct PartOf {
   using type = double;
