@@ -928,6 +928,10 @@ __global__ void k_set_scal(double* scal, double v0) { scal[0] = v0; }
 // sipsol residual (sipsol.f90:66-69) in the hyperplane layout: fi of
 // interior neighbours from the hyperplane copy, of ghost neighbours from the
 // module array; partial sum |res|.
+// FMA: the residual of the refinement form's restarts, with fused multiply-
+// adds (8 FP64 instructions per cell instead of 15; GB300 holds each for 64
+// cycles): not the reference's rounding, which only the FP64 sipsol keeps
+template <bool FMA>
 __global__ void k_resid_d(DG g, const double* __restrict__ ae, const double* __restrict__ aw,
                           const double* __restrict__ an, const double* __restrict__ as,
                           const double* __restrict__ at, const double* __restrict__ ab,
@@ -944,8 +948,13 @@ __global__ void k_resid_d(DG g, const double* __restrict__ ae, const double* __r
     const double fS = b > 0 ? fid[P - g.plane] : fin[n - 1];
     const double fT = c + 1 < g.Nk ? fid[P + g.plane + g.P] : fin[n + g.nij];
     const double fB = c > 0 ? fid[P - g.plane - g.P] : fin[n - g.nij];
-    const double r = ae[P] * fE + aw[P] * fW + an[P] * fN + as[P] * fS + at[P] * fT + ab[P] * fB + su[P] -
-                     ap[P] * fid[P];
+    double r;
+    if constexpr (FMA) {
+      r = fma(ae[P], fE, fma(aw[P], fW, fma(an[P], fN, fma(as[P], fS, fma(at[P], fT, fma(ab[P], fB,
+              fma(-ap[P], fid[P], su[P])))))));
+    } else {
+      r = ae[P] * fE + aw[P] * fW + an[P] * fN + as[P] * fS + at[P] * fT + ab[P] * fB + su[P] - ap[P] * fid[P];
+    }
     res[P] = r;
     v[0] += fabs(r);
   });
@@ -1595,7 +1604,7 @@ int sipsol_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   int n;
   bool done = false;
   for (n = 1; n <= ns; ++n) {
-    launch(k_resid_d, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
+    launch(k_resid_d<false>, kRedBlocks, kThreads, c.st, F.g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
            (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
            (const double*)F.d[D_AP], (const double*)F.d[D_SU], (const double*)F.d[D_FI], (const double*)c.f[fif],
            F.d[D_RES], c.partials);
@@ -1664,7 +1673,7 @@ int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
   int n;
   bool done = false;
   for (n = 1; n <= ns; ++n) {
-    launch(k_resid_d, kRedBlocks, kThreads, c.st, g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
+    launch(k_resid_d<true>, kRedBlocks, kThreads, c.st, g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
            (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
            (const double*)F.d[D_AP], (const double*)F.d[D_SU], (const double*)F.d[D_FI], (const double*)c.f[fif],
            F.d[D_RES], c.partials);
@@ -1749,7 +1758,7 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
   bool done = false, bad = false;
   for (int outer = 0; outer < 64; ++outer) {
     // FP64 residual of the current iterate and its L1 norm
-    launch(k_resid_d, kRedBlocks, kThreads, c.st, g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
+    launch(k_resid_d<true>, kRedBlocks, kThreads, c.st, g, (const double*)F.d[D_AE], (const double*)F.d[D_AW],
            (const double*)F.d[D_AN], (const double*)F.d[D_AS], (const double*)F.d[D_AT], (const double*)F.d[D_AB],
            (const double*)F.d[D_AP], (const double*)F.d[D_SU], (const double*)F.d[D_FI], (const double*)c.f[fif],
            F.d[D_RES], c.partials);
