@@ -47,3 +47,16 @@ def test_calls_without_init_fail_cleanly():
         lib.dims = (8, 8, 8)
         lib.get_field("u")
     assert lib.lib.cappgpu_ijkpr() < 0
+
+
+def test_every_run_time_option_is_documented():
+    """Every key cappgpu_set_option accepts (csrc/context.cu) is described
+    in the header, and the header names no key the library refuses."""
+    src = (ROOT / "cappuccino-ghostcells-mpi_gb300" / "csrc" / "context.cu").read_text()
+    accepted = set(re.findall(r'strcmp\(key, "(\w+)"\)', src))
+    assert {"sip_slabs", "fused_dot", "sweep_timing", "learn_loss"} <= accepted
+    doc = HEADER.read_text()
+    i = doc.index("cappgpu_set_option")
+    documented = set(re.findall(r'"(\w+)":', doc[doc.rfind("/*", 0, i):i]))
+    assert accepted - documented == set(), accepted - documented
+    assert documented - accepted == set(), documented - accepted
