@@ -189,6 +189,46 @@ __global__ void k_nat_to_d(DG g, const double* __restrict__ src, T* __restrict__
   }
 }
 
+// natural -> diagonal copies of up to kConvMax fields in one launch, and
+// FP32 copies of those with a non-null dst32.  A block transposes a 32 x 32
+// (a, b) tile of one c-plane through shared memory: it reads the tile along
+// b (contiguous in the natural layout) and writes it by anti-diagonals
+// a + b = const, each a contiguous run of one hyperplane row -- the
+// one-thread-per-cell copy above reads coalesced but writes every element
+// one hyperplane apart.  Grid: (ceil(Ni/32), ceil(Nj/32), Nk), 256 threads.
+constexpr int kConvMax = 9;
+struct ConvList {
+  const double* src[kConvMax];
+  double* dst[kConvMax];    // null: no FP64 copy
+  float* dst32[kConvMax];   // null: no FP32 copy
+  int n;
+};
+
+static __global__ void __launch_bounds__(256) k_nat_to_d_tiles(DG g, ConvList L) {
+  __shared__ double tile[32][34];   // row pitch 34: the anti-diagonal reads fall in distinct banks
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int a0 = blockIdx.x * 32, b0 = blockIdx.y * 32, c = blockIdx.z;
+  for (int q = 0; q < L.n; ++q) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = ty + 8 * k, a = a0 + i, b = b0 + tx;
+      if (a < g.Ni && b < g.Nj) tile[i][tx] = L.src[q][g.nat(a, b, c)];
+    }
+    __syncthreads();
+    for (int m = ty; m < 63; m += 8) {   // anti-diagonal i + j = m of the tile
+      const int i = (m > 31 ? m - 31 : 0) + tx, j = m - i;
+      const int a = a0 + i, b = b0 + j;
+      if (i <= (m < 31 ? m : 31) && a < g.Ni && b < g.Nj) {
+        const double v = tile[i][j];
+        const long long d = g.d(a, b, c);
+        if (L.dst[q]) L.dst[q][d] = v;
+        if (L.dst32[q]) L.dst32[q][d] = (float)v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // diagonal -> natural for the interior box
 template <typename T>
 __global__ void k_d_to_nat(DG g, const T* __restrict__ src, double* __restrict__ dst) {

@@ -1249,18 +1249,28 @@ static int factor_wave() {
   return run_wave<SipFactorD, false>(op);
 }
 
-static int to_d(int field, int dbuf) {
-  Ctx& c = ctx();
-  launch(k_nat_to_d<double>, grid_for((long long)F.g.Ni * F.g.Nj * F.g.Nk), kThreads, c.st, F.g,
-         (const double*)c.f[field], F.d[dbuf]);
-  CAP_CHECK_LAUNCH();
-  return CAPPGPU_OK;
-}
-
 static int from_d(int dbuf, int field) {
   Ctx& c = ctx();
   launch(k_d_to_nat<double>, grid_for((long long)F.g.Ni * F.g.Nj * F.g.Nk), kThreads, c.st, F.g,
          (const double*)F.d[dbuf], c.f[field]);
+  CAP_CHECK_LAUNCH();
+  return CAPPGPU_OK;
+}
+
+// natural -> hyperplane copies of n fields into the buffers dbufs[], in one
+// launch of tiled transposes; f32[q] (may be null) also receives an FP32
+// copy of field q
+static int to_d_multi(const int* fields, const int* dbufs, float* const* f32, int n) {
+  Ctx& c = ctx();
+  ConvList L{};
+  L.n = n;
+  for (int q = 0; q < n; ++q) {
+    L.src[q] = c.f[fields[q]];
+    L.dst[q] = F.d[dbufs[q]];
+    L.dst32[q] = f32 ? f32[q] : nullptr;
+  }
+  const dim3 grid((unsigned)((F.g.Ni + 31) / 32), (unsigned)((F.g.Nj + 31) / 32), (unsigned)F.g.Nk);
+  launch(k_nat_to_d_tiles, grid, 256, c.st, F.g, L);
   CAP_CHECK_LAUNCH();
   return CAPPGPU_OK;
 }
@@ -1309,11 +1319,11 @@ int pcgsip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   double res0 = 0.0;
   if ((rc = resid_natural(fif, &res0))) return rc;
   // hyperplane copies of the matrix, residual and solution
-  const int cf[7] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP};
-  for (int q = 0; q < 7; ++q)
-    if ((rc = to_d(cf[q], D_AE + q))) return rc;
-  if ((rc = to_d(CAP_RES, D_RES))) return rc;
-  if ((rc = to_d(fif, D_FI))) return rc;
+  {
+    const int fields[9] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_RES, fif};
+    const int dbufs[9] = {D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_RES, D_FI};
+    if ((rc = to_d_multi(fields, dbufs, nullptr, 9))) return rc;
+  }
   const size_t nb = sizeof(double) * (size_t)F.g.size();
   CAP_CUDA(cudaMemsetAsync(F.d[D_PK0], 0, nb, c.st));   // pk = 0 (pcg-sip.f90:42)
   CAP_CUDA(cudaMemsetAsync(F.d[D_Z], 0, nb, c.st));     // zk = 0 (pcg-sip.f90:43)
@@ -1405,11 +1415,11 @@ int cgstab_sip_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   // res over the box and res0 (cgstab_sip.f90:45-57)
   double res0 = 0.0;
   if ((rc = resid_natural_k(fif, 2, d.nkm, &res0))) return rc;
-  const int cf[7] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP};
-  for (int q = 0; q < 7; ++q)
-    if ((rc = to_d(cf[q], D_AE + q))) return rc;
-  if ((rc = to_d(CAP_RES, D_RES))) return rc;
-  if ((rc = to_d(fif, D_FI))) return rc;
+  {
+    const int fields[9] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_RES, fif};
+    const int dbufs[9] = {D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_RES, D_FI};
+    if ((rc = to_d_multi(fields, dbufs, nullptr, 9))) return rc;
+  }
   // reso = res; pk = uk = zk = vk = 0 (cgstab_sip.f90:83-94); reso in D_SU,
   // pk in D_PK0, uk in D_ZZ, vk in D_PK1
   const size_t nb = sizeof(double) * (size_t)F.g.size();
@@ -1498,11 +1508,11 @@ int iccg_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   CAP_CUDA(cudaMemsetAsync(c.f[CAP_RES], 0, sizeof(double) * d.nijk, c.st));
   double res0 = 0.0;
   if ((rc = resid_natural_k(fif, 2, d.nkm, &res0))) return rc;
-  const int cf[7] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP};
-  for (int q = 0; q < 7; ++q)
-    if ((rc = to_d(cf[q], D_AE + q))) return rc;
-  if ((rc = to_d(CAP_RES, D_RES))) return rc;
-  if ((rc = to_d(fif, D_FI))) return rc;
+  {
+    const int fields[9] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_RES, fif};
+    const int dbufs[9] = {D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_RES, D_FI};
+    if ((rc = to_d_multi(fields, dbufs, nullptr, 9))) return rc;
+  }
   // pk = zk = d = 0; d in D_SU
   const size_t nb = sizeof(double) * (size_t)F.g.size();
   for (int q : {D_PK0, D_Z, D_SU}) CAP_CUDA(cudaMemsetAsync(F.d[q], 0, nb, c.st));
@@ -1590,10 +1600,11 @@ int sipsol_fast(int fif, int ifi, cappgpu_solve_report* rep) {
   int rc = fast_setup();
   if (rc) return rc;
   CAP_CUDA(cudaMemsetAsync(F.flags, 0, sizeof(int) * 2, c.st));
-  const int cf[8] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_SU};
-  for (int q = 0; q < 8; ++q)
-    if ((rc = to_d(cf[q], D_AE + q))) return rc;
-  if ((rc = to_d(fif, D_FI))) return rc;
+  {
+    const int fields[9] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_SU, fif};
+    const int dbufs[9] = {D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_SU, D_FI};
+    if ((rc = to_d_multi(fields, dbufs, nullptr, 9))) return rc;
+  }
   // RES is not cleared by sipsol: its interior is rewritten each sweep, its
   // ghost layers keep whatever earlier routines left there
   if ((rc = factor_wave())) return rc;
@@ -1650,14 +1661,14 @@ int sipsol_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
   if (rc) return rc;
   if ((rc = fast32_setup())) return rc;
   CAP_CUDA(cudaMemsetAsync(F.flags, 0, sizeof(int) * 2, c.st));
-  const int cf[8] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_SU};
-  for (int q = 0; q < 8; ++q)
-    if ((rc = to_d(cf[q], D_AE + q))) return rc;
-  if ((rc = to_d(fif, D_FI))) return rc;
+  {   // FP64 hyperplane copies, and FP32 ones of the coefficients
+    const int fields[9] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_SU, fif};
+    const int dbufs[9] = {D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_SU, D_FI};
+    float* const f32[9] = {G.e[E_AE], G.e[E_AW], G.e[E_AN], G.e[E_AS], G.e[E_AT], G.e[E_AB], G.e[E_AP], nullptr,
+                           nullptr};
+    if ((rc = to_d_multi(fields, dbufs, f32, 9))) return rc;
+  }
   const DG& g = F.g;
-  for (int q = 0; q < 7; ++q)
-    launch(k_d_to_f, grid_for(g.ncell / 4), kThreads, c.st, g, (const double*)F.d[D_AE + q], G.e[E_AE + q]);
-  CAP_CHECK_LAUNCH();
   {   // FP32 SIP factorisation
     SipFactorF op;
     op.bnn = c.f[CAP_BN];
@@ -1734,14 +1745,14 @@ int pcgsip_mixed(int fif, int ifi, cappgpu_solve_report* rep) {
   // kept only if it lowers the FP64 residual (the exit test below stays
   // relative to res0)
   if ((rc = learned_solve_start(fif, res0))) return rc;
-  const int cf[8] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_SU};
-  for (int q = 0; q < 8; ++q)
-    if ((rc = to_d(cf[q], D_AE + q))) return rc;
-  if ((rc = to_d(fif, D_FI))) return rc;
+  {   // FP64 hyperplane copies, and FP32 ones of the coefficients
+    const int fields[9] = {CAP_AE, CAP_AW, CAP_AN, CAP_AS, CAP_AT, CAP_AB, CAP_AP, CAP_SU, fif};
+    const int dbufs[9] = {D_AE, D_AW, D_AN, D_AS, D_AT, D_AB, D_AP, D_SU, D_FI};
+    float* const f32[9] = {G.e[E_AE], G.e[E_AW], G.e[E_AN], G.e[E_AS], G.e[E_AT], G.e[E_AB], G.e[E_AP], nullptr,
+                           nullptr};
+    if ((rc = to_d_multi(fields, dbufs, f32, 9))) return rc;
+  }
   const DG& g = F.g;
-  for (int q = 0; q < 7; ++q)
-    launch(k_d_to_f, grid_for(g.ncell / 4), kThreads, c.st, g, (const double*)F.d[D_AE + q], G.e[E_AE + q]);
-  CAP_CHECK_LAUNCH();
   {   // FP32 SIP factorisation
     SipFactorF op;
     op.bnn = c.f[CAP_BN];
