@@ -580,14 +580,7 @@ SOLVER_ENTRY(pcgsip, CAPPGPU_SOLVER_PCGSIP)
 SOLVER_ENTRY(iccg, CAPPGPU_SOLVER_ICCG)
 SOLVER_ENTRY(cgstab, CAPPGPU_SOLVER_CGSTAB)
 SOLVER_ENTRY(cgstab_sip, CAPPGPU_SOLVER_CGSTAB_SIP)
-
-int cappgpu_dpcg(int fi, int ifi, cappgpu_solve_report* rep) {
-  int rc = check_solver_args(fi, ifi);
-  if (rc) return rc;
-  rc = dpcg(fi, ifi, rep);
-  CAP_CUDA(cudaStreamSynchronize(ctx().st));
-  return rc;
-}
+SOLVER_ENTRY(dpcg, CAPPGPU_SOLVER_DPCG)
 
 int cappgpu_spmv(int pk, int zk, double* dot) {
   CAP_REQUIRE_INIT();

@@ -185,6 +185,11 @@ module cappgpu
       real(c_double), intent(inout) :: fi(*)
       integer(c_int), value :: ifi
     end function
+    integer(c_int) function cappgpu_dpcg_h(fi, ifi) bind(c, name="cappgpu_dpcg_h")
+      import :: c_int, c_double
+      real(c_double), intent(inout) :: fi(*)
+      integer(c_int), value :: ifi
+    end function
     integer(c_int) function cappgpu_last_report(solver, ifi, rep) bind(c, name="cappgpu_last_report")
       import :: c_int, cappgpu_solve_report
       integer(c_int), intent(out) :: solver, ifi
@@ -539,6 +544,18 @@ subroutine cgstab_sip(fi, ifi)
   real(prec), dimension(nxyza) :: fi
   call cappgpu_push_params()
   call run_solver(cappgpu_cgstab_sip_h(fi, int(ifi, c_int)), 'cgstab_sip')
+end subroutine
+
+! pcg-jacobi.f90:3-155
+subroutine Diagonally_Preconditioned_CG(fi, ifi)
+  use types
+  use parameters
+  use cappgpu
+  implicit none
+  integer, intent(in) :: ifi
+  real(prec), dimension(nxyza) :: fi
+  call cappgpu_push_params()
+  call run_solver(cappgpu_dpcg_h(fi, int(ifi, c_int)), 'dpcg')
 end subroutine
 
 ! GRAD_GAUSS.f90:1-105 (the gfortran temporaries of gradu(1,:) sections

@@ -56,6 +56,7 @@ SIGNATURES = {
     "cappgpu_iccg_h": [_DP, _INT],
     "cappgpu_cgstab_h": [_DP, _INT],
     "cappgpu_cgstab_sip_h": [_DP, _INT],
+    "cappgpu_dpcg_h": [_DP, _INT],
     "cappgpu_spmv": [_INT, _INT, _DP],
     "cappgpu_spmv_noalloc": [_INT, _INT, _DP],
     "cappgpu_precision": [_INT],

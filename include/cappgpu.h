@@ -438,6 +438,7 @@ int cappgpu_pcgsip_h(double* fi, int ifi);
 int cappgpu_iccg_h(double* fi, int ifi);
 int cappgpu_cgstab_h(double* fi, int ifi);
 int cappgpu_cgstab_sip_h(double* fi, int ifi);
+int cappgpu_dpcg_h(double* fi, int ifi);
 
 /* 7-point product z = A p (the pcgsip SpMV pass, pcg-sip.f90:142-153) with
    the fused dot pk.z over the interior; exposed for tests and benches.

@@ -229,6 +229,38 @@ def test_solver_host_pointer_dropin(gpu_lib, oracle_mod):
         assert gpu_lib.lib.cappgpu_pcgsip_h(host["p"].ctypes.data_as(ctypes.POINTER(ctypes.c_double)), IP) == 0
 
 
+@pytest.mark.parametrize("solver,code,symmetric", [("sipsol", 1, False), ("cgstab", 2, False), ("iccg", 3, True),
+                                                   ("pcgsip", 4, True), ("cgstab_sip", 5, False),
+                                                   ("dpcg", 6, True)])
+def test_every_solver_host_pointer_dropin_reports(gpu_lib, oracle_mod, solver, code, symmetric):
+    """The host-pointer form of each solver (what the Fortran drop-ins
+    pcgsip, sipsol, iccg, cgstab, cgstab_sip and
+    Diagonally_Preconditioned_CG call) solves the registered host array
+    as the oracle does and leaves the numbers of the solve's unit-66 line
+    (pcg-sip.f90:195-197, pcg-jacobi.f90:150-152) for cappgpu_last_report."""
+    st = solver_state(oracle_mod, 20, symmetric)
+    push(gpu_lib, st)
+    host = {n: st.field(n).copy() for n in FIELD_NAMES}
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    for n in ("ae", "aw", "an", "as", "at", "ab", "ap", "su", "p", "res",
+              "bb", "bs", "bw", "bp", "bn", "be", "bt"):
+        assert gpu_lib.lib.cappgpu_register(cappgpu.FIELD[n], dp(host[n])) == 0
+    try:
+        rc = getattr(gpu_lib.lib, f"cappgpu_{solver}_h")(dp(host["p"]), IP)
+        ro = st.solve(solver, "p", IP)
+        assert rc == ro.status
+        ref = st.field("p")
+        assert np.linalg.norm(host["p"] - ref) <= RTOL * np.linalg.norm(ref)
+        assert np.abs(host["res"] - st.field("res")).max() <= 1e-8 * np.abs(st.field("res")).max() + 1e-12
+        s, i, rep = ctypes.c_int(), ctypes.c_int(), cappgpu.SolveReport()
+        assert gpu_lib.lib.cappgpu_last_report(ctypes.byref(s), ctypes.byref(i), ctypes.byref(rep)) == 0
+        assert (s.value, i.value) == (code, IP)
+        assert (rep.iters, rep.status) == (ro.iters, ro.status)
+        assert abs(rep.res0 - ro.res0) <= 1e-12 * ro.res0
+    finally:
+        gpu_lib.lib.cappgpu_unregister_all()
+
+
 # ------------------------------------------------------------------- assembly
 
 def assembly_state(oracle_mod, kind, seed):
