@@ -162,6 +162,50 @@ static int face_geo(int idew, int idns, int idtb, int arvx, int arvy, int arvz, 
   return CAPPGPU_OK;
 }
 
+// QUICK's high-order fluxes of face inp (fluxuvw-overrelaxed-correction.f90:388-409)
+template <typename R>
+__device__ inline void quick_face(const FluxArgs& A, int inp, R& fu, R& fv, R& fw) {
+  const double *u = A.u, *v = A.v, *w = A.w;
+  const int ine = inp + A.idew, inw = inp - A.idew, inee = inp + 2 * A.idew;
+  const R flcf = R(A.fcf[inp]);
+  const R ce = dmin_(flcf, R(A.zero)), cp = dmax_(flcf, R(A.zero));
+  R fm = R(A.fif[inw]), f0 = R(A.fif[inp]), fpl = R(A.fif[ine]);
+  R g11 = ((2 - fm) * (f0 * f0)) / (1 + f0 - fm);
+  R g12 = ((1 - f0) * ((1 - fm) * (1 - fm))) / (1 + f0 - fm);
+  R g21 = ((1 + fpl) * ((1 - f0) * (1 - f0))) / (1 + fpl - f0);
+  R g22 = ((fpl * fpl) * f0) / (1 + fpl - f0);
+  fu = ce * (g21 * R(u[inp]) + (1 - g21 + g22) * R(u[ine]) - g22 * R(u[inee])) +
+       cp * (g11 * R(u[ine]) + (1 - g11 + g12) * R(u[inp]) - g12 * R(u[inw]));
+  fv = ce * (g21 * R(v[inp]) + (1 - g21 + g22) * R(v[ine]) - g22 * R(v[inee])) +
+       cp * (g11 * R(v[ine]) + (1 - g11 + g12) * R(v[inp]) - g12 * R(v[inw]));
+  fw = ce * (g21 * R(w[inp]) + (1 - g21 + g22) * R(w[ine]) - g22 * R(w[inee])) +
+       cp * (g11 * R(w[ine]) + (1 - g11 + g12) * R(w[inp]) - g12 * R(w[inw]));
+}
+
+// The reference zeroes fuhigh, fvhigh, fwhigh once, before its face loop
+// (fluxuvw-overrelaxed-correction.f90:90-92), and QUICK assigns them only
+// inside 2 < i,j,k < n-1 (:383-385): a face outside that box where no
+// earlier scheme assigned them carries the values of the last face of the
+// loop order (k, i, j) that was inside.  The loop boxes (:96-110) leave
+// out only the plane i = 2 (x faces), j = 2 (y faces) or k = 2 (z faces);
+// the face carried is (k-1, nimm, njmm) or (k, i-1, njmm), and none at the
+// start of the loop (the zeros).
+__device__ inline bool quick_carried_face(const Dims& d, int idew, int i, int j, int k, int* pinp) {
+  (void)j;
+  if (idew == d.nj) {                  // x faces: k 3..nkmm, i 2..nimm, j 3..njmm
+    if (k <= 3) return false;
+    *pinp = ixk(d, d.nimm, d.njmm, k - 1);
+    return true;
+  }
+  if (idew == 1) {                     // y faces: k 3..nkmm, i 3..nimm, j 2..njmm
+    if (i > 3) { *pinp = ixk(d, i - 1, d.njmm, k); return true; }
+    if (k <= 3) return false;
+    *pinp = ixk(d, d.nimm, d.njmm, k - 1);
+    return true;
+  }
+  return false;                        // z faces: the plane k = 2 opens the loop
+}
+
 // fluxuvw-overrelaxed-correction.f90:121-637 for one face inp; GEO: the
 // geometric terms come from the per-face cache (FP64 form only)
 template <typename R, bool GEO>
@@ -239,17 +283,20 @@ __global__ void k_fluxuvw_faces(Dims d, Box b, FluxArgs A, FaceGeoPtrs G) {
     R fvuds = cp * R(v[inp]) + ce * R(v[ine]);
     R fwuds = cp * R(w[inp]) + ce * R(w[ine]);
     R fuhigh = R(0.0), fvhigh = R(0.0), fwhigh = R(0.0);
+    bool assigned = false;             // a scheme before QUICK set this face's fluxes
     if (A.lcds) {
       R ue = R(u[inp]) * fxp + R(u[ine]) * fxe + (duxi * dxf + duyi * dyf + duzi * dzf);
       R ve = R(v[inp]) * fxp + R(v[ine]) * fxe + (dvxi * dxf + dvyi * dyf + dvzi * dzf);
       R we = R(w[inp]) * fxp + R(w[ine]) * fxe + (dwxi * dxf + dwyi * dyf + dwzi * dzf);
       fuhigh = flcf * ue; fvhigh = flcf * ve; fwhigh = flcf * we;
+      assigned = true;
     }
     if (A.lcds4 && (A.idew == d.nj || A.idew == 1)) {
       R ue = R(1.0) / R(48.0) * (R(27.0) * R(u[inp]) + R(27.0) * R(u[ine]) - R(3.0) * R(u[inw]) - R(3.0) * R(u[inee]));
       R ve = R(1.0) / R(48.0) * (R(27.0) * R(v[inp]) + R(27.0) * R(v[ine]) - R(3.0) * R(v[inw]) - R(3.0) * R(v[inee]));
       R we = R(1.0) / R(48.0) * (R(27.0) * R(w[inp]) + R(27.0) * R(w[ine]) - R(3.0) * R(w[inw]) - R(3.0) * R(w[inee]));
       fuhigh = flcf * ue; fvhigh = flcf * ve; fwhigh = flcf * we;
+      assigned = true;
     }
     if (A.lluds) {
       R xf = R(0.25) * (R(A.x[inp]) + R(A.x[ins]) + R(A.x[inb]) + R(A.x[inbs]));
@@ -266,19 +313,14 @@ __global__ void k_fluxuvw_faces(Dims d, Box b, FluxArgs A, FaceGeoPtrs G) {
       fuhigh = ce * (R(u[ine]) + dxe * dfidx_u1) + cp * (R(u[inp]) + dxc * dfidx_u);
       fvhigh = ce * (R(v[ine]) + dye * dfidy_u1) + cp * (R(v[inp]) + dyc * dfidy_u);
       fwhigh = ce * (R(w[ine]) + dze * dfidz_u1) + cp * (R(w[inp]) + dzc * dfidz_u);
+      assigned = true;
     }
-    if (A.lquds && k > 2 && k < d.nk - 1 && j > 2 && j < d.nj - 1 && i > 2 && i < d.ni - 1) {
-      R fm = R(A.fif[inp - A.idew]), f0 = R(A.fif[inp]), fpl = R(A.fif[inp + A.idew]);
-      R g11 = ((2 - fm) * (f0 * f0)) / (1 + f0 - fm);
-      R g12 = ((1 - f0) * ((1 - fm) * (1 - fm))) / (1 + f0 - fm);
-      R g21 = ((1 + fpl) * ((1 - f0) * (1 - f0))) / (1 + fpl - f0);
-      R g22 = ((fpl * fpl) * f0) / (1 + fpl - f0);
-      fuhigh = ce * (g21 * R(u[inp]) + (1 - g21 + g22) * R(u[ine]) - g22 * R(u[inee])) +
-               cp * (g11 * R(u[ine]) + (1 - g11 + g12) * R(u[inp]) - g12 * R(u[inw]));
-      fvhigh = ce * (g21 * R(v[inp]) + (1 - g21 + g22) * R(v[ine]) - g22 * R(v[inee])) +
-               cp * (g11 * R(v[ine]) + (1 - g11 + g12) * R(v[inp]) - g12 * R(v[inw]));
-      fwhigh = ce * (g21 * R(w[inp]) + (1 - g21 + g22) * R(w[ine]) - g22 * R(w[inee])) +
-               cp * (g11 * R(w[ine]) + (1 - g11 + g12) * R(w[inp]) - g12 * R(w[inw]));
+    if (A.lquds) {
+      int qf;
+      if (k > 2 && k < d.nk - 1 && j > 2 && j < d.nj - 1 && i > 2 && i < d.ni - 1)
+        quick_face<R>(A, inp, fuhigh, fvhigh, fwhigh);
+      else if (!assigned && quick_carried_face(d, A.idew, i, j, k, &qf))
+        quick_face<R>(A, qf, fuhigh, fvhigh, fwhigh);
     }
     if (A.flux_limiter) {
       R rr[6];

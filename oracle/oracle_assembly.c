@@ -2,7 +2,7 @@
  * oracle_assembly.c -- momentum assembly (fluxuvw, calcuvw), PISO and
  * SIMPLE pressure-velocity coupling, Courant number, continuity errors and
  * the step drivers, restated line by line from the reference (TEST
- * INFRASTRUCTURE ONLY; parity unpinned against the reference binary, see
+ * INFRASTRUCTURE ONLY; pinned against the reference's own routines, see
  * oracle.h).
  */
 #include "oracle.h"
@@ -44,6 +44,10 @@ void cap_fluxuvw(cap_state* s, int idew, int idns, int idtb, int arvxf, int arvy
   if (dir == 1) { jst = 3; kst = 3; }
   else if (dir == 2) { ist = 3; kst = 3; }
   else if (dir == 3) { ist = 3; jst = 3; }
+  /* :90-92 zero the high-order fluxes once, before the face loop: a face
+     where no scheme assigns them (QUICK outside its box, :383-385) keeps
+     the previous face's values */
+  double fuhigh = 0.0, fvhigh = 0.0, fwhigh = 0.0;
   for (int k = kst; k <= kend; ++k)
     for (int i = ist; i <= iend; ++i)
       for (int j = jst; j <= jend; ++j) {
@@ -103,7 +107,7 @@ void cap_fluxuvw(cap_state* s, int idew, int idns, int idtb, int arvxf, int arvy
         double fuuds = cp * u[inp] + ce * u[ine];
         double fvuds = cp * v[inp] + ce * v[ine];
         double fwuds = cp * w[inp] + ce * w[ine];
-        double fuhigh = 0.0, fvhigh = 0.0, fwhigh = 0.0, ue, ve, we;
+        double ue, ve, we;
         if (P->lcds) { /* :297-314 */
           ue = u[inp] * fxp + u[ine] * fxe + (duxi * (xf - xi) + duyi * (yf - yi) + duzi * (zf - zi));
           ve = v[inp] * fxp + v[ine] * fxe + (dvxi * (xf - xi) + dvyi * (yf - yi) + dvzi * (zf - zi));
