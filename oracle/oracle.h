@@ -3,14 +3,20 @@
  * INFRASTRUCTURE ONLY: the checker for the CUDA library, never shipped or
  * timed as the product).
  *
- * Parity status: the reference is Fortran and no Fortran compiler exists
- * in the build container, so the reference cannot be compiled or run here.
- * The only known-answer vectors the reference holds for this path are the
- * two find_intersection_point cases of test_intersection_point.f90:8-38,
- * which pin find_intersection_point.  Every other routine is pinned by
- * line-by-line restatement plus analytic known-answer tests (linear-field
- * gradients, manufactured Poisson solutions); solver and stencil parity
- * against the reference binary itself is "parity unpinned".
+ * Parity status: pinned against the reference's own source.  The
+ * reference is Fortran and no Fortran compiler exists in the build
+ * container, so it is not compiled; instead tests/golden/make_golden.py
+ * runs the reference's subroutines, read from their source files, through
+ * a Fortran-subset executor (tests/golden/f90exec.py: gfortran -O2
+ * arithmetic, default-real literals in single precision) on 75 seeded
+ * cases -- setind, all six solvers, ghost cells, grad_gauss, bpres,
+ * correctBoundaryConditions, fluxuvw (10 schemes x 3 directions), both
+ * pressure assemblies, fluxmass, PISO_getHbyA, calcuvw,
+ * PISO_multiple_correction, calcp, outbc, the LES viscosity, calcscm and
+ * modvis -- and tests/test_golden_reference.py holds this restatement to
+ * those outputs bit for bit (every module array, the module scalars and
+ * the unit-66 solver lines).  The reference's own known-answer vectors
+ * (test_intersection_point.f90:8-38) pin find_intersection_point.
  *
  * Layout: the state mirrors the reference's Fortran modules.  Each module
  * array is a 0-based double array of length nijk whose element ijk-1 is

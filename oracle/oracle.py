@@ -3,9 +3,9 @@
 The oracle (oracle_*.c) restates the reference's hot-path routines line by
 line on the same full-extent module arrays as the GPU library; tests run
 a routine on both from identical state and compare every array it writes.
-Parity status: see oracle.h (find_intersection_point pinned by the
-reference's own known-answer test; the rest is unpinned against the
-reference binary, which cannot be built without a Fortran compiler).
+Parity status: see oracle.h (pinned bit for bit against the reference's
+own Fortran routines, run from their source by tests/golden/f90exec.py;
+find_intersection_point also by the reference's known-answer test).
 """
 import ctypes
 import pathlib

@@ -2,9 +2,9 @@
  * oracle_core.c -- state, index maps, geometry, ghost cells, gradient,
  * bpres.  TEST INFRASTRUCTURE ONLY (the checker for the CUDA library).
  * Parity: find_intersection_point pinned by the reference's own
- * known-answer test (test_intersection_point.f90:8-38); the rest is a
- * line-faithful restatement ("parity unpinned" against the reference
- * binary, which cannot be built without a Fortran compiler).
+ * known-answer test (test_intersection_point.f90:8-38); setind, the ghost
+ * cells, grad_gauss and bpres pinned against the reference's own routines
+ * run from their source (see oracle.h).
  */
 #include "oracle.h"
 #include "oracle_internal.h"

@@ -1,7 +1,7 @@
 /*
  * oracle_solvers.c -- 7-diagonal linear solvers of the reference, restated
- * line by line (TEST INFRASTRUCTURE ONLY; parity unpinned against the
- * reference binary, see oracle.h).
+ * line by line (TEST INFRASTRUCTURE ONLY; pinned against the reference's
+ * own routines, see oracle.h).
  *
  * Work arrays that the reference declares as automatic arrays of size
  * nxyza (e.g. pk,zk in pcg-sip.f90:33) are allocated here with nijk
