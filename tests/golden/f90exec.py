@@ -579,10 +579,11 @@ def fortran_format(fmt, values):
 class Translator:
     """One subroutine -> Python source of a function f(M, *args)."""
 
-    def __init__(self, mod_syms, routines, stub_functions=()):
+    def __init__(self, mod_syms, routines, stub_functions=(), functions=None):
         self.mod = mod_syms          # name -> Sym (scope 'mod')
         self.routines = routines     # name -> (dummies) of routines that can be called
         self.stub_functions = set(stub_functions)
+        self.functions = dict(functions or {})   # translated functions -> result type
         self.consts = {}
 
     # -- names
@@ -634,6 +635,8 @@ class Translator:
                 return s.typ
             if e[1] in self.stub_functions:
                 return "r8"
+            if e[1] in self.functions:
+                return self.functions[e[1]]
             if e[1] == "real":
                 kw = [a for a in e[2] if a[0] == "kw"]
                 pos = [a for a in e[2] if a[0] != "kw"]
@@ -711,6 +714,12 @@ class Translator:
             raise NotImplementedError("substrings")
         if n in self.stub_functions:
             return f"_fstub({n!r})"
+        if n in self.functions:
+            codes = []
+            for a in args:
+                s2 = self.sym(a[1]) if a[0] == "name" else None
+                codes.append(self.var(a[1]) if s2 is not None and s2.rank else self.ex(a))
+            return f"M.call({n!r}{''.join(', ' + c for c in codes)})"
         if n == "real":
             kw = [a for a in args if a[0] == "kw"]
             pos = [a for a in args if a[0] != "kw"]
@@ -740,8 +749,9 @@ class Translator:
         return self.ex(a)
 
     # -- statements
-    def translate(self, name, dummies, body):
+    def translate(self, name, dummies, body, result=None):
         self.rname = name
+        self.result = result
         self.loc = {}
         self.dummies = dummies
         self.lines = []
@@ -793,6 +803,8 @@ class Translator:
         return "\n".join([head] + self.lines)
 
     def ret_tuple(self):
+        if self.result is not None:          # a function returns its result variable
+            return f"L_{self.result}"
         return "(" + "".join(f"L_{d}, " for d in self.dummies) + ")"
 
     def zero(self, typ):
@@ -1071,6 +1083,10 @@ class Namespace:
         return self._prog.funcs[name](self, *args)
 
 
+_FUNCTION = re.compile(r"(?:(?:pure|elemental|recursive)\s+)*(?:(?:real|integer|logical)(?:\([^)]*\))?\s+)?"
+                       r"function\s+(\w+)\s*\(([^)]*)\)\s*(?:result\s*\(\s*(\w+)\s*\))?\s*$")
+
+
 def _stub(name):
     def f(*_):
         raise RuntimeError(f"{name} was called: it is outside the executed set")
@@ -1086,6 +1102,7 @@ class Program:
         self.funcs = {}
         self.sources = {}
         self.subs = {}
+        self.fsubs = {}      # functions: name -> (dummies, body, result variable)
         for st in statements(module_text):
             if st.startswith(("module", "end module", "use ", "implicit", "end")):
                 continue
@@ -1121,18 +1138,24 @@ class Program:
         i = 0
         while i < len(st):
             m = re.match(r"subroutine\s+(\w+)\s*(\((.*)\))?\s*$", st[i])
-            if not m:
+            fm = _FUNCTION.match(st[i])
+            if not m and not fm:
                 i += 1
                 continue
-            name = m.group(1)
-            dummies = split_top(m.group(3)) if m.group(3) else []
+            kind = "subroutine" if m else "function"
+            name = (m or fm).group(1)
+            arglist = m.group(3) if m else fm.group(2)
+            dummies = split_top(arglist) if arglist else []
             j = i + 1
-            while not re.match(r"end(\s*subroutine\b.*)?$", st[j]):
-                if st[j].startswith(("contains", "subroutine ", "function ")) or " function " in st[j]:
+            while not re.match(r"end(\s*%s\b.*)?$" % kind, st[j]):
+                if st[j].startswith(("contains", "subroutine ")) or _FUNCTION.match(st[j]):
                     raise NotImplementedError(f"internal procedures in {name}")
                 j += 1
             if only is None or name in only:
-                self.subs[name] = (dummies, st[i + 1:j])
+                if m:
+                    self.subs[name] = (dummies, st[i + 1:j])
+                else:
+                    self.fsubs[name] = (dummies, st[i + 1:j], fm.group(3) or name)
             i = j + 1
 
     def compile(self, stubs=()):
@@ -1142,7 +1165,16 @@ class Program:
         routines = {n: d for n, (d, _) in self.subs.items()}
         for n in stubs:
             routines.setdefault(n, None)
-        tr = Translator(self.mod, routines, stub_functions=stubs)
+        ftypes = {}
+        for n, (dummies, body, res) in self.fsubs.items():
+            for st in body:
+                d = parse_declaration(st)
+                for ent in d or []:
+                    if ent[0] == res:
+                        ftypes[n] = ent[1]
+            if n not in ftypes:
+                raise NameError(f"function {n}: no declaration of its result {res}")
+        tr = Translator(self.mod, routines, stub_functions=stubs, functions=ftypes)
         mod_consts = []
         for n, s in self.mod.items():
             if s.param is not None:
@@ -1155,6 +1187,8 @@ class Program:
         srcs = []
         for n, (dummies, body) in self.subs.items():
             srcs.append(tr.translate(n, dummies, body))
+        for n, (dummies, body, res) in self.fsubs.items():
+            srcs.append(tr.translate(n, dummies, body, result=res))
         konst = [f"{v} = {'exact_f32' if k[1] == 'r4' else 'F8'}({k[0]!r})" for k, v in tr.consts.items()]
         code = "\n".join(konst + mod_consts + srcs)
         g = dict(_RUNTIME)
@@ -1162,7 +1196,7 @@ class Program:
         g["_fstub"] = lambda name: _stub(name)()
         exec(compile(code, "<reference>", "exec"), g)
         self.code = code
-        for n in self.subs:
+        for n in list(self.subs) + list(self.fsubs):
             self.funcs[n] = g["R_" + n]
         for n in stubs:
             if n not in self.subs:

@@ -44,9 +44,12 @@ class Case:
     oracle: callable(st) running the oracle's restatement;
     stubs: routines called only on branches the case does not take."""
 
-    def __init__(self, name, build, files, ref, oracle, stubs=(), setup=(), switches=None):
+    def __init__(self, name, build, files, ref, oracle, stubs=(), setup=(), switches=None, snippets=()):
         self.name, self.build, self.files, self.ref, self.oracle = name, build, files, ref, oracle
         self.stubs = tuple(stubs)
+        # (name, statements) wrapped as subroutines: the reference's include
+        # fragments with the locals main.f90 declares for them
+        self.snippets = tuple(snippets)
         # (file, first line, last line) of reference statements run before
         # the case, and module switches of the configuration (input file)
         self.setup = tuple(setup)
@@ -277,6 +280,35 @@ def all_cases():
     cases.append(Case("modvis_rans_channel", sst_state, ["modvis.f90", "calculate_stuff_for_sst.f90"],
                       ("modvis", []), lambda st: st.modvis(), stubs=sst_stubs, setup=sst_setup,
                       switches=sst_switches))
+
+    # main.f90's include fragments, with the locals main.f90:32-37 declares
+    def build_courant(O, conumfix=1):
+        case, st = assembly_state(O, "channel", 80)
+        st.params.update(dict(ltransient=1, conumfix=conumfix, conumfixvalue=0.5, timestep=0.01))
+        return case, st
+    for conumfix in (0, 1):
+        cases.append(Case(f"courant_number_conumfix{conumfix}", lambda O, c=conumfix: build_courant(O, c), [],
+                          ("courantno", []), lambda st: st.courant(),
+                          snippets=[("courantno", "integer :: i, j, k, inp\nreal(prec) :: suma, dt\n"
+                                                  "include 'CourantNo.h'")]))
+    cases.append(Case("continuity_errors_channel", build_courant, [], ("continuityerrors", []),
+                      lambda st: st.continuity_errors(),
+                      snippets=[("continuityerrors", "integer :: i, j, k, inp, idew, idns, idtb\n"
+                                                     "include 'continuityErrors.h'")]))
+
+    def build_cmf(O):
+        case, st = state(O, "channel")
+        rng = np.random.default_rng(5)
+        st.set_field("apu", 0.01 + 0.01 * rng.random(st.field("apu").size))
+        st.params.uin = 1.3
+        st.params.gradpcmf = 0.2
+        return case, st
+    cases.append(Case("const_massflux_correction_channel", build_cmf, [("fieldManipulation.f90",
+                                                                         ["volumeweightedaverage"])],
+                      ("constmflux", []), lambda st: st.const_massflux_correction(),
+                      setup=[("init.f90", 356, 356)],          # magUbar = UIN
+                      snippets=[("constmflux", "real(prec) :: magubarstar, ruaw, gragpplus, flowdirection\n"
+                                               "include 'const_massflux_correction.f90'")]))
     return cases
 
 

@@ -106,7 +106,10 @@ def run_case(ref, c):
     params_before = G.oracle_params(st)
     prog = F.Program((ref / "modules_allocatable.f90").read_text())
     for f in ["setind.f90"] + list(c.files):
-        prog.add_source((ref / f).read_text(), include_dir=ref)
+        f, only = (f, None) if isinstance(f, str) else (f[0], set(f[1]))
+        prog.add_source((ref / f).read_text(), only=only, include_dir=ref)
+    for name, text in c.snippets:
+        prog.add_snippet(name, text, include_dir=ref)
     for q, (f, a, b) in enumerate(c.setup):
         prog.add_snippet(f"setup{q}", "\n".join((ref / f).read_text().splitlines()[a - 1:b]), include_dir=ref)
     prog.compile(stubs=c.stubs)
@@ -128,7 +131,8 @@ def run_case(ref, c):
     after = {n: G.field_digest(module_array(ns, n)[1:]) for n in FIELD_NAMES}
     params = read_params(prog, ns, st)
     return {
-        "routine": [sub for sub, _ in calls], "files": list(c.files), "inputs": inputs,
+        "routine": [sub for sub, _ in calls], "files": [f if isinstance(f, str) else f[0] for f in c.files],
+        "inputs": inputs,
         # digests of the arrays the routine changed, and one over all arrays
         "fields": {n: d for n, d in after.items() if d != before[n]},
         "all_fields": G.all_fields_digest(after),

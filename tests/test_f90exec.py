@@ -242,3 +242,36 @@ def test_exact_single_rounding_of_decimal_literals():
         for c in nb:
             if np.isfinite(c):
                 assert abs(Fraction(float(f)) - v) <= abs(Fraction(float(c)) - v)
+
+
+def test_module_functions_return_their_result_variable():
+    prog = F.Program(MODULES)
+    prog.add_source("""
+module stuff
+contains
+  pure function wsum(a, n) result(s)
+  use types
+  real(prec), dimension(nxyza), intent(in) :: a
+  integer, intent(in) :: n
+  real(prec) :: s
+  integer :: i
+  s = 0.0_dp
+  do i=1,n
+    s = s + a(i)*2
+  end do
+  end function
+  subroutine noisy
+  call random_number(x)
+  end subroutine
+end module
+subroutine t(n, r)
+  use types
+  use coef
+  integer :: n
+  real(prec) :: r
+  r = wsum(ae, n) + 1
+end subroutine""", only={"wsum", "t"})
+    prog.compile()
+    ns = prog.namespace((4, 4, 4))
+    ns.get("ae")[1:4] = [0.5, 1.25, 2.0]
+    assert ns.call("t", 3, F.F8(0)) == (3, 2 * (0.5 + 1.25 + 2.0) + 1)
