@@ -20,7 +20,10 @@ static int check_top_wall_index() {
   return CAPPGPU_OK;
 }
 
-// main.f90:140-157: time-level shift at the start of a time step
+// main.f90:140-157: time-level shift at the start of a time step; te and
+// ed shift on every step, with or without the turbulence equations, as
+// the reference's unconditional assignments do (the LES path writes te's
+// ghost cells)
 static int shift_time_levels() {
   Ctx& c = ctx();
   size_t nb = sizeof(double) * c.d.nijk;
@@ -29,18 +32,14 @@ static int shift_time_levels() {
     CAP_CUDA(cudaMemcpyAsync(F[CAP_UOO], F[CAP_UO], nb, cudaMemcpyDeviceToDevice, c.st));
     CAP_CUDA(cudaMemcpyAsync(F[CAP_VOO], F[CAP_VO], nb, cudaMemcpyDeviceToDevice, c.st));
     CAP_CUDA(cudaMemcpyAsync(F[CAP_WOO], F[CAP_WO], nb, cudaMemcpyDeviceToDevice, c.st));
+    CAP_CUDA(cudaMemcpyAsync(F[CAP_TEOO], F[CAP_TEO], nb, cudaMemcpyDeviceToDevice, c.st));
+    CAP_CUDA(cudaMemcpyAsync(F[CAP_EDOO], F[CAP_EDO], nb, cudaMemcpyDeviceToDevice, c.st));
   }
   CAP_CUDA(cudaMemcpyAsync(F[CAP_UO], F[CAP_U], nb, cudaMemcpyDeviceToDevice, c.st));
   CAP_CUDA(cudaMemcpyAsync(F[CAP_VO], F[CAP_V], nb, cudaMemcpyDeviceToDevice, c.st));
   CAP_CUDA(cudaMemcpyAsync(F[CAP_WO], F[CAP_W], nb, cudaMemcpyDeviceToDevice, c.st));
-  if (c.prm.lcal[CAP_ITE - 1] || c.prm.lcal[CAP_IED - 1]) {   // main.f90:144-145, 153-154
-    if (c.prm.bdf) {
-      CAP_CUDA(cudaMemcpyAsync(F[CAP_TEOO], F[CAP_TEO], nb, cudaMemcpyDeviceToDevice, c.st));
-      CAP_CUDA(cudaMemcpyAsync(F[CAP_EDOO], F[CAP_EDO], nb, cudaMemcpyDeviceToDevice, c.st));
-    }
-    CAP_CUDA(cudaMemcpyAsync(F[CAP_TEO], F[CAP_TE], nb, cudaMemcpyDeviceToDevice, c.st));
-    CAP_CUDA(cudaMemcpyAsync(F[CAP_EDO], F[CAP_ED], nb, cudaMemcpyDeviceToDevice, c.st));
-  }
+  CAP_CUDA(cudaMemcpyAsync(F[CAP_TEO], F[CAP_TE], nb, cudaMemcpyDeviceToDevice, c.st));
+  CAP_CUDA(cudaMemcpyAsync(F[CAP_EDO], F[CAP_ED], nb, cudaMemcpyDeviceToDevice, c.st));
   return CAPPGPU_OK;
 }
 

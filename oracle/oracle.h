@@ -8,13 +8,14 @@
  * container, so it is not compiled; instead tests/golden/make_golden.py
  * runs the reference's subroutines, read from their source files, through
  * a Fortran-subset executor (tests/golden/f90exec.py: gfortran -O2
- * arithmetic, default-real literals in single precision) on 79 seeded
+ * arithmetic, default-real literals in single precision) on 82 seeded
  * cases -- setind, all six solvers, ghost cells, grad_gauss, bpres,
  * correctBoundaryConditions, fluxuvw (10 schemes x 3 directions), both
  * pressure assemblies, fluxmass, PISO_getHbyA, calcuvw,
  * PISO_multiple_correction, calcp, outbc, the LES viscosity, calcscm,
- * modvis, and main.f90's Courant-number, continuity-error and constant
- * mass-flux fragments -- and tests/test_golden_reference.py holds this restatement to
+ * modvis, main.f90's Courant-number, continuity-error and constant
+ * mass-flux fragments, and its time-loop body (PISO and SIMPLE steps) --
+ * and tests/test_golden_reference.py holds this restatement to
  * those outputs bit for bit (every module array, the module scalars and
  * the unit-66 solver lines).  The reference's own known-answer vectors
  * (test_intersection_point.f90:8-38) pin find_intersection_point.

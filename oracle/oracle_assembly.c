@@ -1067,24 +1067,20 @@ int cap_piso_steps(cap_state* s, int nsteps, cappgpu_solve_report* last) {
   cappgpu_params* P = &s->prm;
   const size_t nb = sizeof(double) * s->nijk;
   int rc = 0;
-  const int turb = P->lcal[CAP_ITE - 1] || P->lcal[CAP_IED - 1];
   for (int st = 0; st < nsteps; ++st) {
+    /* main.f90:140-157: te and ed shift whether or not their equations run */
     if (P->bdf) {
       memcpy(s->f[CAP_UOO], s->f[CAP_UO], nb);
       memcpy(s->f[CAP_VOO], s->f[CAP_VO], nb);
       memcpy(s->f[CAP_WOO], s->f[CAP_WO], nb);
-      if (turb) {   /* main.f90:144-145 */
-        memcpy(s->f[CAP_TEOO], s->f[CAP_TEO], nb);
-        memcpy(s->f[CAP_EDOO], s->f[CAP_EDO], nb);
-      }
+      memcpy(s->f[CAP_TEOO], s->f[CAP_TEO], nb);
+      memcpy(s->f[CAP_EDOO], s->f[CAP_EDO], nb);
     }
     memcpy(s->f[CAP_UO], s->f[CAP_U], nb);
     memcpy(s->f[CAP_VO], s->f[CAP_V], nb);
     memcpy(s->f[CAP_WO], s->f[CAP_W], nb);
-    if (turb) {   /* main.f90:153-154 */
-      memcpy(s->f[CAP_TEO], s->f[CAP_TE], nb);
-      memcpy(s->f[CAP_EDO], s->f[CAP_ED], nb);
-    }
+    memcpy(s->f[CAP_TEO], s->f[CAP_TE], nb);
+    memcpy(s->f[CAP_EDO], s->f[CAP_ED], nb);
     cap_courant(s);
     cap_update_values_at_ghostcells(s);
     cappgpu_solve_report r3[3];

@@ -47,8 +47,10 @@ class Case:
     def __init__(self, name, build, files, ref, oracle, stubs=(), setup=(), switches=None, snippets=()):
         self.name, self.build, self.files, self.ref, self.oracle = name, build, files, ref, oracle
         self.stubs = tuple(stubs)
-        # (name, statements) wrapped as subroutines: the reference's include
-        # fragments with the locals main.f90 declares for them
+        # (name, parts) wrapped as subroutines, each part a statement text
+        # or a (file, first line, last line) range of the reference: the
+        # include fragments and the time-loop body of main.f90, with the
+        # locals main.f90 declares for them
         self.snippets = tuple(snippets)
         # (file, first line, last line) of reference statements run before
         # the case, and module switches of the configuration (input file)
@@ -309,6 +311,60 @@ def all_cases():
                       setup=[("init.f90", 356, 356)],          # magUbar = UIN
                       snippets=[("constmflux", "real(prec) :: magubarstar, ruaw, gragpplus, flowdirection\n"
                                                "include 'const_massflux_correction.f90'")]))
+
+    # one PISO time step as main.f90's time loop runs it (:140-157 time
+    # levels, :169 Courant number, :185-205 the iteration, :252 the mass-flux
+    # correction), one iteration per step.  Left out, as the oracle's
+    # drivers leave them out: bcin, abort_mission (:162, :171), the
+    # residual normalisation and exit test (:218-240), and the output
+    # calls.  find_strain_rate runs before calc_vis_les, which reads the
+    # strain (calc_vis_les.f90:64) the LES path never forms.
+    step = ["integer :: i, j, k, inp",
+            "real(prec) :: suma, dt, magubarstar, ruaw, gragpplus, flowdirection",
+            ("main.f90", 140, 157), ("main.f90", 169, 169), ("main.f90", 185, 203),
+            "if(lcal(ivis) .and. lles) call find_strain_rate",
+            ("main.f90", 205, 205),
+            "if (ltransient .and. const_mflux) then", ("main.f90", 252, 252), "endif"]
+    step_files = ["calcuvw.f90", "GRAD_GAUSS.f90", "fluxuvw-overrelaxed-correction.f90", "sipsol.f90",
+                  "cgstab_sip.f90", "calcstress.f90", "outbc.f90", "PISO_multiple_correction.f90",
+                  "PISO_getHbyA.f90", "PISO_assemble_pressure_eq.f90", "bpres.f90", "pcg-sip.f90",
+                  "find_strain_rate.f90", "calc_vis_les.f90", "modvis.f90", "calcscm.f90",
+                  "calculate_stuff_for_sst.f90", "fluxscm-overrelaxed-correction.f90",
+                  ("fieldManipulation.f90", ["volumeweightedaverage"])]
+    step_stubs = ["grad_lsq_qr", "additional_algebraic_stress_terms", "calcp", "pimple_multiple_correction",
+                  "calcsct", "calculate_stuff_for_earsm", "von_karman_lengthscale"]
+
+    def build_les_channel(O):
+        case, st = state(O, "channel")
+        st.params.lles = 1
+        st.params.lcal[cappgpu.params.IVIS - 1] = 1
+        return case, st
+    cases.append(Case("piso_steps_les_channel_2", build_les_channel,
+                      ["update_values_at_ghostcells.f90"] + step_files, [("pisostep", []), ("pisostep", [])],
+                      lambda st: st.piso_steps(2), stubs=step_stubs, setup=[("init.f90", 356, 356)],
+                      switches={"piso": True}, snippets=[("pisostep", step)]))
+    cases.append(Case("piso_step_sst_channel", sst_state,
+                      ["update_values_at_ghostcells.f90"] + step_files, ("pisostep", []),
+                      lambda st: st.piso_steps(1), stubs=step_stubs,
+                      setup=[("init.f90", 229, 245), ("init.f90", 356, 356)],
+                      switches={"piso": True, "lturb": True, "levm": True}, snippets=[("pisostep", step)]))
+
+    # SIMPLE outer iterations: the iteration body of main.f90 (:185-205), steady
+    simple_files = [f for f in step_files if f not in ("PISO_multiple_correction.f90", "PISO_getHbyA.f90",
+                                                       "PISO_assemble_pressure_eq.f90")]
+    simple_files += ["calcp-multiple_correction_SIMPLE.f90", "fluxmass2.f90", "fluxmc.f90",
+                     "correctBoundaryConditions.f90", "iccg.f90", "cgstab.f90"]
+
+    def build_simple(O):
+        case, st = state(O, "cavity")
+        st.params.isol_p = cappgpu.SOLVER["cgstab_sip"]    # calcp's own choice, isol = 5
+        return case, st
+    cases.append(Case("simple_iters_cavity_2", build_simple,
+                      ["update_values_at_ghostcells_nonperiodic.f90"] + simple_files,
+                      [("simpleiter", []), ("simpleiter", [])], lambda st: st.simple_iters(2),
+                      stubs=[x for x in step_stubs if x != "calcp"] + ["piso_multiple_correction"],
+                      switches={"simple": True},
+                      snippets=[("simpleiter", [("main.f90", 185, 205)])]))
     return cases
 
 

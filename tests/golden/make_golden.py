@@ -108,7 +108,11 @@ def run_case(ref, c):
     for f in ["setind.f90"] + list(c.files):
         f, only = (f, None) if isinstance(f, str) else (f[0], set(f[1]))
         prog.add_source((ref / f).read_text(), only=only, include_dir=ref)
-    for name, text in c.snippets:
+    for name, parts in c.snippets:
+        if isinstance(parts, str):
+            parts = [parts]
+        text = "\n".join(x if isinstance(x, str) else
+                         "\n".join((ref / x[0]).read_text().splitlines()[x[1] - 1:x[2]]) for x in parts)
         prog.add_snippet(name, text, include_dir=ref)
     for q, (f, a, b) in enumerate(c.setup):
         prog.add_snippet(f"setup{q}", "\n".join((ref / f).read_text().splitlines()[a - 1:b]), include_dir=ref)
