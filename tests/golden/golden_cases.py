@@ -349,6 +349,17 @@ def all_cases():
                       setup=[("init.f90", 229, 245), ("init.f90", 356, 356)],
                       switches={"piso": True, "lturb": True, "levm": True}, snippets=[("pisostep", step)]))
 
+    # face areas and interpolation factors as init.f90:50-141 forms them (its
+    # cross products taken as written: the library's orientation 0) with
+    # intfac.f90 and find_intersection_point.f90
+    geo = ["integer :: i, j, k, intc, inbc, inp, ins, inb, inbs, idew, idns, idtb",
+           "real(prec) :: ednom, tenom, dxet, dxzd, dyet, dyzd, dzet, dzzd, perturb",
+           ("init.f90", 50, 141)]
+    for kind in ("cavity", "skewed", "channel"):
+        cases.append(Case(f"geometry_{kind}", lambda O, kind=kind: state(O, kind),
+                          ["intfac.f90", "find_intersection_point.f90"], ("geometry", []),
+                          lambda st: st.geometry(0), snippets=[("geometry", geo)]))
+
     # SIMPLE outer iterations: the iteration body of main.f90 (:185-205), steady
     simple_files = [f for f in step_files if f not in ("PISO_multiple_correction.f90", "PISO_getHbyA.f90",
                                                        "PISO_assemble_pressure_eq.f90")]
