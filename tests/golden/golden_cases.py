@@ -370,6 +370,18 @@ def all_cases():
         case, st = state(O, "cavity")
         st.params.isol_p = cappgpu.SOLVER["cgstab_sip"]    # calcp's own choice, isol = 5
         return case, st
+    def build_simple32(O):
+        case = cappgpu.cases.cavity(N=32)       # the configuration's own size and parameters
+        st = O.State.from_case(case, geometry_orient=1)
+        with_fluxes(case, st)
+        st.params.isol_p = cappgpu.SOLVER["cgstab_sip"]
+        return case, st
+    cases.append(Case("simple_iters_cavity32_2", build_simple32,
+                      ["update_values_at_ghostcells_nonperiodic.f90"] + simple_files,
+                      [("simpleiter", []), ("simpleiter", [])], lambda st: st.simple_iters(2),
+                      stubs=[x for x in step_stubs if x != "calcp"] + ["piso_multiple_correction"],
+                      switches={"simple": True},
+                      snippets=[("simpleiter", [("main.f90", 185, 205)])]))
     cases.append(Case("simple_iters_cavity_2", build_simple,
                       ["update_values_at_ghostcells_nonperiodic.f90"] + simple_files,
                       [("simpleiter", []), ("simpleiter", [])], lambda st: st.simple_iters(2),
