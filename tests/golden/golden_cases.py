@@ -343,6 +343,15 @@ def all_cases():
                       ["update_values_at_ghostcells.f90"] + step_files, [("pisostep", []), ("pisostep", [])],
                       lambda st: st.piso_steps(2), stubs=step_stubs, setup=[("init.f90", 356, 356)],
                       switches={"piso": True}, snippets=[("pisostep", step)]))
+    def build_channel32(O):
+        case = cappgpu.cases.channel(N=(32, 32, 32))   # the channel configuration (LES, mass flux) at 32^3
+        st = O.State.from_case(case)
+        with_fluxes(case, st)
+        return case, st
+    cases.append(Case("piso_step_channel32", build_channel32,
+                      ["update_values_at_ghostcells.f90"] + step_files, ("pisostep", []),
+                      lambda st: st.piso_steps(1), stubs=step_stubs, setup=[("init.f90", 356, 356)],
+                      switches={"piso": True}, snippets=[("pisostep", step)]))
     cases.append(Case("piso_step_sst_channel", sst_state,
                       ["update_values_at_ghostcells.f90"] + step_files, ("pisostep", []),
                       lambda st: st.piso_steps(1), stubs=step_stubs,
