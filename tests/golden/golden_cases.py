@@ -124,6 +124,14 @@ def all_cases():
             cases.append(Case(f"solve_{oname}_{seed}", build, [f], (sub, ["p", IP]),
                               lambda st, o=oname: st.solve(o, "p", IP)))
 
+        # stopped by the sweep limit: the report prints the loop index nsw + 1
+        def build_short(O, sym=sym):
+            _, st = solver_state(O, 22, sym)
+            st.params.nsw[IP - 1] = 3
+            return None, st
+        cases.append(Case(f"solve_{oname}_nsw3", build_short, [f], (sub, ["p", IP]),
+                          lambda st, o=oname: st.solve(o, "p", IP)))
+
     for periodic, f in ((0, "update_values_at_ghostcells_nonperiodic.f90"), (1, "update_values_at_ghostcells.f90")):
         def build(O, periodic=periodic):
             case, st = state(O, "skewed")

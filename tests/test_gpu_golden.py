@@ -8,9 +8,11 @@ ghost cells, gradient, bpres, boundary correction, fluxuvw (10 schemes x 3
 directions), both pressure assemblies, fluxmass, PISO_getHbyA, outbc and
 the grid geometry -- on the same inputs, and every module array must have
 the reference's digest: the GPU matches the reference bit for bit.  The
-other cases (solver sums, CUDA's pow/exp/log/tanh) are held to the oracle
-at 1e-10 by the other GPU tests, and the oracle to the reference bit for
-bit by tests/test_golden_reference.py."""
+solvers, whose sums run in another order, leave the reference's own
+unit-66 report line.  The other cases (CUDA's pow/exp/log/tanh, composite
+routines) are held to the oracle at 1e-10 by the other GPU tests, and the
+oracle to the reference bit for bit by tests/test_golden_reference.py."""
+import ctypes
 import json
 import pathlib
 import sys
@@ -20,7 +22,7 @@ import pytest
 HERE = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE / "golden"))
 
-from cappgpu import FIELD_NAMES  # noqa: E402
+from cappgpu import FIELD_NAMES, SOLVER  # noqa: E402
 import golden_cases as G  # noqa: E402
 from helpers import push  # noqa: E402
 
@@ -52,3 +54,28 @@ def test_gpu_matches_the_reference(gpu_lib, oracle_mod, name):
     differing = [n for n, d in rec["fields"].items() if got[n] != d]
     assert not differing, f"{name}: arrays differing from the reference's: {differing}"
     assert G.all_fields_digest(got) == rec["all_fields"], f"{name}: an array the reference left alone changed"
+
+
+SOLVER_CASES = sorted(n for n in GOLDEN if n.startswith("solve_"))
+
+
+@pytest.mark.parametrize("name", SOLVER_CASES)
+def test_gpu_solver_report_is_the_reference_line(gpu_lib, oracle_mod, name):
+    """The solvers sum in another order than the reference (block
+    reductions), so their fields agree to 1e-10, not bit for bit.  The
+    report a solve leaves is the reference's: the unit-66 line that the
+    reference's own routine wrote (residuals to its four digits, the
+    iteration index exactly, nsw + 1 when the sweep limit stopped it), and
+    resor(ifi) to 1e-12."""
+    rec, c = GOLDEN[name], CASES[name]
+    solver = max((o for o, *_ in G.SOLVERS if name.startswith(f"solve_{o}_")), key=len)
+    grid_case, st = c.build(oracle_mod)
+    assert G.state_digest(st) == rec["inputs"]
+    push(gpu_lib, st)
+    rep = gpu_lib.solve(solver, "p", G.IP)
+    buf = ctypes.create_string_buffer(256)
+    assert gpu_lib.lib.cappgpu_solver_report_line(SOLVER[solver], G.IP, ctypes.byref(rep), 0, 0, buf, 256) == 0
+    assert buf.value.decode() == rec["unit66"][-1]
+    ref_resor = float.fromhex(rec["params"]["resor"][G.IP - 1]) if "resor" in rec["params"] else None
+    if ref_resor is not None:
+        assert abs(gpu_lib.get_params().resor[G.IP - 1] - ref_resor) <= 1e-12 * abs(ref_resor)
