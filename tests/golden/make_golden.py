@@ -13,6 +13,7 @@ scalars and the unit-66 lines afterwards.  The reference directory is read
 here only; the fixture it writes is all the tests need.
 """
 import argparse
+import hashlib
 import json
 import pathlib
 import re
@@ -133,10 +134,25 @@ def run_case(ref, c):
         ns.call(sub, *[module_array(ns, a) if isinstance(a, str) else a for a in args])
     dt = time.time() - t
     after = {n: G.field_digest(module_array(ns, n)[1:]) for n in FIELD_NAMES}
+    used = ["modules_allocatable.f90", "setind.f90"] + [f if isinstance(f, str) else f[0] for f in c.files]
+    used += [f for f, _, _ in c.setup]
+    for _, parts in c.snippets:
+        for x in ([parts] if isinstance(parts, str) else parts):
+            if isinstance(x, tuple):
+                used.append(x[0])
+            else:
+                used += re.findall(r"include '([^']+)'", x)
+    for f in list(used):                  # files that INCLUDE lines of those bring in
+        for line in (ref / f).read_text().splitlines():
+            m = re.match(r"\s*include\s+'([^']+)'", line, re.I)
+            if m and (ref / m.group(1)).exists():
+                used.append(m.group(1))
+    sources = {f: hashlib.sha256((ref / f).read_bytes()).hexdigest()[:16] for f in sorted(set(used))}
     params = read_params(prog, ns, st)
     return {
-        "routine": [sub for sub, _ in calls], "files": [f if isinstance(f, str) else f[0] for f in c.files],
-        "inputs": inputs,
+        "routine": [sub for sub, _ in calls], "inputs": inputs,
+        # the reference source files this record was computed from (sha256)
+        "sources": sources,
         # digests of the arrays the routine changed, and one over all arrays
         "fields": {n: d for n, d in after.items() if d != before[n]},
         "all_fields": G.all_fields_digest(after),
