@@ -8,7 +8,7 @@
  * container, so it is not compiled; instead tests/golden/make_golden.py
  * runs the reference's subroutines, read from their source files, through
  * a Fortran-subset executor (tests/golden/f90exec.py: gfortran -O2
- * arithmetic, default-real literals in single precision) on 93 seeded
+ * arithmetic, default-real literals in single precision) on 96 seeded
  * cases -- setind, the grid geometry of init.f90 with intfac.f90, all six
  * solvers, ghost cells, grad_gauss, bpres,
  * correctBoundaryConditions, fluxuvw (10 schemes x 3 directions), both

@@ -237,6 +237,26 @@ def all_cases():
         cases.append(Case(f"calcuvw_{kind}", build, calcuvw_files, ("calcuvw", []), lambda st: st.calcuvw(),
                           stubs=["grad_lsq_qr", "additional_algebraic_stress_terms"]))
 
+    def build_calcuvw_cn(O):
+        case, st = state(O, "channel")
+        st.update_values_at_ghostcells()
+        st.params.update(dict(timestep=0.05, bdf=0, cn=1))
+        return case, st
+    cases.append(Case("calcuvw_channel_crank_nicolson", build_calcuvw_cn, calcuvw_files, ("calcuvw", []),
+                      lambda st: st.calcuvw(), stubs=["grad_lsq_qr", "additional_algebraic_stress_terms"]))
+
+    def build_piso_npcor2(O):
+        case, st = state(O, "channel")
+        st.params.update(dict(timestep=0.05, npcor=2))
+        st.update_values_at_ghostcells()
+        st.calcuvw()
+        return case, st
+    cases.append(Case("piso_multiple_correction_channel_npcor2", build_piso_npcor2,
+                      ["PISO_multiple_correction.f90", "PISO_getHbyA.f90", "PISO_assemble_pressure_eq.f90",
+                       "GRAD_GAUSS.f90", "bpres.f90", "outbc.f90", "pcg-sip.f90"],
+                      ("piso_multiple_correction", []), lambda st: st.piso_multiple_correction(),
+                      stubs=["grad_lsq_qr"]))
+
     def build_piso(O):
         case, st = state(O, "channel")
         st.params.update(dict(timestep=0.05))
@@ -394,6 +414,19 @@ def all_cases():
         st.params.isol_p = cappgpu.SOLVER["cgstab_sip"]
         return case, st
     cases.append(Case("simple_iters_cavity32_2", build_simple32,
+                      ["update_values_at_ghostcells_nonperiodic.f90"] + simple_files,
+                      [("simpleiter", []), ("simpleiter", [])], lambda st: st.simple_iters(2),
+                      stubs=[x for x in step_stubs if x != "calcp"] + ["piso_multiple_correction"],
+                      switches={"simple": True},
+                      snippets=[("simpleiter", [("main.f90", 185, 205)])]))
+    def build_simple_outlet(O):
+        case, st = state(O, "cavity")
+        st.bc("lbw")[:] = 1
+        st.bc("lbe")[:] = 2
+        st.params.update(dict(uin=0.5, lout=1, loe=1, flowin=0.02, const_mflux=0,
+                              isol_p=cappgpu.SOLVER["cgstab_sip"]))
+        return case, st
+    cases.append(Case("simple_iters_cavity_inflow_outflow_2", build_simple_outlet,
                       ["update_values_at_ghostcells_nonperiodic.f90"] + simple_files,
                       [("simpleiter", []), ("simpleiter", [])], lambda st: st.simple_iters(2),
                       stubs=[x for x in step_stubs if x != "calcp"] + ["piso_multiple_correction"],
