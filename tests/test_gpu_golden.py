@@ -22,7 +22,8 @@ import pytest
 HERE = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE / "golden"))
 
-from cappgpu import FIELD_NAMES, SOLVER  # noqa: E402
+from cappgpu import FIELD_NAMES, SOLVER, SolveReport  # noqa: E402
+import f90exec as F  # noqa: E402
 import golden_cases as G  # noqa: E402
 from helpers import push  # noqa: E402
 
@@ -79,3 +80,38 @@ def test_gpu_solver_report_is_the_reference_line(gpu_lib, oracle_mod, name):
     ref_resor = float.fromhex(rec["params"]["resor"][G.IP - 1]) if "resor" in rec["params"] else None
     if ref_resor is not None:
         assert abs(gpu_lib.get_params().resor[G.IP - 1] - ref_resor) <= 1e-12 * abs(ref_resor)
+
+
+COMPOSITE_CASES = sorted(n for n in GOLDEN if n.startswith(("calcuvw_", "piso_multiple_correction_")))
+
+
+def report_line(gpu_lib, solver, ifi, rep):
+    buf = ctypes.create_string_buffer(256)
+    r = SolveReport(res0=rep.res0, resl=rep.resl, iters=rep.iters, status=rep.status)
+    assert gpu_lib.lib.cappgpu_solver_report_line(SOLVER[solver], ifi, ctypes.byref(r), 0, 0, buf, 256) == 0
+    return buf.value.decode()
+
+
+@pytest.mark.parametrize("name", COMPOSITE_CASES)
+def test_gpu_composite_reports_are_the_reference_lines(gpu_lib, oracle_mod, name):
+    """calcuvw and PISO_multiple_correction on the GPU leave the unit-66
+    lines the reference's routines wrote: the three momentum SIP lines
+    (calcuvw.f90:388-460 through sipsol.f90:101-103), and the PCG(SIP) line
+    of every pressure solve with the last continuity-error line
+    (continuityErrors.h), formatted from the GPU's scalars."""
+    rec, c = GOLDEN[name], CASES[name]
+    grid_case, st = c.build(oracle_mod)
+    assert G.state_digest(st) == rec["inputs"]
+    push(gpu_lib, st)
+    reps = G.run_oracle(c, grid_case, gpu_lib)
+    if name.startswith("calcuvw_"):
+        got = [report_line(gpu_lib, "sipsol", ifi, reps[ifi - 1]) for ifi in (1, 2, 3)]
+        assert got == [x for x in rec["unit66"] if x.startswith("SIP:")]
+        return
+    P = gpu_lib.get_params()
+    got = [report_line(gpu_lib, "pcgsip", G.IP, r) for r in reps[:P.ncorr * P.npcor]]
+    assert got == [x for x in rec["unit66"] if x.startswith("PCG(SIP)")]
+    cont = F.fortran_format("(3(a,es10.3))", ["time step continuity errors : sum local = ", P.sumlocalconterr,
+                                               ", global = ", P.globalconterr, ", cumulative = ",
+                                               P.cumulativeconterr])
+    assert cont == [x for x in rec["unit66"] if x.startswith("time step continuity")][-1]
